@@ -1,0 +1,145 @@
+/*
+ * mdt_gpu.h -- C ABI of the md_tian2 GB300 force-and-propagation engine (libmdt_gpu.so).
+ *
+ * The reference (maurergroup/md_tian2) exposes its hot path as Fortran module
+ * procedures operating on one `type(universe)`.  This library replaces that path for a
+ * BATCH of independent trajectories on one GPU.  Every entry point:
+ *   - returns int32_t status: 0 = MDT_OK, negative = error (never aborts the process;
+ *     the reference's `print + stop` becomes an error code + mdt_last_error text);
+ *   - takes plain pointers and sizes; host arrays use the reference's Fortran order,
+ *     i.e. per trajectory r(3, nbeads, natoms) with the x/y/z index fastest, and the
+ *     trajectories concatenated;
+ *   - is callable from Fortran through iso_c_binding (include/mdt_gpu.f90).
+ * Threading: one context per host thread; calls on one context are serialised on the
+ * context's CUDA stream.  The caller owns host memory, the library owns device memory.
+ */
+#ifndef MDT_GPU_H
+#define MDT_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define MDT_OK 0
+#define MDT_ERR_ARG -1         /* invalid argument (the reference would `stop`) */
+#define MDT_ERR_CUDA -2        /* CUDA runtime error */
+#define MDT_ERR_STATE -3       /* call order violated (e.g. no batch defined) */
+#define MDT_ERR_UNSUPPORTED -4 /* configuration outside what this engine implements */
+#define MDT_ERR_NOMEM -5       /* device allocation failed */
+
+/* ids shared with the reference, src/constants.f90:64-71,107-115 */
+#define MDT_PES_EMT 2003
+#define MDT_PES_NENE 2008
+#define MDT_PROP_VERLET 1001
+#define MDT_PROP_LANGEVIN 1003       /* LDFA friction from the EMT density */
+#define MDT_PROP_ANDERSEN 1005
+#define MDT_PROP_PILE 1006
+#define MDT_PROP_LANGEVIN_CONST 1007 /* constant friction; no reference counterpart */
+#define MDT_ENERGY_AND_FORCE 3001
+#define MDT_ENERGY_ONLY 3002
+
+/* force arithmetic */
+#define MDT_PREC_FP64 0
+#define MDT_PREC_FP32 1
+
+/* trajectory status (mdt_traj_summary.status) */
+#define MDT_TRAJ_RUNNING 0
+#define MDT_TRAJ_EXIT_UPPER 1   /* projectile above pul, md_tian2.f90:88-89 */
+#define MDT_TRAJ_EXIT_LOWER 2   /* projectile below pll, md_tian2.f90:91-92 */
+#define MDT_TRAJ_ERR_DENSITY -10 /* negative EMT density in ldfa, md_algo.f90:551-554 */
+
+typedef struct mdt_ctx mdt_ctx;
+
+/* Propagation parameters: the simparams fields the hot path reads
+   (src/run_config.f90:34-85). */
+typedef struct mdt_prop_params {
+    double step;          /* fs */
+    double Tsurf, Tproj;  /* K */
+    double pile_tau;      /* fs, default 200 (run_config.f90:120) */
+    double andersen_time; /* fs, default 30 (run_config.f90:119) */
+    double gamma_const;   /* 1/fs, MDT_PROP_LANGEVIN_CONST only */
+    double pul, pll;      /* projectile exit limits, A */
+    uint64_t seed;        /* counter-based RNG key; each trajectory adds its index */
+    int32_t use_exit;     /* 1: stop a trajectory when its projectile passes pul/pll */
+    int32_t rng_mode;     /* 0: on-device Philox; 1: arrays from mdt_set_random_arrays */
+} mdt_prop_params;
+
+typedef struct mdt_traj_summary {
+    int32_t status;       /* MDT_TRAJ_* */
+    int32_t steps_done;
+    double epot;          /* mean bead potential energy, eV */
+    double ekin_p, ekin_l;/* atom_ekin, universe_mod.f90:433-458 */
+    double ebead;         /* ring-polymer spring energy, rpmd.f90:244-267 */
+} mdt_traj_summary;
+
+/* ---- context ------------------------------------------------------------- */
+int32_t mdt_create(int32_t device, mdt_ctx **out);
+int32_t mdt_destroy(mdt_ctx *ctx);
+const char *mdt_last_error(const mdt_ctx *ctx);
+int32_t mdt_synchronize(mdt_ctx *ctx);
+/* use an existing cudaStream_t (0 = the context's own stream) */
+int32_t mdt_set_stream(mdt_ctx *ctx, void *cuda_stream);
+
+/* ---- PES parameters --------------------------------------------------------
+ * Replaces read_emt (src/pes_emt_mod.f90:49-190): per-type EMT parameters
+ * (eta2 [1/A], n0 [1/A^3], E0 [eV], lambda [1/A], V0 [eV], kappa [1/A], s0 [A]) and
+ * the (ntypes x ntypes) column-major pes table (MDT_PES_EMT where EMT acts). */
+int32_t mdt_emt_set_params(mdt_ctx *ctx, int32_t ntypes, const double *eta2, const double *n0,
+                           const double *e0, const double *lambda, const double *v0, const double *kappa,
+                           const double *s0, const int32_t *pes);
+
+/* ---- batch geometry --------------------------------------------------------
+ * Replaces the universe constructor new_atoms (src/universe_mod.f90:77-115) for T
+ * trajectories at once.  natoms[T], nbeads[T]; idx: 1-based type per atom
+ * (concatenated); mass: per atom in eV fs^2/A^2 (amu * 103.638239276);
+ * is_fixed: (3, nb, N) per trajectory, 1 = frozen; simbox: 9 doubles per trajectory
+ * (column-major (3,3), cell vectors as columns); algo/is_proj: per type.
+ * Projectile atoms must precede lattice atoms, as md_init's merge_universes makes them
+ * (src/md_init.f90:559-625). */
+int32_t mdt_batch_define(mdt_ctx *ctx, int32_t ntraj, const int32_t *natoms, const int32_t *nbeads,
+                         const int32_t *idx, const double *mass, const uint8_t *is_fixed,
+                         const double *simbox, int32_t ntypes, const int32_t *algo, const uint8_t *is_proj);
+
+/* Upload positions / velocities (Fortran order, see above); resets trajectory status. */
+int32_t mdt_state_upload(mdt_ctx *ctx, const double *r, const double *v);
+/* Download any subset (NULL skips).  dens is (nb, N) per trajectory: the EMT embedded
+   density, or the friction coefficient after propagate_2 for LDFA atoms (the
+   reference's shared `dens` array, pes_emt_mod.f90:45 / md_algo.f90:556-558). */
+int32_t mdt_state_download(mdt_ctx *ctx, double *r, double *v, double *f, double *a, double *epot,
+                           double *dens);
+
+/* ---- hot path --------------------------------------------------------------
+ * calc_force (src/force.f90:40-86): zero f/a/epot, free ring-polymer step when
+ * nbeads > 1 (force.f90:54), EMT energies and forces, a = f/m for mobile atoms. */
+int32_t mdt_calc_force(mdt_ctx *ctx, int32_t flag, int32_t precision, const mdt_prop_params *p);
+/* propagate_1 / propagate_2 (src/md_algo.f90:37-106) */
+int32_t mdt_propagate_1(mdt_ctx *ctx, const mdt_prop_params *p);
+int32_t mdt_propagate_2(mdt_ctx *ctx, const mdt_prop_params *p);
+/* nsteps of propagate_1 -> calc_force -> propagate_2 with the exit test
+   (md_tian2.f90:78-92) in one fused launch. */
+int32_t mdt_md_steps(mdt_ctx *ctx, int32_t nsteps, int32_t precision, const mdt_prop_params *p);
+
+/* Deviates for rng_mode 1, each in Fortran order per trajectory: randy/zeta/andersen_v
+   (3, nb, N) normal deviates, andersen_u (nb, N) uniforms.  NULL leaves one unset. */
+int32_t mdt_set_random_arrays(mdt_ctx *ctx, const double *randy, const double *zeta, const double *andersen_v,
+                              const double *andersen_u);
+
+/* per-trajectory status, steps and energies (output_mod.f90:658-697 fields) */
+int32_t mdt_query(mdt_ctx *ctx, const mdt_prop_params *p, mdt_traj_summary *out);
+
+/* device pointers of the SoA state (x,y,z arrays of r, v, f, a) for zero-copy callers;
+   ptrs must hold 12 entries; *nslots receives the number of bead-atom slots. */
+int32_t mdt_device_state(mdt_ctx *ctx, void **ptrs, int64_t *nslots);
+
+/* ---- work counters ---------------------------------------------------------- */
+/* number of kernel launches this context issued since creation */
+int64_t mdt_launch_count(const mdt_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MDT_GPU_H */

@@ -1,0 +1,664 @@
+// mdt_api.cu -- the C ABI (include/mdt_gpu.h): context, batch layout, transfers and
+// launch orchestration.  No torch types; plain pointers and sizes only.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "../../include/mdt_gpu.h"
+#include "mdt_common.cuh"
+#include "mdt_internal.h"
+
+using namespace mdt;
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+};
+
+struct mdt_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    std::string err;
+    int64_t launches = 0;
+    int num_sms = 0;
+
+    // PES
+    bool have_emt = false;
+    EmtConst E{};
+    int pes_ntypes = 0;
+
+    // batch
+    bool have_batch = false;
+    int T = 0, ntypes = 0, max_atoms = 0, max_beads = 0;
+    int64_t total_ba = 0, total_pairs = 0;
+    int total_atoms = 0, total_beads = 0;
+    std::vector<int> natoms, nbeads, atom_off, bead_off;
+    std::vector<int64_t> ba_off;
+    Batch B{};
+    std::vector<DevBuf> bufs;
+    double *stage = nullptr;   // 3 * total_ba doubles (Fortran-order transfers)
+    int *order = nullptr, *counter = nullptr, *ba_traj = nullptr;
+    double *rnd[4] = {nullptr, nullptr, nullptr, nullptr};
+    double *summary = nullptr;
+    size_t scratch_prec_bytes = 0;
+};
+
+namespace {
+
+int fail(mdt_ctx *c, int code, const std::string &msg) {
+    if (c) c->err = msg;
+    return code;
+}
+
+int cuda_fail(mdt_ctx *c, cudaError_t e, const char *where) {
+    return fail(c, MDT_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+template <typename T> T *dalloc(mdt_ctx *c, size_t n, cudaError_t &e) {
+    void *p = nullptr;
+    const size_t bytes = std::max<size_t>(n * sizeof(T), 16);
+    e = cudaMalloc(&p, bytes);
+    if (e != cudaSuccess) return nullptr;
+    c->bufs.push_back(DevBuf{p, bytes});
+    return (T *)p;
+}
+
+void free_batch(mdt_ctx *c) {
+    for (auto &b : c->bufs) cudaFree(b.p);
+    c->bufs.clear();
+    c->have_batch = false;
+    c->stage = nullptr;
+    c->order = c->counter = c->ba_traj = nullptr;
+    for (auto &r : c->rnd) r = nullptr;
+    c->summary = nullptr;
+}
+
+// cjk normal-mode matrix, src/rpmd.f90:36-59 (column major, j 1-based in the arguments)
+void build_cjk(int nb, double *c) {
+    const double pi = kPi;
+    for (int j = 1; j <= nb; ++j)
+        for (int k = 0; k <= nb - 1; ++k) {
+            double v;
+            if (k == 0) v = std::sqrt(1.0 / nb);
+            else if (1 <= k && k <= nb / 2 - 1) v = std::sqrt(2.0 / nb) * std::cos(2.0 * pi * j * k / nb);
+            else if (k == nb / 2) v = std::sqrt(1.0 / nb) * ((j % 2) ? -1.0 : 1.0);
+            else v = std::sqrt(2.0 / nb) * std::sin(2.0 * pi * j * k / nb);
+            c[(size_t)k * nb + (j - 1)] = v;
+        }
+}
+
+// invert_matrix, src/useful_things.f90:296-321 (column major)
+bool invert3(const double *A, double *B) {
+    auto a = [&](int i, int j) { return A[(j - 1) * 3 + (i - 1)]; };
+    const double det = a(1, 1) * a(2, 2) * a(3, 3) - a(1, 1) * a(2, 3) * a(3, 2) - a(1, 2) * a(2, 1) * a(3, 3) +
+                       a(1, 2) * a(2, 3) * a(3, 1) + a(1, 3) * a(2, 1) * a(3, 2) - a(1, 3) * a(2, 2) * a(3, 1);
+    if (det < kTolerance) return false;
+    const double di = 1 / det;
+    auto b = [&](int i, int j) -> double & { return B[(j - 1) * 3 + (i - 1)]; };
+    b(1, 1) = +di * (a(2, 2) * a(3, 3) - a(2, 3) * a(3, 2));
+    b(2, 1) = -di * (a(2, 1) * a(3, 3) - a(2, 3) * a(3, 1));
+    b(3, 1) = +di * (a(2, 1) * a(3, 2) - a(2, 2) * a(3, 1));
+    b(1, 2) = -di * (a(1, 2) * a(3, 3) - a(1, 3) * a(3, 2));
+    b(2, 2) = +di * (a(1, 1) * a(3, 3) - a(1, 3) * a(3, 1));
+    b(3, 2) = -di * (a(1, 1) * a(3, 2) - a(1, 2) * a(3, 1));
+    b(1, 3) = +di * (a(1, 2) * a(2, 3) - a(1, 3) * a(2, 2));
+    b(2, 3) = -di * (a(1, 1) * a(2, 3) - a(1, 3) * a(2, 1));
+    b(3, 3) = +di * (a(1, 1) * a(2, 2) - a(1, 2) * a(2, 1));
+    return true;
+}
+
+PropParams to_dev(const mdt_ctx *c, const mdt_prop_params *p) {
+    PropParams P{};
+    P.step = p->step;
+    P.Tsurf = p->Tsurf;
+    P.Tproj = p->Tproj;
+    P.pile_tau = p->pile_tau;
+    P.andersen_time = p->andersen_time;
+    P.gamma_const = p->gamma_const;
+    P.pul = p->pul;
+    P.pll = p->pll;
+    P.seed = p->seed;
+    P.use_exit = p->use_exit;
+    P.rng_mode = p->rng_mode;
+    P.randy = c->rnd[0];
+    P.zeta = c->rnd[1];
+    P.andersen_v = c->rnd[2];
+    P.andersen_u = c->rnd[3];
+    return P;
+}
+
+int check_ready(mdt_ctx *c, bool need_emt) {
+    if (!c) return MDT_ERR_ARG;
+    if (!c->have_batch) return fail(c, MDT_ERR_STATE, "no batch defined (call mdt_batch_define)");
+    if (need_emt && !c->have_emt) return fail(c, MDT_ERR_STATE, "no PES parameters (call mdt_emt_set_params)");
+    if (need_emt && c->pes_ntypes != c->ntypes)
+        return fail(c, MDT_ERR_ARG, "PES and batch disagree on the number of types");
+    return MDT_OK;
+}
+
+LaunchCfg cfg(mdt_ctx *c, int precision) {
+    const int per_sm = max_resident_ctas(c->max_atoms, c->max_beads, precision);
+    const int grid = std::max(1, std::min(c->T, c->num_sms * per_sm));
+    return LaunchCfg{c->stream, grid, c->order, c->counter};
+}
+
+int ensure_scratch(mdt_ctx *c, int precision) {
+    const size_t rs = precision == MDT_PREC_FP32 ? 4 : 8;
+    const size_t need = std::max<size_t>(16, 5 * rs * (size_t)c->total_pairs);
+    if (c->B.pair_scratch && c->scratch_prec_bytes >= need) return MDT_OK;
+    cudaError_t e;
+    void *p = dalloc<unsigned char>(c, need, e);
+    if (!p) return fail(c, MDT_ERR_NOMEM, "pair scratch allocation failed");
+    c->B.pair_scratch = p;
+    c->scratch_prec_bytes = need;
+    return MDT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t mdt_create(int32_t device, mdt_ctx **out) {
+    if (!out) return MDT_ERR_ARG;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) return MDT_ERR_CUDA;
+    auto *c = new mdt_ctx();
+    c->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+    if (e != cudaSuccess) {
+        delete c;
+        return MDT_ERR_CUDA;
+    }
+    c->own_stream = true;
+    *out = c;
+    return MDT_OK;
+}
+
+int32_t mdt_destroy(mdt_ctx *c) {
+    if (!c) return MDT_ERR_ARG;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    free_batch(c);
+    if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return MDT_OK;
+}
+
+const char *mdt_last_error(const mdt_ctx *c) { return c ? c->err.c_str() : "null context"; }
+
+int64_t mdt_launch_count(const mdt_ctx *c) { return c ? c->launches : -1; }
+
+int32_t mdt_synchronize(mdt_ctx *c) {
+    if (!c) return MDT_ERR_ARG;
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    return e == cudaSuccess ? MDT_OK : cuda_fail(c, e, "mdt_synchronize");
+}
+
+int32_t mdt_set_stream(mdt_ctx *c, void *s) {
+    if (!c) return MDT_ERR_ARG;
+    if (c->own_stream && c->stream) {
+        cudaStreamSynchronize(c->stream);
+        cudaStreamDestroy(c->stream);
+    }
+    if (s) {
+        c->stream = (cudaStream_t)s;
+        c->own_stream = false;
+    } else {
+        cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+        c->own_stream = true;
+    }
+    return MDT_OK;
+}
+
+// Derived constants of compute_emt_1species / compute_emt_2species
+// (src/pes_emt_mod.f90:258-307 and 521-592), computed in the same order.
+int32_t mdt_emt_set_params(mdt_ctx *c, int32_t ntypes, const double *eta2, const double *n0, const double *e0,
+                           const double *lambda, const double *v0, const double *kappa, const double *s0,
+                           const int32_t *pes) {
+    if (!c) return MDT_ERR_ARG;
+    if (ntypes < 1 || ntypes > kMaxTypes || !eta2 || !n0 || !e0 || !lambda || !v0 || !kappa || !s0 || !pes)
+        return fail(c, MDT_ERR_ARG, "mdt_emt_set_params: bad arguments (1 <= ntypes <= 4)");
+    EmtConst E{};
+    int slots[2] = {-1, -1}, ns = 0;
+    for (int t = 0; t < kMaxTypes; ++t) E.slot_of_type[t] = -1;
+    for (int t = 0; t < ntypes; ++t)
+        if (pes[t * ntypes + t] == MDT_PES_EMT) {
+            if (ns >= 2) return fail(c, MDT_ERR_UNSUPPORTED, "more than two EMT species (compute_emt_nspecies)");
+            slots[ns] = t;
+            E.slot_of_type[t] = ns++;
+        }
+    if (ns == 0) return fail(c, MDT_ERR_ARG, "no EMT species in the pes table");
+    E.nspecies = ns;
+    E.pair_mask = 0;
+    for (int a = 0; a < ntypes; ++a)
+        for (int b = 0; b < ntypes; ++b)
+            if (pes[b * ntypes + a] == MDT_PES_EMT && E.slot_of_type[a] >= 0 && E.slot_of_type[b] >= 0)
+                E.pair_mask |= 1u << (a * kMaxTypes + b);
+    const double beta = std::pow(16.0 * kPi / 3.0, 1.0 / 3.0) * (1.0 / kSqrt2);
+    const double nneighs[3] = {12.0, 6.0, 24.0};
+    double bs0[2] = {0, 0};
+    for (int s = 0; s < ns; ++s) {
+        const int t = slots[s];
+        E.eta2[s] = eta2[t];
+        E.n0[s] = n0[t];
+        E.e0[s] = e0[t];
+        E.lambda[s] = lambda[t];
+        E.kappa[s] = kappa[t];
+        E.v0[s] = v0[t];
+        bs0[s] = beta * s0[t];
+        E.betas0[s] = bs0[s];
+        E.betaeta2[s] = beta * eta2[t];
+        E.kappadbeta[s] = kappa[t] / beta;
+    }
+    const double rcut = (ns == 2 ? std::max(bs0[0], bs0[1]) : bs0[0]) * kSqrt3;
+    const double rr = 4.0 * rcut / (kSqrt3 + 2);
+    const double acut = 9.21034037197618 / (rr - rcut);
+    E.rcut = rcut;
+    E.acut = acut;
+    E.cut = 1.5 * rcut;
+    E.cut2 = E.cut * E.cut;
+    for (int s = 0; s < ns; ++s) {
+        const double rnn[3] = {bs0[s], bs0[s] * kSqrt2, bs0[s] * kSqrt3};
+        double x[3], g1 = 0, g2 = 0;
+        for (int k = 0; k < 3; ++k) x[k] = nneighs[k] * kTwelfth / (1 + std::exp(acut * (rnn[k] - rcut)));
+        for (int k = 0; k < 3; ++k) g1 += x[k] * std::exp(-E.eta2[s] * (rnn[k] - bs0[s]));
+        for (int k = 0; k < 3; ++k) g2 += x[k] * std::exp(-E.kappadbeta[s] * (rnn[k] - bs0[s]));
+        E.igamma1[s] = 1.0 / g1;
+        E.g2v0[s] = (1.0 / g2) * E.v0[s];
+        E.dens_exp[s] = 0.5 / kBohr2Ang - E.betaeta2[s];
+    }
+    E.chi[0][0] = E.chi[1][1] = 1.0;
+    E.chi[0][1] = E.chi[1][0] = 1.0;
+    if (ns == 2) {
+        const int t1 = slots[0], t2 = slots[1];
+        const double chi_21 = n0[t1] / n0[t2] * std::exp(0.5 / kBohr2Ang * (s0[t2] - s0[t1]));
+        const double chi_12 = 1.0 / chi_21;
+        E.chi[0][1] = chi_12;  // density at a type1 atom from a type2 neighbour
+        E.chi[1][0] = chi_21;
+        E.hh_quirk = 1;
+    }
+    c->E = E;
+    c->have_emt = true;
+    c->pes_ntypes = ntypes;
+    return MDT_OK;
+}
+
+int32_t mdt_batch_define(mdt_ctx *c, int32_t ntraj, const int32_t *natoms, const int32_t *nbeads,
+                         const int32_t *idx, const double *mass, const uint8_t *is_fixed, const double *simbox,
+                         int32_t ntypes, const int32_t *algo, const uint8_t *is_proj) {
+    if (!c) return MDT_ERR_ARG;
+    if (ntraj < 1 || !natoms || !nbeads || !idx || !mass || !is_fixed || !simbox || !algo || !is_proj ||
+        ntypes < 1 || ntypes > kMaxTypes)
+        return fail(c, MDT_ERR_ARG, "mdt_batch_define: bad arguments");
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    free_batch(c);
+    c->T = ntraj;
+    c->ntypes = ntypes;
+    c->natoms.assign(natoms, natoms + ntraj);
+    c->nbeads.assign(nbeads, nbeads + ntraj);
+    c->ba_off.resize(ntraj);
+    c->atom_off.resize(ntraj);
+    c->bead_off.resize(ntraj);
+    std::vector<int64_t> pair_off(ntraj);
+    std::vector<int> cjk_off(ntraj, 0);
+    std::vector<int> nb_tables;  // distinct bead counts
+    std::vector<double> cjk_host;
+    int64_t ba = 0, pairs = 0;
+    int at = 0, bd = 0;
+    c->max_atoms = 0;
+    c->max_beads = 0;
+    for (int t = 0; t < ntraj; ++t) {
+        const int N = natoms[t], nb = nbeads[t];
+        if (N < 1 || nb < 1 || nb > 32)
+            return fail(c, MDT_ERR_ARG, "natoms must be >= 1 and 1 <= nbeads <= 32");
+        c->ba_off[t] = ba;
+        c->atom_off[t] = at;
+        c->bead_off[t] = bd;
+        pair_off[t] = pairs;
+        ba += (int64_t)N * nb;
+        at += N;
+        bd += nb;
+        pairs += (int64_t)nb * N * (N / 2);
+        c->max_atoms = std::max(c->max_atoms, N);
+        c->max_beads = std::max(c->max_beads, nb);
+        auto it = std::find(nb_tables.begin(), nb_tables.end(), nb);
+        if (it == nb_tables.end()) {
+            nb_tables.push_back(nb);
+            const size_t off = cjk_host.size();
+            cjk_host.resize(off + (size_t)nb * nb);
+            build_cjk(nb, cjk_host.data() + off);
+        }
+    }
+    {
+        // offsets of each trajectory's cjk table
+        std::vector<int> table_off(nb_tables.size());
+        int o = 0;
+        for (size_t k = 0; k < nb_tables.size(); ++k) {
+            table_off[k] = o;
+            o += nb_tables[k] * nb_tables[k];
+        }
+        for (int t = 0; t < ntraj; ++t) {
+            const size_t k = std::find(nb_tables.begin(), nb_tables.end(), nbeads[t]) - nb_tables.begin();
+            cjk_off[t] = table_off[k];
+        }
+    }
+    c->total_ba = ba;
+    c->total_atoms = at;
+    c->total_beads = bd;
+    c->total_pairs = pairs;
+    if (c->max_atoms > 4096) return fail(c, MDT_ERR_UNSUPPORTED, "more than 4096 atoms in one trajectory");
+    for (int a = 0; a < at; ++a)
+        if (idx[a] < 1 || idx[a] > ntypes) return fail(c, MDT_ERR_ARG, "atom type index out of range");
+
+    // host-side derived arrays
+    std::vector<int8_t> type(at);
+    for (int a = 0; a < at; ++a) type[a] = (int8_t)(idx[a] - 1);
+    std::vector<uint8_t> fixed(ba);
+    std::vector<int> ba_traj(ba);
+    for (int t = 0; t < ntraj; ++t) {
+        const int N = natoms[t], nb = nbeads[t];
+        for (int i = 0; i < N; ++i)
+            for (int b = 0; b < nb; ++b) {
+                const int64_t f = (c->ba_off[t] + (int64_t)i * nb + b) * 3;
+                const int64_t s = c->ba_off[t] + (int64_t)b * N + i;
+                fixed[s] = (uint8_t)((is_fixed[f] ? 1 : 0) | (is_fixed[f + 1] ? 2 : 0) | (is_fixed[f + 2] ? 4 : 0));
+                ba_traj[s] = t;
+            }
+    }
+    std::vector<double> ibox(9 * (size_t)ntraj);
+    for (int t = 0; t < ntraj; ++t)
+        if (!invert3(simbox + 9 * t, ibox.data() + 9 * t))
+            return fail(c, MDT_ERR_ARG, "simulation cell is singular (invert_matrix)");
+    std::vector<int> order(ntraj);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        const double ca = (double)nbeads[a] * natoms[a] * natoms[a], cb = (double)nbeads[b] * natoms[b] * natoms[b];
+        return ca > cb;
+    });
+
+    cudaError_t e = cudaSuccess;
+    Batch &B = c->B;
+    B = Batch{};
+    B.ntraj = ntraj;
+    B.ntypes = ntypes;
+    B.max_atoms = c->max_atoms;
+    B.max_beads = c->max_beads;
+    for (int t = 0; t < kMaxTypes; ++t) {
+        B.algo[t] = t < ntypes ? algo[t] : 0;
+        B.is_proj[t] = t < ntypes ? (is_proj[t] ? 1 : 0) : 0;
+    }
+    for (int t = 0; t < ntypes; ++t)
+        if (algo[t] != MDT_PROP_VERLET && algo[t] != MDT_PROP_LANGEVIN && algo[t] != MDT_PROP_ANDERSEN &&
+            algo[t] != MDT_PROP_PILE && algo[t] != MDT_PROP_LANGEVIN_CONST)
+            return fail(c, MDT_ERR_ARG, "unknown propagation algorithm");
+#define ALLOC(ptr, T_, n)                                                          \
+    do {                                                                           \
+        ptr = dalloc<T_>(c, (n), e);                                               \
+        if (!ptr) {                                                                \
+            free_batch(c);                                                         \
+            return fail(c, MDT_ERR_NOMEM, "device allocation failed: " #ptr);      \
+        }                                                                          \
+    } while (0)
+    int *d_natoms, *d_nbeads, *d_atom_off, *d_bead_off, *d_cjk_off, *d_status, *d_steps;
+    int64_t *d_ba_off, *d_pair_off;
+    double *d_mass, *d_box, *d_ibox, *d_cjk;
+    int8_t *d_type;
+    uint8_t *d_fixed;
+    ALLOC(d_natoms, int, ntraj);
+    ALLOC(d_nbeads, int, ntraj);
+    ALLOC(d_atom_off, int, ntraj);
+    ALLOC(d_bead_off, int, ntraj);
+    ALLOC(d_cjk_off, int, ntraj);
+    ALLOC(d_status, int, ntraj);
+    ALLOC(d_steps, int, ntraj);
+    ALLOC(d_ba_off, int64_t, ntraj);
+    ALLOC(d_pair_off, int64_t, ntraj);
+    ALLOC(d_mass, double, at);
+    ALLOC(d_box, double, 9 * (size_t)ntraj);
+    ALLOC(d_ibox, double, 9 * (size_t)ntraj);
+    ALLOC(d_cjk, double, cjk_host.size());
+    ALLOC(d_type, int8_t, at);
+    ALLOC(d_fixed, uint8_t, ba);
+    double *arr[12];
+    for (int k = 0; k < 12; ++k) ALLOC(arr[k], double, ba);
+    ALLOC(B.dens, double, ba);
+    ALLOC(B.epot, double, bd);
+    ALLOC(c->stage, double, 3 * (size_t)ba);
+    ALLOC(c->order, int, ntraj);
+    ALLOC(c->counter, int, 4);
+    ALLOC(c->ba_traj, int, ba);
+    ALLOC(c->summary, double, 5 * (size_t)ntraj);
+#undef ALLOC
+    auto up = [&](void *dst, const void *src, size_t bytes) {
+        if (e == cudaSuccess && bytes) e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, c->stream);
+    };
+    up(d_natoms, natoms, sizeof(int) * ntraj);
+    up(d_nbeads, nbeads, sizeof(int) * ntraj);
+    up(d_atom_off, c->atom_off.data(), sizeof(int) * ntraj);
+    up(d_bead_off, c->bead_off.data(), sizeof(int) * ntraj);
+    up(d_cjk_off, cjk_off.data(), sizeof(int) * ntraj);
+    up(d_ba_off, c->ba_off.data(), sizeof(int64_t) * ntraj);
+    up(d_pair_off, pair_off.data(), sizeof(int64_t) * ntraj);
+    up(d_mass, mass, sizeof(double) * at);
+    up(d_box, simbox, sizeof(double) * 9 * ntraj);
+    up(d_ibox, ibox.data(), sizeof(double) * 9 * ntraj);
+    up(d_cjk, cjk_host.data(), sizeof(double) * cjk_host.size());
+    up(d_type, type.data(), at);
+    up(d_fixed, fixed.data(), ba);
+    up(c->order, order.data(), sizeof(int) * ntraj);
+    up(c->ba_traj, ba_traj.data(), sizeof(int) * ba);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_status, 0, sizeof(int) * ntraj, c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_steps, 0, sizeof(int) * ntraj, c->stream);
+    for (int k = 0; k < 12 && e == cudaSuccess; ++k) e = cudaMemsetAsync(arr[k], 0, sizeof(double) * ba, c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(B.dens, 0, sizeof(double) * ba, c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(B.epot, 0, sizeof(double) * bd, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);  // host vectors go out of scope
+    if (e != cudaSuccess) {
+        free_batch(c);
+        return cuda_fail(c, e, "mdt_batch_define upload");
+    }
+    B.natoms = d_natoms;
+    B.nbeads = d_nbeads;
+    B.ba_off = d_ba_off;
+    B.atom_off = d_atom_off;
+    B.bead_off = d_bead_off;
+    B.pair_off = d_pair_off;
+    B.rx = arr[0]; B.ry = arr[1]; B.rz = arr[2];
+    B.vx = arr[3]; B.vy = arr[4]; B.vz = arr[5];
+    B.ax = arr[6]; B.ay = arr[7]; B.az = arr[8];
+    B.fx = arr[9]; B.fy = arr[10]; B.fz = arr[11];
+    B.mass = d_mass;
+    B.type = d_type;
+    B.fixed = d_fixed;
+    B.box = d_box;
+    B.ibox = d_ibox;
+    B.status = d_status;
+    B.steps_done = d_steps;
+    B.cjk_off = d_cjk_off;
+    B.cjk = d_cjk;
+    B.pair_scratch = nullptr;
+    c->scratch_prec_bytes = 0;
+    c->have_batch = true;
+    return MDT_OK;
+}
+
+int32_t mdt_state_upload(mdt_ctx *c, const double *r, const double *v) {
+    int rc = check_ready(c, false);
+    if (rc) return rc;
+    cudaError_t e = cudaSuccess;
+    const size_t bytes = sizeof(double) * 3 * (size_t)c->total_ba;
+    Batch &B = c->B;
+    if (r) {
+        e = cudaMemcpyAsync(c->stage, r, bytes, cudaMemcpyHostToDevice, c->stream);
+        if (e == cudaSuccess) e = launch_unpack(c->stream, B, c->stage, B.rx, B.ry, B.rz, c->total_ba, c->ba_traj);
+        c->launches++;
+    }
+    if (v && e == cudaSuccess) {
+        e = cudaMemcpyAsync(c->stage, v, bytes, cudaMemcpyHostToDevice, c->stream);
+        if (e == cudaSuccess) e = launch_unpack(c->stream, B, c->stage, B.vx, B.vy, B.vz, c->total_ba, c->ba_traj);
+        c->launches++;
+    }
+    if (e == cudaSuccess) e = cudaMemsetAsync(B.status, 0, sizeof(int) * c->T, c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(B.steps_done, 0, sizeof(int) * c->T, c->stream);
+    return e == cudaSuccess ? MDT_OK : cuda_fail(c, e, "mdt_state_upload");
+}
+
+int32_t mdt_state_download(mdt_ctx *c, double *r, double *v, double *f, double *a, double *epot, double *dens) {
+    int rc = check_ready(c, false);
+    if (rc) return rc;
+    cudaError_t e = cudaSuccess;
+    const size_t bytes = sizeof(double) * 3 * (size_t)c->total_ba;
+    Batch &B = c->B;
+    double *outs[4] = {r, v, f, a};
+    double *src[4][3] = {{B.rx, B.ry, B.rz}, {B.vx, B.vy, B.vz}, {B.fx, B.fy, B.fz}, {B.ax, B.ay, B.az}};
+    for (int k = 0; k < 4 && e == cudaSuccess; ++k) {
+        if (!outs[k]) continue;
+        e = launch_pack(c->stream, B, c->stage, src[k][0], src[k][1], src[k][2], c->total_ba, c->ba_traj);
+        c->launches++;
+        if (e == cudaSuccess) e = cudaMemcpyAsync(outs[k], c->stage, bytes, cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);  // stage is reused
+    }
+    if (dens && e == cudaSuccess) {
+        e = launch_pack_scalar(c->stream, B, c->stage, B.dens, c->total_ba, c->ba_traj);
+        c->launches++;
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(dens, c->stage, sizeof(double) * c->total_ba, cudaMemcpyDeviceToHost, c->stream);
+    }
+    if (epot && e == cudaSuccess)
+        e = cudaMemcpyAsync(epot, B.epot, sizeof(double) * c->total_beads, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    return e == cudaSuccess ? MDT_OK : cuda_fail(c, e, "mdt_state_download");
+}
+
+int32_t mdt_set_random_arrays(mdt_ctx *c, const double *randy, const double *zeta, const double *andersen_v,
+                              const double *andersen_u) {
+    int rc = check_ready(c, false);
+    if (rc) return rc;
+    const double *src[4] = {randy, zeta, andersen_v, andersen_u};
+    const size_t n[4] = {3 * (size_t)c->total_ba, 3 * (size_t)c->total_ba, 3 * (size_t)c->total_ba,
+                         (size_t)c->total_ba};
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < 4 && e == cudaSuccess; ++k) {
+        if (!src[k]) continue;
+        if (!c->rnd[k]) {
+            c->rnd[k] = dalloc<double>(c, n[k], e);
+            if (!c->rnd[k]) return fail(c, MDT_ERR_NOMEM, "random array allocation failed");
+        }
+        e = cudaMemcpyAsync(c->rnd[k], src[k], sizeof(double) * n[k], cudaMemcpyHostToDevice, c->stream);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    return e == cudaSuccess ? MDT_OK : cuda_fail(c, e, "mdt_set_random_arrays");
+}
+
+static int check_params(mdt_ctx *c, const mdt_prop_params *p) {
+    if (!p) return fail(c, MDT_ERR_ARG, "null mdt_prop_params");
+    if (!(p->step > 0)) return fail(c, MDT_ERR_ARG, "step must be > 0");
+    if (p->rng_mode == 1) {
+        bool need_l = false, need_p = false, need_a = false;
+        for (int t = 0; t < c->ntypes; ++t) {
+            need_l |= c->B.algo[t] == MDT_PROP_LANGEVIN || c->B.algo[t] == MDT_PROP_LANGEVIN_CONST;
+            need_p |= c->B.algo[t] == MDT_PROP_PILE;
+            need_a |= c->B.algo[t] == MDT_PROP_ANDERSEN;
+        }
+        if ((need_l && !c->rnd[0]) || (need_p && !c->rnd[1]) || (need_a && (!c->rnd[2] || !c->rnd[3])))
+            return fail(c, MDT_ERR_STATE, "rng_mode 1 needs mdt_set_random_arrays first");
+    }
+    return MDT_OK;
+}
+
+int32_t mdt_calc_force(mdt_ctx *c, int32_t flag, int32_t precision, const mdt_prop_params *p) {
+    int rc = check_ready(c, true);
+    if (rc) return rc;
+    if (flag != MDT_ENERGY_AND_FORCE && flag != MDT_ENERGY_ONLY) return fail(c, MDT_ERR_ARG, "bad flag");
+    if (precision != MDT_PREC_FP64 && precision != MDT_PREC_FP32) return fail(c, MDT_ERR_ARG, "bad precision");
+    if ((rc = check_params(c, p))) return rc;
+    if ((rc = ensure_scratch(c, precision))) return rc;
+    const PropParams P = to_dev(c, p);
+    cudaError_t e = launch_phase(cfg(c, precision), c->B, c->E, P,
+                                 flag == MDT_ENERGY_ONLY ? kPhaseEnergyOnly : kPhaseForce, precision);
+    c->launches++;
+    return e == cudaSuccess ? MDT_OK : cuda_fail(c, e, "mdt_calc_force");
+}
+
+int32_t mdt_propagate_1(mdt_ctx *c, const mdt_prop_params *p) {
+    int rc = check_ready(c, false);
+    if (rc) return rc;
+    if ((rc = check_params(c, p))) return rc;
+    const PropParams P = to_dev(c, p);
+    cudaError_t e = launch_phase(cfg(c, 0), c->B, c->E, P, kPhaseProp1, 0);
+    c->launches++;
+    return e == cudaSuccess ? MDT_OK : cuda_fail(c, e, "mdt_propagate_1");
+}
+
+int32_t mdt_propagate_2(mdt_ctx *c, const mdt_prop_params *p) {
+    int rc = check_ready(c, false);
+    if (rc) return rc;
+    if ((rc = check_params(c, p))) return rc;
+    const PropParams P = to_dev(c, p);
+    cudaError_t e = launch_phase(cfg(c, 0), c->B, c->E, P, kPhaseProp2, 0);
+    c->launches++;
+    return e == cudaSuccess ? MDT_OK : cuda_fail(c, e, "mdt_propagate_2");
+}
+
+int32_t mdt_md_steps(mdt_ctx *c, int32_t nsteps, int32_t precision, const mdt_prop_params *p) {
+    int rc = check_ready(c, true);
+    if (rc) return rc;
+    if (nsteps < 0) return fail(c, MDT_ERR_ARG, "nsteps < 0");
+    if (precision != MDT_PREC_FP64 && precision != MDT_PREC_FP32) return fail(c, MDT_ERR_ARG, "bad precision");
+    if ((rc = check_params(c, p))) return rc;
+    if (p->rng_mode == 1 && nsteps > 1) return fail(c, MDT_ERR_ARG, "rng_mode 1 supports one step per call");
+    if ((rc = ensure_scratch(c, precision))) return rc;
+    if (nsteps == 0) return MDT_OK;
+    const PropParams P = to_dev(c, p);
+    cudaError_t e = launch_md_steps(cfg(c, precision), c->B, c->E, P, nsteps, precision);
+    c->launches++;
+    return e == cudaSuccess ? MDT_OK : cuda_fail(c, e, "mdt_md_steps");
+}
+
+int32_t mdt_query(mdt_ctx *c, const mdt_prop_params *p, mdt_traj_summary *out) {
+    int rc = check_ready(c, false);
+    if (rc) return rc;
+    if (!out || !p) return fail(c, MDT_ERR_ARG, "mdt_query: null argument");
+    const PropParams P = to_dev(c, p);
+    cudaError_t e = launch_summary(c->stream, c->B, P, c->summary);
+    c->launches++;
+    std::vector<double> s(5 * (size_t)c->T);
+    std::vector<int> st(c->T);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(s.data(), c->summary, sizeof(double) * s.size(), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(st.data(), c->B.status, sizeof(int) * c->T, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "mdt_query");
+    for (int t = 0; t < c->T; ++t) {
+        out[t].status = st[t];
+        out[t].steps_done = (int32_t)s[5 * t + 4];
+        out[t].epot = s[5 * t + 0];
+        out[t].ekin_p = s[5 * t + 1];
+        out[t].ekin_l = s[5 * t + 2];
+        out[t].ebead = s[5 * t + 3];
+    }
+    return MDT_OK;
+}
+
+int32_t mdt_device_state(mdt_ctx *c, void **ptrs, int64_t *nslots) {
+    int rc = check_ready(c, false);
+    if (rc) return rc;
+    if (!ptrs) return fail(c, MDT_ERR_ARG, "null ptrs");
+    Batch &B = c->B;
+    void *p[12] = {B.rx, B.ry, B.rz, B.vx, B.vy, B.vz, B.fx, B.fy, B.fz, B.ax, B.ay, B.az};
+    for (int k = 0; k < 12; ++k) ptrs[k] = p[k];
+    if (nslots) *nslots = c->total_ba;
+    return MDT_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,32 @@
+// mdt_internal.h -- launchers shared between the engine's translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "mdt_common.cuh"
+
+namespace mdt {
+
+struct LaunchCfg {
+    cudaStream_t stream;
+    int grid;
+    const int *order;  // trajectory work order (largest first)
+    int *counter;      // device work-queue counter (reset by the launcher)
+};
+
+cudaError_t launch_phase(const LaunchCfg &c, const Batch &B, const EmtConst &E, const PropParams &P, int phase,
+                         int precision);
+cudaError_t launch_md_steps(const LaunchCfg &c, const Batch &B, const EmtConst &E, const PropParams &P, int nsteps,
+                            int precision);
+cudaError_t launch_unpack(cudaStream_t s, const Batch &B, const double *src, double *x, double *y, double *z,
+                          int64_t total_ba, const int *ba_traj);
+cudaError_t launch_pack(cudaStream_t s, const Batch &B, double *dst, const double *x, const double *y,
+                        const double *z, int64_t total_ba, const int *ba_traj);
+cudaError_t launch_pack_scalar(cudaStream_t s, const Batch &B, double *dst, const double *x, int64_t total_ba,
+                               const int *ba_traj);
+cudaError_t launch_summary(cudaStream_t s, const Batch &B, const PropParams &P, double *out5);
+int max_resident_ctas(int max_atoms, int max_beads, int precision);
+size_t smem_bytes(int max_atoms, int max_beads, size_t rsize);
+
+enum { kPhaseForce = 0, kPhaseProp1 = 1, kPhaseProp2 = 2, kPhaseEnergyOnly = 3 };
+
+}  // namespace mdt

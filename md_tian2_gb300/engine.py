@@ -1,0 +1,184 @@
+"""Host-side mirror of the reference's force/propagation interface for a batch.
+
+The reference drives one ``universe`` through ``calc_force`` (src/force.f90:40),
+``propagate_1``/``propagate_2`` (src/md_algo.f90:37,80) and the step loop of
+src/md_tian2.f90:78-92.  :class:`Engine` drives T universes at once through
+libmdt_gpu.so with the same names, argument meaning and error behaviour: a bad input
+raises (the reference would ``stop``), nothing is silently skipped.
+"""
+from __future__ import annotations
+
+import ctypes as ct
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import constants as C
+from ._lib import EngineError, PropParams, TrajSummary, load
+from .io import EmtParams
+from .universe import Universe
+
+PREC = {"fp64": 0, "fp32": 1}
+
+
+@dataclass
+class SimParams:
+    """The ``simparams`` fields the hot path reads (src/run_config.f90:34-85)."""
+
+    step: float = 0.1
+    Tsurf: float = 300.0
+    Tproj: float = 300.0
+    pile_tau: float = 200.0        # run_config.f90:120
+    andersen_time: float = 30.0    # run_config.f90:119
+    gamma_const: float = 0.001     # 1/fs (1/ps), constant-friction Langevin only
+    pul: float = float("inf")
+    pll: float = float("-inf")
+    seed: int = 12345
+    use_exit: bool = False
+    rng_mode: int = 0
+
+    def c(self) -> PropParams:
+        return PropParams(self.step, self.Tsurf, self.Tproj, self.pile_tau, self.andersen_time, self.gamma_const,
+                          self.pul, self.pll, self.seed & 0xFFFFFFFFFFFFFFFF, int(self.use_exit), int(self.rng_mode))
+
+
+def _p(a, ctype):
+    return a.ctypes.data_as(ct.POINTER(ctype))
+
+
+class Engine:
+    """A batch of trajectories on one GPU."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load()
+        h = ct.c_void_p()
+        rc = self.lib.mdt_create(device, ct.byref(h))
+        if rc != 0:
+            raise EngineError(f"mdt_create failed ({rc}): no usable CUDA device {device}")
+        self.h = h
+        self.T = 0
+        self.universes: list[Universe] = []
+
+    # -- errors ----------------------------------------------------------------
+    def _check(self, rc: int, what: str) -> None:
+        if rc != 0:
+            msg = self.lib.mdt_last_error(self.h)
+            raise EngineError(f"{what} failed ({rc}): {msg.decode() if msg else ''}")
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.mdt_destroy(self.h)
+            self.h = None
+
+    def __del__(self):  # pragma: no cover - interpreter shutdown order varies
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- set-up ----------------------------------------------------------------
+    def read_emt(self, params: EmtParams) -> None:
+        """read_emt (src/pes_emt_mod.f90:49-190) equivalent: install EMT parameters."""
+        arrs = params.arrays()
+        pes = np.ascontiguousarray(params.pes.T, dtype=np.int32)  # column major (ntypes, ntypes)
+        self._check(self.lib.mdt_emt_set_params(self.h, params.ntypes, *[_p(a, ct.c_double) for a in arrs],
+                                                _p(pes, ct.c_int32)), "mdt_emt_set_params")
+        self._keep_params = (arrs, pes)
+
+    def define(self, universes: list[Universe]) -> None:
+        """Lay out T universes (ragged sizes and bead counts) on the device."""
+        if not universes:
+            raise ValueError("empty batch")
+        u0 = universes[0]
+        for u in universes:
+            if u.ntypes != u0.ntypes or list(u.names) != list(u0.names):
+                raise ValueError("all trajectories of a batch share one type table")
+        self.universes = list(universes)
+        self.T = len(universes)
+        natoms = np.array([u.natoms for u in universes], np.int32)
+        nbeads = np.array([u.nbeads for u in universes], np.int32)
+        idx = np.concatenate([np.asarray(u.idx, np.int32) for u in universes])
+        mass = np.concatenate([np.asarray(u.m, np.float64) for u in universes])
+        fixed = np.concatenate([np.asarray(u.is_fixed, np.uint8).reshape(-1) for u in universes])
+        box = np.concatenate([np.asarray(u.simbox, np.float64).T.reshape(-1) for u in universes])  # column major
+        algo = np.ascontiguousarray(u0.algo, np.int32)
+        is_proj = np.ascontiguousarray(u0.is_proj, np.uint8)
+        self._check(self.lib.mdt_batch_define(self.h, self.T, _p(natoms, ct.c_int32), _p(nbeads, ct.c_int32),
+                                              _p(idx, ct.c_int32), _p(mass, ct.c_double), _p(fixed, ct.c_uint8),
+                                              _p(box, ct.c_double), u0.ntypes, _p(algo, ct.c_int32),
+                                              _p(is_proj, ct.c_uint8)), "mdt_batch_define")
+        self.natoms, self.nbeads = natoms, nbeads
+        self.nslots = int(np.sum(natoms.astype(np.int64) * nbeads))
+        self.ba_off = np.concatenate([[0], np.cumsum(natoms.astype(np.int64) * nbeads)])
+        self.bead_off = np.concatenate([[0], np.cumsum(nbeads)])
+
+    def upload(self, r: np.ndarray | None = None, v: np.ndarray | None = None) -> None:
+        """Positions/velocities of all trajectories, Fortran order, concatenated.
+        Defaults to the universes given to :meth:`define`."""
+        if r is None:
+            r = np.concatenate([u.r.reshape(-1) for u in self.universes])
+        if v is None:
+            v = np.concatenate([u.v.reshape(-1) for u in self.universes])
+        r = np.ascontiguousarray(r, np.float64).reshape(-1)
+        v = np.ascontiguousarray(v, np.float64).reshape(-1)
+        if r.size != 3 * self.nslots or v.size != 3 * self.nslots:
+            raise ValueError("state arrays do not match the batch layout")
+        self._check(self.lib.mdt_state_upload(self.h, r.ctypes.data, v.ctypes.data), "mdt_state_upload")
+
+    def upload_ptr(self, r_ptr: int, v_ptr: int) -> None:
+        """Upload from raw host pointers (e.g. pinned buffers)."""
+        self._check(self.lib.mdt_state_upload(self.h, r_ptr, v_ptr), "mdt_state_upload")
+
+    def set_random_arrays(self, randy=None, zeta=None, andersen_v=None, andersen_u=None) -> None:
+        keep = [None if a is None else np.ascontiguousarray(a, np.float64).reshape(-1)
+                for a in (randy, zeta, andersen_v, andersen_u)]
+        ptrs = [None if a is None else a.ctypes.data for a in keep]
+        self._check(self.lib.mdt_set_random_arrays(self.h, *ptrs), "mdt_set_random_arrays")
+
+    # -- hot path ----------------------------------------------------------------
+    def calc_force(self, sp: SimParams, flag: int = C.ENERGY_AND_FORCE, precision: str = "fp64") -> None:
+        p = sp.c()
+        self._check(self.lib.mdt_calc_force(self.h, flag, PREC[precision], ct.byref(p)), "mdt_calc_force")
+
+    def propagate_1(self, sp: SimParams) -> None:
+        p = sp.c()
+        self._check(self.lib.mdt_propagate_1(self.h, ct.byref(p)), "mdt_propagate_1")
+
+    def propagate_2(self, sp: SimParams) -> None:
+        p = sp.c()
+        self._check(self.lib.mdt_propagate_2(self.h, ct.byref(p)), "mdt_propagate_2")
+
+    def md_steps(self, nsteps: int, sp: SimParams, precision: str = "fp64") -> None:
+        p = sp.c()
+        self._check(self.lib.mdt_md_steps(self.h, nsteps, PREC[precision], ct.byref(p)), "mdt_md_steps")
+
+    def synchronize(self) -> None:
+        self._check(self.lib.mdt_synchronize(self.h), "mdt_synchronize")
+
+    # -- results -----------------------------------------------------------------
+    def download(self):
+        """Returns dict of r, v, f, a (3*nslots, Fortran order), epot (total beads), dens."""
+        out = {k: np.empty(3 * self.nslots) for k in ("r", "v", "f", "a")}
+        out["epot"] = np.empty(int(self.bead_off[-1]))
+        out["dens"] = np.empty(self.nslots)
+        self._check(self.lib.mdt_state_download(self.h, *[out[k].ctypes.data for k in
+                                                         ("r", "v", "f", "a", "epot", "dens")]),
+                    "mdt_state_download")
+        return out
+
+    def split(self, flat: np.ndarray, t: int, per: int = 3) -> np.ndarray:
+        """Slice trajectory t out of a flat Fortran-order array -> (N, nb, per)."""
+        a, b = self.ba_off[t], self.ba_off[t + 1]
+        x = flat[per * a: per * b]
+        return x.reshape(self.natoms[t], self.nbeads[t], per) if per > 1 else x.reshape(self.natoms[t], self.nbeads[t])
+
+    def query(self, sp: SimParams) -> np.ndarray:
+        arr = (TrajSummary * self.T)()
+        p = sp.c()
+        self._check(self.lib.mdt_query(self.h, ct.byref(p), arr), "mdt_query")
+        return np.array([(s.status, s.steps_done, s.epot, s.ekin_p, s.ekin_l, s.ebead) for s in arr],
+                        dtype=[("status", "i4"), ("steps_done", "i4"), ("epot", "f8"), ("ekin_p", "f8"),
+                               ("ekin_l", "f8"), ("ebead", "f8")])
+
+    def launch_count(self) -> int:
+        return int(self.lib.mdt_launch_count(self.h))
