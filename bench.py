@@ -1,0 +1,385 @@
+#!/usr/bin/env python
+"""Throughput benchmark of the md_tian2 GB300 engine.
+
+Workload (per GPU): 4096 H/Au(111) trajectories, slabs of 4 layers x {3x3,4x4,5x5,6x6}
+(37-145 atoms) drawn from a seed, Einc ~ U(0.5,5) eV, polar ~ U(0,60), azimuth ~
+U(0,360), Tsurf = 300 K, constant-friction Langevin on Au and velocity Verlet on H,
+dt = 0.1 fs.  One bench step = one MD step (propagate_1 -> calc_force ->
+propagate_2) of every trajectory.  Metric: atom-steps/s = sum over trajectories of
+natoms x completed steps / time.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+N > 1 runs under torchrun as independent replicas (weak scaling): trajectories are
+independent, the path has no exchange step.  ``--impl reference`` times the CPU
+restatement of the reference's Fortran (oracle/, the same loops and dense arrays) on
+the host cores, on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "atom-steps/s, 1 GB300: NN surrogate vs plain FP64 EMT at force RMSE ≤20 meV/Å"
+UNIT = "atom-steps/s"
+
+# Algorithmic FLOP convention for EMT (exp/log = 20 FLOP, sqrt/div = 10 FLOP):
+# same-species pair 110 FLOP + 3 exp + 1 sqrt + 2 div, H-metal pair 150 FLOP + 5 exp +
+# 1 sqrt + 2 div, per-atom epilogue 1 log + 3 exp + 20 FLOP.
+FLOP_SAME_PAIR = 110 + 3 * 20 + 10 + 2 * 10
+FLOP_MIXED_PAIR = 150 + 5 * 20 + 10 + 2 * 10
+FLOP_ATOM = 4 * 20 + 20
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--ntraj", type=int, default=4096)
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+# workload
+# ---------------------------------------------------------------------------
+def workload(ntraj, seed):
+    from md_tian2_gb300 import workloads as W
+    return W.config2(ntraj, seed=seed), W.emt_params()
+
+
+def sim_params():
+    from md_tian2_gb300.engine import SimParams
+    return SimParams(step=0.1, Tsurf=300.0, Tproj=300.0, gamma_const=1e-3, pul=6.05, use_exit=True, seed=2024)
+
+
+def count_pairs(universes, cut):
+    """Same-species and mixed minimum-image pairs within 1.5*rcut, per trajectory."""
+    same = mixed = atoms = 0
+    for u in universes:
+        r = u.r[:, 0, :]
+        ib = np.linalg.inv(u.simbox)
+        d = r[:, None, :] - r[None, :, :]
+        w = d @ ib.T
+        w -= np.round(w)
+        d = w @ u.simbox.T
+        r2 = (d * d).sum(-1)
+        iu = np.triu_indices(len(r), 1)
+        inside = r2[iu] <= cut * cut
+        t = np.asarray(u.idx)
+        mix = t[iu[0]] != t[iu[1]]
+        same += int(np.sum(inside & ~mix)) * u.nbeads
+        mixed += int(np.sum(inside & mix)) * u.nbeads
+        atoms += u.natoms * u.nbeads
+    return same, mixed, atoms
+
+
+def emt_cut(emt):
+    from md_tian2_gb300 import constants as C
+    beta = (16.0 * C.PI / 3.0) ** (1.0 / 3.0) / C.SQRT2
+    s0 = [emt.values["s0"][t] for t in range(emt.ntypes) if emt.pes[t, t] == C.PES_ID_EMT]
+    return 1.5 * max(s0) * beta * C.SQRT3
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.p is not None:
+            time.sleep(0.25)
+            self.p.terminate()
+            try:
+                out, _ = self.p.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.p.kill()
+                out, _ = self.p.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# CPU side: the oracle (restatement of the reference) on host cores
+# ---------------------------------------------------------------------------
+def _cpu_worker(args):
+    ntraj, seed, nsteps, budget = args
+    sys.path.insert(0, str(ROOT))
+    from md_tian2_gb300 import workloads as W
+    from oracle.oracle import OracleUniverse
+    us = W.config2(ntraj, seed=seed)
+    emt = W.emt_params()
+    sp = sim_params()
+    rng = np.random.default_rng(seed)
+    orcs = [OracleUniverse(u, emt) for u in us]
+    for o in orcs:
+        o.calc_force(sp)
+    t0 = time.perf_counter()
+    atom_steps = 0
+    for s in range(nsteps):
+        for o in orcs:
+            randy = rng.normal(size=o.r.shape)
+            o.propagate_1(sp, randy)
+            o.calc_force(sp)
+            o.propagate_2(sp, randy)
+            atom_steps += o.N * o.nb
+        if budget and time.perf_counter() - t0 > budget:
+            break
+    return atom_steps, time.perf_counter() - t0
+
+
+def cpu_baseline(seconds, cores=None):
+    """Oracle on `cores` processes, each advancing its own sample of trajectories."""
+    import multiprocessing as mp
+    from oracle import oracle
+    oracle.build()
+    cores = cores or os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    per = 8
+    with ctx.Pool(cores) as pool:
+        t0 = time.perf_counter()
+        res = pool.map(_cpu_worker, [(per, 1000 + k, 10 ** 6, seconds) for k in range(cores)])
+        wall = time.perf_counter() - t0
+    atom_steps = sum(r[0] for r in res)
+    busy = max(r[1] for r in res)
+    return {"value": atom_steps / busy, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{cores} processes x {per} config-2 trajectories (seeded), FP64 oracle "
+                      f"(C++ restatement of the reference's loops), {busy:.1f} s of stepping each, "
+                      f"{atom_steps} atom-steps; pool wall {wall:.1f} s incl. start-up"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import multiprocessing as mp
+    from oracle import oracle
+    oracle.build()
+    cores = os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    per = 4
+    times, total = [], 0
+    with ctx.Pool(cores) as pool:
+        for s in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            res = pool.map(_cpu_worker, [(per, 5000 + k, 1, 0) for k in range(cores)])
+            dt = time.perf_counter() - t0
+            if s >= args.warmup:
+                times.append(dt)
+                total += sum(r[0] for r in res)
+    el = sum(times)
+    val = total / el
+    line = {"impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "config-2 H/Au(111) EMT trajectories, bounded CPU sample",
+                       "sample_per_step": f"{cores} processes x {per} trajectories, build + 1 MD step each",
+                       "l2": "n/a (CPU)"},
+            "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": "oracle/md_oracle.cpp restatement of the reference (no Fortran compiler "
+                                       "on this box), one MD step of a fresh trajectory sample per step"},
+            "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def run_ours(args):
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(args.cpu_seconds)  # before the first GPU call of this process's pool
+
+    from md_tian2_gb300._lib import load
+    from md_tian2_gb300.engine import Engine
+    lib = load()
+    universes, emt = workload(args.ntraj, seed=7 + rank)
+    sp = sim_params()
+    eng = Engine(local)
+    stream = torch.cuda.current_stream()
+    eng.lib.mdt_set_stream(eng.h, stream.cuda_stream)
+    eng.read_emt(emt)
+    eng.define(universes)
+    eng.upload()
+    eng.calc_force(sp, precision=args.precision)
+    natoms = np.array([u.natoms * u.nbeads for u in universes], np.int64)
+
+    def atom_steps_now():
+        return int(np.sum(natoms * eng.query(sp)["steps_done"]))
+
+    same, mixed, nat = count_pairs(universes, emt_cut(emt))
+    flop_per_step = FLOP_SAME_PAIR * same + FLOP_MIXED_PAIR * mixed + FLOP_ATOM * nat
+
+    for _ in range(args.warmup):
+        eng.md_steps(1, sp, precision=args.precision)
+    torch.cuda.synchronize()
+    s0 = atom_steps_now()
+    launches0 = eng.launch_count()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            eng.md_steps(1, sp, precision=args.precision)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    ms = ev0.elapsed_time(ev1)
+    launches = eng.launch_count() - launches0
+    s1 = atom_steps_now()
+    done = s1 - s0
+
+    # end-to-end through the C ABI with pinned host buffers
+    nslots = eng.nslots
+    h_r = torch.empty(3 * nslots, dtype=torch.float64).pin_memory()
+    h_v = torch.empty(3 * nslots, dtype=torch.float64).pin_memory()
+    h_e = torch.empty(int(eng.bead_off[-1]), dtype=torch.float64).pin_memory()
+    lib.mdt_state_download(eng.h, h_r.data_ptr(), h_v.data_ptr(), None, None, h_e.data_ptr(), None)
+    e2e_steps = max(3, args.steps // 2)
+    for w in range(2):
+        eng.upload_ptr(h_r.data_ptr(), h_v.data_ptr())
+        eng.md_steps(1, sp, precision=args.precision)
+        lib.mdt_state_download(eng.h, h_r.data_ptr(), h_v.data_ptr(), None, None, h_e.data_ptr(), None)
+    torch.cuda.synchronize()
+    e_atoms = 0
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        eng.upload_ptr(h_r.data_ptr(), h_v.data_ptr())
+        eng.md_steps(1, sp, precision=args.precision)
+        rc = lib.mdt_state_download(eng.h, h_r.data_ptr(), h_v.data_ptr(), None, None, h_e.data_ptr(), None)
+        if rc != 0:
+            raise RuntimeError("download failed")
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    # upload resets status, so every trajectory runs every e2e step
+    e_atoms = int(natoms.sum()) * e2e_steps
+    h2d = 2 * 3 * nslots * 8
+    d2h = 2 * 3 * nslots * 8 + 8 * int(eng.bead_off[-1])
+
+    # roofline: FP64 (or FP32) FMA peak measured on this GPU
+    import ctypes as ct
+    peak = ct.c_double()
+    lib.mdt_peak_fma(1 if args.precision == "fp32" else 0, 2000 if args.precision == "fp64" else 20000,
+                     ct.byref(peak))
+    achieved = flop_per_step / (ms / args.steps * 1e-3)
+    traffic = None
+    prof = ROOT / "profiles" / "emt_fused_traffic.json"
+    if prof.exists():
+        try:
+            traffic = json.loads(prof.read_text()).get(args.precision)
+        except Exception:
+            traffic = None
+
+    elapsed = ms * 1e-3
+    if dist:
+        t = torch.tensor([elapsed, float(done), e2e_s, float(e_atoms)], device="cuda")
+        mx = t.clone()
+        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+        sm = t.clone()
+        dist.all_reduce(sm, op=dist.ReduceOp.SUM)
+        elapsed, done_all, e2e_s, e_atoms_all = mx[0].item(), sm[1].item(), mx[2].item(), sm[3].item()
+    else:
+        done_all, e_atoms_all = done, e_atoms
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": done_all / elapsed, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32",
+            "data": "synthetic (seeded H/Au(111) slabs, see workloads.py)",
+            "config": {"workload": f"plain {args.precision.upper()} EMT, {args.ntraj} ragged H/Au(111) trajectories "
+                                   "(37-145 atoms), Verlet H + constant-friction Langevin Au, dt 0.1 fs; "
+                                   "one bench step = one MD step of every trajectory",
+                       "ntraj_per_gpu": args.ntraj, "parallelism": f"replicas x{world}",
+                       "l2": "pair scratch (>0.7 GB) rewritten every step: inputs larger than L2",
+                       "surrogate": "not built yet; value is the plain EMT path"},
+            "clocks": clk.summary(),
+            "e2e": {"value": e_atoms_all / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": int(launches),
+            "roofline": {"bound": "fp64" if args.precision == "fp64" else "fp32",
+                         "achieved": achieved / 1e12, "peak": peak.value / 1e12, "unit": "TFLOP/s",
+                         "frac": achieved / peak.value if peak.value > 0 else None, "traffic": traffic,
+                         "peak_source": "measured FMA microbenchmark (mdt_peak_fma), MEASURED_PEAKS.json has no "
+                                        "FP64/FP32 entry",
+                         "flop_per_step": flop_per_step, "pairs_same": same, "pairs_mixed": mixed},
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    eng.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

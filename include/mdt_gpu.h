@@ -134,6 +134,12 @@ int32_t mdt_query(mdt_ctx *ctx, const mdt_prop_params *p, mdt_traj_summary *out)
    ptrs must hold 12 entries; *nslots receives the number of bead-atom slots. */
 int32_t mdt_device_state(mdt_ctx *ctx, void **ptrs, int64_t *nslots);
 
+/* ---- measurement -------------------------------------------------------------
+ * FMA throughput of the current device (FP64 or FP32 CUDA cores): the roofline
+ * denominator of the EMT kernels, which are arithmetic-bound.  No reference
+ * counterpart (the reference has no GPU code). */
+int32_t mdt_peak_fma(int32_t precision, int32_t iters, double *flops_per_s);
+
 /* ---- work counters ---------------------------------------------------------- */
 /* number of kernel launches this context issued since creation */
 int64_t mdt_launch_count(const mdt_ctx *ctx);

@@ -51,6 +51,7 @@ SIGNATURES = {
     "mdt_query": (ct.c_int32, [ct.c_void_p, ct.POINTER(PropParams), ct.POINTER(TrajSummary)]),
     "mdt_device_state": (ct.c_int32, [ct.c_void_p, ct.POINTER(ct.c_void_p), ct.POINTER(ct.c_int64)]),
     "mdt_launch_count": (ct.c_int64, [ct.c_void_p]),
+    "mdt_peak_fma": (ct.c_int32, [ct.c_int32, ct.c_int32, c_double_p]),
 }
 
 _lib = None

@@ -76,23 +76,22 @@ def test_emt_fp64_hpt_and_beads(built_lib, oracle_lib):
     emt = W.emt_params("H", "Pt")
     sp = SimParams()
     eng = make_engine(us, emt)
-    # energy-only avoids the free ring-polymer step inside calc_force
+    # calc_force performs the free ring-polymer step first for nbeads > 1 (force.f90:54),
+    # also when only energies are requested
     eng.calc_force(sp, flag=C.ENERGY_ONLY)
+    e_only = eng.download()
+    eng.upload()
+    eng.calc_force(sp)
     out = eng.download()
     orcs = oracle_list(us, emt)
-    # oracle energy per bead without the RP step: compute with nbeads=1 copies
-    from md_tian2_gb300.universe import Universe
-    e_ref = []
-    for u in us:
-        for b in range(u.nbeads):
-            ub = Universe(u.r[:, b:b + 1].copy(), u.v[:, b:b + 1].copy(), u.m, u.idx, u.is_fixed[:, b:b + 1].copy(),
-                          u.simbox, u.names, u.is_proj, u.algo)
-            from oracle.oracle import OracleUniverse
-            o = OracleUniverse(ub, emt)
-            o.calc_force(sp)
-            e_ref.append(o.epot[0])
-    assert max_abs(out["epot"], np.array(e_ref)) < EPOT_TOL
-    del orcs
+    for o in orcs:
+        o.calc_force(sp)
+    ref = {k: np.concatenate([getattr(o, k).reshape(-1) for o in orcs]) for k in ("r", "v", "f", "epot")}
+    assert max_abs(e_only["epot"], ref["epot"]) < EPOT_TOL
+    assert max_abs(out["epot"], ref["epot"]) < EPOT_TOL
+    for k in ("r", "v", "f"):
+        assert max_abs(out[k], ref[k]) < FORCE_TOL, k
+    eng.close()
 
 
 def test_emt_single_species_pt(built_lib, oracle_lib):
