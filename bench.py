@@ -237,6 +237,8 @@ def run_reference(args):
 # GPU arm
 # ---------------------------------------------------------------------------
 def run_ours(args):
+    import ctypes as ct
+
     import torch
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -257,8 +259,8 @@ def run_ours(args):
     universes, emt = workload(args.ntraj, seed=7 + rank)
     sp = sim_params()
     eng = Engine(local)
-    stream = torch.cuda.current_stream()
-    eng.lib.mdt_set_stream(eng.h, stream.cuda_stream)
+    stream = torch.cuda.Stream()  # a real stream handle: the library and the events share it
+    eng.lib.mdt_set_stream(eng.h, ct.c_void_p(stream.cuda_stream))
     eng.read_emt(emt)
     eng.define(universes)
     eng.upload()
@@ -321,7 +323,6 @@ def run_ours(args):
     d2h = 2 * 3 * nslots * 8 + 8 * int(eng.bead_off[-1])
 
     # roofline: FP64 (or FP32) FMA peak measured on this GPU
-    import ctypes as ct
     peak = ct.c_double()
     lib.mdt_peak_fma(1 if args.precision == "fp32" else 0, 2000 if args.precision == "fp64" else 20000,
                      ct.byref(peak))

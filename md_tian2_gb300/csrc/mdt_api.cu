@@ -149,7 +149,7 @@ LaunchCfg cfg(mdt_ctx *c, int precision) {
 
 int ensure_scratch(mdt_ctx *c, int precision) {
     const size_t rs = precision == MDT_PREC_FP32 ? 4 : 8;
-    const size_t need = std::max<size_t>(16, 5 * rs * (size_t)c->total_pairs);
+    const size_t need = std::max<size_t>(16, 6 * rs * (size_t)c->total_pairs);
     if (c->B.pair_scratch && c->scratch_prec_bytes >= need) return MDT_OK;
     cudaError_t e;
     void *p = dalloc<unsigned char>(c, need, e);
@@ -559,10 +559,10 @@ int32_t mdt_set_random_arrays(mdt_ctx *c, const double *randy, const double *zet
     return e == cudaSuccess ? MDT_OK : cuda_fail(c, e, "mdt_set_random_arrays");
 }
 
-static int check_params(mdt_ctx *c, const mdt_prop_params *p) {
+static int check_params(mdt_ctx *c, const mdt_prop_params *p, bool draws = true) {
     if (!p) return fail(c, MDT_ERR_ARG, "null mdt_prop_params");
     if (!(p->step > 0)) return fail(c, MDT_ERR_ARG, "step must be > 0");
-    if (p->rng_mode == 1) {
+    if (draws && p->rng_mode == 1) {
         bool need_l = false, need_p = false, need_a = false;
         for (int t = 0; t < c->ntypes; ++t) {
             need_l |= c->B.algo[t] == MDT_PROP_LANGEVIN || c->B.algo[t] == MDT_PROP_LANGEVIN_CONST;
@@ -580,7 +580,7 @@ int32_t mdt_calc_force(mdt_ctx *c, int32_t flag, int32_t precision, const mdt_pr
     if (rc) return rc;
     if (flag != MDT_ENERGY_AND_FORCE && flag != MDT_ENERGY_ONLY) return fail(c, MDT_ERR_ARG, "bad flag");
     if (precision != MDT_PREC_FP64 && precision != MDT_PREC_FP32) return fail(c, MDT_ERR_ARG, "bad precision");
-    if ((rc = check_params(c, p))) return rc;
+    if ((rc = check_params(c, p, false))) return rc;
     if ((rc = ensure_scratch(c, precision))) return rc;
     const PropParams P = to_dev(c, p);
     cudaError_t e = launch_phase(cfg(c, precision), c->B, c->E, P,

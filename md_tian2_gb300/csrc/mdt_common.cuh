@@ -78,7 +78,7 @@ struct Batch {
     int *steps_done;           // per trajectory
     const int *cjk_off;        // per trajectory: offset of its nbeads x nbeads table
     const double *cjk;         // normal-mode tables, column major cjk(j,k)
-    void *pair_scratch;        // per pair slot: dx, dy, dz, Q_ij, Q_ji (FP64 or FP32)
+    void *pair_scratch;        // per pair slot: dx, dy, dz, Q_ij, Q_ji, F_V (FP64 or FP32)
     int max_atoms, max_beads;
     int algo[kMaxTypes];       // propagator per type
     int is_proj[kMaxTypes];
