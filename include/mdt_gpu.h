@@ -33,6 +33,7 @@ extern "C" {
 /* ids shared with the reference, src/constants.f90:64-71,107-115 */
 #define MDT_PES_EMT 2003
 #define MDT_PES_NENE 2008
+#define MDT_PES_SURROGATE 2100 /* ACSF->MLP surrogate of EMT with EMT fallback; no reference id */
 #define MDT_PROP_VERLET 1001
 #define MDT_PROP_LANGEVIN 1003       /* LDFA friction from the EMT density */
 #define MDT_PROP_ANDERSEN 1005
@@ -90,6 +91,63 @@ int32_t mdt_set_stream(mdt_ctx *ctx, void *cuda_stream);
 int32_t mdt_emt_set_params(mdt_ctx *ctx, int32_t ntypes, const double *eta2, const double *n0,
                            const double *e0, const double *lambda, const double *v0, const double *kappa,
                            const double *s0, const int32_t *pes);
+
+/* HDNNP model: what read_nene (src/pes_nene_mod.f90:123-5759) extracts from input.nn,
+   scaling.data and weights.XXX.data.  Arrays per element e (ascending nuclear charge) and
+   symmetry function s (RuNNer's canonical order, RuNNer_src/sortsymfunctions.f90) at
+   [e*maxsf + s]; lengths in bohr, energies in Hartree, as inside RuNNer.  Supported
+   subset: symmetry-function types 2 and 3 with one cutoff radius per element, cutoff
+   types 0-8, activations t g l c s S e p h, at most 4 elements, 64 symmetry functions,
+   4 layers of 64 nodes. */
+typedef struct mdt_nn_model {
+    int32_t nelem;
+    const int32_t *z;          /* nuclear charge per element */
+    int32_t maxsf;
+    const int32_t *nsf;        /* symmetry functions per element */
+    const int32_t *sftype;     /* 2 (radial) or 3 (angular) */
+    const double *eta, *rshift, *lambda, *zeta, *rc;
+    const int32_t *e1, *e2;    /* neighbour nuclear charges */
+    const double *smin, *smax, *savg;  /* scaling.data columns */
+    int32_t scalesym, centersym;
+    double scmin, scmax;
+    int32_t cutoff_type;
+    double cutoff_alpha;
+    int32_t nlayers;           /* hidden + output layers */
+    int32_t maxnodes;
+    const int32_t *nodes;      /* per element nlayers+1 entries, nodes[0] = nsf */
+    const uint8_t *act;        /* per element nlayers*maxnodes activation letters */
+    int32_t maxweights;
+    const double *weights;     /* per element maxweights, calconenn order */
+    int32_t normnodes;
+    int32_t remove_atom_energies;
+    const double *atom_energy; /* Ha per element */
+} mdt_nn_model;
+
+/* Replaces read_nene: install an HDNNP.  z_of_type[ntypes] gives the nuclear charge of
+   each universe type (0: type not handled by the network); max_neighbors bounds the
+   per-atom neighbour list (0 = 192). */
+int32_t mdt_nn_set_model(mdt_ctx *ctx, const mdt_nn_model *model, int32_t ntypes, const int32_t *z_of_type,
+                         int32_t max_neighbors);
+
+/* Select the potential used by mdt_calc_force / mdt_md_steps: MDT_PES_EMT, MDT_PES_NENE
+   or MDT_PES_SURROGATE (network forces; a bead whose symmetry functions leave
+   [min - margin*(max-min), max + margin*(max-min)] is evaluated with FP64 EMT instead). */
+int32_t mdt_set_pes(mdt_ctx *ctx, int32_t pes_kind, double range_margin);
+
+/* per trajectory: number of bead evaluations that fell back to EMT, and 1 if a
+   neighbour list overflowed max_neighbors (either may be NULL) */
+int32_t mdt_nn_stats(mdt_ctx *ctx, int32_t *fallbacks, int32_t *overflow);
+
+/* Raw (unscaled) symmetry functions of every bead-atom, G[slot*maxsf + s] with slots in
+   Fortran (nb, N) order per trajectory; computes energies as a side effect (like
+   RuNNer's mode 1, which derives scaling.data from them). */
+int32_t mdt_nn_descriptors(mdt_ctx *ctx, int32_t precision, double *G);
+
+/* neighbour lists of the last network evaluation, bead 1 of every trajectory:
+   counts[total atoms], words[total atoms * max_neighbors] packed as
+   j | (n1+8)<<16 | (n2+8)<<20 | (n3+8)<<24 (0-based atom j, image n1..n3), in the order
+   of RuNNer_src/neighbor_para_short.f90:117-163 */
+int32_t mdt_nn_neighbors(mdt_ctx *ctx, int32_t *counts, int32_t *words);
 
 /* ---- batch geometry --------------------------------------------------------
  * Replaces the universe constructor new_atoms (src/universe_mod.f90:77-115) for T

@@ -31,6 +31,19 @@ class TrajSummary(ct.Structure):
                 ("ekin_p", ct.c_double), ("ekin_l", ct.c_double), ("ebead", ct.c_double)]
 
 
+class NNModelC(ct.Structure):
+    """mdt_nn_model (include/mdt_gpu.h)."""
+    _fields_ = [("nelem", ct.c_int32), ("z", ct.c_void_p), ("maxsf", ct.c_int32), ("nsf", ct.c_void_p),
+                ("sftype", ct.c_void_p), ("eta", ct.c_void_p), ("rshift", ct.c_void_p), ("lambda_", ct.c_void_p),
+                ("zeta", ct.c_void_p), ("rc", ct.c_void_p), ("e1", ct.c_void_p), ("e2", ct.c_void_p),
+                ("smin", ct.c_void_p), ("smax", ct.c_void_p), ("savg", ct.c_void_p),
+                ("scalesym", ct.c_int32), ("centersym", ct.c_int32), ("scmin", ct.c_double), ("scmax", ct.c_double),
+                ("cutoff_type", ct.c_int32), ("cutoff_alpha", ct.c_double), ("nlayers", ct.c_int32),
+                ("maxnodes", ct.c_int32), ("nodes", ct.c_void_p), ("act", ct.c_void_p), ("maxweights", ct.c_int32),
+                ("weights", ct.c_void_p), ("normnodes", ct.c_int32), ("remove_atom_energies", ct.c_int32),
+                ("atom_energy", ct.c_void_p)]
+
+
 # name -> (restype, argtypes); every symbol declared in include/mdt_gpu.h
 SIGNATURES = {
     "mdt_create": (ct.c_int32, [ct.c_int32, ct.POINTER(ct.c_void_p)]),
@@ -52,6 +65,11 @@ SIGNATURES = {
     "mdt_device_state": (ct.c_int32, [ct.c_void_p, ct.POINTER(ct.c_void_p), ct.POINTER(ct.c_int64)]),
     "mdt_launch_count": (ct.c_int64, [ct.c_void_p]),
     "mdt_peak_fma": (ct.c_int32, [ct.c_int32, ct.c_int32, c_double_p]),
+    "mdt_nn_set_model": (ct.c_int32, [ct.c_void_p, ct.POINTER(NNModelC), ct.c_int32, c_int32_p, ct.c_int32]),
+    "mdt_set_pes": (ct.c_int32, [ct.c_void_p, ct.c_int32, ct.c_double]),
+    "mdt_nn_stats": (ct.c_int32, [ct.c_void_p, ct.c_void_p, ct.c_void_p]),
+    "mdt_nn_neighbors": (ct.c_int32, [ct.c_void_p, ct.c_void_p, ct.c_void_p]),
+    "mdt_nn_descriptors": (ct.c_int32, [ct.c_void_p, ct.c_int32, ct.c_void_p]),
 }
 
 _lib = None

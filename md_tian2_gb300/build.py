@@ -29,7 +29,7 @@ def nvcc() -> str:
 
 
 def _compile(src: Path, obj: Path, extra: list[str]) -> None:
-    cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
+    cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off", "--expt-relaxed-constexpr",
            "-I", str(CSRC), "-I", str(PKG.parent / "include"), "-c", str(src), "-o", str(obj), *extra]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

@@ -46,6 +46,16 @@ struct mdt_ctx {
     double *rnd[4] = {nullptr, nullptr, nullptr, nullptr};
     double *summary = nullptr;
     size_t scratch_prec_bytes = 0;
+
+    // HDNNP / surrogate
+    bool have_nn = false;
+    NNDev M{};
+    int ngeta_max = 0;
+    std::vector<void *> nnbufs;  // model arrays (live across batches)
+    int pes_kind = MDT_PES_EMT;
+    double margin = 0.1;
+    NNScratch X{};
+    int nn_maxnb_alloc = 0;
 };
 
 namespace {
@@ -69,6 +79,8 @@ template <typename T> T *dalloc(mdt_ctx *c, size_t n, cudaError_t &e) {
 }
 
 void free_batch(mdt_ctx *c) {
+    c->X = NNScratch{};
+    c->nn_maxnb_alloc = 0;
     for (auto &b : c->bufs) cudaFree(b.p);
     c->bufs.clear();
     c->have_batch = false;
@@ -159,6 +171,79 @@ int ensure_scratch(mdt_ctx *c, int precision) {
     return MDT_OK;
 }
 
+
+// image counts of neighbor_para_short.f90:59-108 for one cell (columns in A)
+void image_counts(const double *box, double cutoff_bohr, int *out) {
+    const double a2b = 1.0 / kBohr2Ang;
+    auto L = [&](int i, int k) { return box[3 * (i - 1) + (k - 1)] * a2b; };
+    double axb[3] = {L(1, 2) * L(2, 3) - L(1, 3) * L(2, 2), L(1, 3) * L(2, 1) - L(1, 1) * L(2, 3),
+                     L(1, 1) * L(2, 2) - L(1, 2) * L(2, 1)};
+    double axc[3] = {L(1, 2) * L(3, 3) - L(1, 3) * L(3, 2), L(1, 3) * L(3, 1) - L(1, 1) * L(3, 3),
+                     L(1, 1) * L(3, 2) - L(1, 2) * L(3, 1)};
+    double bxc[3] = {L(2, 2) * L(3, 3) - L(2, 3) * L(3, 2), L(2, 3) * L(3, 1) - L(2, 1) * L(3, 3),
+                     L(2, 1) * L(3, 2) - L(2, 2) * L(3, 1)};
+    auto nrm = [](double *v) {
+        const double a = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+        v[0] /= a; v[1] /= a; v[2] /= a;
+    };
+    nrm(axb); nrm(axc); nrm(bxc);
+    const double pa = std::fabs(L(1, 1) * bxc[0] + L(1, 2) * bxc[1] + L(1, 3) * bxc[2]);
+    const double pb = std::fabs(L(2, 1) * axc[0] + L(2, 2) * axc[1] + L(2, 3) * axc[2]);
+    const double pc = std::fabs(L(3, 1) * axb[0] + L(3, 2) * axb[1] + L(3, 3) * axb[2]);
+    int na = 0, nb = 0, nc = 0;
+    while ((double)na * pa <= cutoff_bohr) ++na;
+    while ((double)nb * pb <= cutoff_bohr) ++nb;
+    while ((double)nc * pc <= cutoff_bohr) ++nc;
+    out[0] = na; out[1] = nb; out[2] = nc;
+}
+
+int ensure_nn_scratch(mdt_ctx *c) {
+    if (c->X.nbw && c->nn_maxnb_alloc == c->M.maxnb) return MDT_OK;
+    cudaError_t e = cudaSuccess;
+    int *nbw = dalloc<int>(c, (size_t)c->total_ba * c->M.maxnb, e);
+    int *nbcnt = dalloc<int>(c, (size_t)c->total_ba, e);
+    int *img = dalloc<int>(c, 3 * (size_t)c->T, e);
+    int *fb = dalloc<int>(c, (size_t)c->T, e);
+    int *st = dalloc<int>(c, (size_t)c->T, e);
+    if (!nbw || !nbcnt || !img || !fb || !st) return fail(c, MDT_ERR_NOMEM, "neighbour-list scratch allocation failed");
+    std::vector<int> h(3 * (size_t)c->T);
+    std::vector<double> box(9 * (size_t)c->T);
+    e = cudaMemcpy(box.data(), c->B.box, sizeof(double) * box.size(), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(c, e, "cell download");
+    for (int t = 0; t < c->T; ++t) {
+        image_counts(box.data() + 9 * t, c->M.maxcut, h.data() + 3 * t);
+        for (int k = 0; k < 3; ++k)
+            if (h[3 * t + k] > 7) return fail(c, MDT_ERR_UNSUPPORTED, "cell too small for the cutoff (more than 7 images)");
+    }
+    if (c->max_atoms > 65535) return fail(c, MDT_ERR_UNSUPPORTED, "more than 65535 atoms");
+    e = cudaMemcpyAsync(img, h.data(), sizeof(int) * h.size(), cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(fb, 0, sizeof(int) * c->T, c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(st, 0, sizeof(int) * c->T, c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(nbcnt, 0, sizeof(int) * c->total_ba, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "neighbour-list scratch set-up");
+    c->X = NNScratch{nbw, nbcnt, img, fb, st};
+    c->nn_maxnb_alloc = c->M.maxnb;
+    return MDT_OK;
+}
+
+LaunchCfg nn_cfg(mdt_ctx *c, int precision) {
+    const int per_sm = nn_resident_ctas(c->M, c->max_atoms, c->max_beads, c->ngeta_max, precision,
+                                        c->pes_kind == MDT_PES_SURROGATE);
+    const int grid = std::max(1, std::min(c->T, c->num_sms * per_sm));
+    return LaunchCfg{c->stream, grid, c->order, c->counter};
+}
+
+int check_nn_ready(mdt_ctx *c) {
+    if (!c->have_nn) return fail(c, MDT_ERR_STATE, "no network installed (call mdt_nn_set_model)");
+    if (c->pes_kind == MDT_PES_SURROGATE && !c->have_emt)
+        return fail(c, MDT_ERR_STATE, "the surrogate needs EMT parameters for its fallback");
+    for (int t = 0; t < c->ntypes; ++t)
+        if (c->B.algo[t] == MDT_PROP_LANGEVIN)
+            return fail(c, MDT_ERR_UNSUPPORTED,
+                        "ldfa friction needs the EMT density (md_algo.f90:533-536); use MDT_PES_EMT");
+    return ensure_nn_scratch(c);
+}
 }  // namespace
 
 extern "C" {
@@ -187,6 +272,7 @@ int32_t mdt_destroy(mdt_ctx *c) {
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     free_batch(c);
+    for (void *p : c->nnbufs) cudaFree(p);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return MDT_OK;
@@ -576,11 +662,20 @@ static int check_params(mdt_ctx *c, const mdt_prop_params *p, bool draws = true)
 }
 
 int32_t mdt_calc_force(mdt_ctx *c, int32_t flag, int32_t precision, const mdt_prop_params *p) {
-    int rc = check_ready(c, true);
+    int rc = check_ready(c, c && c->pes_kind == MDT_PES_EMT);
     if (rc) return rc;
     if (flag != MDT_ENERGY_AND_FORCE && flag != MDT_ENERGY_ONLY) return fail(c, MDT_ERR_ARG, "bad flag");
     if (precision != MDT_PREC_FP64 && precision != MDT_PREC_FP32) return fail(c, MDT_ERR_ARG, "bad precision");
     if ((rc = check_params(c, p, false))) return rc;
+    if (c->pes_kind != MDT_PES_EMT) {
+        if ((rc = check_nn_ready(c))) return rc;
+        if (c->pes_kind == MDT_PES_SURROGATE && (rc = ensure_scratch(c, MDT_PREC_FP64))) return rc;
+        const PropParams P = to_dev(c, p);
+        cudaError_t e = launch_nn(nn_cfg(c, precision), c->B, c->M, c->E, c->X, P, c->ngeta_max, 0,
+                                  flag == MDT_ENERGY_ONLY ? 1 : 0, precision, c->pes_kind == MDT_PES_SURROGATE);
+        c->launches++;
+        return e == cudaSuccess ? MDT_OK : cuda_fail(c, e, "mdt_calc_force (network)");
+    }
     if ((rc = ensure_scratch(c, precision))) return rc;
     const PropParams P = to_dev(c, p);
     cudaError_t e = launch_phase(cfg(c, precision), c->B, c->E, P,
@@ -610,12 +705,22 @@ int32_t mdt_propagate_2(mdt_ctx *c, const mdt_prop_params *p) {
 }
 
 int32_t mdt_md_steps(mdt_ctx *c, int32_t nsteps, int32_t precision, const mdt_prop_params *p) {
-    int rc = check_ready(c, true);
+    int rc = check_ready(c, c && c->pes_kind == MDT_PES_EMT);
     if (rc) return rc;
     if (nsteps < 0) return fail(c, MDT_ERR_ARG, "nsteps < 0");
     if (precision != MDT_PREC_FP64 && precision != MDT_PREC_FP32) return fail(c, MDT_ERR_ARG, "bad precision");
     if ((rc = check_params(c, p))) return rc;
     if (p->rng_mode == 1 && nsteps > 1) return fail(c, MDT_ERR_ARG, "rng_mode 1 supports one step per call");
+    if (c->pes_kind != MDT_PES_EMT) {
+        if ((rc = check_nn_ready(c))) return rc;
+        if (c->pes_kind == MDT_PES_SURROGATE && (rc = ensure_scratch(c, MDT_PREC_FP64))) return rc;
+        if (nsteps == 0) return MDT_OK;
+        const PropParams P = to_dev(c, p);
+        cudaError_t e = launch_nn(nn_cfg(c, precision), c->B, c->M, c->E, c->X, P, c->ngeta_max, nsteps, 2,
+                                  precision, c->pes_kind == MDT_PES_SURROGATE);
+        c->launches++;
+        return e == cudaSuccess ? MDT_OK : cuda_fail(c, e, "mdt_md_steps (network)");
+    }
     if ((rc = ensure_scratch(c, precision))) return rc;
     if (nsteps == 0) return MDT_OK;
     const PropParams P = to_dev(c, p);
@@ -658,6 +763,216 @@ int32_t mdt_device_state(mdt_ctx *c, void **ptrs, int64_t *nslots) {
     void *p[12] = {B.rx, B.ry, B.rz, B.vx, B.vy, B.vz, B.fx, B.fy, B.fz, B.ax, B.ay, B.az};
     for (int k = 0; k < 12; ++k) ptrs[k] = p[k];
     if (nslots) *nslots = c->total_ba;
+    return MDT_OK;
+}
+
+
+int32_t mdt_nn_set_model(mdt_ctx *c, const mdt_nn_model *m, int32_t ntypes, const int32_t *z_of_type,
+                         int32_t max_neighbors) {
+    if (!c) return MDT_ERR_ARG;
+    if (!m || !z_of_type || ntypes < 1 || ntypes > kMaxTypes) return fail(c, MDT_ERR_ARG, "mdt_nn_set_model: bad arguments");
+    if (m->nelem < 1 || m->nelem > kMaxElem || m->maxsf < 1 || m->maxsf > kMaxSF || m->nlayers < 1 ||
+        m->nlayers > kMaxLayers || m->maxnodes < 1 || m->maxnodes > kMaxNodes)
+        return fail(c, MDT_ERR_UNSUPPORTED, "network larger than 4 elements / 64 functions / 4 layers of 64 nodes");
+    NNDev M{};
+    M.nelem = m->nelem;
+    M.maxsf = m->maxsf;
+    M.nlayers = m->nlayers;
+    M.maxnodes = kMaxNodes;
+    M.maxweights = m->maxweights;
+    M.maxnb = max_neighbors > 0 ? max_neighbors : 192;
+    M.cutoff_type = m->cutoff_type;
+    M.cutoff_alpha = m->cutoff_alpha;
+    M.scalesym = m->scalesym;
+    M.centersym = m->centersym;
+    M.normnodes = m->normnodes;
+    M.remove_atom_energies = m->remove_atom_energies;
+    M.scmin = m->scmin;
+    M.scmax = m->scmax;
+    M.margin = (float)c->margin;
+    if (M.cutoff_type < 0 || M.cutoff_type > 8) return fail(c, MDT_ERR_ARG, "cutoff_type must be 0..8");
+    for (int t = 0; t < kMaxTypes; ++t) M.elem_of_type[t] = -1;
+    for (int t = 0; t < ntypes; ++t)
+        for (int e = 0; e < m->nelem; ++e)
+            if (z_of_type[t] != 0 && m->z[e] == z_of_type[t]) M.elem_of_type[t] = e;
+    const int ne = m->nelem, ms = m->maxsf;
+    std::vector<int> e1(ne * ms, -1), e2(ne * ms, -1), izeta(ne * ms, -1), etaslot(ne * ms, 0);
+    std::vector<double> pnorm(ne * ms, 1.0);
+    auto elem_of_z = [&](int z) {
+        for (int e = 0; e < ne; ++e)
+            if (m->z[e] == z) return e;
+        return -1;
+    };
+    int ngmax = 0;
+    M.maxcut = 0.0;
+    for (int e = 0; e < ne; ++e) {
+        const int nsf = m->nsf[e];
+        if (nsf < 1 || nsf > ms) return fail(c, MDT_ERR_ARG, "bad symmetry-function count");
+        M.nsf[e] = nsf;
+        M.rc[e] = m->rc[e * ms];
+        int ng = 0, ng3 = 0;
+        for (int s = 0; s < nsf; ++s) {
+            const int k = e * ms + s;
+            if (m->sftype[k] != 2 && m->sftype[k] != 3)
+                return fail(c, MDT_ERR_UNSUPPORTED, "only symmetry-function types 2 and 3 are supported");
+            if (m->rc[k] != M.rc[e])
+                return fail(c, MDT_ERR_UNSUPPORTED, "all symmetry functions of an element must share one cutoff");
+            e1[k] = elem_of_z(m->e1[k]);
+            if (m->sftype[k] == 3) {
+                ++ng3;
+                e2[k] = elem_of_z(m->e2[k]);
+                const double zm1 = m->zeta[k] - 1.0;
+                if (zm1 >= 0.0 && zm1 <= 64.0 && zm1 == std::floor(zm1)) izeta[k] = (int)zm1;
+                pnorm[k] = std::pow(2.0, 1.0 - m->zeta[k]);
+                int slot = -1;
+                for (int q = 0; q < ng; ++q)
+                    if (M.g3eta[e][q] == m->eta[k]) slot = q;
+                if (slot < 0) {
+                    if (ng >= kMaxEta) return fail(c, MDT_ERR_UNSUPPORTED, "more than 6 distinct G3 eta values");
+                    M.g3eta[e][ng] = m->eta[k];
+                    slot = ng++;
+                }
+                etaslot[k] = slot;
+            }
+        }
+        if (ng3 > 24) return fail(c, MDT_ERR_UNSUPPORTED, "more than 24 G3 functions per element");
+        M.ng3eta[e] = ng;
+        ngmax = std::max(ngmax, ng);
+        M.maxcut = std::max(M.maxcut, M.rc[e]);
+        int off = 0;
+        for (int l = 0; l <= m->nlayers; ++l) {
+            M.nodes[e][l] = m->nodes[e * (m->nlayers + 1) + l];
+            if (M.nodes[e][l] < 1 || M.nodes[e][l] > kMaxNodes) return fail(c, MDT_ERR_ARG, "bad node count");
+        }
+        if (M.nodes[e][0] != nsf || M.nodes[e][m->nlayers] != 1) return fail(c, MDT_ERR_ARG, "bad layer sizes");
+        for (int l = 1; l <= m->nlayers; ++l) {
+            M.woff[e][l] = off;
+            off += M.nodes[e][l - 1] * M.nodes[e][l] + M.nodes[e][l];
+        }
+        if (off > m->maxweights) return fail(c, MDT_ERR_ARG, "maxweights smaller than the network");
+        M.atom_energy[e] = (m->remove_atom_energies && m->atom_energy) ? m->atom_energy[e] : 0.0;
+    }
+    std::vector<uint8_t> act((size_t)ne * kMaxLayers * kMaxNodes, 'l');
+    for (int e = 0; e < ne; ++e)
+        for (int l = 0; l < m->nlayers; ++l)
+            for (int n = 0; n < M.nodes[e][l + 1]; ++n) {
+                const uint8_t a = m->act[((size_t)e * m->nlayers + l) * m->maxnodes + n];
+                if (!std::strchr("tglcsSeph", (int)a) || a == 0) return fail(c, MDT_ERR_ARG, "unknown activation");
+                act[((size_t)e * kMaxLayers + l) * kMaxNodes + n] = a;
+            }
+    std::vector<float> wf((size_t)ne * m->maxweights);
+    for (size_t k = 0; k < wf.size(); ++k) wf[k] = (float)m->weights[k];
+    // device copies
+    for (void *p : c->nnbufs) cudaFree(p);
+    c->nnbufs.clear();
+    cudaError_t e = cudaSuccess;
+    auto up = [&](const void *src, size_t bytes) -> void * {
+        void *d = nullptr;
+        if (e != cudaSuccess) return nullptr;
+        e = cudaMalloc(&d, std::max<size_t>(bytes, 16));
+        if (e != cudaSuccess) return nullptr;
+        c->nnbufs.push_back(d);
+        e = cudaMemcpy(d, src, bytes, cudaMemcpyHostToDevice);
+        return d;
+    };
+    const size_t nk = (size_t)ne * ms;
+    M.sftype = (const int *)up(m->sftype, 4 * nk);
+    M.e1 = (const int *)up(e1.data(), 4 * nk);
+    M.e2 = (const int *)up(e2.data(), 4 * nk);
+    M.izeta = (const int *)up(izeta.data(), 4 * nk);
+    M.etaslot = (const int *)up(etaslot.data(), 4 * nk);
+    M.eta = (const double *)up(m->eta, 8 * nk);
+    M.rs = (const double *)up(m->rshift, 8 * nk);
+    M.lam = (const double *)up(m->lambda, 8 * nk);
+    M.zeta = (const double *)up(m->zeta, 8 * nk);
+    M.pnorm = (const double *)up(pnorm.data(), 8 * nk);
+    M.smin = (const double *)up(m->smin, 8 * nk);
+    M.smax = (const double *)up(m->smax, 8 * nk);
+    M.savg = (const double *)up(m->savg, 8 * nk);
+    M.act = (const uint8_t *)up(act.data(), act.size());
+    M.wd = (const double *)up(m->weights, 8 * (size_t)ne * m->maxweights);
+    M.wf = (const float *)up(wf.data(), 4 * wf.size());
+    if (e != cudaSuccess) return cuda_fail(c, e, "mdt_nn_set_model upload");
+    c->M = M;
+    c->ngeta_max = ngmax;
+    c->have_nn = true;
+    c->X = NNScratch{};  // re-allocated for the new neighbour bound on next use
+    c->nn_maxnb_alloc = 0;
+    return MDT_OK;
+}
+
+int32_t mdt_set_pes(mdt_ctx *c, int32_t pes_kind, double range_margin) {
+    if (!c) return MDT_ERR_ARG;
+    if (pes_kind != MDT_PES_EMT && pes_kind != MDT_PES_NENE && pes_kind != MDT_PES_SURROGATE)
+        return fail(c, MDT_ERR_ARG, "unknown PES kind");
+    if (!(range_margin >= 0.0)) return fail(c, MDT_ERR_ARG, "range margin must be >= 0");
+    c->pes_kind = pes_kind;
+    c->margin = range_margin;
+    c->M.margin = (float)range_margin;
+    return MDT_OK;
+}
+
+int32_t mdt_nn_stats(mdt_ctx *c, int32_t *fallbacks, int32_t *overflow) {
+    int rc = check_ready(c, false);
+    if (rc) return rc;
+    if (!c->X.nbw) return fail(c, MDT_ERR_STATE, "no network evaluation yet");
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (fallbacks && e == cudaSuccess)
+        e = cudaMemcpy(fallbacks, c->X.fallback, sizeof(int) * c->T, cudaMemcpyDeviceToHost);
+    if (overflow && e == cudaSuccess) e = cudaMemcpy(overflow, c->X.nnstatus, sizeof(int) * c->T, cudaMemcpyDeviceToHost);
+    return e == cudaSuccess ? MDT_OK : cuda_fail(c, e, "mdt_nn_stats");
+}
+
+int32_t mdt_nn_neighbors(mdt_ctx *c, int32_t *counts, int32_t *words) {
+    int rc = check_ready(c, false);
+    if (rc) return rc;
+    if (!c->X.nbw) return fail(c, MDT_ERR_STATE, "no network evaluation yet");
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    int a = 0;
+    for (int t = 0; t < c->T && e == cudaSuccess; ++t) {
+        const int N = c->natoms[t];
+        const int64_t base = c->ba_off[t];  // bead 0
+        if (counts) e = cudaMemcpy(counts + a, c->X.nbcnt + base, sizeof(int) * N, cudaMemcpyDeviceToHost);
+        if (words && e == cudaSuccess)
+            e = cudaMemcpy(words + (size_t)a * c->M.maxnb, c->X.nbw + base * c->M.maxnb,
+                           sizeof(int) * (size_t)N * c->M.maxnb, cudaMemcpyDeviceToHost);
+        a += N;
+    }
+    return e == cudaSuccess ? MDT_OK : cuda_fail(c, e, "mdt_nn_neighbors");
+}
+
+
+int32_t mdt_nn_descriptors(mdt_ctx *c, int32_t precision, double *G) {
+    int rc = check_ready(c, false);
+    if (rc) return rc;
+    if (!G) return fail(c, MDT_ERR_ARG, "null output");
+    if ((rc = check_nn_ready(c))) return rc;
+    cudaError_t e = cudaSuccess;
+    double *d = dalloc<double>(c, (size_t)c->total_ba * c->M.maxsf, e);
+    if (!d) return fail(c, MDT_ERR_NOMEM, "descriptor buffer");
+    e = cudaMemsetAsync(d, 0, sizeof(double) * c->total_ba * c->M.maxsf, c->stream);
+    NNScratch X = c->X;
+    X.gout = d;
+    mdt_prop_params p{};
+    p.step = 1.0;
+    const PropParams P = to_dev(c, &p);
+    if (e == cudaSuccess)
+        e = launch_nn(nn_cfg(c, precision), c->B, c->M, c->E, X, P, c->ngeta_max, 0, 1, precision, false);
+    c->launches++;
+    std::vector<double> h((size_t)c->total_ba * c->M.maxsf);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h.data(), d, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "mdt_nn_descriptors");
+    // device slot order (bead-major) -> Fortran (nb, N) order per trajectory
+    const int ms = c->M.maxsf;
+    for (int t = 0; t < c->T; ++t) {
+        const int N = c->natoms[t], nb = c->nbeads[t];
+        for (int b = 0; b < nb; ++b)
+            for (int i = 0; i < N; ++i) {
+                const int64_t src = c->ba_off[t] + (int64_t)b * N + i, dst = c->ba_off[t] + (int64_t)i * nb + b;
+                std::memcpy(G + dst * ms, h.data() + src * ms, sizeof(double) * ms);
+            }
+    }
     return MDT_OK;
 }
 

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include "mdt_common.cuh"
+#include "mdt_nn.cuh"
 
 namespace mdt {
 
@@ -25,7 +26,10 @@ cudaError_t launch_pack_scalar(cudaStream_t s, const Batch &B, double *dst, cons
                                const int *ba_traj);
 cudaError_t launch_summary(cudaStream_t s, const Batch &B, const PropParams &P, double *out5);
 int max_resident_ctas(int max_atoms, int max_beads, int precision);
-size_t smem_bytes(int max_atoms, int max_beads, size_t rsize);
+
+cudaError_t launch_nn(const LaunchCfg &c, const Batch &B, const NNDev &M, const EmtConst &E, const NNScratch &X,
+                      const PropParams &P, int ngeta, int nsteps, int mode, int precision, bool surrogate);
+int nn_resident_ctas(const NNDev &M, int max_atoms, int max_beads, int ngeta, int precision, bool surrogate);
 
 enum { kPhaseForce = 0, kPhaseProp1 = 1, kPhaseProp2 = 2, kPhaseEnergyOnly = 3 };
 

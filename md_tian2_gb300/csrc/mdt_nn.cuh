@@ -1,0 +1,193 @@
+// mdt_nn.cuh -- atom-centred symmetry functions (G2/G3), per-element MLP and analytic
+// forces for one bead inside a CTA: the RuNNer short-range prediction of md_tian2's
+// compute_nene (src/pes_nene_mod.f90:7145-7368), restated for the GPU.
+//
+//   neighbour list  thread per atom, in RuNNer's order i -> j -> n1 -> n2 -> n3
+//                   (RuNNer_src/neighbor_para_short.f90:117-163), packed (j, image)
+//                   words in a global scratch slot per bead-atom;
+//   descriptors     warp per central atom: the neighbour cache (relative vector,
+//                   distance, cutoff value/derivative, exp(-eta r^2) per distinct G3 eta)
+//                   sits in the warp's shared memory, lanes stride over the first
+//                   neighbour j of a triplet and loop over k > j, so the triplet term
+//                   needs no transcendental beyond exp(-eta r_jk^2) and the r_jk cutoff;
+//   network         lanes are the nodes of a layer (weights in shared memory);
+//   forces          reverse mode: dE/dG from the network, then a second walk over the
+//                   same pairs/triplets scatters dE/dG . dG/dx into per-slot force
+//                   accumulators (RuNNer builds dG/dx explicitly and contracts it
+//                   forward-mode, RuNNer_src/getshortatomic.f90:263-322; both give the
+//                   same forces).
+#pragma once
+#include "mdt_common.cuh"
+
+namespace mdt {
+
+constexpr int kMaxElem = 4;
+constexpr int kMaxSF = 64;
+constexpr int kMaxNodes = 64;
+constexpr int kMaxLayers = 4;
+constexpr int kMaxEta = 6;
+constexpr int kNNWarps = 4;  // warps (central atoms in flight) per CTA
+
+struct NNDev {
+    int nelem, maxsf, nlayers, maxnodes, maxweights, maxnb;
+    int elem_of_type[kMaxTypes];  // universe type -> element index (-1: not NN)
+    int cutoff_type;
+    double cutoff_alpha;
+    int scalesym, centersym, normnodes, remove_atom_energies;
+    double scmin, scmax;
+    double rc[kMaxElem];          // cutoff shared by all symmetry functions of an element (bohr)
+    double maxcut;                // neighbour-list cutoff (bohr)
+    int ng3eta[kMaxElem];
+    double g3eta[kMaxElem][kMaxEta];
+    int nsf[kMaxElem];
+    int nodes[kMaxElem][kMaxLayers + 1];
+    int woff[kMaxElem][kMaxLayers + 1];  // offset of each layer's weights
+    // per element e and symmetry function s at [e*maxsf + s]
+    const int *sftype, *e1, *e2, *izeta, *etaslot;
+    const double *eta, *rs, *lam, *zeta, *pnorm, *smin, *smax, *savg;
+    const uint8_t *act;           // [e][layer][node]
+    const double *wd;             // weights, FP64
+    const float *wf;              // weights, FP32 copy
+    double atom_energy[kMaxElem]; // Ha
+    float margin;                 // descriptor range margin (fraction of max-min) for the fallback
+};
+
+// ---------------------------------------------------------------------------
+// Host-visible launch parameters of the NN kernels
+// ---------------------------------------------------------------------------
+struct NNScratch {
+    int *nbw;          // packed neighbour words, [ba][maxnb]
+    int *nbcnt;        // neighbour count per bead-atom
+    const int *img;    // per trajectory 3 image counts (na, nb, nc)
+    int *fallback;     // per trajectory: beads that fell back to EMT (surrogate)
+    int *nnstatus;     // per trajectory: 1 = neighbour list overflow
+    double *gout;      // optional: raw symmetry functions [ba][maxsf] (descriptor export)
+};
+
+// ---------------------------------------------------------------------------
+template <typename R> struct NM;
+template <> struct NM<double> {
+    static __device__ __forceinline__ double ex(double x) { return exp(x); }
+    static __device__ __forceinline__ double sq(double x) { return sqrt(x); }
+    static __device__ __forceinline__ void sc(double x, double *s, double *c) { sincospi(x, s, c); }
+    static __device__ __forceinline__ double th(double x) { return tanh(x); }
+    static __device__ __forceinline__ double lg(double x) { return log(x); }
+    static __device__ __forceinline__ double pw(double a, double b) { return pow(a, b); }
+    static __device__ __forceinline__ const double *w(const NNDev &M) { return M.wd; }
+};
+template <> struct NM<float> {
+    static __device__ __forceinline__ float ex(float x) { return __expf(x); }
+    static __device__ __forceinline__ float sq(float x) { return sqrtf(x); }
+    static __device__ __forceinline__ void sc(float x, float *s, float *c) { sincospif(x, s, c); }
+    static __device__ __forceinline__ float th(float x) { return tanhf(x); }
+    static __device__ __forceinline__ float lg(float x) { return __logf(x); }
+    static __device__ __forceinline__ float pw(float a, float b) { return powf(a, b); }
+    static __device__ __forceinline__ const float *w(const NNDev &M) { return M.wf; }
+};
+
+// cutoff function and derivative, RuNNer_src/getcutoff.f90:51-162
+template <typename R>
+__device__ __forceinline__ void cutoff_fn(const NNDev &M, R rc, R r, R &fc, R &dfc) {
+    const R rci = (R)M.cutoff_alpha * rc, iw = R(1) / (rc - rci);
+    const int type = M.cutoff_type;
+    if (type == 0) { fc = R(1); dfc = R(0); return; }
+    if (type == 1) {
+        if (r <= rci) { fc = R(1); dfc = R(0); return; }
+        const R x = (r - rci) * iw;
+        R s, c;
+        NM<R>::sc(x, &s, &c);
+        fc = R(0.5) * (c + R(1));
+        dfc = -s * (R(kPi) / R(2)) * iw;
+        return;
+    }
+    if (type == 2 || type == 3) {
+        const R pref = type == 3 ? (R)(((2.718281828459045 + 1.0) / (2.718281828459045 - 1.0)) *
+                                       ((2.718281828459045 + 1.0) / (2.718281828459045 - 1.0)) *
+                                       ((2.718281828459045 + 1.0) / (2.718281828459045 - 1.0)))
+                                 : R(1);
+        if (r <= rci) {
+            const R t = NM<R>::th(R(1));
+            fc = pref * t * t * t;
+            dfc = R(0);
+            return;
+        }
+        const R t = NM<R>::th(R(1) - r / rc);
+        fc = pref * t * t * t;
+        dfc = pref * (R(-3) / rc) * (t * t - t * t * t * t);
+        return;
+    }
+    if (r <= rci) { fc = R(1); dfc = R(0); return; }
+    const R x = (r - rci) * iw;
+    if (type == 4) {
+        const R q = R(1) - x * x;
+        fc = NM<R>::ex(R(1) - R(1) / q);
+        dfc = (R(-2) * iw * x / (q * q)) * fc;
+    } else if (type == 5) {
+        fc = (R(2) * x - R(3)) * x * x + R(1);
+        dfc = iw * x * (R(6) * x - R(6));
+    } else if (type == 6) {
+        fc = ((R(15) - R(6) * x) * x - R(10)) * x * x * x + R(1);
+        dfc = iw * x * x * ((R(60) - R(30) * x) * x - R(30));
+    } else if (type == 7) {
+        fc = (x * (x * (R(20) * x - R(70)) + R(84)) - R(35)) * x * x * x * x + R(1);
+        dfc = x * x * x * iw * (x * (x * (R(140) * x - R(420)) + R(420)) - R(140));
+    } else {
+        const R x4 = x * x * x * x;
+        fc = (x * (x * (x * (R(315) - R(70) * x) - R(540)) + R(420)) - R(126)) * x4 * x + R(1);
+        dfc = iw * x4 * (x * (x * ((R(2520) - R(630) * x) * x - R(3780)) + R(2520)) - R(630));
+    }
+}
+
+// activation and derivative, RuNNer_src/calconenn.f90:124-146, getdnodes_values.f90:76-108
+template <typename R> __device__ __forceinline__ R act_fn(uint8_t a, R x) {
+    switch (a) {
+        case 't': return NM<R>::th(x);
+        case 'g': return NM<R>::ex(R(-0.5) * x * x);
+        case 'c': return cos(x);
+        case 's': return R(1) / (R(1) + NM<R>::ex(-x));
+        case 'S': return R(1) - R(1) / (R(1) + NM<R>::ex(-x));
+        case 'e': return NM<R>::ex(-x);
+        case 'p': return NM<R>::lg(NM<R>::ex(x) + R(1));
+        case 'h': return x * x;
+        default: return x;  // 'l'
+    }
+}
+template <typename R> __device__ __forceinline__ R act_dfn(uint8_t a, R sum, R val) {
+    switch (a) {
+        case 't': return R(1) - val * val;
+        case 'g': return R(-1) * sum * val;
+        case 'c': return -sin(sum);
+        case 's': { const R e = NM<R>::ex(-sum); return e / ((R(1) + e) * (R(1) + e)); }
+        case 'S': { const R e = NM<R>::ex(-sum); return -e / ((R(1) + e) * (R(1) + e)); }
+        case 'e': return -val;
+        case 'p': { const R e = NM<R>::ex(val); return (e - R(1)) / e; }
+        case 'h': return R(2) * sum;
+        default: return R(1);
+    }
+}
+
+// second derivative of the activation (used by the force-loss training gradient)
+template <typename R> __device__ __forceinline__ R act_ddfn(uint8_t a, R sum, R val) {
+    switch (a) {
+        case 't': return R(-2) * val * (R(1) - val * val);
+        case 'p': { const R e = NM<R>::ex(-sum); const R s = R(1) / (R(1) + e); return s * (R(1) - s); }
+        case 's': { const R s = val; return s * (R(1) - s) * (R(1) - R(2) * s); }
+        case 'g': return (sum * sum - R(1)) * val;
+        case 'e': return val;
+        case 'h': return R(2);
+        default: return R(0);
+    }
+}
+
+// Integer power by squaring (G3 (1 + lambda cos)^(zeta-1) for integer zeta).
+template <typename R> __device__ __forceinline__ R ipow(R x, int n) {
+    R r = R(1);
+    while (n > 0) {
+        if (n & 1) r *= x;
+        x *= x;
+        n >>= 1;
+    }
+    return r;
+}
+
+}  // namespace mdt

@@ -1,0 +1,379 @@
+// mdt_prop.cuh -- propagators (src/md_algo.f90, src/rpmd.f90) as CTA-level device
+// functions, shared by every fused step kernel.
+#pragma once
+#include "mdt_common.cuh"
+#include "mdt_emt.cuh"
+
+namespace mdt {
+
+
+// ---------------------------------------------------------------------------
+// Propagators (src/md_algo.f90).  Thread per atom, all beads of the atom.
+// ---------------------------------------------------------------------------
+struct TrajView {
+    int t, N, nb, aoff;
+    int64_t base;
+};
+
+static __device__ __forceinline__ TrajView traj_view(const Batch &B, int t) {
+    return TrajView{t, B.natoms[t], B.nbeads[t], B.atom_off[t], B.ba_off[t]};
+}
+
+static __device__ __forceinline__ double temp_of(const Batch &B, const PropParams &P, int ty) {
+    return B.is_proj[ty] ? P.Tproj : P.Tsurf;
+}
+
+// Deviate for (bead b, atom i, dimension d).  Host-provided arrays use the reference's
+// Fortran order (3, nb, N) per trajectory, concatenated.
+static __device__ __forceinline__ double rand_normal(const PropParams &P, const TrajView &T, int step, int b, int i,
+                                              int d, uint32_t stream, const double *injected) {
+    if (P.rng_mode == 1) return injected[(T.base + (int64_t)i * T.nb + b) * 3 + d];
+    return normal_deviate(P.seed, (uint32_t)T.t, (uint32_t)step, (uint32_t)((b * T.N + i) * 3 + d), stream);
+}
+
+static __device__ __forceinline__ double &comp(double *x, double *y, double *z, int d, int64_t k) {
+    return d == 0 ? x[k] : (d == 1 ? y[k] : z[k]);
+}
+
+// verlet_1 / verlet_2, md_algo.f90:110-142
+static __device__ void verlet_half(const Batch &B, const PropParams &P, const TrajView &T, int i, bool move_r) {
+    for (int b = 0; b < T.nb; ++b) {
+        const int64_t k = T.base + (int64_t)b * T.N + i;
+        const uint8_t fx = B.fixed[k];
+        for (int d = 0; d < 3; ++d) {
+            double &v = comp(B.vx, B.vy, B.vz, d, k);
+            if (!(fx >> d & 1)) v = v + 0.5 * P.step * comp(B.ax, B.ay, B.az, d, k);
+            else v = 0.0;
+        }
+    }
+    if (move_r && T.nb == 1) {
+        const int64_t k = T.base + i;
+        const uint8_t fx = B.fixed[k];
+        for (int d = 0; d < 3; ++d)
+            if (!(fx >> d & 1)) comp(B.rx, B.ry, B.rz, d, k) += P.step * comp(B.vx, B.vy, B.vz, d, k);
+    }
+}
+
+struct LangCoef { double c0, c1, c2, sigma_r, sigma_v, c_rv; };
+
+// md_algo.f90:165-198 (first half) and 253-285 (second half)
+static __device__ void langevin_coef(double xi, double step, double temp, bool all_big, bool second, LangCoef &c) {
+    const double xidt = xi * step, xidt2 = xidt * xidt, ixidt = step / xidt;
+    if (all_big && temp > kTolerance) {
+        c.c0 = exp(-xidt);
+        c.c1 = (1 - c.c0) * ixidt;
+        c.c2 = (1 - c.c1 / step) * ixidt;
+        c.sigma_r = ixidt * sqrt(temp * (2 * xidt - 3 + 4 * c.c0 - c.c0 * c.c0));
+        c.sigma_v = sqrt(temp * (1 - c.c0 * c.c0));
+        c.c_rv = ixidt * temp * (1 - c.c0) * (1 - c.c0) / (c.sigma_r * c.sigma_v);
+    } else {
+        c.c0 = 1 - xidt + 0.5 * xidt2;
+        c.c1 = (1 - 0.5 * xidt + 2 * kTwelfth * xidt2) * step;
+        c.c2 = (0.5 - 2 * kTwelfth * xidt + 0.5 * kTwelfth * xidt2) * step;
+        c.sigma_r = second ? 0.0 : step * sqrt(temp * (8 * kTwelfth * xidt - 0.5 * xidt2));
+        c.sigma_v = sqrt(2 * temp * xidt * (1 - xidt));
+        c.c_rv = 0.5 * kSqrt3 * (1 - 0.125 * xidt);
+    }
+}
+
+static __device__ __forceinline__ double friction(const Batch &B, const PropParams &P, int algo, int64_t k) {
+    return algo == kPropLangevinConst ? P.gamma_const : B.dens[k];
+}
+
+static __device__ bool all_xidt_big(const Batch &B, const PropParams &P, const TrajView &T, int i, int algo) {
+    bool all_big = true;
+    for (int b = 0; b < T.nb; ++b)
+        if (!(friction(B, P, algo, T.base + (int64_t)b * T.N + i) * P.step > (double)1e-2f)) all_big = false;
+    return all_big;
+}
+
+// langevin_1, md_algo.f90:146-232
+static __device__ void langevin_1(const Batch &B, const PropParams &P, const TrajView &T, int i, int step, int algo) {
+    const int ty = B.type[T.aoff + i];
+    const double temp = kBoltz * T.nb * temp_of(B, P, ty) / B.mass[T.aoff + i];
+    const bool all_big = all_xidt_big(B, P, T, i, algo);
+    for (int b = 0; b < T.nb; ++b) {
+        const int slot = b * T.N + i;
+        const int64_t k = T.base + slot;
+        LangCoef c;
+        langevin_coef(friction(B, P, algo, k), P.step, temp, all_big, false, c);
+        const uint8_t fx = B.fixed[k];
+        for (int d = 0; d < 3; ++d) {
+            double &v = comp(B.vx, B.vy, B.vz, d, k);
+            if (!(fx >> d & 1)) {
+                const double rnd = rand_normal(P, T, step, b, i, d, kStreamLangevin, P.randy);
+                const double a = comp(B.ax, B.ay, B.az, d, k);
+                comp(B.rx, B.ry, B.rz, d, k) += c.c1 * v + c.c2 * P.step * a + c.sigma_r * rnd;
+                v = c.c0 * v + (c.c1 - c.c2) * a + c.sigma_v * c.c_rv * rnd;
+            } else {
+                v = 0.0;
+            }
+        }
+    }
+}
+
+// ldfa, md_algo.f90:506-570 -- dens(:,i) becomes the friction coefficient in place
+static __device__ bool ldfa(const Batch &B, const TrajView &T, int i) {
+    const double coefs[12] = {0.0802484, -1.12851, 9.28508, 2.10064, -843.419, 8.85354e3, -4.89023e4,
+                              1.6741e5, -3.67098e5, 5.03476e5, -3.9426e5, 1.34763e5};
+    const double convert = 1.00794 * kAmu2Mass;
+    const double m = B.mass[T.aoff + i];
+    bool ok = true;
+    for (int b = 0; b < T.nb; ++b) {
+        const int64_t k = T.base + (int64_t)b * T.N + i;
+        const double d0 = B.dens[k];
+        double fric;
+        if ((double)-1e-12f <= d0 && d0 <= (double)0.36f) {
+            fric = 0.0;
+            double temp = d0;
+            for (int j = 0; j < 12; ++j) {
+                fric = fric + coefs[j] * temp;
+                temp = temp * d0;
+            }
+        } else if (d0 > (double)0.36f) {
+            fric = 0.001 * (4.7131 - exp(-4.41305 * d0));
+        } else {
+            ok = false;
+            fric = 0.0;
+        }
+        B.dens[k] = fric * convert / kHbar / m;
+    }
+    return ok;
+}
+
+// langevin_2, md_algo.f90:236-300
+static __device__ void langevin_2(const Batch &B, const PropParams &P, const TrajView &T, int i, int step, int algo) {
+    const int ty = B.type[T.aoff + i];
+    const double temp = kBoltz * T.nb * temp_of(B, P, ty) / B.mass[T.aoff + i];
+    const bool all_big = all_xidt_big(B, P, T, i, algo);
+    for (int b = 0; b < T.nb; ++b) {
+        const int slot = b * T.N + i;
+        const int64_t k = T.base + slot;
+        LangCoef c;
+        langevin_coef(friction(B, P, algo, k), P.step, temp, all_big, true, c);
+        const uint8_t fx = B.fixed[k];
+        const double sv = c.sigma_v * sqrt(1 - c.c_rv * c.c_rv);
+        for (int d = 0; d < 3; ++d) {
+            double &v = comp(B.vx, B.vy, B.vz, d, k);
+            if (!(fx >> d & 1)) {
+                const double rnd = rand_normal(P, T, step, b, i, d, kStreamLangevin, P.randy);
+                v = v + c.c2 * comp(B.ax, B.ay, B.az, d, k) + sv * rnd;
+            } else {
+                v = 0.0;
+            }
+        }
+    }
+}
+
+// andersen, md_algo.f90:402-432
+static __device__ void andersen(const Batch &B, const PropParams &P, const TrajView &T, int i, int step) {
+    const int ty = B.type[T.aoff + i];
+    const double ibetaN = T.nb * kBoltz * temp_of(B, P, ty);
+    const double sd = sqrt(ibetaN / B.mass[T.aoff + i]);
+    const double thr = P.step / P.andersen_time;
+    for (int b = 0; b < T.nb; ++b) {
+        const int slot = b * T.N + i;
+        const int64_t k = T.base + slot;
+        const double u = P.rng_mode == 1 ? P.andersen_u[T.base + (int64_t)i * T.nb + b]
+                                         : uniform_deviate(P.seed, (uint32_t)T.t, (uint32_t)step, (uint32_t)slot,
+                                                           kStreamAndersenU);
+        if (u < thr) {
+            const uint8_t fx = B.fixed[k];
+            for (int d = 0; d < 3; ++d)
+                if (!(fx >> d & 1))
+                    comp(B.vx, B.vy, B.vz, d, k) =
+                        rand_normal(P, T, step, b, i, d, kStreamAndersenV, P.andersen_v) * sd;
+        }
+    }
+}
+
+// pile_thermostat, md_algo.f90:440-502 (one thread per atom, all three dimensions)
+static __device__ void pile(const Batch &B, const PropParams &P, const TrajView &T, const double *cjk, int i, int step) {
+    const int nb = T.nb;
+    const int ty = B.type[T.aoff + i];
+    const double m = B.mass[T.aoff + i];
+    const double betaN = 1.0 / (kBoltz * temp_of(B, P, ty) * nb);
+    const double sq = sqrt(m / betaN);
+    for (int d = 0; d < 3; ++d) {
+        double newP[32], atomP[32];
+        for (int b = 0; b < nb; ++b) atomP[b] = m * comp(B.vx, B.vy, B.vz, d, T.base + (int64_t)b * T.N + i);
+        for (int b = 0; b < nb; ++b) {
+            double s = 0.0;
+            for (int k = 0; k < nb; ++k) s = s + atomP[k] * cjk[b * nb + k];  // cjk(k,b)
+            newP[b] = s;
+        }
+        for (int kk = 0; kk < nb; ++kk) {
+            double gam;
+            if (kk == 0) gam = 1 / P.pile_tau;
+            else gam = 2 * (2 * (1 / betaN / kHbar) * sin(kk * kPi / nb));
+            const double c1 = exp(-0.5 * P.step * gam), c2 = sqrt(1 - c1 * c1);
+            const double z = rand_normal(P, T, step, kk, i, d, kStreamPile, P.zeta);
+            newP[kk] = c1 * newP[kk] + sq * c2 * z;
+        }
+        for (int b = 0; b < nb; ++b) {
+            const int64_t k = T.base + (int64_t)b * T.N + i;
+            double s = 0.0;
+            if (!(B.fixed[k] >> d & 1))
+                for (int kk = 0; kk < nb; ++kk) s = s + newP[kk] * cjk[kk * nb + b];  // cjk(b,kk)
+            comp(B.vx, B.vy, B.vz, d, k) = s / m;
+        }
+    }
+}
+
+// remove_com_velocity, universe_mod.f90:222-241.  Its 1000 subtraction sweeps have the
+// closed form v -= v_cm0 * N * (1 - (1 - 1/N)^1000), applied to every bead-atom.
+static __device__ void remove_com(const Batch &B, const TrajView &T, double *red) {
+    double sx = 0, sy = 0, sz = 0, ms = 0;
+    for (int i = threadIdx.x; i < T.N; i += blockDim.x) {
+        const double m = B.mass[T.aoff + i];
+        double ax = 0, ay = 0, az = 0;
+        for (int b = 0; b < T.nb; ++b) {
+            const int64_t k = T.base + (int64_t)b * T.N + i;
+            ax += B.vx[k];
+            ay += B.vy[k];
+            az += B.vz[k];
+        }
+        sx += ax * m;
+        sy += ay * m;
+        sz += az * m;
+        ms += m;
+    }
+    sx = block_sum(sx, red);
+    sy = block_sum(sy, red);
+    sz = block_sum(sz, red);
+    ms = block_sum(ms, red);
+    const double n = (double)T.N;
+    const double fac = n * (1.0 - pow(1.0 - 1.0 / n, 1000.0));
+    const double cx = sx / ms / T.nb / n * fac, cy = sy / ms / T.nb / n * fac, cz = sz / ms / T.nb / n * fac;
+    const int tot = T.N * T.nb;
+    for (int s = threadIdx.x; s < tot; s += blockDim.x) {
+        const int64_t k = T.base + s;
+        B.vx[k] -= cx;
+        B.vy[k] -= cy;
+        B.vz[k] -= cz;
+    }
+    __syncthreads();
+}
+
+static __device__ bool traj_has_algo(const Batch &B, int id) {
+    for (int ty = 0; ty < B.ntypes; ++ty)
+        if (B.algo[ty] == id) return true;
+    return false;
+}
+
+// propagate_1, md_algo.f90:37-76
+static __device__ void propagate_1(const Batch &B, const PropParams &P, const TrajView &T, const double *cjk, int step,
+                            double *red) {
+    for (int i = threadIdx.x; i < T.N; i += blockDim.x) {
+        const int algo = B.algo[B.type[T.aoff + i]];
+        switch (algo) {
+            case kPropVerlet: verlet_half(B, P, T, i, true); break;
+            case kPropAndersen:
+                verlet_half(B, P, T, i, true);
+                andersen(B, P, T, i, step);
+                break;
+            case kPropPile:
+                pile(B, P, T, cjk, i, step);
+                verlet_half(B, P, T, i, true);
+                break;
+            case kPropLangevin:
+            case kPropLangevinConst: langevin_1(B, P, T, i, step, algo); break;
+            default: break;
+        }
+    }
+    __syncthreads();
+    if (traj_has_algo(B, kPropAndersen) || traj_has_algo(B, kPropPile)) remove_com(B, T, red);
+}
+
+// propagate_2, md_algo.f90:80-106
+static __device__ void propagate_2(const Batch &B, const PropParams &P, const TrajView &T, int step) {
+    bool bad = false;
+    for (int i = threadIdx.x; i < T.N; i += blockDim.x) {
+        const int algo = B.algo[B.type[T.aoff + i]];
+        if (algo == kPropLangevin) {
+            if (!ldfa(B, T, i)) bad = true;
+            langevin_2(B, P, T, i, step, algo);
+        } else if (algo == kPropLangevinConst) {
+            langevin_2(B, P, T, i, step, algo);
+        } else {
+            verlet_half(B, P, T, i, false);
+        }
+    }
+    if (bad) B.status[T.t] = kStatusErrDensity;
+    __syncthreads();
+}
+
+// do_ring_polymer_step, rpmd.f90:309-452.  Thread per (atom, dimension).
+static __device__ void ring_polymer_step(const Batch &B, const PropParams &P, const TrajView &T, const double *cjk) {
+    const int nb = T.nb;
+    const double prefactor = -1 * B.mass[T.aoff] * pow(kBoltz * P.Tproj * nb / kHbar, 2.0);
+    const double piN = kPi / nb;
+    for (int w = threadIdx.x; w < 3 * T.N; w += blockDim.x) {
+        const int i = w / 3, d = w - 3 * (w / 3);
+        const int ty = B.type[T.aoff + i];
+        const double m = B.mass[T.aoff + i];
+        double p[32], q[32], np[32], nq[32];
+        for (int b = 0; b < nb; ++b) {
+            const int64_t k = T.base + (int64_t)b * T.N + i;
+            p[b] = m * comp(B.vx, B.vy, B.vz, d, k);
+            q[b] = comp(B.rx, B.ry, B.rz, d, k);
+        }
+        for (int b = 0; b < nb; ++b) {
+            double sp = 0.0, sq = 0.0;
+            for (int k = 0; k < nb; ++k) {
+                sp = sp + p[k] * cjk[b * nb + k];
+                sq = sq + q[k] * cjk[b * nb + k];
+            }
+            np[b] = sp;
+            nq[b] = sq;
+        }
+        const double betaN = 1.0 / (kBoltz * temp_of(B, P, ty) * nb);
+        const double twown = 2.0 / betaN / kHbar;
+        for (int b = 0; b < nb; ++b) {
+            double c0 = 1.0, c1 = 0.0, c2 = P.step / m, c3 = 1.0;
+            if (nb > 1 && b > 0) {
+                const int bb = (b <= nb / 2) ? b : nb - b;
+                const double wk = twown * sin(bb * piN), wt = wk * P.step, wm = wk * m;
+                const double cw = cos(wt), sw = sin(wt);
+                c0 = cw; c1 = -wm * sw; c2 = sw / wm; c3 = cw;
+            }
+            const double pn = np[b] * c0 + nq[b] * c1;
+            nq[b] = np[b] * c2 + nq[b] * c3;
+            np[b] = pn;
+        }
+        const int algo = B.algo[ty];
+        const bool revert = (algo == kPropLangevin || algo == kPropLangevinConst);
+        for (int b = 0; b < nb; ++b) {
+            const int64_t k = T.base + (int64_t)b * T.N + i;
+            if (revert) continue;
+            if (B.fixed[k] >> d & 1) continue;
+            double sr = 0.0, sv = 0.0;
+            for (int kk = 0; kk < nb; ++kk) {
+                sr = sr + nq[kk] * cjk[kk * nb + b];
+                sv = sv + np[kk] * cjk[kk * nb + b] / m;
+            }
+            comp(B.rx, B.ry, B.rz, d, k) = sr;
+            comp(B.vx, B.vy, B.vz, d, k) = sv;
+        }
+        if (revert) {
+            // rpmd.f90:418-435: positions/velocities kept, spring force set instead
+            for (int b = 0; b < nb; ++b) {
+                const int prev = (b == 0) ? nb - 1 : b - 1, next = (b == nb - 1) ? 0 : b + 1;
+                const int64_t k = T.base + (int64_t)b * T.N + i;
+                const double rb = q[b], rp = q[prev], rn = q[next];
+                comp(B.fx, B.fy, B.fz, d, k) = prefactor * (2 * rb - rp - rn);
+            }
+        }
+    }
+    __syncthreads();
+}
+
+static __device__ void load_cjk(const Batch &B, int t, double *cjk_s) {
+    const int nb = B.nbeads[t];
+    if (nb <= 1) return;
+    const double *src = B.cjk + B.cjk_off[t];
+    for (int k = threadIdx.x; k < nb * nb; k += blockDim.x) cjk_s[k] = src[k];
+    __syncthreads();
+}
+
+}  // namespace mdt

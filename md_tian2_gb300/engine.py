@@ -14,11 +14,12 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import constants as C
-from ._lib import EngineError, PropParams, TrajSummary, load
+from ._lib import EngineError, NNModelC, PropParams, TrajSummary, load
 from .io import EmtParams
 from .universe import Universe
 
 PREC = {"fp64": 0, "fp32": 1}
+PES_EMT, PES_NENE, PES_SURROGATE = C.PES_ID_EMT, C.PES_ID_NENE, 2100
 
 
 @dataclass
@@ -84,6 +85,52 @@ class Engine:
         self._check(self.lib.mdt_emt_set_params(self.h, params.ntypes, *[_p(a, ct.c_double) for a in arrs],
                                                 _p(pes, ct.c_int32)), "mdt_emt_set_params")
         self._keep_params = (arrs, pes)
+
+    def read_nene(self, model, type_names: list, max_neighbors: int = 0) -> None:
+        """read_nene (src/pes_nene_mod.f90:123) equivalent: install an HDNNP
+        (``nene.NNModel``).  ``type_names``: element symbol of each universe type."""
+        from .nene import Z_OF
+        f = model.flat()
+        keep = {k: (np.ascontiguousarray(v) if isinstance(v, np.ndarray) else v) for k, v in f.items()}
+        c = NNModelC()
+        c.nelem, c.maxsf = model.nelem, model.maxsf
+        for name in ("z", "nsf", "sftype", "eta", "rshift", "zeta", "rc", "e1", "e2", "smin", "smax", "savg",
+                     "nodes", "act", "weights", "atom_energy"):
+            setattr(c, name, keep[name].ctypes.data)
+        c.lambda_ = keep["lambda"].ctypes.data
+        c.scalesym, c.centersym = int(model.scalesym), int(model.centersym)
+        c.scmin, c.scmax = model.scmin, model.scmax
+        c.cutoff_type, c.cutoff_alpha = model.cutoff_type, model.cutoff_alpha
+        c.nlayers, c.maxnodes, c.maxweights = keep["nlayers"], keep["maxnodes"], keep["maxweights"]
+        c.normnodes = int(model.normnodes)
+        c.remove_atom_energies = int(bool(model.atom_energy))
+        zt = np.array([Z_OF.get(n, 0) if n in model.elements else 0 for n in type_names], np.int32)
+        self._check(self.lib.mdt_nn_set_model(self.h, ct.byref(c), len(type_names), _p(zt, ct.c_int32),
+                                              max_neighbors), "mdt_nn_set_model")
+        self.nn_model = model
+        self.max_neighbors = max_neighbors or 192
+
+    def set_pes(self, kind: int, range_margin: float = 0.1) -> None:
+        self._check(self.lib.mdt_set_pes(self.h, kind, range_margin), "mdt_set_pes")
+
+    def nn_stats(self):
+        fb = np.zeros(self.T, np.int32)
+        ov = np.zeros(self.T, np.int32)
+        self._check(self.lib.mdt_nn_stats(self.h, fb.ctypes.data, ov.ctypes.data), "mdt_nn_stats")
+        return fb, ov
+
+    def nn_descriptors(self, precision: str = "fp64") -> np.ndarray:
+        """Raw symmetry functions, shape (nslots, maxsf), Fortran slot order."""
+        G = np.zeros((self.nslots, self.nn_model.maxsf))
+        self._check(self.lib.mdt_nn_descriptors(self.h, PREC[precision], G.ctypes.data), "mdt_nn_descriptors")
+        return G
+
+    def nn_neighbors(self):
+        tot = int(np.sum(self.natoms))
+        counts = np.zeros(tot, np.int32)
+        words = np.zeros(tot * self.max_neighbors, np.int32)
+        self._check(self.lib.mdt_nn_neighbors(self.h, counts.ctypes.data, words.ctypes.data), "mdt_nn_neighbors")
+        return counts, words.reshape(tot, self.max_neighbors)
 
     def define(self, universes: list[Universe]) -> None:
         """Lay out T universes (ragged sizes and bead counts) on the device."""

@@ -134,3 +134,53 @@ def config3(ntraj: int = 1024, seed: int = 3, beads=(4, 8, 16, 32)):
         out.append(h_on_metal(rng, "Pt", 4, rng.uniform(0.1, 1.0), 0.0, 0.0, 300.0, C.PROP_ID_PILE, C.PROP_ID_PILE,
                               nbeads=nb))
     return out
+
+
+# ---------------------------------------------------------------------------
+# H on graphene (HDNNP workload)
+# ---------------------------------------------------------------------------
+def graphene(k: int = 6, a: float = 2.46, c: float = 20.0, ripple: float = 0.05, rng=None):
+    """k x k hexagonal graphene supercell (2 atoms per primitive cell) at z = 0 with a
+    Gaussian z-ripple; returns positions (n, 3) and cell (columns)."""
+    rng = rng or np.random.default_rng(0)
+    a1 = np.array([a, 0.0, 0.0])
+    a2 = np.array([a / 2, a * math.sqrt(3.0) / 2, 0.0])
+    pos = []
+    for i in range(k):
+        for j in range(k):
+            o = i * a1 + j * a2
+            pos.append(o)
+            pos.append(o + (a1 + a2) / 3.0)
+    pos = np.array(pos)
+    pos[:, 2] = rng.normal(scale=ripple, size=len(pos))
+    cell = np.zeros((3, 3))
+    cell[:, 0] = k * a1
+    cell[:, 1] = k * a2
+    cell[:, 2] = [0.0, 0.0, c]
+    return pos, cell
+
+
+def h_on_graphene(rng, einc: float, Tsurf: float = 300.0, z0: float = 4.0, k: int = 6, algo=C.PROP_ID_VERLET):
+    """One H/graphene trajectory start: H first (projectile), normal incidence."""
+    pos, cell = graphene(k, rng=rng)
+    n = len(pos) + 1
+    masses = np.empty(n)
+    masses[0] = C.MASS_AMU["H"] * C.AMU2MASS
+    masses[1:] = C.MASS_AMU["C"] * C.AMU2MASS
+    r = np.zeros((n, 3))
+    frac = rng.random(2)
+    r[0, :2] = frac[0] * cell[:2, 0] + frac[1] * cell[:2, 1]
+    r[0, 2] = z0
+    r[1:] = pos
+    v = np.zeros((n, 3))
+    v[1:] = maxwell_boltzmann(rng, masses[1:], np.ones(n - 1, bool), Tsurf)
+    v[0, 2] = -math.sqrt(2.0 * einc / masses[0])
+    return Universe(r=r[:, None, :].copy(), v=v[:, None, :].copy(), m=masses, idx=np.array([1] + [2] * (n - 1), np.int32),
+                    is_fixed=np.zeros((n, 1, 3), bool), simbox=cell, names=["H", "C"], is_proj=np.array([True, False]),
+                    algo=np.array([algo, algo], np.int32))
+
+
+def config4(ntraj: int = 2048, seed: int = 4):
+    """H on 6x6 graphene (72 C + 1 H), Einc ~ U(0.5, 2) eV, Tsurf = 300 K."""
+    rng = np.random.default_rng(seed)
+    return [h_on_graphene(rng, rng.uniform(0.5, 2.0)) for _ in range(ntraj)]

@@ -17,7 +17,7 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 BUILD = HERE / "build"
 LIB = BUILD / "libmd_oracle.so"
-SOURCES = ["md_oracle.cpp"]
+SOURCES = ["md_oracle.cpp", "nene_oracle.cpp"]
 
 ORC_VERLET, ORC_LANGEVIN, ORC_ANDERSEN, ORC_PILE, ORC_LANGEVIN_CONST = 1001, 1003, 1005, 1006, 1007
 
@@ -28,7 +28,7 @@ def build(force: bool = False) -> Path:
         return LIB
     BUILD.mkdir(exist_ok=True)
     tmp = LIB.with_suffix(".tmp.so")
-    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-o", str(tmp)] + [str(HERE / s) for s in SOURCES]
+    cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-o", str(tmp)] + [str(HERE / s) for s in SOURCES]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"oracle build failed:\n{r.stderr}")
@@ -148,3 +148,78 @@ class OracleUniverse:
     def bead_epot(self, sp):
         p = self.params(sp)
         return lib().orc_bead_epot(ct.byref(self.c), ct.byref(p))
+
+
+# ---------------------------------------------------------------------------
+# RuNNer HDNNP oracle (nene_oracle.cpp)
+# ---------------------------------------------------------------------------
+class CNN(ct.Structure):
+    _fields_ = [("nelem", ct.c_int), ("z", ct.c_void_p), ("maxsf", ct.c_int), ("nsf", ct.c_void_p),
+                ("sftype", ct.c_void_p), ("eta", ct.c_void_p), ("rshift", ct.c_void_p), ("lambda_", ct.c_void_p),
+                ("zeta", ct.c_void_p), ("rc", ct.c_void_p), ("e1", ct.c_void_p), ("e2", ct.c_void_p),
+                ("smin", ct.c_void_p), ("smax", ct.c_void_p), ("savg", ct.c_void_p),
+                ("scalesym", ct.c_int), ("centersym", ct.c_int), ("scmin", ct.c_double), ("scmax", ct.c_double),
+                ("cutoff_type", ct.c_int), ("cutoff_alpha", ct.c_double), ("nlayers", ct.c_int),
+                ("maxnodes", ct.c_int), ("nodes", ct.c_void_p), ("act", ct.c_void_p), ("maxweights", ct.c_int),
+                ("weights", ct.c_void_p), ("normnodes", ct.c_int), ("remove_atom_energies", ct.c_int),
+                ("atom_energy", ct.c_void_p)]
+
+
+class NNOracle:
+    """compute_nene on the CPU for one bead (positions in A, cell columns in A)."""
+
+    def __init__(self, model):
+        f = model.flat()
+        self.keep = {k: (np.ascontiguousarray(v) if isinstance(v, np.ndarray) else v) for k, v in f.items()}
+        k = self.keep
+        self.model = model
+        self.c = CNN()
+        c = self.c
+        c.nelem, c.maxsf = model.nelem, model.maxsf
+        for name in ("z", "nsf", "sftype", "eta", "rshift", "zeta", "rc", "e1", "e2", "smin", "smax", "savg",
+                     "nodes", "act", "weights", "atom_energy"):
+            setattr(c, name, k[name].ctypes.data)
+        c.lambda_ = k["lambda"].ctypes.data
+        c.scalesym, c.centersym = int(model.scalesym), int(model.centersym)
+        c.scmin, c.scmax = model.scmin, model.scmax
+        c.cutoff_type, c.cutoff_alpha = model.cutoff_type, model.cutoff_alpha
+        c.nlayers, c.maxnodes, c.maxweights = k["nlayers"], k["maxnodes"], k["maxweights"]
+        c.normnodes = int(model.normnodes)
+        c.remove_atom_energies = int(bool(model.atom_energy))
+        L = lib()
+        L.orc_nene_energy_force.argtypes = [ct.POINTER(CNN), ct.c_int] + [ct.c_void_p] * 7
+        L.orc_nene_neighbors.argtypes = [ct.c_int, ct.c_void_p, ct.c_void_p, ct.c_int, ct.c_double] + \
+            [ct.c_void_p] * 4 + [ct.c_int]
+
+    def energy_force(self, elem, r_ang, simbox, want_G=False):
+        """elem: 0-based element index per atom; r_ang (N,3); simbox (3,3) columns."""
+        N = len(elem)
+        e = np.ascontiguousarray(elem, np.int32)
+        r = np.ascontiguousarray(r_ang, np.float64).reshape(N, 3)
+        box = np.ascontiguousarray(np.asarray(simbox, np.float64).T)  # column major
+        f = np.zeros((N, 3))
+        en = ct.c_double()
+        G = np.zeros((N, self.model.maxsf)) if want_G else None
+        ea = np.zeros(N)
+        rc = lib().orc_nene_energy_force(ct.byref(self.c), N, e.ctypes.data, r.ctypes.data, box.ctypes.data,
+                                         ct.addressof(en), f.ctypes.data, None if G is None else G.ctypes.data,
+                                         ea.ctypes.data)
+        if rc:
+            raise RuntimeError(f"orc_nene_energy_force {rc}")
+        return (en.value, f, G, ea) if want_G else (en.value, f)
+
+    @staticmethod
+    def neighbors(r_bohr, lat_rows_bohr, cutoff, periodic=True, max_total=2_000_000):
+        N = len(r_bohr)
+        xyz = np.ascontiguousarray(r_bohr, np.float64)
+        lat = np.ascontiguousarray(lat_rows_bohr, np.float64)
+        counts = np.zeros(N, np.int32)
+        oj = np.zeros(max_total, np.int32)
+        on = np.zeros(3 * max_total, np.int32)
+        orr = np.zeros(max_total)
+        tot = lib().orc_nene_neighbors(N, xyz.ctypes.data, lat.ctypes.data, int(periodic), cutoff,
+                                       counts.ctypes.data, oj.ctypes.data, on.ctypes.data, orr.ctypes.data,
+                                       max_total)
+        if tot < 0:
+            raise RuntimeError("neighbour list larger than max_total")
+        return counts, oj[:tot], on[:3 * tot].reshape(-1, 3), orr[:tot]

@@ -1,0 +1,54 @@
+"""Regenerate the golden fixtures of this directory from the reference's own data.
+
+Reads (only in the development container, where the reference tree is mounted):
+  pes/EMT-HAu.pes, pes/EMT-HPt.pes          -> emt_params.json (parsed parameter blocks)
+  conf/latt/mxt_00000001.dat                 -> mxt_latt.npz (decoded geometry)
+  example/md/RuNNer_input/{input.nn,scaling.data,weights.006.data}
+  example/md/conf/latt/mxt_00000001.dat      -> runner_cgraphene.npz (parsed network +
+                                               geometry) and runner_cgraphene_ref.npz
+                                               (oracle energy/forces/descriptors/neighbours)
+Usage:  python tests/golden/make_golden.py /root/reference
+"""
+import json
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE.parent.parent))
+
+from md_tian2_gb300 import io, nene  # noqa: E402
+from md_tian2_gb300 import constants as C  # noqa: E402
+
+
+def main(ref):
+    ref = Path(ref)
+    out = {}
+    for name, names in (("EMT-HAu.pes", ["H", "Au"]), ("EMT-HPt.pes", ["H", "Pt"])):
+        p = io.read_pes(ref / "pes" / name, names, [True, False])
+        out[name] = {k: p.values[k].tolist() for k in io.EMT_KEYS}
+    (HERE / "emt_params.json").write_text(json.dumps(out, indent=1))
+
+    u = io.read_mxt(ref / "conf" / "latt" / "mxt_00000001.dat")
+    np.savez(HERE / "mxt_latt.npz", r=u.r, v=u.v, simbox=u.simbox, idx=u.idx, is_fixed=u.is_fixed,
+             names=np.array(u.names), is_proj=u.is_proj)
+
+    m = nene.read_runner(ref / "example" / "md" / "RuNNer_input")
+    nene.save_npz(m, HERE / "runner_cgraphene.npz")
+    g = io.read_mxt(ref / "example" / "md" / "conf" / "latt" / "mxt_00000001.dat")
+    np.savez(HERE / "cgraphene_geometry.npz", r=g.r[:, 0, :], simbox=g.simbox)
+
+    from oracle.oracle import NNOracle
+    o = NNOracle(m)
+    E, F, G, ea = o.energy_force(np.zeros(g.natoms, int), g.r[:, 0, :], g.simbox, want_G=True)
+    x = g.r[:, 0, :] * C.ANG2BOHR
+    lat = g.simbox.T * C.ANG2BOHR
+    counts, nj, nn, nr = NNOracle.neighbors(x, lat, m.maxcut)
+    np.savez(HERE / "runner_cgraphene_ref.npz", energy=E, forces=F, G=G, eatom=ea, nb_counts=counts, nb_j=nj,
+             nb_n=nn)
+    print("golden fixtures written")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
