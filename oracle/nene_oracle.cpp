@@ -209,14 +209,16 @@ void wrap(int N, double *xyz, const double *lat) {
 
 extern "C" {
 
-/* Neighbour list in RuNNer order for the bit-exact test.  Positions in bohr, lattice
-   rows in bohr.  out_j/out_n (3 per entry) sized by the caller (max_total); returns the
+/* Neighbour list in RuNNer order for the bit-exact test.  Positions in bohr (folded
+   into the cell first, as in orc_nene_energy_force), lattice rows in bohr.  out_j/out_n (3 per entry) sized by the caller (max_total); returns the
    number of entries, counts[i] = neighbours of atom i; -1 if max_total is too small. */
 int orc_nene_neighbors(int N, const double *xyz_bohr, const double *lat_bohr, int periodic, double cutoff,
                        int *counts, int *out_j, int *out_n, double *out_r, int max_total) {
     std::vector<int> z(N, 0);
+    std::vector<double> xyz(xyz_bohr, xyz_bohr + 3 * N);
+    if (periodic) wrap(N, xyz.data(), lat_bohr);  // same cell folding as compute_nene
     std::vector<std::vector<Neighbor>> nb;
-    build_neighbors(N, xyz_bohr, lat_bohr, periodic != 0, cutoff, z.data(), nb);
+    build_neighbors(N, xyz.data(), lat_bohr, periodic != 0, cutoff, z.data(), nb);
     int tot = 0;
     for (int i = 0; i < N; ++i) {
         counts[i] = (int)nb[i].size();

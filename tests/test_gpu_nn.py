@@ -102,8 +102,9 @@ def test_two_element_network_fp64(built_lib, oracle_lib):
     for t, u in enumerate(us):
         elem = np.array([0] + [1] * (u.natoms - 1))
         E, F = o.energy_force(elem, u.r[:, 0, :], u.simbox)
-        assert abs(out["epot"][t] - E) < 1e-9
-        assert np.abs(eng.split(out["f"], t)[:, 0, :] - F).max() < 1e-10
+        # the random network's forces reach 1e2 eV/A: hold them to 1e-12 relative
+        assert abs(out["epot"][t] - E) < 1e-9 * max(1.0, abs(E))
+        assert np.abs(eng.split(out["f"], t)[:, 0, :] - F).max() < 1e-12 * max(1.0, np.abs(F).max())
     eng.close()
 
 
