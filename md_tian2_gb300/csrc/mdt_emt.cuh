@@ -126,12 +126,16 @@ static __device__ __forceinline__ void load_cell(const Batch &B, int t, Cell &c)
 }
 
 // image index n = anint(w) for one fractional coordinate (Fortran anint: half away
-// from zero).  FP32 decides unless it is within 1e-4 of a tie.
+// from zero).  FP32 decides unless it is within 1e-4 of a tie; then the fractional
+// coordinate is recomputed in FP64 with the oracle's operation order and no fused
+// multiply-add, so that exact ties (pairs half a cell apart on a perfect lattice) pick
+// the same image on both sides.
 static __device__ __forceinline__ double image_shift(float wf, const double *hi_row3, double ex, double ey, double ez,
-                                              int row) {
+                                                     int row) {
     const float n = roundf(wf);
     if (fabsf(fabsf(wf - n) - 0.5f) > 1e-4f) return (double)n;
-    const double w = hi_row3[row] * ex + hi_row3[row + 3] * ey + hi_row3[row + 6] * ez;
+    const double w = __dadd_rn(__dadd_rn(__dmul_rn(hi_row3[row], ex), __dmul_rn(hi_row3[row + 3], ey)),
+                               __dmul_rn(hi_row3[row + 6], ez));
     return round(w);
 }
 
