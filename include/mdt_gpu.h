@@ -29,6 +29,7 @@ extern "C" {
 #define MDT_ERR_STATE -3       /* call order violated (e.g. no batch defined) */
 #define MDT_ERR_UNSUPPORTED -4 /* configuration outside what this engine implements */
 #define MDT_ERR_NOMEM -5       /* device allocation failed */
+#define MDT_ERR_TOO_LARGE -6   /* configuration beyond a fixed maximum size */
 
 /* ids shared with the reference, src/constants.f90:64-71,107-115 */
 #define MDT_PES_EMT 2003
@@ -191,6 +192,28 @@ int32_t mdt_query(mdt_ctx *ctx, const mdt_prop_params *p, mdt_traj_summary *out)
 /* device pointers of the SoA state (x,y,z arrays of r, v, f, a) for zero-copy callers;
    ptrs must hold 12 entries; *nslots receives the number of bead-atom slots. */
 int32_t mdt_device_state(mdt_ctx *ctx, void **ptrs, int64_t *nslots);
+
+/* ---- allocation-free EMT -------------------------------------------------------
+ * No counterpart in the reference.  EMT energy, forces and embedded densities of ONE
+ * configuration (one bead) for callers that must not allocate device memory -- a
+ * program whose GPU memory is handed out by another runtime's pool, a loop that may
+ * never enter the CUDA allocator, a caller without a library context.  Nothing is
+ * allocated: the pair scratch lives in a 1.5 MiB file-scope device array that every
+ * GPU loading the library keeps until process exit.  At most 256 atoms
+ * (MDT_ERR_TOO_LARGE beyond).  All array arguments except simbox and the EMT
+ * parameters are DEVICE pointers: idx (natoms, 1-based types), x/y/z positions (A),
+ * outputs fx/fy/fz (eV/A, overwritten), energy (one double, eV, overwritten; NaN if a
+ * type index is out of range), dens (embedded density per atom, may be NULL).
+ * simbox: host, 9 doubles column major.  EMT parameters and the pes table: host, as
+ * for mdt_emt_set_params.  The call is asynchronous on `stream` (NULL = default
+ * stream).  The first call on a device looks up the scratch array's address and must
+ * come before any stream capture.  Calls share the scratch: calls that overlap on the
+ * GPU race and must be serialised by the caller. */
+int32_t mdt_emt_force_noalloc(int32_t natoms, const int32_t *idx, const double *x, const double *y,
+                              const double *z, const double *simbox, int32_t ntypes, const double *eta2,
+                              const double *n0, const double *e0, const double *lambda, const double *v0,
+                              const double *kappa, const double *s0, const int32_t *pes, double *fx, double *fy,
+                              double *fz, double *energy, double *dens, void *stream);
 
 /* ---- measurement -------------------------------------------------------------
  * FMA throughput of the current device (FP64 or FP32 CUDA cores): the roofline

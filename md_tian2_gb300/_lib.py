@@ -70,6 +70,8 @@ SIGNATURES = {
     "mdt_nn_stats": (ct.c_int32, [ct.c_void_p, ct.c_void_p, ct.c_void_p]),
     "mdt_nn_neighbors": (ct.c_int32, [ct.c_void_p, ct.c_void_p, ct.c_void_p]),
     "mdt_nn_descriptors": (ct.c_int32, [ct.c_void_p, ct.c_int32, ct.c_void_p]),
+    "mdt_emt_force_noalloc": (ct.c_int32, [ct.c_int32] + [ct.c_void_p] * 5 + [ct.c_int32] + [ct.c_void_p] * 8 +
+                              [ct.c_void_p] * 5 + [ct.c_void_p]),
 }
 
 _lib = None
