@@ -150,6 +150,35 @@ int32_t mdt_nn_descriptors(mdt_ctx *ctx, int32_t precision, double *G);
    of RuNNer_src/neighbor_para_short.f90:117-163 */
 int32_t mdt_nn_neighbors(mdt_ctx *ctx, int32_t *counts, int32_t *words);
 
+/* ---- training of the network (learned EMT surrogate) -------------------------
+ * No counterpart in the reference's MD path (its fit.f90 fits EMT/REBO parameters
+ * with MKL).  Every trajectory of the current batch is one training configuration
+ * (nbeads must be 1).  Loss per configuration:
+ *   w_energy * ((E - E_ref)/N)^2 + w_force * sum |F - F_ref|^2 / (3N)   (eV, eV/A),
+ * averaged over the configurations of a step; Adam on FP32 master weights.
+ * Requires scale_symmetry_functions, no centering, no normalize_nodes. */
+typedef struct mdt_train_opts {
+    double w_energy, w_force;
+    double lr, beta1, beta2, eps;
+    int32_t precision;          /* MDT_PREC_FP32 for training, MDT_PREC_FP64 for gradient checks */
+} mdt_train_opts;
+
+/* Labels: energy[T] (eV), forces (3, 1, N) per trajectory (eV/A).  Computes the raw
+   symmetry functions and neighbour lists once and starts the optimiser from the
+   installed network's weights. */
+int32_t mdt_train_set_labels(mdt_ctx *ctx, const double *energy, const double *forces);
+/* One optimiser step on configurations conf_ids[n] (0-based trajectory indices).
+   stats (may be NULL): [mean ((E-E_ref)/N)^2 in eV^2, mean squared force error per
+   component in (eV/A)^2, loss]. */
+int32_t mdt_train_step(mdt_ctx *ctx, const mdt_train_opts *opts, const int32_t *conf_ids, int32_t n, double *stats);
+/* Gradient of the mean loss over conf_ids with respect to the weights (nelem *
+   maxweights doubles, calconenn order per element), without updating them. */
+int32_t mdt_train_gradient(mdt_ctx *ctx, const mdt_train_opts *opts, const int32_t *conf_ids, int32_t n,
+                           double *grad);
+/* Install the current master weights as the network used by mdt_calc_force /
+   mdt_md_steps; weights (may be NULL) receives them (nelem * maxweights doubles). */
+int32_t mdt_train_commit(mdt_ctx *ctx, double *weights);
+
 /* ---- batch geometry --------------------------------------------------------
  * Replaces the universe constructor new_atoms (src/universe_mod.f90:77-115) for T
  * trajectories at once.  natoms[T], nbeads[T]; idx: 1-based type per atom

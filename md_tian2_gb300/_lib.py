@@ -44,6 +44,12 @@ class NNModelC(ct.Structure):
                 ("atom_energy", ct.c_void_p)]
 
 
+class TrainOpts(ct.Structure):
+    """mdt_train_opts (include/mdt_gpu.h)."""
+    _fields_ = [("w_energy", ct.c_double), ("w_force", ct.c_double), ("lr", ct.c_double), ("beta1", ct.c_double),
+                ("beta2", ct.c_double), ("eps", ct.c_double), ("precision", ct.c_int32)]
+
+
 # name -> (restype, argtypes); every symbol declared in include/mdt_gpu.h
 SIGNATURES = {
     "mdt_create": (ct.c_int32, [ct.c_int32, ct.POINTER(ct.c_void_p)]),
@@ -70,6 +76,10 @@ SIGNATURES = {
     "mdt_nn_stats": (ct.c_int32, [ct.c_void_p, ct.c_void_p, ct.c_void_p]),
     "mdt_nn_neighbors": (ct.c_int32, [ct.c_void_p, ct.c_void_p, ct.c_void_p]),
     "mdt_nn_descriptors": (ct.c_int32, [ct.c_void_p, ct.c_int32, ct.c_void_p]),
+    "mdt_train_set_labels": (ct.c_int32, [ct.c_void_p, ct.c_void_p, ct.c_void_p]),
+    "mdt_train_step": (ct.c_int32, [ct.c_void_p, ct.POINTER(TrainOpts), ct.c_void_p, ct.c_int32, ct.c_void_p]),
+    "mdt_train_gradient": (ct.c_int32, [ct.c_void_p, ct.POINTER(TrainOpts), ct.c_void_p, ct.c_int32, ct.c_void_p]),
+    "mdt_train_commit": (ct.c_int32, [ct.c_void_p, ct.c_void_p]),
     "mdt_emt_force_noalloc": (ct.c_int32, [ct.c_int32] + [ct.c_void_p] * 5 + [ct.c_int32] + [ct.c_void_p] * 8 +
                               [ct.c_void_p] * 5 + [ct.c_void_p]),
 }

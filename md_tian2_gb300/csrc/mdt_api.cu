@@ -56,6 +56,14 @@ struct mdt_ctx {
     double margin = 0.1;
     NNScratch X{};
     int nn_maxnb_alloc = 0;
+
+    // training (buffers live with the batch)
+    bool have_labels = false;
+    double *t_E = nullptr, *t_fx = nullptr, *t_fy = nullptr, *t_fz = nullptr, *t_G = nullptr;
+    double *t_grad = nullptr, *t_loss = nullptr;
+    float *t_theta = nullptr, *t_m = nullptr, *t_v = nullptr;
+    int *t_conf = nullptr;
+    int t_step = 0;
 };
 
 namespace {
@@ -80,6 +88,7 @@ template <typename T> T *dalloc(mdt_ctx *c, size_t n, cudaError_t &e) {
 
 void free_batch(mdt_ctx *c) {
     c->X = NNScratch{};
+    c->have_labels = false;
     c->nn_maxnb_alloc = 0;
     for (auto &b : c->bufs) cudaFree(b.p);
     c->bufs.clear();
@@ -974,6 +983,125 @@ int32_t mdt_nn_descriptors(mdt_ctx *c, int32_t precision, double *G) {
             }
     }
     return MDT_OK;
+}
+
+
+int32_t mdt_train_set_labels(mdt_ctx *c, const double *energy, const double *forces) {
+    int rc = check_ready(c, false);
+    if (rc) return rc;
+    if (!energy || !forces) return fail(c, MDT_ERR_ARG, "null labels");
+    if (!c->have_nn) return fail(c, MDT_ERR_STATE, "no network installed (call mdt_nn_set_model)");
+    if (c->max_beads != 1) return fail(c, MDT_ERR_ARG, "training configurations must have one bead");
+    if (!c->M.scalesym || c->M.centersym || c->M.normnodes)
+        return fail(c, MDT_ERR_UNSUPPORTED, "training needs scale_symmetry_functions without centering/normalize_nodes");
+    if ((rc = ensure_nn_scratch(c))) return rc;
+    cudaError_t e = cudaSuccess;
+    const size_t nw = (size_t)c->M.nelem * c->M.maxweights;
+    c->t_E = dalloc<double>(c, c->T, e);
+    c->t_fx = dalloc<double>(c, c->total_ba, e);
+    c->t_fy = dalloc<double>(c, c->total_ba, e);
+    c->t_fz = dalloc<double>(c, c->total_ba, e);
+    c->t_G = dalloc<double>(c, (size_t)c->total_ba * c->M.maxsf, e);
+    c->t_grad = dalloc<double>(c, nw, e);
+    c->t_loss = dalloc<double>(c, 4, e);
+    c->t_theta = dalloc<float>(c, nw, e);
+    c->t_m = dalloc<float>(c, nw, e);
+    c->t_v = dalloc<float>(c, nw, e);
+    c->t_conf = dalloc<int>(c, c->T, e);
+    if (!c->t_E || !c->t_fx || !c->t_fy || !c->t_fz || !c->t_G || !c->t_grad || !c->t_loss || !c->t_theta ||
+        !c->t_m || !c->t_v || !c->t_conf)
+        return fail(c, MDT_ERR_NOMEM, "training buffers");
+    e = cudaMemcpyAsync(c->t_E, energy, sizeof(double) * c->T, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(c->stage, forces, sizeof(double) * 3 * c->total_ba, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = launch_unpack(c->stream, c->B, c->stage, c->t_fx, c->t_fy, c->t_fz, c->total_ba, c->ba_traj);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->t_G, 0, sizeof(double) * c->total_ba * c->M.maxsf, c->stream);
+    // raw symmetry functions and neighbour lists, computed once
+    NNScratch X = c->X;
+    X.gout = c->t_G;
+    mdt_prop_params p{};
+    p.step = 1.0;
+    const PropParams P = to_dev(c, &p);
+    if (e == cudaSuccess) e = launch_nn(nn_cfg(c, MDT_PREC_FP64), c->B, c->M, c->E, X, P, c->ngeta_max, 0, 1,
+                                        MDT_PREC_FP64, false);
+    c->launches += 2;
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(c->t_theta, c->M.wf, sizeof(float) * nw, cudaMemcpyDeviceToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->t_m, 0, sizeof(float) * nw, c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->t_v, 0, sizeof(float) * nw, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "mdt_train_set_labels");
+    c->t_step = 0;
+    c->have_labels = true;
+    return MDT_OK;
+}
+
+static int train_run(mdt_ctx *c, const mdt_train_opts *o, const int32_t *conf, int32_t n, bool update,
+                     double *stats, double *grad_out) {
+    int rc = check_ready(c, false);
+    if (rc) return rc;
+    if (!c->have_labels) return fail(c, MDT_ERR_STATE, "no training labels (call mdt_train_set_labels)");
+    if (!o || !conf || n < 1 || n > c->T) return fail(c, MDT_ERR_ARG, "bad training arguments");
+    if (o->precision != MDT_PREC_FP32 && o->precision != MDT_PREC_FP64) return fail(c, MDT_ERR_ARG, "bad precision");
+    for (int k = 0; k < n; ++k)
+        if (conf[k] < 0 || conf[k] >= c->T) return fail(c, MDT_ERR_ARG, "configuration index out of range");
+    const size_t nw = (size_t)c->M.nelem * c->M.maxweights;
+    cudaError_t e = cudaMemcpyAsync(c->t_conf, conf, sizeof(int) * n, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->t_grad, 0, sizeof(double) * nw, c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->t_loss, 0, sizeof(double) * 4, c->stream);
+    TrainArgs A{c->t_E, c->t_fx, c->t_fy, c->t_fz, c->t_G, c->t_conf, n, o->w_energy, o->w_force, c->t_theta,
+                c->t_grad, c->t_loss};
+    if (e == cudaSuccess)
+        e = launch_train(c->stream, c->num_sms, c->B, c->M, c->X, A, c->max_atoms, c->ngeta_max, c->counter,
+                         o->precision);
+    c->launches++;
+    if (update && e == cudaSuccess) {
+        ++c->t_step;
+        e = launch_adam(c->stream, c->t_theta, c->t_m, c->t_v, c->t_grad, (int)nw, 1.0 / n, o->lr, o->beta1, o->beta2,
+                        o->eps, c->t_step, nullptr);
+        c->launches++;
+    }
+    double loss[4] = {0, 0, 0, 0};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(loss, c->t_loss, sizeof(loss), cudaMemcpyDeviceToHost, c->stream);
+    std::vector<double> g;
+    if (grad_out && e == cudaSuccess) {
+        g.resize(nw);
+        e = cudaMemcpyAsync(g.data(), c->t_grad, sizeof(double) * nw, cudaMemcpyDeviceToHost, c->stream);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "training step");
+    if (stats) {
+        stats[0] = loss[3] > 0 ? loss[0] / loss[3] : 0.0;
+        stats[1] = loss[2] > 0 ? loss[1] / loss[2] : 0.0;
+        stats[2] = o->w_energy * stats[0] + o->w_force * stats[1];
+    }
+    if (grad_out)
+        for (size_t k = 0; k < nw; ++k) grad_out[k] = g[k] / n;
+    return MDT_OK;
+}
+
+int32_t mdt_train_step(mdt_ctx *c, const mdt_train_opts *opts, const int32_t *conf_ids, int32_t n, double *stats) {
+    return train_run(c, opts, conf_ids, n, true, stats, nullptr);
+}
+
+int32_t mdt_train_gradient(mdt_ctx *c, const mdt_train_opts *opts, const int32_t *conf_ids, int32_t n,
+                           double *grad) {
+    if (!grad) return c ? fail(c, MDT_ERR_ARG, "null gradient output") : MDT_ERR_ARG;
+    return train_run(c, opts, conf_ids, n, false, nullptr, grad);
+}
+
+int32_t mdt_train_commit(mdt_ctx *c, double *weights) {
+    int rc = check_ready(c, false);
+    if (rc) return rc;
+    if (!c->have_labels) return fail(c, MDT_ERR_STATE, "nothing trained");
+    const int nw = c->M.nelem * c->M.maxweights;
+    cudaError_t e = launch_weights_to_model(c->stream, c->t_theta, const_cast<float *>(c->M.wf),
+                                            const_cast<double *>(c->M.wd), nw);
+    c->launches++;
+    if (weights && e == cudaSuccess)
+        e = cudaMemcpyAsync(weights, c->M.wd, sizeof(double) * nw, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    return e == cudaSuccess ? MDT_OK : cuda_fail(c, e, "mdt_train_commit");
 }
 
 }  // extern "C"

@@ -31,6 +31,23 @@ cudaError_t launch_nn(const LaunchCfg &c, const Batch &B, const NNDev &M, const 
                       const PropParams &P, int ngeta, int nsteps, int mode, int precision, bool surrogate);
 int nn_resident_ctas(const NNDev &M, int max_atoms, int max_beads, int ngeta, int precision, bool surrogate);
 
+struct TrainArgs {
+    const double *E_ref;
+    const double *fx_ref, *fy_ref, *fz_ref;
+    const double *G;
+    const int *conf;
+    int nconf;
+    double wE, wF;
+    const float *theta;
+    double *grad;
+    double *loss;
+};
+cudaError_t launch_train(cudaStream_t s, int num_sms, const Batch &B, const NNDev &M, const NNScratch &X,
+                         const TrainArgs &A, int max_atoms, int ngeta, int *counter, int precision);
+cudaError_t launch_adam(cudaStream_t s, float *theta, float *m, float *v, const double *grad, int n, double scale,
+                        double lr, double b1, double b2, double eps, int step, const uint8_t *frozen);
+cudaError_t launch_weights_to_model(cudaStream_t s, const float *theta, float *wf, double *wd, int n);
+
 enum { kPhaseForce = 0, kPhaseProp1 = 1, kPhaseProp2 = 2, kPhaseEnergyOnly = 3 };
 
 }  // namespace mdt

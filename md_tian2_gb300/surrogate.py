@@ -1,0 +1,157 @@
+"""Learned EMT surrogate: a per-element ACSF -> MLP network trained on the GPU on
+energies and forces that the batched FP64 EMT kernels generate.
+
+* dataset: ragged H/Au(111) trajectories (the ``config2`` generator) propagated with
+  plain FP64 EMT; every ``every`` steps each trajectory contributes its positions, EMT
+  total energy and forces;
+* model: 8 G2 + 16 G3 per element (neighbour element Au, 6.5 A cosine cutoff, see
+  ``nene.acsf_set``) -> 24-32-32-1 softplus network per element (H, Au);
+* training: libmdt_gpu's fused training kernels (network forward/backward, descriptor
+  VJP for forces, descriptor JVP + forward-over-reverse sweep for the force-loss
+  gradient) and Adam on FP32 master weights;
+* use: ``PES_SURROGATE`` in the engine, with FP64 EMT as the fallback for beads whose
+  symmetry functions leave the training range.
+"""
+from __future__ import annotations
+
+import ctypes as ct
+import time
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import constants as C
+from . import nene
+from . import workloads as W
+from ._lib import TrainOpts
+from .engine import PES_EMT, PES_NENE, PES_SURROGATE, Engine, SimParams
+
+
+@dataclass
+class Dataset:
+    universes: list         # one single-bead Universe per configuration
+    energy: np.ndarray      # eV per configuration
+    forces: list            # (N, 3) eV/A per configuration
+
+
+def generate_dataset(ntraj: int = 4096, nsamples: int = 8, every: int = 50, seed: int = 7, device: int = 0,
+                     precision: str = "fp64") -> Dataset:
+    """Propagate ``ntraj`` config-2 trajectories with EMT and sample every ``every`` steps."""
+    us = W.config2(ntraj, seed=seed)
+    emt = W.emt_params()
+    sp = SimParams(step=0.1, gamma_const=1e-3, seed=seed)
+    eng = Engine(device)
+    eng.read_emt(emt)
+    eng.define(us)
+    eng.upload()
+    eng.calc_force(sp, precision=precision)
+    out_u, out_e, out_f = [], [], []
+    for s in range(nsamples):
+        eng.md_steps(every, sp, precision=precision)
+        o = eng.download()  # forces and energies of the current positions (precision given)
+        for t, u in enumerate(us):
+            r = eng.split(o["r"], t)
+            f = eng.split(o["f"], t)[:, 0, :]
+            v = W.Universe(r=r.copy(), v=np.zeros_like(r), m=u.m, idx=u.idx, is_fixed=u.is_fixed, simbox=u.simbox,
+                           names=u.names, is_proj=u.is_proj, algo=u.algo)
+            out_u.append(v)
+            out_e.append(o["epot"][eng.bead_off[t]])
+            out_f.append(f.copy())
+    eng.close()
+    return Dataset(out_u, np.array(out_e), out_f)
+
+
+def surrogate_model(seed: int = 11) -> nene.NNModel:
+    return nene.random_model(["H", "Au"], hidden=(32, 32), act="p", seed=seed, neighbours=["Au"])
+
+
+def _opts(lr, w_energy, w_force, precision):
+    return TrainOpts(w_energy, w_force, lr, 0.9, 0.999, 1e-8, 0 if precision == "fp64" else 1)
+
+
+class Trainer:
+    """Holds a training set on the GPU (one configuration per batch trajectory)."""
+
+    def __init__(self, data: Dataset, model: nene.NNModel, device: int = 0, scale_margin: float = 0.0):
+        self.data = data
+        self.model = model
+        self.eng = Engine(device)
+        self.eng.define(data.universes)
+        self.eng.upload()
+        # scaling.data from the training set's own descriptors (RuNNer's scaling mode)
+        self.eng.read_nene(model, data.universes[0].names)
+        self.eng.set_pes(PES_NENE, 0.0)
+        G = self.eng.nn_descriptors()
+        elem = np.concatenate([[model.elements.index(u.names[i - 1]) for i in u.idx] for u in data.universes])
+        nene.set_scaling(model, G, elem, margin=scale_margin)
+        self.eng.read_nene(model, data.universes[0].names)
+        self.eng.set_pes(PES_NENE, 0.0)
+        forces = np.concatenate([f.reshape(-1) for f in data.forces])
+        self.eng._check(self.eng.lib.mdt_train_set_labels(self.eng.h, np.ascontiguousarray(data.energy).ctypes.data,
+                                                          np.ascontiguousarray(forces).ctypes.data),
+                        "mdt_train_set_labels")
+        self.n = len(data.universes)
+
+    def gradient(self, conf_ids, w_energy=1.0, w_force=1.0, precision="fp64"):
+        ids = np.ascontiguousarray(conf_ids, np.int32)
+        nw = self.model.nelem * max(self.model.n_weights(e) for e in range(self.model.nelem))
+        g = np.zeros(nw)
+        o = _opts(0.0, w_energy, w_force, precision)
+        self.eng._check(self.eng.lib.mdt_train_gradient(self.eng.h, ct.byref(o), ids.ctypes.data, len(ids),
+                                                        g.ctypes.data), "mdt_train_gradient")
+        return g
+
+    def train(self, epochs: float = 10, batch: int = 256, lr: float = 2e-3, lr_final: float = 2e-4,
+              w_energy: float = 10.0, w_force: float = 1.0, seed: int = 0, time_budget: float | None = None,
+              log=None):
+        rng = np.random.default_rng(seed)
+        nsteps = max(1, int(epochs * self.n / batch))
+        stats = np.zeros(3)
+        t0 = time.perf_counter()
+        order = rng.permutation(self.n)
+        pos = 0
+        hist = []
+        for k in range(nsteps):
+            if pos + batch > self.n:
+                order = rng.permutation(self.n)
+                pos = 0
+            ids = np.ascontiguousarray(order[pos:pos + batch], np.int32)
+            pos += batch
+            frac = k / max(1, nsteps - 1)
+            o = _opts(lr * (lr_final / lr) ** frac, w_energy, w_force, "fp32")
+            self.eng._check(self.eng.lib.mdt_train_step(self.eng.h, ct.byref(o), ids.ctypes.data, len(ids),
+                                                        stats.ctypes.data), "mdt_train_step")
+            hist.append((k, float(np.sqrt(stats[0])), float(np.sqrt(stats[1]))))
+            if log and (k % 50 == 0 or k == nsteps - 1):
+                log(f"step {k}/{nsteps} energy rmse/atom {np.sqrt(stats[0]) * 1e3:.2f} meV "
+                    f"force rmse {np.sqrt(stats[1]) * 1e3:.2f} meV/A")
+            if time_budget and time.perf_counter() - t0 > time_budget:
+                break
+        self.seconds = time.perf_counter() - t0
+        self.steps = len(hist)
+        self.atoms_trained = self.steps * batch * float(np.mean([u.natoms for u in self.data.universes]))
+        w = np.zeros(self.model.nelem * max(self.model.n_weights(e) for e in range(self.model.nelem)))
+        self.eng._check(self.eng.lib.mdt_train_commit(self.eng.h, w.ctypes.data), "mdt_train_commit")
+        mw = max(self.model.n_weights(e) for e in range(self.model.nelem))
+        for e in range(self.model.nelem):
+            self.model.weights[e] = w[e * mw: e * mw + self.model.n_weights(e)].copy()
+        return hist
+
+    def close(self):
+        self.eng.close()
+
+
+def force_rmse(model: nene.NNModel, data: Dataset, device: int = 0, precision: str = "fp32") -> tuple:
+    """Force RMSE (eV/A) and per-atom energy RMSE (eV) of the network on a dataset."""
+    eng = Engine(device)
+    eng.define(data.universes)
+    eng.upload()
+    eng.read_nene(model, data.universes[0].names)
+    eng.set_pes(PES_NENE, 0.0)
+    eng.calc_force(SimParams(), precision=precision)
+    out = eng.download()
+    eng.close()
+    f = np.concatenate([fr.reshape(-1) for fr in data.forces])
+    nat = np.array([u.natoms for u in data.universes])
+    return (float(np.sqrt(np.mean((out["f"] - f) ** 2))),
+            float(np.sqrt(np.mean(((out["epot"] - data.energy) / nat) ** 2))))
