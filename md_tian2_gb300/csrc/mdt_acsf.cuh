@@ -117,6 +117,7 @@ static __device__ __forceinline__ void acsf_wrap_one(double xa, double ya, doubl
 static __device__ int acsf_neighbors_one(const NNDev &M, int i, int N, const double *px, const double *py,
                                          const double *pz, const double *L, int na, int nbi, int nc, int *out) {
     const double cut2 = __dmul_rn(M.maxcut, M.maxcut);
+    const float cut2f_hi = (float)cut2 * 1.0001f, cut2f_lo = (float)cut2 * 0.9999f;
     int cnt = 0;
     const double xi = px[i], yi = py[i], zi = pz[i];
     for (int j = 0; j < N; ++j) {
@@ -126,6 +127,21 @@ static __device__ int acsf_neighbors_one(const NNDev &M, int i, int N, const dou
                 for (int n3 = -nc; n3 <= nc; ++n3) {
                     if (n1 == 0 && n2 == 0 && n3 == 0 && i == j) continue;
                     const double d1n = n1, d2n = n2, d3n = n3;
+                    // FP32 screen; the exact FP64 test (the oracle's operation order, no
+                    // fused multiply-add) only within 1e-4 (relative) of the cutoff
+                    const float fx = (float)(xj - xi) + (float)d1n * (float)L[0] + (float)d2n * (float)L[3] +
+                                     (float)d3n * (float)L[6];
+                    const float fy = (float)(yj - yi) + (float)d1n * (float)L[1] + (float)d2n * (float)L[4] +
+                                     (float)d3n * (float)L[7];
+                    const float fz = (float)(zj - zi) + (float)d1n * (float)L[2] + (float)d2n * (float)L[5] +
+                                     (float)d3n * (float)L[8];
+                    const float rf = fx * fx + fy * fy + fz * fz;
+                    if (rf > cut2f_hi) continue;
+                    if (rf < cut2f_lo) {
+                        if (cnt < M.maxnb) out[cnt] = pack_nb(j, n1, n2, n3);
+                        ++cnt;
+                        continue;
+                    }
                     const double xt = __dadd_rn(__dadd_rn(__dadd_rn(xj, __dmul_rn(d1n, L[0])), __dmul_rn(d2n, L[3])),
                                                 __dmul_rn(d3n, L[6]));
                     const double yt = __dadd_rn(__dadd_rn(__dadd_rn(yj, __dmul_rn(d1n, L[1])), __dmul_rn(d2n, L[4])),
@@ -238,6 +254,16 @@ __device__ __forceinline__ bool g3_term(const NNDev &M, int k, const Triplet<R> 
     return true;
 }
 
+// grid-form G3 walks, defined at the end of this file
+template <typename R> __device__ void acsf_g3_forward_fast(const NNDev &M, const WarpCache<R> &C, int ei, int cnt,
+                                                           R *G);
+template <typename R>
+__device__ void acsf_g3_vjp_fast(const NNDev &M, const WarpCache<R> &C, int ei, int cnt, const R *c, R &fix, R &fiy,
+                                 R &fiz);
+template <typename R>
+__device__ void acsf_g3_jvp_fast(const NNDev &M, const WarpCache<R> &C, int ei, int cnt, int i, const R *ux,
+                                 const R *uy, const R *uz, R *v);
+
 // ---- forward ------------------------------------------------------------------------
 template <typename R> __device__ void acsf_forward(const NNDev &M, const WarpCache<R> &C, int ei, int cnt, R *G) {
     const int lane = threadIdx.x & 31;
@@ -255,6 +281,10 @@ template <typename R> __device__ void acsf_forward(const NNDev &M, const WarpCac
         }
         acc = warp_sum(acc);
         if (lane == 0) G[s] = acc;
+    }
+    if (M.g3fast[ei]) {
+        acsf_g3_forward_fast<R>(M, C, ei, cnt, G);
+        return;
     }
     const G3List g3 = g3_list(M, ei);
     R acc[kMaxG3];
@@ -313,6 +343,14 @@ __device__ void acsf_vjp(const NNDev &M, const WarpCache<R> &C, int ei, int cnt,
         fiz += fr * e[2];
     }
     __syncwarp();
+    if (M.g3fast[ei]) {
+        acsf_g3_vjp_fast<R>(M, C, ei, cnt, c, fix, fiy, fiz);
+        __syncwarp();
+        fix = warp_sum(fix);
+        fiy = warp_sum(fiy);
+        fiz = warp_sum(fiz);
+        return;
+    }
     const G3List g3 = g3_list(M, ei);
     TriWalk tw;
     tw.init(cnt, lane);
@@ -382,6 +420,10 @@ __device__ void acsf_jvp(const NNDev &M, const WarpCache<R> &C, int ei, int cnt,
         acc = warp_sum(acc);
         if (lane == 0) v[s] = acc;
     }
+    if (M.g3fast[ei]) {
+        acsf_g3_jvp_fast<R>(M, C, ei, cnt, i, ux, uy, uz, v);
+        return;
+    }
     const G3List g3 = g3_list(M, ei);
     R acc[kMaxG3];
 #pragma unroll
@@ -423,6 +465,225 @@ __device__ void acsf_jvp(const NNDev &M, const WarpCache<R> &C, int ei, int cnt,
         const R val = warp_sum(acc[u]);
         if (lane == 0) v[g3.idx[u]] = val;
     }
+    __syncwarp();
+}
+
+// ---------------------------------------------------------------------------
+// Grid form of the G3 functions (NNDev::g3fast): cells (eta slot m, (lambda, zeta)
+// slot q) share one neighbour pair; per triplet the ng exponentials and nlz angular
+// powers meet in an outer product accumulated in registers.
+// ---------------------------------------------------------------------------
+constexpr int kGM = 4, kGQ = 8;
+
+__device__ __forceinline__ bool fast_pair(const NNDev &M, int ei, int ej, int ek) {
+    const int p1 = M.g3pair[ei][0], p2 = M.g3pair[ei][1];
+    return (p1 == ej && p2 == ek) || (p2 == ej && p1 == ek);
+}
+
+// geometry of a triplet without the per-eta exponentials (computed by the caller)
+template <typename R>
+__device__ __forceinline__ bool triplet_geom(const NNDev &M, const WarpCache<R> &C, int q3, int q4, R rc,
+                                             Triplet<R> &T) {
+    T.a = C.nb + q3 * C.st;
+    T.c = C.nb + q4 * C.st;
+    if (!(T.a[3] <= rc && T.c[3] <= rc)) return false;
+    T.jx = T.a[0] - T.c[0];
+    T.jy = T.a[1] - T.c[1];
+    T.jz = T.a[2] - T.c[2];
+    T.rjk2 = T.jx * T.jx + T.jy * T.jy + T.jz * T.jz;
+    if (!(T.rjk2 <= rc * rc)) return false;
+    T.rjk = NM<R>::sq(T.rjk2);
+    cutoff_fn<R>(M, rc, T.rjk, T.fcjk, T.dfcjk);
+    T.rinv0 = R(1) / (T.a[3] * T.c[3]);
+    T.cost0 = (T.a[0] * T.c[0] + T.a[1] * T.c[1] + T.a[2] * T.c[2]) * T.rinv0;
+    T.pfc = T.a[4] * T.c[4] * T.fcjk;
+    return true;
+}
+
+template <typename R> struct GridConst {
+    R lam[kGQ], zl[kGQ], pn[kGQ], eta[kGM];
+    int zm1[kGQ];
+    int ng, nq;
+};
+
+template <typename R> __device__ __forceinline__ GridConst<R> grid_const(const NNDev &M, int ei) {
+    GridConst<R> g;
+    g.ng = M.ng3eta[ei];
+    g.nq = M.nlz[ei];
+#pragma unroll
+    for (int q = 0; q < kGQ; ++q) {
+        g.lam[q] = (R)M.lz_lam[ei][q];
+        g.zl[q] = (R)M.lz_zl[ei][q];
+        g.pn[q] = (R)M.lz_pnorm[ei][q];
+        g.zm1[q] = M.lz_zm1[ei][q];
+    }
+#pragma unroll
+    for (int m = 0; m < kGM; ++m) g.eta[m] = (R)(m < g.ng ? M.g3eta[ei][m] : 0.0);
+    return g;
+}
+
+// exp(-eta_m (r_ij^2 + r_ik^2 + r_jk^2)) for every eta slot
+template <typename R>
+__device__ __forceinline__ void grid_pexp(const GridConst<R> &g, const Triplet<R> &T, R *E) {
+#pragma unroll
+    for (int m = 0; m < kGM; ++m) E[m] = (m < g.ng) ? T.a[6 + m] * T.c[6 + m] * NM<R>::ex(-g.eta[m] * T.rjk2) : R(0);
+}
+
+template <typename R> __device__ void acsf_g3_forward_fast(const NNDev &M, const WarpCache<R> &C, int ei, int cnt,
+                                                           R *G) {
+    const int lane = threadIdx.x & 31;
+    const R rc = (R)M.rc[ei];
+    const GridConst<R> g = grid_const<R>(M, ei);
+    R acc[kGM][kGQ];
+#pragma unroll
+    for (int m = 0; m < kGM; ++m)
+#pragma unroll
+        for (int q = 0; q < kGQ; ++q) acc[m][q] = R(0);
+    TriWalk tw;
+    tw.init(cnt, lane);
+    while (tw.valid) {
+        Triplet<R> T;
+        if (fast_pair(M, ei, C.nbelem[tw.q3], C.nbelem[tw.q4]) && triplet_geom<R>(M, C, tw.q3, tw.q4, rc, T)) {
+            R E[kGM];
+            grid_pexp<R>(g, T, E);
+#pragma unroll
+            for (int m = 0; m < kGM; ++m) E[m] *= T.pfc;
+#pragma unroll
+            for (int q = 0; q < kGQ; ++q) {
+                if (q >= g.nq) break;
+                const R plam = R(1) + g.lam[q] * T.cost0;
+                if (plam <= R(0)) continue;
+                const R pw = ipow<R>(plam, g.zm1[q]) * plam;
+#pragma unroll
+                for (int m = 0; m < kGM; ++m) acc[m][q] += E[m] * pw;
+            }
+        }
+        tw.next();
+    }
+#pragma unroll
+    for (int m = 0; m < kGM; ++m)
+#pragma unroll
+        for (int q = 0; q < kGQ; ++q) {
+            if (m >= g.ng || q >= g.nq) continue;
+            const R v = warp_sum(acc[m][q]);
+            const int s = M.sf_of[ei][m][q];
+            if (lane == 0 && s >= 0) G[s] = v * g.pn[q];
+        }
+    __syncwarp();
+}
+
+// G3 part of the VJP in grid form; adds into fix/fiy/fiz and the slot forces
+template <typename R>
+__device__ void acsf_g3_vjp_fast(const NNDev &M, const WarpCache<R> &C, int ei, int cnt, const R *c, R &fix, R &fiy,
+                                 R &fiz) {
+    const int lane = threadIdx.x & 31;
+    const R rc = (R)M.rc[ei];
+    const GridConst<R> g = grid_const<R>(M, ei);
+    R Wc[kGM][kGQ];
+#pragma unroll
+    for (int m = 0; m < kGM; ++m)
+#pragma unroll
+        for (int q = 0; q < kGQ; ++q) {
+            const int s = (m < g.ng && q < g.nq) ? M.sf_of[ei][m][q] : -1;
+            Wc[m][q] = s >= 0 ? c[s] * g.pn[q] : R(0);
+        }
+    TriWalk tw;
+    tw.init(cnt, lane);
+    while (tw.valid) {
+        Triplet<R> T;
+        if (fast_pair(M, ei, C.nbelem[tw.q3], C.nbelem[tw.q4]) && triplet_geom<R>(M, C, tw.q3, tw.q4, rc, T)) {
+            R E[kGM];
+            grid_pexp<R>(g, T, E);
+            R A1 = R(0), A2 = R(0), A3 = R(0);
+#pragma unroll
+            for (int q = 0; q < kGQ; ++q) {
+                if (q >= g.nq) break;
+                const R plam = R(1) + g.lam[q] * T.cost0;
+                if (plam <= R(0)) continue;
+                const R pp = ipow<R>(plam, g.zm1[q]);
+                R S = R(0), Tq = R(0);
+#pragma unroll
+                for (int m = 0; m < kGM; ++m) {
+                    const R w = Wc[m][q] * E[m];
+                    S += w;
+                    Tq += g.eta[m] * w;
+                }
+                A1 += g.zl[q] * pp * S;
+                A2 += plam * pp * Tq;
+                A3 += plam * pp * S;
+            }
+            const R rij = T.a[3], rik = T.c[3];
+            const R P1 = T.pfc * (T.rinv0 - T.cost0 / (rij * rij)) * A1 - R(2) * T.pfc * A2 +
+                         T.c[4] * T.fcjk * T.a[5] / rij * A3;
+            const R P2 = T.pfc * (T.rinv0 - T.cost0 / (rik * rik)) * A1 - R(2) * T.pfc * A2 +
+                         T.a[4] * T.fcjk * T.c[5] / rik * A3;
+            const R P3 = T.pfc * T.rinv0 * A1 + R(2) * T.pfc * A2 - T.a[4] * T.c[4] * T.dfcjk / T.rjk * A3;
+            fix += T.a[0] * P1 + T.c[0] * P2;
+            fiy += T.a[1] * P1 + T.c[1] * P2;
+            fiz += T.a[2] * P1 + T.c[2] * P2;
+            atomicAdd(&C.slotf[3 * tw.q3], -T.a[0] * P1 + T.jx * P3);
+            atomicAdd(&C.slotf[3 * tw.q3 + 1], -T.a[1] * P1 + T.jy * P3);
+            atomicAdd(&C.slotf[3 * tw.q3 + 2], -T.a[2] * P1 + T.jz * P3);
+            atomicAdd(&C.slotf[3 * tw.q4], -T.c[0] * P2 - T.jx * P3);
+            atomicAdd(&C.slotf[3 * tw.q4 + 1], -T.c[1] * P2 - T.jy * P3);
+            atomicAdd(&C.slotf[3 * tw.q4 + 2], -T.c[2] * P2 - T.jz * P3);
+        }
+        tw.next();
+    }
+}
+
+// G3 part of the JVP in grid form; lane 0 writes v[s]
+template <typename R>
+__device__ void acsf_g3_jvp_fast(const NNDev &M, const WarpCache<R> &C, int ei, int cnt, int i, const R *ux,
+                                 const R *uy, const R *uz, R *v) {
+    const int lane = threadIdx.x & 31;
+    const R rc = (R)M.rc[ei];
+    const GridConst<R> g = grid_const<R>(M, ei);
+    const R uix = ux[i], uiy = uy[i], uiz = uz[i];
+    R acc[kGM][kGQ];
+#pragma unroll
+    for (int m = 0; m < kGM; ++m)
+#pragma unroll
+        for (int q = 0; q < kGQ; ++q) acc[m][q] = R(0);
+    TriWalk tw;
+    tw.init(cnt, lane);
+    while (tw.valid) {
+        Triplet<R> T;
+        if (fast_pair(M, ei, C.nbelem[tw.q3], C.nbelem[tw.q4]) && triplet_geom<R>(M, C, tw.q3, tw.q4, rc, T)) {
+            const int j = C.nbatom[tw.q3], kk = C.nbatom[tw.q4];
+            const R q1 = -(T.a[0] * (uix - ux[j]) + T.a[1] * (uiy - uy[j]) + T.a[2] * (uiz - uz[j]));
+            const R q2 = -(T.c[0] * (uix - ux[kk]) + T.c[1] * (uiy - uy[kk]) + T.c[2] * (uiz - uz[kk]));
+            const R q3 = T.jx * (ux[kk] - ux[j]) + T.jy * (uy[kk] - uy[j]) + T.jz * (uz[kk] - uz[j]);
+            const R rij = T.a[3], rik = T.c[3];
+            const R b1 = T.pfc * (T.rinv0 - T.cost0 / (rij * rij)), b2 = T.pfc * (T.rinv0 - T.cost0 / (rik * rik));
+            const R d1 = T.c[4] * T.fcjk * T.a[5] / rij, d2 = T.a[4] * T.fcjk * T.c[5] / rik;
+            const R d3 = T.a[4] * T.c[4] * T.dfcjk / T.rjk;
+            const R X1 = b1 * q1 + b2 * q2 + T.pfc * T.rinv0 * q3, X2 = T.pfc * (q1 + q2 - q3),
+                    X3 = d1 * q1 + d2 * q2 - d3 * q3;
+            R E[kGM];
+            grid_pexp<R>(g, T, E);
+#pragma unroll
+            for (int q = 0; q < kGQ; ++q) {
+                if (q >= g.nq) break;
+                const R plam = R(1) + g.lam[q] * T.cost0;
+                if (plam <= R(0)) continue;
+                const R base = ipow<R>(plam, g.zm1[q]) * g.pn[q];
+                const R t1 = g.zl[q] * X1 + plam * X3, t2 = R(2) * plam * X2;
+#pragma unroll
+                for (int m = 0; m < kGM; ++m) acc[m][q] -= base * E[m] * (t1 - g.eta[m] * t2);
+            }
+        }
+        tw.next();
+    }
+#pragma unroll
+    for (int m = 0; m < kGM; ++m)
+#pragma unroll
+        for (int q = 0; q < kGQ; ++q) {
+            if (m >= g.ng || q >= g.nq) continue;
+            const R val = warp_sum(acc[m][q]);
+            const int s = M.sf_of[ei][m][q];
+            if (lane == 0 && s >= 0) v[s] = val;
+        }
     __syncwarp();
 }
 

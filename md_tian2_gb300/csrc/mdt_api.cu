@@ -861,6 +861,41 @@ int32_t mdt_nn_set_model(mdt_ctx *c, const mdt_nn_model *m, int32_t ntypes, cons
         if (off > m->maxweights) return fail(c, MDT_ERR_ARG, "maxweights smaller than the network");
         M.atom_energy[e] = (m->remove_atom_energies && m->atom_energy) ? m->atom_energy[e] : 0.0;
     }
+    // grid form of the G3 functions (see NNDev::g3fast)
+    for (int e = 0; e < ne; ++e) {
+        M.g3fast[e] = 0;
+        M.nlz[e] = 0;
+        for (int m = 0; m < 4; ++m)
+            for (int q = 0; q < 8; ++q) M.sf_of[e][m][q] = -1;
+        bool ok = M.ng3eta[e] <= 4;
+        int pe1 = -2, pe2 = -2, nq = 0;
+        for (int s = 0; s < M.nsf[e] && ok; ++s) {
+            const int k = e * ms + s;
+            if (m->sftype[k] != 3) continue;
+            if (izeta[k] < 0 || izeta[k] > 31) { ok = false; break; }
+            if (pe1 == -2) { pe1 = e1[k]; pe2 = e2[k]; }
+            if (!((e1[k] == pe1 && e2[k] == pe2) || (e1[k] == pe2 && e2[k] == pe1))) { ok = false; break; }
+            int q = -1;
+            for (int r = 0; r < nq; ++r)
+                if (M.lz_lam[e][r] == (float)m->lambda[k] && M.lz_zm1[e][r] == izeta[k]) q = r;
+            if (q < 0) {
+                if (nq >= 8) { ok = false; break; }
+                q = nq++;
+                M.lz_lam[e][q] = (float)m->lambda[k];
+                M.lz_zm1[e][q] = izeta[k];
+                M.lz_zl[e][q] = (float)(m->zeta[k] * m->lambda[k]);
+                M.lz_pnorm[e][q] = (float)pnorm[k];
+            }
+            if (M.sf_of[e][etaslot[k]][q] != -1) { ok = false; break; }
+            M.sf_of[e][etaslot[k]][q] = (int8_t)s;
+        }
+        if (ok && pe1 != -2) {
+            M.g3fast[e] = 1;
+            M.nlz[e] = nq;
+            M.g3pair[e][0] = pe1;
+            M.g3pair[e][1] = pe2;
+        }
+    }
     std::vector<uint8_t> act((size_t)ne * kMaxLayers * kMaxNodes, 'l');
     for (int e = 0; e < ne; ++e)
         for (int l = 0; l < m->nlayers; ++l)

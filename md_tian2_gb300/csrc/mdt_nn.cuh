@@ -50,6 +50,15 @@ struct NNDev {
     const float *wf;              // weights, FP32 copy
     double atom_energy[kMaxElem]; // Ha
     float margin;                 // descriptor range margin (fraction of max-min) for the fallback
+    // G3 "grid" form: every G3 function of the element is one (eta slot m, (lambda,zeta)
+    // slot q) cell and all share one neighbour-element pair; then the per-triplet work
+    // is an outer product of ng exponentials with nlz angular powers held in registers.
+    int g3fast[kMaxElem];
+    int nlz[kMaxElem];
+    float lz_lam[kMaxElem][8], lz_zl[kMaxElem][8], lz_pnorm[kMaxElem][8];
+    int lz_zm1[kMaxElem][8];             // zeta - 1 (integer)
+    int8_t sf_of[kMaxElem][4][8];        // symmetry-function index of cell (m, q), -1 if none
+    int g3pair[kMaxElem][2];             // the shared neighbour-element pair
 };
 
 // ---------------------------------------------------------------------------

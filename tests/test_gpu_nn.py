@@ -79,9 +79,9 @@ def test_shipped_network_perturbed_batch(built_lib, oracle_lib):
                 assert abs(out["epot"][t] - E) < 5e-3
 
 
-def _hgraphene_model(us, seed=5):
+def _hgraphene_model(us, seed=5, neighbours=("C",)):
     """Random two-element network whose scaling comes from the GPU's own descriptors."""
-    m = nene.random_model(["H", "C"], hidden=(25, 25), act="t", seed=seed, neighbours=["C"])
+    m = nene.random_model(["H", "C"], hidden=(25, 25), act="t", seed=seed, neighbours=list(neighbours))
     eng = _engine_nn(us, m, ["H", "C"])
     G = eng.nn_descriptors()
     eng.close()
@@ -90,11 +90,14 @@ def _hgraphene_model(us, seed=5):
     return m
 
 
-def test_two_element_network_fp64(built_lib, oracle_lib):
+@pytest.mark.parametrize("neighbours", [("C",), ("H", "C")])
+def test_two_element_network_fp64(built_lib, oracle_lib, neighbours):
+    """("C",): every G3 shares one neighbour pair (grid-form kernels); ("H", "C"): G3 over
+    three neighbour pairs (general kernels)."""
     from oracle.oracle import NNOracle
     rng = np.random.default_rng(9)
     us = [W.h_on_graphene(rng, 1.0, z0=z) for z in (1.2, 1.8, 3.0)]
-    m = _hgraphene_model(us)
+    m = _hgraphene_model(us, neighbours=neighbours)
     o = NNOracle(m)
     eng = _engine_nn(us, m, ["H", "C"])
     eng.calc_force(SimParams())
