@@ -63,6 +63,50 @@ struct TriWalk {
     }
 };
 
+// Balanced row walk over the same triangle: lane L owns the row pairs (r, nrows-1-r)
+// for r = L, L+32, ...; each pair holds cnt pairs (q3, q4) in total, so every lane runs
+// the same number of iterations, and because a lane keeps its row q3 for many
+// iterations, the q3 side of a triplet can be accumulated in registers (flushed when
+// the row changes) while the q4 sides of the 32 lanes are distinct atoms.
+struct RowWalk {
+    int cnt, nrows, p, it, len0, q3, q4;
+    bool valid, row_end;  // row_end: q3 changes after this triplet
+    __device__ __forceinline__ void init(int c, int lane) {
+        cnt = c;
+        nrows = c - 1;
+        p = lane;
+        start();
+    }
+    __device__ __forceinline__ void start() {
+        it = 0;
+        const int npairs = (nrows + 1) / 2;
+        valid = p < npairs;
+        if (!valid) return;
+        len0 = nrows - p;  // row p holds q4 = p+1 .. cnt-1
+        set();
+    }
+    __device__ __forceinline__ int total() const { return (nrows - 1 - p == p) ? len0 : cnt; }
+    __device__ __forceinline__ void set() {
+        if (it < len0) {
+            q3 = p;
+            q4 = p + 1 + it;
+        } else {
+            q3 = nrows - 1 - p;
+            q4 = q3 + 1 + (it - len0);
+        }
+        row_end = (it == len0 - 1) || (it == total() - 1);
+    }
+    __device__ __forceinline__ void next() {
+        ++it;
+        if (it >= total()) {
+            p += 32;
+            start();
+            return;
+        }
+        set();
+    }
+};
+
 __device__ __forceinline__ int pack_nb(int j, int n1, int n2, int n3) {
     return j | ((n1 + 8) << 16) | ((n2 + 8) << 20) | ((n3 + 8) << 24);
 }
@@ -503,8 +547,36 @@ __device__ __forceinline__ bool triplet_geom(const NNDev &M, const WarpCache<R> 
 template <typename R> struct GridConst {
     R lam[kGQ], zl[kGQ], pn[kGQ], eta[kGM];
     int zm1[kGQ];
-    int ng, nq;
+    int lidx[kGQ];   // which distinct lambda (0/1) the cell uses
+    R lams[2];
+    int ng, nq, nl;
 };
+
+// (1 + lambda cos) for the (at most two) distinct lambdas and its squaring ladder
+// p, p^2, p^4, p^8, p^16, from which every integer power up to 31 is a product.
+template <typename R> struct Ladder {
+    R pw[2][5];
+    bool pos[2];
+};
+
+template <typename R>
+__device__ __forceinline__ void ladder_make(const GridConst<R> &g, R cost, Ladder<R> &L) {
+#pragma unroll
+    for (int l = 0; l < 2; ++l) {
+        const R p = R(1) + g.lams[l] * cost;
+        L.pos[l] = (l < g.nl) && (p > R(0));
+        L.pw[l][0] = p;
+#pragma unroll
+        for (int b = 1; b < 5; ++b) L.pw[l][b] = L.pw[l][b - 1] * L.pw[l][b - 1];
+    }
+}
+
+template <typename R> __device__ __forceinline__ R ladder_pow(const Ladder<R> &L, int l, int e) {
+    R r = R(1);
+#pragma unroll
+    for (int b = 0; b < 5; ++b) r *= ((e >> b) & 1) ? L.pw[l][b] : R(1);
+    return r;
+}
 
 template <typename R> __device__ __forceinline__ GridConst<R> grid_const(const NNDev &M, int ei) {
     GridConst<R> g;
@@ -519,6 +591,16 @@ template <typename R> __device__ __forceinline__ GridConst<R> grid_const(const N
     }
 #pragma unroll
     for (int m = 0; m < kGM; ++m) g.eta[m] = (R)(m < g.ng ? M.g3eta[ei][m] : 0.0);
+    g.nl = 0;
+    g.lams[0] = g.lams[1] = R(0);
+#pragma unroll
+    for (int q = 0; q < kGQ; ++q) {
+        g.lidx[q] = 0;
+        if (q >= g.nq) continue;
+        if (g.nl > 0 && g.lams[0] == g.lam[q]) g.lidx[q] = 0;
+        else if (g.nl > 1 && g.lams[1] == g.lam[q]) g.lidx[q] = 1;
+        else if (g.nl < 2) { g.lams[g.nl] = g.lam[q]; g.lidx[q] = g.nl; ++g.nl; }
+    }
     return g;
 }
 
@@ -539,7 +621,7 @@ template <typename R> __device__ void acsf_g3_forward_fast(const NNDev &M, const
     for (int m = 0; m < kGM; ++m)
 #pragma unroll
         for (int q = 0; q < kGQ; ++q) acc[m][q] = R(0);
-    TriWalk tw;
+    RowWalk tw;
     tw.init(cnt, lane);
     while (tw.valid) {
         Triplet<R> T;
@@ -548,12 +630,14 @@ template <typename R> __device__ void acsf_g3_forward_fast(const NNDev &M, const
             grid_pexp<R>(g, T, E);
 #pragma unroll
             for (int m = 0; m < kGM; ++m) E[m] *= T.pfc;
+            Ladder<R> L;
+            ladder_make<R>(g, T.cost0, L);
 #pragma unroll
             for (int q = 0; q < kGQ; ++q) {
                 if (q >= g.nq) break;
-                const R plam = R(1) + g.lam[q] * T.cost0;
-                if (plam <= R(0)) continue;
-                const R pw = ipow<R>(plam, g.zm1[q]) * plam;
+                const int l = g.lidx[q];
+                if (!L.pos[l]) continue;
+                const R pw = ladder_pow<R>(L, l, g.zm1[q]) * L.pw[l][0];
 #pragma unroll
                 for (int m = 0; m < kGM; ++m) acc[m][q] += E[m] * pw;
             }
@@ -587,20 +671,24 @@ __device__ void acsf_g3_vjp_fast(const NNDev &M, const WarpCache<R> &C, int ei, 
             const int s = (m < g.ng && q < g.nq) ? M.sf_of[ei][m][q] : -1;
             Wc[m][q] = s >= 0 ? c[s] * g.pn[q] : R(0);
         }
-    TriWalk tw;
+    R sjx = R(0), sjy = R(0), sjz = R(0);  // force on the current row's neighbour q3
+    RowWalk tw;
     tw.init(cnt, lane);
     while (tw.valid) {
         Triplet<R> T;
         if (fast_pair(M, ei, C.nbelem[tw.q3], C.nbelem[tw.q4]) && triplet_geom<R>(M, C, tw.q3, tw.q4, rc, T)) {
             R E[kGM];
             grid_pexp<R>(g, T, E);
+            Ladder<R> L;
+            ladder_make<R>(g, T.cost0, L);
             R A1 = R(0), A2 = R(0), A3 = R(0);
 #pragma unroll
             for (int q = 0; q < kGQ; ++q) {
                 if (q >= g.nq) break;
-                const R plam = R(1) + g.lam[q] * T.cost0;
-                if (plam <= R(0)) continue;
-                const R pp = ipow<R>(plam, g.zm1[q]);
+                const int l = g.lidx[q];
+                if (!L.pos[l]) continue;
+                const R plam = L.pw[l][0];
+                const R pp = ladder_pow<R>(L, l, g.zm1[q]);
                 R S = R(0), Tq = R(0);
 #pragma unroll
                 for (int m = 0; m < kGM; ++m) {
@@ -621,12 +709,18 @@ __device__ void acsf_g3_vjp_fast(const NNDev &M, const WarpCache<R> &C, int ei, 
             fix += T.a[0] * P1 + T.c[0] * P2;
             fiy += T.a[1] * P1 + T.c[1] * P2;
             fiz += T.a[2] * P1 + T.c[2] * P2;
-            atomicAdd(&C.slotf[3 * tw.q3], -T.a[0] * P1 + T.jx * P3);
-            atomicAdd(&C.slotf[3 * tw.q3 + 1], -T.a[1] * P1 + T.jy * P3);
-            atomicAdd(&C.slotf[3 * tw.q3 + 2], -T.a[2] * P1 + T.jz * P3);
+            sjx += -T.a[0] * P1 + T.jx * P3;
+            sjy += -T.a[1] * P1 + T.jy * P3;
+            sjz += -T.a[2] * P1 + T.jz * P3;
             atomicAdd(&C.slotf[3 * tw.q4], -T.c[0] * P2 - T.jx * P3);
             atomicAdd(&C.slotf[3 * tw.q4 + 1], -T.c[1] * P2 - T.jy * P3);
             atomicAdd(&C.slotf[3 * tw.q4 + 2], -T.c[2] * P2 - T.jz * P3);
+        }
+        if (tw.row_end) {
+            atomicAdd(&C.slotf[3 * tw.q3], sjx);
+            atomicAdd(&C.slotf[3 * tw.q3 + 1], sjy);
+            atomicAdd(&C.slotf[3 * tw.q3 + 2], sjz);
+            sjx = sjy = sjz = R(0);
         }
         tw.next();
     }
@@ -645,7 +739,7 @@ __device__ void acsf_g3_jvp_fast(const NNDev &M, const WarpCache<R> &C, int ei, 
     for (int m = 0; m < kGM; ++m)
 #pragma unroll
         for (int q = 0; q < kGQ; ++q) acc[m][q] = R(0);
-    TriWalk tw;
+    RowWalk tw;
     tw.init(cnt, lane);
     while (tw.valid) {
         Triplet<R> T;
@@ -662,12 +756,15 @@ __device__ void acsf_g3_jvp_fast(const NNDev &M, const WarpCache<R> &C, int ei, 
                     X3 = d1 * q1 + d2 * q2 - d3 * q3;
             R E[kGM];
             grid_pexp<R>(g, T, E);
+            Ladder<R> L;
+            ladder_make<R>(g, T.cost0, L);
 #pragma unroll
             for (int q = 0; q < kGQ; ++q) {
                 if (q >= g.nq) break;
-                const R plam = R(1) + g.lam[q] * T.cost0;
-                if (plam <= R(0)) continue;
-                const R base = ipow<R>(plam, g.zm1[q]) * g.pn[q];
+                const int l = g.lidx[q];
+                if (!L.pos[l]) continue;
+                const R plam = L.pw[l][0];
+                const R base = ladder_pow<R>(L, l, g.zm1[q]) * g.pn[q];
                 const R t1 = g.zl[q] * X1 + plam * X3, t2 = R(2) * plam * X2;
 #pragma unroll
                 for (int m = 0; m < kGM; ++m) acc[m][q] -= base * E[m] * (t1 - g.eta[m] * t2);

@@ -80,8 +80,24 @@ def test_shipped_network_perturbed_batch(built_lib, oracle_lib):
 
 
 def _hgraphene_model(us, seed=5, neighbours=("C",)):
-    """Random two-element network whose scaling comes from the GPU's own descriptors."""
+    """Random two-element network whose scaling comes from the GPU's own descriptors.
+    With both H and C as neighbours the G3 set is cut to 24 functions over two neighbour
+    pairs, which exercises the general (non-grid) G3 kernels."""
     m = nene.random_model(["H", "C"], hidden=(25, 25), act="t", seed=seed, neighbours=list(neighbours))
+    if len(neighbours) > 1:
+        rng = np.random.default_rng(seed)
+        for e in range(m.nelem):
+            sfs = [sf for sf in m.sfs[e] if sf.type == 2 or ((sf.e1, sf.e2) in ((1, 6), (6, 6)) and sf.zeta != 16.0)]
+            m.sfs[e] = sfs
+            n = m.nodes[e]
+            n[0] = len(sfs)
+            w = []
+            for l in range(1, len(n)):
+                lim = np.sqrt(6.0 / (n[l - 1] + n[l]))
+                w.extend(rng.uniform(-lim, lim, size=n[l - 1] * n[l]))
+                w.extend(np.zeros(n[l]))
+            m.weights[e] = np.array(w)
+            m.smin[e], m.smax[e], m.savg[e] = np.zeros(len(sfs)), np.ones(len(sfs)), np.zeros(len(sfs))
     eng = _engine_nn(us, m, ["H", "C"])
     G = eng.nn_descriptors()
     eng.close()
