@@ -126,6 +126,12 @@ module mdt_gpu
             real(c_double), value :: range_margin
         end function
 
+        integer(c_int32_t) function mdt_nn_fast_path(ctx, enable) bind(C, name="mdt_nn_fast_path")
+            import :: c_int32_t, c_ptr
+            type(c_ptr), value :: ctx
+            integer(c_int32_t), value :: enable
+        end function
+
     end interface
 
 contains

@@ -135,6 +135,14 @@ int32_t mdt_nn_set_model(mdt_ctx *ctx, const mdt_nn_model *model, int32_t ntypes
    [min - margin*(max-min), max + margin*(max-min)] is evaluated with FP64 EMT instead). */
 int32_t mdt_set_pes(mdt_ctx *ctx, int32_t pes_kind, double range_margin);
 
+/* FP32 network evaluations use a dedicated fast kernel when the model qualifies (G2 and
+   narrow G3 only, one cosine cutoff shared by all functions, G3 of each element over one
+   neighbour-element pair with lambda = +-1 and zeta in {1, 4, 16}, at most 4 G3 eta
+   values, max_neighbors <= 255); results equal the generic kernels within FP32
+   rounding.  enable = 0 forces the generic kernels.  Returns 1 if the installed model
+   qualifies, else 0 (no replacement in the reference: RuNNer has one code path). */
+int32_t mdt_nn_fast_path(mdt_ctx *ctx, int32_t enable);
+
 /* per trajectory: number of bead evaluations that fell back to EMT, and 1 if a
    neighbour list overflowed max_neighbors (either may be NULL) */
 int32_t mdt_nn_stats(mdt_ctx *ctx, int32_t *fallbacks, int32_t *overflow);

@@ -56,6 +56,12 @@ struct mdt_ctx {
     double margin = 0.1;
     NNScratch X{};
     int nn_maxnb_alloc = 0;
+    // FP32 fast path (mdt_nnf.cu): tables, host copies of the scaling data, switch
+    FastNN F{};
+    bool fast_enabled = true;
+    std::vector<double> h_smin, h_smax, h_savg;
+    float4 *d_scal = nullptr;
+    float *d_dscal = nullptr;
 
     // training (buffers live with the batch)
     bool have_labels = false;
@@ -239,6 +245,123 @@ int ensure_nn_scratch(mdt_ctx *c) {
 LaunchCfg nn_cfg(mdt_ctx *c, int precision) {
     const int per_sm = nn_resident_ctas(c->M, c->max_atoms, c->max_beads, c->ngeta_max, precision,
                                         c->pes_kind == MDT_PES_SURROGATE);
+    const int grid = std::max(1, std::min(c->T, c->num_sms * per_sm));
+    return LaunchCfg{c->stream, grid, c->order, c->counter};
+}
+
+// Scaling of the fast path in FP32: scaled = x g + y, range flag outside [z, w], and the
+// factor RuNNer applies to dG/dx (getshortatomic.f90:174-236).
+int upload_fast_scaling(mdt_ctx *c) {
+    if (!c->F.ok || !c->d_scal) return MDT_OK;
+    const NNDev &M = c->M;
+    const size_t n = (size_t)M.nelem * M.maxsf;
+    std::vector<float4> sc(n, make_float4(1.f, 0.f, -INFINITY, INFINITY));
+    std::vector<float> ds(n, 1.f);
+    for (int e = 0; e < M.nelem; ++e)
+        for (int s = 0; s < M.nsf[e]; ++s) {
+            const size_t k = (size_t)e * M.maxsf + s;
+            const double mn = c->h_smin[k], mx = c->h_smax[k], avg = c->h_savg[k], w = mx - mn;
+            double a = 1.0, b = 0.0;
+            if (M.centersym && !M.scalesym) b = -avg;
+            else if (M.scalesym && !M.centersym) { a = (M.scmax - M.scmin) / w; b = M.scmin - mn * a; }
+            else if (M.scalesym && M.centersym) { a = 1.0 / w; b = -avg / w; }
+            sc[k] = make_float4((float)a, (float)b, (float)(mn - c->margin * w), (float)(mx + c->margin * w));
+            ds[k] = M.scalesym ? (float)((M.scmax - M.scmin) / w) : 1.f;
+        }
+    cudaError_t e = cudaMemcpy(c->d_scal, sc.data(), sizeof(float4) * n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(c->d_dscal, ds.data(), sizeof(float) * n, cudaMemcpyHostToDevice);
+    return e == cudaSuccess ? MDT_OK : cuda_fail(c, e, "fast-path scaling upload");
+}
+
+// FastNN tables of a model (FastNN::ok = 0 when it does not qualify).
+FastNN build_fast(const NNDev &M, const mdt_nn_model *m, const std::vector<int> &e1, const std::vector<int> &etaslot) {
+    FastNN F{};
+    F.ok = 0;
+    if (M.cutoff_type != 1 || M.cutoff_alpha != 0.0 || M.maxnb > 255) return F;
+    const int ms = M.maxsf;
+    int zm = 0, ng = 1;
+    for (int e = 0; e < M.nelem; ++e) {
+        if (M.rc[e] != M.maxcut) return F;
+        int n2 = 0, n3 = 0;
+        for (int s = 0; s < M.nsf[e]; ++s) {
+            const int k = e * ms + s;
+            if (m->sftype[k] == 2) {
+                ++n2;
+                continue;
+            }
+            ++n3;
+            const double z = m->zeta[k];
+            int b = -1;
+            for (int t = 0; t < 5; ++t)
+                if (z == (double)(1 << t)) b = t;
+            if (b < 0 || (m->lambda[k] != 1.0 && m->lambda[k] != -1.0)) return F;
+            zm |= 1 << b;
+        }
+        if (n2 > kFMaxG2 || (n3 > 0 && !M.g3fast[e]) || M.ng3eta[e] > 4) return F;
+        ng = std::max(ng, M.ng3eta[e]);
+    }
+    const int zs = nnf_zm_supported(zm);
+    if (!zs) return F;
+    F.zm = zs;
+    F.ng = ng;
+    int bit_index[5], nz = 0;
+    for (int b = 0; b < 5; ++b) bit_index[b] = (zs >> b) & 1 ? nz++ : -1;
+    for (int b = 0; b < 5; ++b)
+        if (bit_index[b] >= 0) {
+            F.cell_lz[2 * bit_index[b]] = (float)(1 << b);
+            F.cell_lz[2 * bit_index[b] + 1] = -(float)(1 << b);
+        }
+    const double rc = M.maxcut;
+    F.rc2 = (float)(rc * rc);
+    F.inv_rc2 = (float)(1.0 / (rc * rc));
+    const double cut2 = rc * rc;
+    F.cut2_hi = (float)cut2 * 1.0001f;
+    F.cut2_lo = (float)cut2 * 0.9999f;
+    const double log2e = 1.4426950408889634;
+    for (int e = 0; e < M.nelem; ++e) {
+        for (int a = 0; a < 4; ++a)
+            for (int q = 0; q < kFNQ; ++q) F.cell_sf[e][a][q] = -1;
+        for (int a = 0; a < 4; ++a) {
+            F.g3eta[e][a] = a < M.ng3eta[e] ? (float)M.g3eta[e][a] : 0.f;
+            F.g3l2[e][a] = a < M.ng3eta[e] ? (float)(-M.g3eta[e][a] * log2e) : 0.f;
+        }
+        F.hasg3[e] = 0;
+        F.pair_a[e] = F.pair_b[e] = -1;
+        F.ng2[e] = 0;
+        for (int s = 0; s < M.nsf[e]; ++s) {
+            const int k = e * ms + s;
+            if (m->sftype[k] == 2) {
+                const int g = F.ng2[e]++;
+                F.g2eta[e][g] = (float)m->eta[k];
+                F.g2l2[e][g] = (float)(-m->eta[k] * log2e);
+                F.g2rs[e][g] = (float)m->rshift[k];
+                F.g2e[e][g] = (int8_t)e1[k];
+                F.g2sf[e][g] = (int8_t)s;
+                continue;
+            }
+            int b = 0;
+            while ((double)(1 << b) != m->zeta[k]) ++b;
+            const int q = 2 * bit_index[b] + (m->lambda[k] < 0.0 ? 1 : 0);
+            F.cell_sf[e][etaslot[k]][q] = (int8_t)s;
+            F.hasg3[e] = 1;
+            F.pair_a[e] = M.g3pair[e][0];
+            F.pair_b[e] = M.g3pair[e][1];
+        }
+    }
+    F.ok = 1;
+    return F;
+}
+
+bool use_fast(mdt_ctx *c, int precision) {
+    if (precision != MDT_PREC_FP32 || !c->F.ok || !c->fast_enabled) return false;
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    return nnf_total_smem(c->B, c->M) <= (size_t)optin;
+}
+
+LaunchCfg nnf_cfg(mdt_ctx *c) {
+    const int per_sm = nnf_resident_ctas(c->B, c->M, c->F);
     const int grid = std::max(1, std::min(c->T, c->num_sms * per_sm));
     return LaunchCfg{c->stream, grid, c->order, c->counter};
 }
@@ -680,8 +803,12 @@ int32_t mdt_calc_force(mdt_ctx *c, int32_t flag, int32_t precision, const mdt_pr
         if ((rc = check_nn_ready(c))) return rc;
         if (c->pes_kind == MDT_PES_SURROGATE && (rc = ensure_scratch(c, MDT_PREC_FP64))) return rc;
         const PropParams P = to_dev(c, p);
-        cudaError_t e = launch_nn(nn_cfg(c, precision), c->B, c->M, c->E, c->X, P, c->ngeta_max, 0,
-                                  flag == MDT_ENERGY_ONLY ? 1 : 0, precision, c->pes_kind == MDT_PES_SURROGATE);
+        const bool surr = c->pes_kind == MDT_PES_SURROGATE;
+        cudaError_t e = use_fast(c, precision)
+                            ? launch_nnf(nnf_cfg(c), c->B, c->M, c->F, c->E, c->X, P, 0,
+                                         flag == MDT_ENERGY_ONLY ? 1 : 0, surr)
+                            : launch_nn(nn_cfg(c, precision), c->B, c->M, c->E, c->X, P, c->ngeta_max, 0,
+                                        flag == MDT_ENERGY_ONLY ? 1 : 0, precision, surr);
         c->launches++;
         return e == cudaSuccess ? MDT_OK : cuda_fail(c, e, "mdt_calc_force (network)");
     }
@@ -725,8 +852,11 @@ int32_t mdt_md_steps(mdt_ctx *c, int32_t nsteps, int32_t precision, const mdt_pr
         if (c->pes_kind == MDT_PES_SURROGATE && (rc = ensure_scratch(c, MDT_PREC_FP64))) return rc;
         if (nsteps == 0) return MDT_OK;
         const PropParams P = to_dev(c, p);
-        cudaError_t e = launch_nn(nn_cfg(c, precision), c->B, c->M, c->E, c->X, P, c->ngeta_max, nsteps, 2,
-                                  precision, c->pes_kind == MDT_PES_SURROGATE);
+        const bool surr = c->pes_kind == MDT_PES_SURROGATE;
+        cudaError_t e = use_fast(c, precision)
+                            ? launch_nnf(nnf_cfg(c), c->B, c->M, c->F, c->E, c->X, P, nsteps, 2, surr)
+                            : launch_nn(nn_cfg(c, precision), c->B, c->M, c->E, c->X, P, c->ngeta_max, nsteps, 2,
+                                        precision, surr);
         c->launches++;
         return e == cudaSuccess ? MDT_OK : cuda_fail(c, e, "mdt_md_steps (network)");
     }
@@ -936,13 +1066,25 @@ int32_t mdt_nn_set_model(mdt_ctx *c, const mdt_nn_model *m, int32_t ntypes, cons
     M.act = (const uint8_t *)up(act.data(), act.size());
     M.wd = (const double *)up(m->weights, 8 * (size_t)ne * m->maxweights);
     M.wf = (const float *)up(wf.data(), 4 * wf.size());
+    FastNN F = build_fast(M, m, e1, etaslot);
+    if (F.ok) {
+        std::vector<float> zeros(5 * nk, 0.f);
+        F.scal = (const float4 *)up(zeros.data(), 16 * nk);
+        F.dscal = (const float *)up(zeros.data(), 4 * nk);
+    }
     if (e != cudaSuccess) return cuda_fail(c, e, "mdt_nn_set_model upload");
+    c->F = F;
+    c->d_scal = (float4 *)F.scal;
+    c->d_dscal = (float *)F.dscal;
+    c->h_smin.assign(m->smin, m->smin + nk);
+    c->h_smax.assign(m->smax, m->smax + nk);
+    c->h_savg.assign(m->savg, m->savg + nk);
     c->M = M;
     c->ngeta_max = ngmax;
     c->have_nn = true;
     c->X = NNScratch{};  // re-allocated for the new neighbour bound on next use
     c->nn_maxnb_alloc = 0;
-    return MDT_OK;
+    return upload_fast_scaling(c);
 }
 
 int32_t mdt_set_pes(mdt_ctx *c, int32_t pes_kind, double range_margin) {
@@ -953,7 +1095,13 @@ int32_t mdt_set_pes(mdt_ctx *c, int32_t pes_kind, double range_margin) {
     c->pes_kind = pes_kind;
     c->margin = range_margin;
     c->M.margin = (float)range_margin;
-    return MDT_OK;
+    return c->have_nn ? upload_fast_scaling(c) : MDT_OK;
+}
+
+int32_t mdt_nn_fast_path(mdt_ctx *c, int32_t enable) {
+    if (!c) return MDT_ERR_ARG;
+    c->fast_enabled = enable != 0;
+    return c->have_nn && c->F.ok ? 1 : 0;
 }
 
 int32_t mdt_nn_stats(mdt_ctx *c, int32_t *fallbacks, int32_t *overflow) {

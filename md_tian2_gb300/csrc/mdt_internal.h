@@ -31,6 +31,13 @@ cudaError_t launch_nn(const LaunchCfg &c, const Batch &B, const NNDev &M, const 
                       const PropParams &P, int ngeta, int nsteps, int mode, int precision, bool surrogate);
 int nn_resident_ctas(const NNDev &M, int max_atoms, int max_beads, int ngeta, int precision, bool surrogate);
 
+// FP32 fast path (mdt_nnf.cu)
+int nnf_zm_supported(int zm);
+size_t nnf_total_smem(const Batch &B, const NNDev &M);
+int nnf_resident_ctas(const Batch &B, const NNDev &M, const FastNN &F);
+cudaError_t launch_nnf(const LaunchCfg &c, const Batch &B, const NNDev &M, const FastNN &F, const EmtConst &E,
+                       const NNScratch &X, const PropParams &P, int nsteps, int mode, bool surrogate);
+
 struct TrainArgs {
     const double *E_ref;
     const double *fx_ref, *fy_ref, *fz_ref;

@@ -62,6 +62,33 @@ struct NNDev {
 };
 
 // ---------------------------------------------------------------------------
+// FP32 fast path (mdt_nnf.cu).  Applies when every symmetry function is a radial G2
+// or a narrow angular G3 with one cosine cutoff (alpha = 0) shared by all functions,
+// and the G3 functions of each element form a grid of eta slots x (lambda = +-1,
+// zeta = 2^b) cells over one neighbour-element pair.
+// ---------------------------------------------------------------------------
+constexpr int kFMaxG2 = 16;  // radial functions per element
+constexpr int kFNQ = 8;      // (lambda, zeta) cells: lambda = +-1 for up to 4 zeta values
+
+struct FastNN {
+    int ok;                        // model qualifies
+    int ng, zm;                    // eta slots; zeta mask (bit b set: zeta = 2^b is used)
+    float rc2, inv_rc2;            // bohr^-2
+    float cut2_hi, cut2_lo;        // FP32 screen of the neighbour list (bohr^2)
+    int hasg3[kMaxElem];
+    int pair_a[kMaxElem], pair_b[kMaxElem];  // G3 neighbour-element pair (element indices)
+    float g3l2[kMaxElem][4];       // -eta_m log2(e), for exp2
+    float g3eta[kMaxElem][4];      // eta_m
+    int8_t cell_sf[kMaxElem][4][kFNQ];  // SF index of cell (m, 2k + [lambda < 0]), -1 if none
+    float cell_lz[kFNQ];           // lambda zeta of cell q
+    int ng2[kMaxElem];
+    float g2l2[kMaxElem][kFMaxG2], g2eta[kMaxElem][kFMaxG2], g2rs[kMaxElem][kFMaxG2];
+    int8_t g2e[kMaxElem][kFMaxG2], g2sf[kMaxElem][kFMaxG2];
+    const float4 *scal;            // [e*maxsf + s]: scaled = x g + y; outside [z, w] raises the flag
+    const float *dscal;            // [e*maxsf + s]: d(scaled)/dG as RuNNer applies it
+};
+
+// ---------------------------------------------------------------------------
 // Host-visible launch parameters of the NN kernels
 // ---------------------------------------------------------------------------
 struct NNScratch {

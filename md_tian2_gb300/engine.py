@@ -113,6 +113,13 @@ class Engine:
     def set_pes(self, kind: int, range_margin: float = 0.1) -> None:
         self._check(self.lib.mdt_set_pes(self.h, kind, range_margin), "mdt_set_pes")
 
+    def nn_fast_path(self, enable: bool = True) -> bool:
+        """Allow (default) or forbid the FP32 fast kernels; True if the model qualifies."""
+        r = self.lib.mdt_nn_fast_path(self.h, 1 if enable else 0)
+        if r < 0:
+            self._check(r, "mdt_nn_fast_path")
+        return bool(r)
+
     def nn_stats(self):
         fb = np.zeros(self.T, np.int32)
         ov = np.zeros(self.T, np.int32)
