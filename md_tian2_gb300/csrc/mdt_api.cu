@@ -62,6 +62,8 @@ struct mdt_ctx {
     std::vector<double> h_smin, h_smax, h_savg;
     float4 *d_scal = nullptr;
     float *d_dscal = nullptr;
+    unsigned *mscr = nullptr;  // fast-path mask scratch (grows on demand)
+    size_t mscr_n = 0;
 
     // training (buffers live with the batch)
     bool have_labels = false;
@@ -274,8 +276,10 @@ int upload_fast_scaling(mdt_ctx *c) {
 }
 
 // FastNN tables of a model (FastNN::ok = 0 when it does not qualify).
-FastNN build_fast(const NNDev &M, const mdt_nn_model *m, const std::vector<int> &e1, const std::vector<int> &etaslot) {
+FastNN build_fast(const NNDev &M, const mdt_nn_model *m, const std::vector<int> &e1, const std::vector<int> &etaslot,
+                  std::vector<float4> &g2tab) {
     FastNN F{};
+    g2tab.assign((size_t)kMaxElem * kFMaxG2, make_float4(0.f, 0.f, 0.f, 0.f));
     F.ok = 0;
     if (M.cutoff_type != 1 || M.cutoff_alpha != 0.0 || M.maxnb > 255) return F;
     const int ms = M.maxsf;
@@ -331,12 +335,7 @@ FastNN build_fast(const NNDev &M, const mdt_nn_model *m, const std::vector<int> 
         for (int s = 0; s < M.nsf[e]; ++s) {
             const int k = e * ms + s;
             if (m->sftype[k] == 2) {
-                const int g = F.ng2[e]++;
-                F.g2eta[e][g] = (float)m->eta[k];
-                F.g2l2[e][g] = (float)(-m->eta[k] * log2e);
-                F.g2rs[e][g] = (float)m->rshift[k];
-                F.g2e[e][g] = (int8_t)e1[k];
-                F.g2sf[e][g] = (int8_t)s;
+                ++F.ng2[e];
                 continue;
             }
             int b = 0;
@@ -348,6 +347,52 @@ FastNN build_fast(const NNDev &M, const mdt_nn_model *m, const std::vector<int> 
             F.pair_b[e] = M.g3pair[e][1];
         }
     }
+    // radial functions grouped by neighbour element, ascending eta (then r_s)
+    for (int e = 0; e < M.nelem; ++e) {
+        int pos = 0;
+        for (int a = 0; a < M.nelem; ++a) {
+            std::vector<int> idx;
+            for (int s = 0; s < M.nsf[e]; ++s) {
+                const int k = e * ms + s;
+                if (m->sftype[k] == 2 && e1[k] == a) idx.push_back(s);
+            }
+            std::stable_sort(idx.begin(), idx.end(), [&](int x, int y) {
+                const double ex = m->eta[e * ms + x], ey = m->eta[e * ms + y];
+                return ex != ey ? ex < ey : m->rshift[e * ms + x] < m->rshift[e * ms + y];
+            });
+            F.g2beg[e][a] = pos;
+            F.g2cnt[e][a] = (int)idx.size();
+            int chain = 0;
+            bool centred = true;
+            for (int s : idx) centred = centred && m->rshift[e * ms + s] == 0.0;
+            for (int S = 1; S <= 4 && centred && chain == 0; ++S) {
+                bool ok = (int)idx.size() > S;
+                for (size_t q = S; q < idx.size() && ok; ++q)
+                    ok = m->eta[e * ms + idx[q]] == 2.0 * m->eta[e * ms + idx[q - S]];
+                if (ok) chain = S;
+            }
+            F.g2chain[e][a] = chain;
+            for (int s : idx) {
+                const int k = e * ms + s;
+                float4 v = make_float4((float)(-m->eta[k] * log2e), (float)m->rshift[k], (float)(-2.0 * m->eta[k]), 0.f);
+                std::memcpy(&v.w, &s, 4);
+                g2tab[e * kFMaxG2 + pos++] = v;
+            }
+        }
+    }
+    F.anyg3 = 0;
+    for (int e = 0; e < M.nelem; ++e) F.anyg3 |= F.hasg3[e];
+    // shared-memory weight layout: rows padded to a stride = 4 (mod 8) floats
+    int off = 0;
+    for (int e = 0; e < M.nelem; ++e)
+        for (int l = 1; l <= M.nlayers; ++l) {
+            int str = (M.nodes[e][l] + 3) & ~3;
+            if (str % 8 == 0) str += 4;
+            F.wstr[e][l] = str;
+            F.wofs[e][l] = off;
+            off += (M.nodes[e][l - 1] + 1) * str;
+        }
+    F.wtotal = off;
     F.ok = 1;
     return F;
 }
@@ -357,13 +402,32 @@ bool use_fast(mdt_ctx *c, int precision) {
     int dev = 0, optin = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    return nnf_total_smem(c->B, c->M) <= (size_t)optin;
+    return nnf_total_smem(c->B, c->M, c->F) <= (size_t)optin;
 }
 
 LaunchCfg nnf_cfg(mdt_ctx *c) {
     const int per_sm = nnf_resident_ctas(c->B, c->M, c->F);
     const int grid = std::max(1, std::min(c->T, c->num_sms * per_sm));
     return LaunchCfg{c->stream, grid, c->order, c->counter};
+}
+
+// mask scratch of the fast path: the triplet masks of one bead per CTA (maxnb rows of
+// mw words per atom), written by the descriptor phase and read by the force phase
+int ensure_mscr(mdt_ctx *c, int grid) {
+    const int mw = (c->M.maxnb + 31) / 32;
+    const size_t per = c->F.anyg3 ? (size_t)c->max_atoms * c->M.maxnb * mw : 4;
+    const size_t n = (size_t)grid * per;
+    if (n > c->mscr_n) {
+        if (c->mscr) cudaFree(c->mscr);
+        c->mscr = nullptr;
+        c->mscr_n = 0;
+        cudaError_t e = cudaMalloc(&c->mscr, n * sizeof(unsigned));
+        if (e != cudaSuccess) return cuda_fail(c, e, "fast-path mask scratch");
+        c->mscr_n = n;
+    }
+    c->X.mscr = c->mscr;
+    c->X.mcap = (int)per;
+    return MDT_OK;
 }
 
 int check_nn_ready(mdt_ctx *c) {
@@ -405,6 +469,7 @@ int32_t mdt_destroy(mdt_ctx *c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     free_batch(c);
     for (void *p : c->nnbufs) cudaFree(p);
+    if (c->mscr) cudaFree(c->mscr);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return MDT_OK;
@@ -804,8 +869,11 @@ int32_t mdt_calc_force(mdt_ctx *c, int32_t flag, int32_t precision, const mdt_pr
         if (c->pes_kind == MDT_PES_SURROGATE && (rc = ensure_scratch(c, MDT_PREC_FP64))) return rc;
         const PropParams P = to_dev(c, p);
         const bool surr = c->pes_kind == MDT_PES_SURROGATE;
-        cudaError_t e = use_fast(c, precision)
-                            ? launch_nnf(nnf_cfg(c), c->B, c->M, c->F, c->E, c->X, P, 0,
+        const bool fast = use_fast(c, precision);
+        const LaunchCfg fcfg = fast ? nnf_cfg(c) : LaunchCfg{};
+        if (fast && (rc = ensure_mscr(c, fcfg.grid))) return rc;
+        cudaError_t e = fast
+                            ? launch_nnf(fcfg, c->B, c->M, c->F, c->E, c->X, P, 0,
                                          flag == MDT_ENERGY_ONLY ? 1 : 0, surr)
                             : launch_nn(nn_cfg(c, precision), c->B, c->M, c->E, c->X, P, c->ngeta_max, 0,
                                         flag == MDT_ENERGY_ONLY ? 1 : 0, precision, surr);
@@ -853,8 +921,11 @@ int32_t mdt_md_steps(mdt_ctx *c, int32_t nsteps, int32_t precision, const mdt_pr
         if (nsteps == 0) return MDT_OK;
         const PropParams P = to_dev(c, p);
         const bool surr = c->pes_kind == MDT_PES_SURROGATE;
-        cudaError_t e = use_fast(c, precision)
-                            ? launch_nnf(nnf_cfg(c), c->B, c->M, c->F, c->E, c->X, P, nsteps, 2, surr)
+        const bool fast = use_fast(c, precision);
+        const LaunchCfg fcfg = fast ? nnf_cfg(c) : LaunchCfg{};
+        if (fast && (rc = ensure_mscr(c, fcfg.grid))) return rc;
+        cudaError_t e = fast
+                            ? launch_nnf(fcfg, c->B, c->M, c->F, c->E, c->X, P, nsteps, 2, surr)
                             : launch_nn(nn_cfg(c, precision), c->B, c->M, c->E, c->X, P, c->ngeta_max, nsteps, 2,
                                         precision, surr);
         c->launches++;
@@ -1066,11 +1137,13 @@ int32_t mdt_nn_set_model(mdt_ctx *c, const mdt_nn_model *m, int32_t ntypes, cons
     M.act = (const uint8_t *)up(act.data(), act.size());
     M.wd = (const double *)up(m->weights, 8 * (size_t)ne * m->maxweights);
     M.wf = (const float *)up(wf.data(), 4 * wf.size());
-    FastNN F = build_fast(M, m, e1, etaslot);
+    std::vector<float4> g2tab;
+    FastNN F = build_fast(M, m, e1, etaslot, g2tab);
     if (F.ok) {
         std::vector<float> zeros(5 * nk, 0.f);
         F.scal = (const float4 *)up(zeros.data(), 16 * nk);
         F.dscal = (const float *)up(zeros.data(), 4 * nk);
+        F.g2tab = (const float4 *)up(g2tab.data(), sizeof(float4) * g2tab.size());
     }
     if (e != cudaSuccess) return cuda_fail(c, e, "mdt_nn_set_model upload");
     c->F = F;

@@ -33,7 +33,8 @@ int nn_resident_ctas(const NNDev &M, int max_atoms, int max_beads, int ngeta, in
 
 // FP32 fast path (mdt_nnf.cu)
 int nnf_zm_supported(int zm);
-size_t nnf_total_smem(const Batch &B, const NNDev &M);
+size_t nnf_total_smem(const Batch &B, const NNDev &M, const FastNN &F);
+int nnf_warps_per_cta();
 int nnf_resident_ctas(const Batch &B, const NNDev &M, const FastNN &F);
 cudaError_t launch_nnf(const LaunchCfg &c, const Batch &B, const NNDev &M, const FastNN &F, const EmtConst &E,
                        const NNScratch &X, const PropParams &P, int nsteps, int mode, bool surrogate);

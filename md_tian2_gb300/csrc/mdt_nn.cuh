@@ -67,12 +67,13 @@ struct NNDev {
 // and the G3 functions of each element form a grid of eta slots x (lambda = +-1,
 // zeta = 2^b) cells over one neighbour-element pair.
 // ---------------------------------------------------------------------------
-constexpr int kFMaxG2 = 16;  // radial functions per element
+constexpr int kFMaxG2 = 32;  // radial functions per element
 constexpr int kFNQ = 8;      // (lambda, zeta) cells: lambda = +-1 for up to 4 zeta values
 
 struct FastNN {
     int ok;                        // model qualifies
     int ng, zm;                    // eta slots; zeta mask (bit b set: zeta = 2^b is used)
+    int anyg3;                     // some element has G3 functions
     float rc2, inv_rc2;            // bohr^-2
     float cut2_hi, cut2_lo;        // FP32 screen of the neighbour list (bohr^2)
     int hasg3[kMaxElem];
@@ -82,8 +83,15 @@ struct FastNN {
     int8_t cell_sf[kMaxElem][4][kFNQ];  // SF index of cell (m, 2k + [lambda < 0]), -1 if none
     float cell_lz[kFNQ];           // lambda zeta of cell q
     int ng2[kMaxElem];
-    float g2l2[kMaxElem][kFMaxG2], g2eta[kMaxElem][kFMaxG2], g2rs[kMaxElem][kFMaxG2];
-    int8_t g2e[kMaxElem][kFMaxG2], g2sf[kMaxElem][kFMaxG2];
+    // radial functions of element e grouped by neighbour element: group (e, a) is
+    // g2tab[e*kFMaxG2 + g2beg[e][a] ...) with g2cnt[e][a] entries, ascending eta.  With
+    // g2chain[e][a] = S > 0 the group is centred (r_s = 0) and eta_{k+S} = 2 eta_k, so
+    // exp(-eta_{k+S} r^2) = exp(-eta_k r^2)^2: S exponentials, the rest by squaring.
+    int g2beg[kMaxElem][kMaxElem], g2cnt[kMaxElem][kMaxElem], g2chain[kMaxElem][kMaxElem];
+    const float4 *g2tab;           // [e*kFMaxG2 + s]: (-eta log2 e, r_s, -2 eta, sf index)
+    // network weights as the fast kernels keep them in shared memory: layer l of element
+    // e is a row-major (n_{l-1} + 1) x stride matrix (last row: biases) at wofs[e][l]
+    int wofs[kMaxElem][kMaxLayers + 1], wstr[kMaxElem][kMaxLayers + 1], wtotal;
     const float4 *scal;            // [e*maxsf + s]: scaled = x g + y; outside [z, w] raises the flag
     const float *dscal;            // [e*maxsf + s]: d(scaled)/dG as RuNNer applies it
 };
@@ -98,6 +106,8 @@ struct NNScratch {
     int *fallback;     // per trajectory: beads that fell back to EMT (surrogate)
     int *nnstatus;     // per trajectory: 1 = neighbour list overflow
     double *gout;      // optional: raw symmetry functions [ba][maxsf] (descriptor export)
+    unsigned *mscr;    // fast path: triplet masks of a bead, mcap words per CTA
+    int mcap;
 };
 
 // ---------------------------------------------------------------------------

@@ -5,7 +5,13 @@
 // RuNNer_src/atomsymfunction2.f90 and atomsymfunction3Andi.f90) for the models that
 // FastNN::ok admits, organised for throughput:
 //
-//  * CTA = 8 warps on one bead; warps take central atoms from a shared counter.
+//  * CTA = 8 warps on one bead, in three phases separated by CTA barriers:
+//      descriptors  warp per central atom (atoms from a shared counter): neighbour
+//                   list, neighbour rows, G2 and G3 into the bead's descriptor array;
+//      network      warp per group of 4 atoms of one element (lanes = nodes, four
+//                   independent dot products per lane), dE/dG over the descriptors;
+//      forces       warp per central atom again (rows rebuilt from the neighbour words
+//                   the first phase left in global scratch).
 //  * Neighbour list of atom i, built by its warp: lane L takes atoms j = j0 + L and
 //    visits only the image shifts whose fractional offset can lie inside the cutoff
 //    (|f_d + n_d| <= rc |b_d|, b_d the reciprocal vectors), n1 -> n2 -> n3 ascending, so
@@ -13,18 +19,26 @@
 //    Distances are screened in FP32 from a hi/lo split of the wrapped positions; within
 //    1e-4 (relative) of the cutoff the exact FP64 test of mdt_acsf.cuh decides.
 //  * Neighbour rows (d, 1/r, fc, (dfc/dr)/r, exp(-eta_m r^2)) are computed once per pair.
-//  * Triplets (q3 < q4) with r_jk <= rc and the G3 element pair are compacted per row
-//    pair (rows p and n-2-p hold n candidates together, one lane per row pair) into
-//    byte lists; the forward and the force walk then give every lane an equal share
-//    of the compacted list, so no lane idles on a rejected triplet.
+//  * Radial functions per neighbour-element group; when the group is centred with
+//    eta_{k+S} = 2 eta_k, S exponentials and squarings give all of them.  Per-lane
+//    partial sums are combined by one reduce-scatter (31 shuffles for 32 values).
+//  * Triplets (q3 < q4) with r_jk <= rc and the G3 element pair: lane p owns the row
+//    pair (p, n-2-p) of the upper triangle (n candidates together) and marks the valid
+//    second neighbours of both rows in bit masks; the forward and the force walk visit
+//    only set bits.
 //  * fc(r_jk) and its derivative come from the Taylor series of cos(pi sqrt(s)/2) in
 //    s = r_jk^2 / rc^2 (no square root, sine or cosine per triplet); with
 //    h = (1 + lambda cos)/2, 2^(1-zeta) (1 + lambda cos)^zeta = 2 h^zeta, and every
 //    h^zeta, h^(zeta-1) for zeta = 2^b comes from one squaring ladder.
+//  * Network: weights of all elements in shared memory, rows padded to a stride of
+//    4 (mod 8) floats so that lanes reading different rows hit different banks.
 //  * Forces: reverse mode as in mdt_acsf.cuh (dE/dG from the network, then
-//    dE/dG . dG/dx per triplet in factored form), slot forces of the current row in
-//    registers, of the second neighbour by shared-memory atomics; the central atom's
-//    force is minus the sum of its slot forces (translation invariance of E_i).
+//    dE/dG . dG/dx per triplet in factored form).  The first neighbour's force of a
+//    triplet accumulates in the row owner's registers, the second neighbour's by a
+//    shared-memory atomic; every warp adds its slot forces into its own copy of the
+//    bead's force array (plain adds, atomics only for repeated images of one atom).
+//    The central atom's force is minus the sum of its slot forces (translation
+//    invariance of E_i).
 #include <cstdio>
 
 #include "mdt_common.cuh"
@@ -117,22 +131,26 @@ __device__ __forceinline__ void zeta_powers(float h, float *P, float *Q) {
 }
 
 struct FLaunch {
-    int max_atoms, maxnb, npmax, hsize;  // hsize: floats per warp for the network sums/values
-    int surrogate;
+    int max_atoms, maxnb, mw, ls, sgs;  // mw: mask words per row; ls: node stride; sgs: descriptor stride
+    int surrogate, netshape;            // netshape: all layers fit the 4-atom network kernel
 };
 
-// Shared memory of one CTA.  The per-warp area is also where the EMT fallback of a
-// flagged bead carves its arrays (the network part of that bead is finished by then).
+// Shared memory of one CTA.  The per-warp area also holds the network buffers of the
+// network phase and the EMT fallback of a flagged bead.
 struct SmemF {
     double *px, *py, *pz;                // wrapped positions (bohr)
     float *xh, *yh, *zh, *xl, *yl, *zl;  // their FP32 hi/lo split
     int8_t *elem;
-    float *fx, *fy, *fz;                 // bead force accumulators (Ha/bohr)
+    int *byel;                           // atoms ordered by element; [max_atoms + kMaxElem + 1] offsets after
+    float *fw;                           // [warp][3][max_atoms] force accumulators (Ha/bohr)
+    float *sg;                           // [max_atoms][sgs]: descriptors G, then dE/dG
     double *lat;                         // 9 lattice rows + 9 inverse (bohr)
     float *latf, *ginv, *wk;             // FP32 lattice rows, inverse rows, image half-widths
     double *red;                         // block reductions
     double *cjk;                         // ring-polymer transform of the trajectory
-    int *misc;                           // [0] range flag, [1] atom counter
+    int *misc;                           // [0] range flag, [1..3] work counters of the three phases
+    float *w;                            // network weights (FastNN::wofs layout)
+    float4 *g2;                          // radial-function table (FastNN::g2tab)
     unsigned char *warp_base;            // per-warp areas
     size_t warp_bytes;
 };
@@ -140,35 +158,57 @@ struct SmemF {
 struct WarpF {
     float4 *ra, *rb, *rc;  // [q]: (dx, dy, dz, 1/r), (fc, E0, E1, E2), ((dfc/dr)/r, r, j | elem << 16, E3)
     uint8_t *code;         // [q]: bit 0 elem == pair_a, bit 1 elem == pair_b
-    int *word;             // [q]: packed (j, image)
+    unsigned *mask;        // [q][mw]: valid second neighbours q4 > q of row q
+    int *rcnt;             // [q]: valid triplets of row q
     float *sfx, *sfy, *sfz;
-    uint8_t *tq4;          // [row pair][maxnb] second neighbours of the valid triplets
-    int16_t *tcnt, *tsplit;
-    int *tpre;
-    float *G, *dG, *hs, *hv;
 };
+
+constexpr int kNA = 4;  // atoms per warp in the network phase
 
 __host__ __device__ inline size_t r16f(size_t b) { return (b + 15) & ~size_t(15); }
 
-__host__ __device__ inline size_t warp_bytes_f(int maxnb, int npmax, int hsize) {
-    return 3 * r16f(16 * (size_t)maxnb) + r16f(maxnb) + r16f(4 * (size_t)maxnb) + 3 * r16f(4 * (size_t)maxnb) +
-           r16f((size_t)npmax * maxnb) + 2 * r16f(2 * (size_t)npmax) + r16f(4 * ((size_t)npmax + 1)) +
-           2 * r16f(4 * kMaxSF) + 2 * r16f(4 * (size_t)hsize);
+__host__ __device__ inline size_t warp_bytes_f(int maxnb, int mw, int nlayers, int ls) {
+    const size_t rows = 3 * r16f(16 * (size_t)maxnb) + r16f(maxnb) + r16f(4 * (size_t)maxnb * mw) +
+                        r16f(4 * ((size_t)maxnb + 1)) + 3 * r16f(4 * (size_t)maxnb);
+    const size_t net = 2 * r16f(4 * (size_t)kNA * (nlayers + 1) * ls);
+    return rows > net ? rows : net;
 }
 
-__host__ __device__ inline size_t shared_bytes_f(int max_atoms, int max_beads) {
+__host__ __device__ inline size_t shared_bytes_f(int max_atoms, int max_beads, int wtotal, int nelem, int sgs) {
     return 3 * r16f(8 * (size_t)max_atoms) + 6 * r16f(4 * (size_t)max_atoms) + r16f(max_atoms) +
-           3 * r16f(4 * (size_t)max_atoms) + r16f(8 * 18) + 3 * r16f(4 * 9) + r16f(8 * 64) +
-           r16f(8 * (size_t)max_beads * max_beads) + 16;
+           r16f(4 * ((size_t)max_atoms + kMaxElem + 1)) + r16f(4 * (size_t)kFW * 3 * max_atoms) +
+           r16f(4 * (size_t)max_atoms * sgs) + r16f(8 * 18) + 3 * r16f(4 * 9) + r16f(8 * 64) +
+           r16f(8 * (size_t)max_beads * max_beads) + 16 + r16f(4 * (size_t)wtotal) +
+           r16f(16 * (size_t)nelem * kFMaxG2);
 }
 
-size_t nnf_smem_bytes(int max_atoms, int max_beads, int maxnb, int npmax, int hsize) {
-    const size_t wb = kFW * warp_bytes_f(maxnb, npmax, hsize);
-    const size_t emt = smem_bytes(max_atoms, max_beads, 8);
-    return shared_bytes_f(max_atoms, max_beads) + (wb > emt ? wb : emt);
+FLaunch flaunch(const Batch &B, const NNDev &M, int surrogate) {
+    FLaunch L;
+    L.max_atoms = B.max_atoms;
+    L.maxnb = M.maxnb;
+    L.mw = (M.maxnb + 31) / 32;
+    int mx = 1;
+    for (int e = 0; e < M.nelem; ++e)
+        for (int l = 0; l <= M.nlayers; ++l) mx = mx > M.nodes[e][l] ? mx : M.nodes[e][l];
+    L.ls = (mx + 3) & ~3;
+    L.sgs = (M.maxsf + 3) & ~3;
+    L.surrogate = surrogate;
+    L.netshape = 1;
+    for (int e = 0; e < M.nelem; ++e)
+        for (int l = 1; l <= M.nlayers; ++l)
+            if (M.nodes[e][l] > 32 || M.nodes[e][l - 1] > 32) L.netshape = 0;
+    return L;
 }
 
-__device__ SmemF carve_f(unsigned char *base, const FLaunch &L, int max_beads) {
+size_t nnf_smem_total(const Batch &B, const NNDev &M, const FastNN &F) {
+    const FLaunch L = flaunch(B, M, 0);
+    const size_t wb = kFW * warp_bytes_f(L.maxnb, L.mw, M.nlayers, L.ls);
+    const size_t emt = smem_bytes(B.max_atoms, B.max_beads, 8);
+    return shared_bytes_f(B.max_atoms, B.max_beads, F.wtotal, M.nelem, L.sgs) + (wb > emt ? wb : emt);
+}
+
+__device__ SmemF carve_f(unsigned char *base, const FLaunch &L, int max_beads, int wtotal, int nelem,
+                         int nlayers) {
     SmemF s;
     size_t off = 0;
     auto take = [&](size_t bytes) {
@@ -187,9 +227,9 @@ __device__ SmemF carve_f(unsigned char *base, const FLaunch &L, int max_beads) {
     s.yl = (float *)take(4 * na);
     s.zl = (float *)take(4 * na);
     s.elem = (int8_t *)take(na);
-    s.fx = (float *)take(4 * na);
-    s.fy = (float *)take(4 * na);
-    s.fz = (float *)take(4 * na);
+    s.byel = (int *)take(4 * ((size_t)na + kMaxElem + 1));
+    s.fw = (float *)take(4 * (size_t)kFW * 3 * na);
+    s.sg = (float *)take(4 * (size_t)na * L.sgs);
     s.lat = (double *)take(8 * 18);
     s.latf = (float *)take(4 * 9);
     s.ginv = (float *)take(4 * 9);
@@ -197,8 +237,10 @@ __device__ SmemF carve_f(unsigned char *base, const FLaunch &L, int max_beads) {
     s.red = (double *)take(8 * 64);
     s.cjk = (double *)take(8 * (size_t)max_beads * max_beads);
     s.misc = (int *)take(16);
+    s.w = (float *)take(4 * (size_t)wtotal);
+    s.g2 = (float4 *)take(16 * (size_t)nelem * kFMaxG2);
     s.warp_base = base + off;
-    s.warp_bytes = warp_bytes_f(L.maxnb, L.npmax, L.hsize);
+    s.warp_bytes = warp_bytes_f(L.maxnb, L.mw, nlayers, L.ls);
     return s;
 }
 
@@ -216,18 +258,11 @@ __device__ WarpF carve_warp(const SmemF &S, const FLaunch &L, int warp) {
     w.rb = (float4 *)take(16 * (size_t)nb);
     w.rc = (float4 *)take(16 * (size_t)nb);
     w.code = (uint8_t *)take(nb);
-    w.word = (int *)take(4 * (size_t)nb);
+    w.mask = (unsigned *)take(4 * (size_t)nb * L.mw);
+    w.rcnt = (int *)take(4 * ((size_t)nb + 1));
     w.sfx = (float *)take(4 * (size_t)nb);
     w.sfy = (float *)take(4 * (size_t)nb);
     w.sfz = (float *)take(4 * (size_t)nb);
-    w.tq4 = (uint8_t *)take((size_t)L.npmax * nb);
-    w.tcnt = (int16_t *)take(2 * (size_t)L.npmax);
-    w.tsplit = (int16_t *)take(2 * (size_t)L.npmax);
-    w.tpre = (int *)take(4 * ((size_t)L.npmax + 1));
-    w.G = (float *)take(4 * kMaxSF);
-    w.dG = (float *)take(4 * kMaxSF);
-    w.hs = (float *)take(4 * (size_t)L.hsize);
-    w.hv = (float *)take(4 * (size_t)L.hsize);
     return w;
 }
 
@@ -241,6 +276,31 @@ __device__ __forceinline__ int warp_excl_scan(int v, int &total) {
     }
     total = __shfl_sync(0xffffffffu, x, 31);
     return x - v;
+}
+
+// Reduce-scatter of NV (power of two, <= 32) per-lane partial sums: afterwards v[0] of
+// lane L holds the warp total of index L & (NV - 1).
+template <int NV>
+__device__ __forceinline__ void reduce_scatter(float (&v)[NV]) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int off = 16; off >= NV; off >>= 1)
+#pragma unroll
+        for (int k = 0; k < NV; ++k) v[k] += __shfl_xor_sync(0xffffffffu, v[k], off);
+#pragma unroll
+    for (int w = NV / 2; w >= 1; w >>= 1) {
+        const bool up = (lane & w) != 0;
+#pragma unroll
+        for (int k = 0; k < w; ++k) {
+            const float keep = up ? v[k + w] : v[k], give = up ? v[k] : v[k + w];
+            v[k] = keep + __shfl_xor_sync(0xffffffffu, give, w);
+        }
+    }
+}
+
+__device__ __forceinline__ void red_shared(float *p, float v) {
+    const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+    asm volatile("red.shared.add.f32 [%0], %1;" ::"r"(a), "f"(v) : "memory");
 }
 
 // exact FP64 cutoff test of one image (the oracle's operation order, no fused operations)
@@ -287,47 +347,75 @@ __device__ __forceinline__ int visit_images(const SmemF &S, const FastNN &F, dou
     return c;
 }
 
-// ---- one central atom: neighbour list, rows, descriptors, network, forces ----------
-template <int NG, int ZM>
-__device__ void nnf_atom(const NNDev &M, const FastNN &F, const NNScratch &X, const SmemF &S, const WarpF &W,
-                         const FLaunch &L, int t, int i, int N, const int *na, bool do_forces, double &e_acc) {
-    constexpr int NZ = popc5(ZM), NQ = 2 * NZ;
-    static_assert(NQ <= kFNQ, "too many (lambda, zeta) cells");
-    const int lane = threadIdx.x & 31;
-    const int ei = S.elem[i];
-    const double cut2 = __dmul_rn(M.maxcut, M.maxcut);
-
-    // ---- neighbour list (RuNNer order) ---------------------------------------------------
-    const float xhi = S.xh[i], yhi = S.yh[i], zhi = S.zh[i], xli = S.xl[i], yli = S.yl[i], zli = S.zl[i];
-    int cnt = 0;
-    for (int j0 = 0; j0 < N; j0 += 32) {
-        const int j = j0 + lane;
-        float dx = 0.f, dy = 0.f, dz = 0.f;
-        int c = 0;
-        if (j < N) {
-            dx = (S.xh[j] - xhi) + (S.xl[j] - xli);
-            dy = (S.yh[j] - yhi) + (S.yl[j] - yli);
-            dz = (S.zh[j] - zhi) + (S.zl[j] - zli);
-            c = visit_images<false>(S, F, cut2, i, j, dx, dy, dz, na, nullptr, 0, 0);
+// Iterator over the set bits of one lane's rows (row pair p: rows p and n-2-p) in
+// row-major order; yields (q3, q4).
+struct RowBits {
+    const unsigned *mask;
+    int mw, r1, row, w;
+    unsigned m;
+    __device__ __forceinline__ void start(const unsigned *mk, int mwords, int p, int nrows) {
+        mask = mk;
+        mw = mwords;
+        r1 = nrows - 1 - p;
+        row = p;
+        w = (p + 1) >> 5;
+        m = mask[row * mw + w];
+    }
+    // next valid (q3, q4); the caller knows how many there are
+    __device__ __forceinline__ void next(int &q3, int &q4) {
+        while (m == 0) {
+            if (++w >= mw) {
+                row = r1;
+                w = (r1 + 1) >> 5;
+            }
+            m = mask[row * mw + w];
         }
-        int tot;
-        const int ex = warp_excl_scan(c, tot);
-        if (c > 0) visit_images<true>(S, F, cut2, i, j, dx, dy, dz, na, W.word, cnt + ex, L.maxnb);
-        cnt += tot;
+        const int b = __ffs(m) - 1;
+        m &= m - 1;
+        q3 = row;
+        q4 = (w << 5) + b;
     }
-    if (cnt > L.maxnb) {
-        if (lane == 0) X.nnstatus[t] = 1;
-        cnt = L.maxnb;
-    }
-    __syncwarp();
+};
 
-    // ---- neighbour rows ------------------------------------------------------------------
-    const int pa = F.pair_a[ei], pb = F.pair_b[ei];
-    float g3l2[NG];
+// Radial functions of one neighbour-element group at distance r: calls f(k, exp(-eta_k
+// (r - r_s,k)^2)) for k < n.  S > 0: centred group with eta_{k+S} = 2 eta_k.
+template <int S, typename Fn>
+__device__ __forceinline__ void g2_chain(const float4 *tab, int n, float r, float r2, Fn &&f) {
+    float ev[kFMaxG2];
 #pragma unroll
-    for (int m = 0; m < NG; ++m) g3l2[m] = F.g3l2[ei][m];
+    for (int k = 0; k < kFMaxG2; ++k) {
+        if (k >= n) break;
+        if (S > 0 && k >= S) {
+            ev[k] = ev[k - S] * ev[k - S];
+        } else {
+            const float4 g = tab[k];
+            const float u = S > 0 ? r : r - g.y;
+            ev[k] = exp2f(g.x * (S > 0 ? r2 : u * u));
+        }
+        f(k, ev[k]);
+    }
+}
+
+template <typename Fn>
+__device__ __forceinline__ void g2_group(const float4 *tab, int n, int S, float r, float r2, Fn &&f) {
+    switch (S) {
+        case 1: g2_chain<1>(tab, n, r, r2, f); break;
+        case 2: g2_chain<2>(tab, n, r, r2, f); break;
+        case 3: g2_chain<3>(tab, n, r, r2, f); break;
+        case 4: g2_chain<4>(tab, n, r, r2, f); break;
+        default: g2_chain<0>(tab, n, r, r2, f); break;
+    }
+}
+
+// Neighbour rows of atom i from its packed words (global scratch), elements codes.
+template <int NG>
+__device__ __forceinline__ void build_rows(const FastNN &F, const SmemF &S, const WarpF &W, const int *words,
+                                           int cnt, int i, int ei, const float *g3l2) {
+    const int lane = threadIdx.x & 31;
+    const int pa = F.pair_a[ei], pb = F.pair_b[ei];
+    const float xhi = S.xh[i], yhi = S.yh[i], zhi = S.zh[i], xli = S.xl[i], yli = S.yl[i], zli = S.zl[i];
     for (int q = lane; q < cnt; q += 32) {
-        const int w = W.word[q];
+        const int w = words[q];
         const int j = w & 0xFFFF;
         const float n1 = (float)(((w >> 16) & 15) - 8), n2 = (float)(((w >> 20) & 15) - 8),
                     n3 = (float)(((w >> 24) & 15) - 8);
@@ -350,117 +438,142 @@ __device__ void nnf_atom(const NNDev &M, const FastNN &F, const NNScratch &X, co
         W.code[q] = (uint8_t)((el == pa ? 1 : 0) | (el == pb ? 2 : 0));
     }
     __syncwarp();
+}
 
-    // ---- radial functions ----------------------------------------------------------------
-    const int ng2 = F.ng2[ei];
+// ---- phase 1: neighbour list, rows, descriptors of one central atom ---------------------
+template <int NG, int ZM>
+__device__ void nnf_descriptors(const NNDev &M, const FastNN &F, const NNScratch &X, const SmemF &S,
+                                const WarpF &W, const FLaunch &L, int t, int64_t base, int i, int N, const int *na,
+                                unsigned *mglob) {
+    constexpr int NZ = popc5(ZM), NQ = 2 * NZ;
+    static_assert(NG * NQ <= 32, "too many G3 cells");
+    const int lane = threadIdx.x & 31;
+    const int ei = S.elem[i];
+    const double cut2 = __dmul_rn(M.maxcut, M.maxcut);
+    const int mw = L.mw;
+    int *words = X.nbw + (base + i) * (int64_t)M.maxnb;
+
+    // ---- neighbour list (RuNNer order) into the global word slot of the bead-atom ------
+    int cnt = 0;
     {
+        const float xhi = S.xh[i], yhi = S.yh[i], zhi = S.zh[i], xli = S.xl[i], yli = S.yl[i], zli = S.zl[i];
+        for (int j0 = 0; j0 < N; j0 += 32) {
+            const int j = j0 + lane;
+            float dx = 0.f, dy = 0.f, dz = 0.f;
+            int c = 0;
+            if (j < N) {
+                dx = (S.xh[j] - xhi) + (S.xl[j] - xli);
+                dy = (S.yh[j] - yhi) + (S.yl[j] - yli);
+                dz = (S.zh[j] - zhi) + (S.zl[j] - zli);
+                c = visit_images<false>(S, F, cut2, i, j, dx, dy, dz, na, nullptr, 0, 0);
+            }
+            int tot;
+            const int ex = warp_excl_scan(c, tot);
+            if (c > 0) visit_images<true>(S, F, cut2, i, j, dx, dy, dz, na, words, cnt + ex, L.maxnb);
+            cnt += tot;
+        }
+    }
+    if (cnt > L.maxnb) {
+        if (lane == 0) X.nnstatus[t] = 1;
+        cnt = L.maxnb;
+    }
+    if (lane == 0) X.nbcnt[base + i] = cnt;
+    __syncwarp();
+    float g3l2[NG];
+#pragma unroll
+    for (int m = 0; m < NG; ++m) g3l2[m] = F.g3l2[ei][m];
+    build_rows<NG>(F, S, W, words, cnt, i, ei, g3l2);
+
+    // ---- radial functions, per neighbour-element group -----------------------------------
+    float *G = S.sg + (size_t)i * L.sgs;
+    const float4 *g2e = S.g2 + ei * kFMaxG2;
+    for (int a = 0; a < M.nelem; ++a) {
+        const int n = F.g2cnt[ei][a];
+        if (n == 0) continue;
+        const float4 *tab = g2e + F.g2beg[ei][a];
+        const int chain = F.g2chain[ei][a];
         float acc[kFMaxG2];
 #pragma unroll
-        for (int s = 0; s < kFMaxG2; ++s) acc[s] = 0.f;
+        for (int k = 0; k < kFMaxG2; ++k) acc[k] = 0.f;
         for (int q = lane; q < cnt; q += 32) {
             const float4 b = W.rb[q], c = W.rc[q];
-            const int el = __float_as_int(c.z) >> 16;
-#pragma unroll
-            for (int s = 0; s < kFMaxG2; ++s) {
-                if (s >= ng2) break;
-                if (F.g2e[ei][s] != el) continue;
-                const float u = c.y - F.g2rs[ei][s];
-                acc[s] += exp2f(F.g2l2[ei][s] * u * u) * b.x;
-            }
+            if ((__float_as_int(c.z) >> 16) != a) continue;
+            g2_group(tab, n, chain, c.y, c.y * c.y, [&](int k, float e) { acc[k] = fmaf(e, b.x, acc[k]); });
         }
-#pragma unroll
-        for (int s = 0; s < kFMaxG2; ++s) {
-            if (s >= ng2) break;
-            const float v = warp_sum(acc[s]);
-            if (lane == 0) W.G[F.g2sf[ei][s]] = v;
-        }
+        reduce_scatter<kFMaxG2>(acc);
+        if (lane < n) G[__float_as_int(tab[lane].w)] = acc[0];
     }
 
-    // ---- triplet lists -------------------------------------------------------------------
+    // ---- triplet masks and G3 ----------------------------------------------------------------
     const bool g3 = F.hasg3[ei] != 0;
     const int nrows = cnt - 1, npairs = (g3 && nrows > 0) ? (nrows + 1) / 2 : 0;
-    int T = 0;
-    if (npairs > 0) {
-        const bool same = pa == pb;
-        for (int p = lane; p < npairs; p += 32) {
-            const int r0 = p, r1 = nrows - 1 - p, len0 = cnt - 1 - r0;
-            const int tot = (r1 == r0) ? len0 : cnt;
-            const float4 a0 = W.ra[r0], a1 = W.ra[r1];
-            const int c0 = W.code[r0], c1 = W.code[r1];
-            uint8_t *dst = W.tq4 + (size_t)p * L.maxnb;
-            int n = 0, sp = 0;
-            for (int c = 0; c < tot; ++c) {
-                const bool first = c < len0;
-                if (c == len0) sp = n;
-                const int q4 = first ? r0 + 1 + c : c;
-                const float4 k = W.ra[q4];
-                const int ck = W.code[q4], cj = first ? c0 : c1;
-                const float jx = (first ? a0.x : a1.x) - k.x, jy = (first ? a0.y : a1.y) - k.y,
-                            jz = (first ? a0.z : a1.z) - k.z;
-                const float r2 = jx * jx + jy * jy + jz * jz;
-                const bool ok = r2 <= F.rc2 && (cj | ck) == 3 && (!same || (cj & ck) == 3);
-                if (ok) dst[n++] = (uint8_t)q4;
-            }
-            if (tot == len0) sp = n;
-            W.tcnt[p] = (int16_t)n;
-            W.tsplit[p] = (int16_t)sp;
+    if (g3 && npairs == 0) {
+        for (int q = lane; q < NG * NQ; q += 32) {
+            const int sidx = F.cell_sf[ei][q / NQ][q % NQ];
+            if (sidx >= 0) G[sidx] = 0.f;
         }
-        __syncwarp();
-        int run = 0;
-        for (int p0 = 0; p0 < npairs; p0 += 32) {
-            const int p = p0 + lane;
-            const int v = p < npairs ? W.tcnt[p] : 0;
-            int tot;
-            const int ex = warp_excl_scan(v, tot);
-            if (p < npairs) W.tpre[p] = run + ex;
-            run += tot;
-        }
-        if (lane == 0) W.tpre[npairs] = run;
-        T = run;
-        __syncwarp();
     }
-
-    // equal share of the compacted list: [e0, e1), starting in row pair p at position pos
-    auto share = [&](int &e0, int &e1, int &p, int &pos) {
-        const int K = (T + 31) >> 5;
-        e0 = min(T, lane * K);
-        e1 = min(T, e0 + K);
-        int lo = 0, hi = npairs - 1;  // last p with tpre[p] <= e0
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (W.tpre[mid] <= e0) lo = mid;
-            else hi = mid - 1;
-        }
-        p = lo;
-        pos = e0 - W.tpre[p];
-    };
-
-    // ---- G3 forward ----------------------------------------------------------------------
-    if (T > 0) {
-        float acc[NG][NQ];
-#pragma unroll
-        for (int m = 0; m < NG; ++m)
-#pragma unroll
-            for (int q = 0; q < NQ; ++q) acc[m][q] = 0.f;
-        int e0, e1, p, pos;
-        share(e0, e1, p, pos);
-        int pc = W.tcnt[p], psp = W.tsplit[p], cq3 = -1;
-        float4 JA = make_float4(0.f, 0.f, 0.f, 0.f), JB = JA, JC = JA;
-        for (int e = e0; e < e1; ++e) {
-            while (pos >= pc) {
-                ++p;
-                pos = 0;
-                pc = W.tcnt[p];
-                psp = W.tsplit[p];
+    if (npairs == 0) return;
+    const bool same = F.pair_a[ei] == F.pair_b[ei];
+    for (int k = lane; k < cnt * mw; k += 32) W.mask[k] = 0u;
+    __syncwarp();
+    for (int p = lane; p < npairs; p += 32) {
+        const int r0 = p, r1 = nrows - 1 - p, len0 = cnt - 1 - r0;
+        const int tot = (r1 == r0) ? len0 : cnt;
+        const float4 a0 = W.ra[r0], a1 = W.ra[r1];
+        const int c0 = W.code[r0], c1 = W.code[r1];
+        unsigned word = 0u;
+        int wcur = (r0 + 1) >> 5, row = r0, n0 = 0, n1 = 0;
+        for (int c = 0; c < tot; ++c) {
+            const bool first = c < len0;
+            const int q4 = first ? r0 + 1 + c : c;
+            if (!first && row == r0) {  // switch to the second row
+                W.mask[row * mw + wcur] = word;
+                word = 0u;
+                row = r1;
+                wcur = q4 >> 5;
             }
-            const int q3 = pos < psp ? p : nrows - 1 - p;
-            const int q4 = W.tq4[(size_t)p * L.maxnb + pos];
-            ++pos;
+            if ((q4 >> 5) != wcur) {
+                W.mask[row * mw + wcur] = word;
+                word = 0u;
+                wcur = q4 >> 5;
+            }
+            const float4 k = W.ra[q4];
+            const int ck = W.code[q4], cj = first ? c0 : c1;
+            const float jx = (first ? a0.x : a1.x) - k.x, jy = (first ? a0.y : a1.y) - k.y,
+                        jz = (first ? a0.z : a1.z) - k.z;
+            const float r2 = jx * jx + jy * jy + jz * jz;
+            const bool ok = r2 <= F.rc2 && (cj | ck) == 3 && (!same || (cj & ck) == 3);
+            word |= (ok ? 1u : 0u) << (q4 & 31);
+            if (first) n0 += ok;
+            else n1 += ok;
+        }
+        if (tot > 0) W.mask[row * mw + wcur] = word;
+        W.rcnt[r0] = n0;
+        if (r1 != r0) W.rcnt[r1] = n1;
+    }
+    __syncwarp();
+    for (int k = lane; k < cnt * mw; k += 32) mglob[k] = W.mask[k];  // for the force phase
+
+    float acc[32];
+#pragma unroll
+    for (int c = 0; c < 32; ++c) acc[c] = 0.f;
+    for (int p = lane; p < npairs; p += 32) {
+        const int r1 = nrows - 1 - p;
+        const int ntr = W.rcnt[p] + (r1 != p ? W.rcnt[r1] : 0);
+        RowBits it;
+        it.start(W.mask, mw, p, nrows);
+        int cq3 = -1;
+        float4 JA = make_float4(0.f, 0.f, 0.f, 0.f), JB = JA;
+        float EJ3 = 0.f;
+        for (int e = 0; e < ntr; ++e) {
+            int q3, q4;
+            it.next(q3, q4);
             if (q3 != cq3) {
                 cq3 = q3;
                 JA = W.ra[q3];
                 JB = W.rb[q3];
-                if (NG == 4) JC = W.rc[q3];
+                if (NG == 4) EJ3 = W.rc[q3].w;
             }
             const float4 KA = W.ra[q4], KB = W.rb[q4];
             const float jx = JA.x - KA.x, jy = JA.y - KA.y, jz = JA.z - KA.z;
@@ -468,10 +581,10 @@ __device__ void nnf_atom(const NNDev &M, const FastNN &F, const NNScratch &X, co
             const float fcjk = fc_of_s(fminf(rjk2 * F.inv_rc2, 1.f));
             const float u = (JA.x * KA.x + JA.y * KA.y + JA.z * KA.z) * (JA.w * KA.w);
             const float pf = JB.x * KB.x * fcjk;
-            float Xm[NG];
-            const float Ej[4] = {JB.y, JB.z, JB.w, JC.w};
+            const float Ej[4] = {JB.y, JB.z, JB.w, EJ3};
             float Ek[4] = {KB.y, KB.z, KB.w, 0.f};
             if (NG == 4) Ek[3] = W.rc[q4].w;
+            float Xm[NG];
 #pragma unroll
             for (int m = 0; m < NG; ++m) Xm[m] = Ej[m] * Ek[m] * exp2f(g3l2[m] * rjk2) * pf;
             float Pp[NZ], Pm[NZ];
@@ -480,222 +593,375 @@ __device__ void nnf_atom(const NNDev &M, const FastNN &F, const NNScratch &X, co
 #pragma unroll
             for (int m = 0; m < NG; ++m)
 #pragma unroll
-                for (int k = 0; k < NZ; ++k) {
-                    acc[m][2 * k] = fmaf(Xm[m], Pp[k], acc[m][2 * k]);
-                    acc[m][2 * k + 1] = fmaf(Xm[m], Pm[k], acc[m][2 * k + 1]);
+                for (int z = 0; z < NZ; ++z) {
+                    acc[m * NQ + 2 * z] = fmaf(Xm[m], Pp[z], acc[m * NQ + 2 * z]);
+                    acc[m * NQ + 2 * z + 1] = fmaf(Xm[m], Pm[z], acc[m * NQ + 2 * z + 1]);
                 }
         }
-#pragma unroll
-        for (int m = 0; m < NG; ++m)
-#pragma unroll
-            for (int q = 0; q < NQ; ++q) {
-                const float v = warp_sum(acc[m][q]);
-                const int s = F.cell_sf[ei][m][q];
-                if (lane == 0 && s >= 0) W.G[s] = 2.f * v;
-            }
-    } else if (g3) {
-        for (int q = lane; q < NG * NQ; q += 32) {
-            const int s = F.cell_sf[ei][q / NQ][q % NQ];
-            if (s >= 0) W.G[s] = 0.f;
-        }
     }
-    __syncwarp();
+    reduce_scatter<32>(acc);
+    if (lane < NG * NQ) {
+        const int sidx = F.cell_sf[ei][lane / NQ][lane % NQ];
+        if (sidx >= 0) G[sidx] = 2.f * acc[0];
+    }
+}
 
-    // ---- scaling, range check (getshortatomic.f90:174-236) and network ------------------
+// ---- phase 2: network for up to kNA atoms of element e (lanes = nodes) -----------------
+// calconenn.f90:83-153 forward, getdnodes_values.f90 + getshortatomic.f90:263-291 back;
+// scaling and range check of getshortatomic.f90:174-236.  Replaces the descriptors of
+// the atoms in S.sg by dE/dG (raw G); returns the energy sum of the group (lane 0).
+__device__ float nnf_network4(const NNDev &M, const FastNN &F, const SmemF &S, const FLaunch &L, float *hs,
+                              float *hv, int ei, const int *atoms, int na, bool do_forces) {
+    const int lane = threadIdx.x & 31;
+    const int ls = L.ls, lstr = (M.nlayers + 1) * ls;  // per-atom stride in hs/hv
     const int nsf = M.nsf[ei], sfb = ei * M.maxsf;
     for (int s = lane; s < nsf; s += 32) {
-        const float g = W.G[s];
         const float4 sc = F.scal[sfb + s];
-        if (g < sc.z || g > sc.w) S.misc[0] = 1;
-        W.hv[s] = fmaf(sc.x, g, sc.y);
+#pragma unroll
+        for (int a = 0; a < kNA; ++a) {
+            float v = 0.f;
+            if (a < na) {
+                const float g = S.sg[(size_t)atoms[a] * L.sgs + s];
+                if (g < sc.z || g > sc.w) S.misc[0] = 1;
+                v = fmaf(sc.x, g, sc.y);
+            }
+            hv[a * lstr + s] = v;
+        }
     }
+    for (int s = nsf + lane; s < ls; s += 32)
+#pragma unroll
+        for (int a = 0; a < kNA; ++a) hv[a * lstr + s] = 0.f;
     __syncwarp();
-    const float *we = M.wf + (size_t)ei * M.maxweights;
-    const int hs0 = kMaxNodes;  // stride of a layer in hs/hv is M.maxnodes' bound below
-    const int ls = L.hsize / (M.nlayers + 1);
-    (void)hs0;
+    float eout = 0.f;
     for (int l = 1; l <= M.nlayers; ++l) {
         const int nprev = M.nodes[ei][l - 1], ncur = M.nodes[ei][l];
-        const float *wl = we + M.woff[ei][l];
-        for (int n = lane; n < ncur; n += 32) {
-            float z = 0.f;
-            for (int p = 0; p < nprev; ++p) z = fmaf(__ldg(wl + p * ncur + n), W.hv[(l - 1) * ls + p], z);
-            z += __ldg(wl + nprev * ncur + n);
-            if (M.normnodes) z /= (float)nprev;
-            W.hs[l * ls + n] = z;
-            W.hv[l * ls + n] = act_f(M.act[(ei * kMaxLayers + (l - 1)) * kMaxNodes + n], z);
+        const float *Wl = S.w + F.wofs[ei][l];
+        const int str = F.wstr[ei][l];
+        const float rn = M.normnodes ? 1.f / (float)nprev : 1.f;
+        const uint8_t *act = M.act + (ei * kMaxLayers + (l - 1)) * kMaxNodes;
+        if (ncur == 1) {
+            float z[kNA];
+#pragma unroll
+            for (int a = 0; a < kNA; ++a) z[a] = 0.f;
+            for (int p = lane; p < nprev; p += 32) {
+                const float w = Wl[p * str];
+#pragma unroll
+                for (int a = 0; a < kNA; ++a) z[a] = fmaf(w, hv[a * lstr + (l - 1) * ls + p], z[a]);
+            }
+            const uint8_t ac = __ldg(act);
+#pragma unroll
+            for (int a = 0; a < kNA; ++a) {
+                const float zz = (warp_sum(z[a]) + Wl[nprev * str]) * rn;
+                const float v = act_f(ac, zz);
+                if (lane == 0) {
+                    hs[a * lstr + l * ls] = zz;
+                    hv[a * lstr + l * ls] = v;
+                }
+                if (l == M.nlayers && a < na) eout += v;
+            }
+        } else {
+            for (int n = lane; n < ncur; n += 32) {
+                float z[kNA];
+#pragma unroll
+                for (int a = 0; a < kNA; ++a) z[a] = 0.f;
+                int p = 0;
+                for (; p + 4 <= nprev; p += 4) {
+                    const float w0 = Wl[p * str + n], w1 = Wl[(p + 1) * str + n], w2 = Wl[(p + 2) * str + n],
+                                w3 = Wl[(p + 3) * str + n];
+#pragma unroll
+                    for (int a = 0; a < kNA; ++a) {
+                        const float4 x = *reinterpret_cast<const float4 *>(hv + a * lstr + (l - 1) * ls + p);
+                        z[a] = fmaf(w0, x.x, fmaf(w1, x.y, fmaf(w2, x.z, fmaf(w3, x.w, z[a]))));
+                    }
+                }
+                for (; p < nprev; ++p) {
+                    const float w = Wl[p * str + n];
+#pragma unroll
+                    for (int a = 0; a < kNA; ++a) z[a] = fmaf(w, hv[a * lstr + (l - 1) * ls + p], z[a]);
+                }
+                const float b = Wl[nprev * str + n];
+                const uint8_t ac = __ldg(act + n);
+#pragma unroll
+                for (int a = 0; a < kNA; ++a) {
+                    const float zz = (z[a] + b) * rn;
+                    hs[a * lstr + l * ls + n] = zz;
+                    hv[a * lstr + l * ls + n] = act_f(ac, zz);
+                }
+            }
+            for (int n = ncur + lane; n < ls; n += 32)
+#pragma unroll
+                for (int a = 0; a < kNA; ++a) hv[a * lstr + l * ls + n] = 0.f;
         }
         __syncwarp();
     }
-    if (lane == 0) e_acc += (double)W.hv[M.nlayers * ls] + (M.remove_atom_energies ? M.atom_energy[ei] : 0.0);
-    if (!do_forces) {
-        __syncwarp();
-        return;
-    }
-    float *delta = W.hs;
+    if (!do_forces) return eout;
+    // deltas over hs, from the top layer down
     for (int l = M.nlayers; l >= 1; --l) {
         const int ncur = M.nodes[ei][l];
-        const float norm = M.normnodes ? 1.f / (float)M.nodes[ei][l - 1] : 1.f;
+        const float rn = M.normnodes ? 1.f / (float)M.nodes[ei][l - 1] : 1.f;
+        const uint8_t *act = M.act + (ei * kMaxLayers + (l - 1)) * kMaxNodes;
+        const int nn = l < M.nlayers ? M.nodes[ei][l + 1] : 0;
+        const float *Wn = l < M.nlayers ? S.w + F.wofs[ei][l + 1] : nullptr;
+        const int strn = l < M.nlayers ? F.wstr[ei][l + 1] : 0;
         for (int n = lane; n < ncur; n += 32) {
-            const uint8_t a = M.act[(ei * kMaxLayers + (l - 1)) * kMaxNodes + n];
-            const float dn = norm * act_df(a, W.hs[l * ls + n], W.hv[l * ls + n]);
-            float up = 1.f;
+            const uint8_t ac = __ldg(act + n);
+            float up[kNA];
+#pragma unroll
+            for (int a = 0; a < kNA; ++a) up[a] = 1.f;
             if (l < M.nlayers) {
-                const int nn = M.nodes[ei][l + 1];
-                const float *wl = we + M.woff[ei][l + 1];
-                up = 0.f;
-                for (int m = 0; m < nn; ++m) up = fmaf(__ldg(wl + n * nn + m), delta[(l + 1) * ls + m], up);
+#pragma unroll
+                for (int a = 0; a < kNA; ++a) up[a] = 0.f;
+                const float *row = Wn + n * strn;
+                int m = 0;
+                for (; m + 4 <= nn; m += 4) {
+                    const float4 wv = *reinterpret_cast<const float4 *>(row + m);
+#pragma unroll
+                    for (int a = 0; a < kNA; ++a) {
+                        const float4 dv = *reinterpret_cast<const float4 *>(hs + a * lstr + (l + 1) * ls + m);
+                        up[a] = fmaf(wv.x, dv.x, fmaf(wv.y, dv.y, fmaf(wv.z, dv.z, fmaf(wv.w, dv.w, up[a]))));
+                    }
+                }
+                for (; m < nn; ++m)
+#pragma unroll
+                    for (int a = 0; a < kNA; ++a) up[a] = fmaf(row[m], hs[a * lstr + (l + 1) * ls + m], up[a]);
             }
-            delta[l * ls + n] = dn * up;
+            float d[kNA];
+#pragma unroll
+            for (int a = 0; a < kNA; ++a)
+                d[a] = rn * act_df(ac, hs[a * lstr + l * ls + n], hv[a * lstr + l * ls + n]) * up[a];
+#pragma unroll
+            for (int a = 0; a < kNA; ++a) hs[a * lstr + l * ls + n] = d[a];
         }
+        for (int n = ncur + lane; n < ls; n += 32)
+#pragma unroll
+            for (int a = 0; a < kNA; ++a) hs[a * lstr + l * ls + n] = 0.f;
         __syncwarp();
     }
     {
         const int n1 = M.nodes[ei][1];
-        const float *wl = we + M.woff[ei][1];
         for (int s = lane; s < nsf; s += 32) {
-            float v = 0.f;
-            for (int n = 0; n < n1; ++n) v = fmaf(__ldg(wl + s * n1 + n), delta[ls + n], v);
-            W.dG[s] = v * F.dscal[sfb + s];
-        }
-    }
-    __syncwarp();
-
-    // ---- forces: radial part ---------------------------------------------------------------
-    for (int q = lane; q < cnt; q += 32) {
-        const float4 a = W.ra[q], b = W.rb[q], c = W.rc[q];
-        const int el = __float_as_int(c.z) >> 16;
-        const float dfc = c.x * c.y;
-        float dsum = 0.f;
+            const float *row = S.w + F.wofs[ei][1] + s * F.wstr[ei][1];
+            float u[kNA];
 #pragma unroll
-        for (int s = 0; s < kFMaxG2; ++s) {
-            if (s >= ng2) break;
-            if (F.g2e[ei][s] != el) continue;
-            const float u = c.y - F.g2rs[ei][s];
-            const float ex = exp2f(F.g2l2[ei][s] * u * u);
-            dsum = fmaf(W.dG[F.g2sf[ei][s]], ex * fmaf(-2.f * F.g2eta[ei][s] * u, b.x, dfc), dsum);
+            for (int a = 0; a < kNA; ++a) u[a] = 0.f;
+            int m = 0;
+            for (; m + 4 <= n1; m += 4) {
+                const float4 wv = *reinterpret_cast<const float4 *>(row + m);
+#pragma unroll
+                for (int a = 0; a < kNA; ++a) {
+                    const float4 dv = *reinterpret_cast<const float4 *>(hs + a * lstr + ls + m);
+                    u[a] = fmaf(wv.x, dv.x, fmaf(wv.y, dv.y, fmaf(wv.z, dv.z, fmaf(wv.w, dv.w, u[a]))));
+                }
+            }
+            for (; m < n1; ++m)
+#pragma unroll
+                for (int a = 0; a < kNA; ++a) u[a] = fmaf(row[m], hs[a * lstr + ls + m], u[a]);
+            const float dsc = F.dscal[sfb + s];
+#pragma unroll
+            for (int a = 0; a < kNA; ++a)
+                if (a < na) S.sg[(size_t)atoms[a] * L.sgs + s] = u[a] * dsc;
         }
-        const float fr = dsum * a.w;
-        W.sfx[q] = -fr * a.x;
-        W.sfy[q] = -fr * a.y;
-        W.sfz[q] = -fr * a.z;
     }
     __syncwarp();
+    return eout;
+}
 
-    // ---- forces: angular part ----------------------------------------------------------------
-    if (T > 0) {
+// ---- phase 3: forces of one central atom ---------------------------------------------
+template <int NG, int ZM>
+__device__ void nnf_forces(const NNDev &M, const FastNN &F, const NNScratch &X, const SmemF &S, const WarpF &W,
+                           const FLaunch &L, int64_t base, int i, const unsigned *mglob) {
+    constexpr int NZ = popc5(ZM), NQ = 2 * NZ;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int ei = S.elem[i];
+    const int mw = L.mw;
+    const int cnt = X.nbcnt[base + i];
+    const int *words = X.nbw + (base + i) * (int64_t)M.maxnb;
+    float g3l2[NG];
+#pragma unroll
+    for (int m = 0; m < NG; ++m) g3l2[m] = F.g3l2[ei][m];
+    build_rows<NG>(F, S, W, words, cnt, i, ei, g3l2);
+    const float *dG = S.sg + (size_t)i * L.sgs;
+
+    // ---- radial part: slot forces start here -----------------------------------------------
+    for (int q = lane; q < cnt; q += 32) {
+        W.sfx[q] = 0.f;
+        W.sfy[q] = 0.f;
+        W.sfz[q] = 0.f;
+    }
+    const float4 *g2e = S.g2 + ei * kFMaxG2;
+    for (int a = 0; a < M.nelem; ++a) {
+        const int n = F.g2cnt[ei][a];
+        if (n == 0) continue;
+        const float4 *tab = g2e + F.g2beg[ei][a];
+        const int chain = F.g2chain[ei][a];
+        float cw[kFMaxG2];
+#pragma unroll
+        for (int k = 0; k < kFMaxG2; ++k) cw[k] = k < n ? dG[__float_as_int(tab[k].w)] : 0.f;
+        for (int q = lane; q < cnt; q += 32) {
+            const float4 c = W.rc[q];
+            if ((__float_as_int(c.z) >> 16) != a) continue;
+            const float4 av = W.ra[q];
+            const float fc = W.rb[q].x, dfc = c.x * c.y, r = c.y;
+            float dsum = 0.f;
+            g2_group(tab, n, chain, r, r * r, [&](int k, float e) {
+                dsum = fmaf(cw[k] * e, fmaf(tab[k].z * (r - tab[k].y), fc, dfc), dsum);
+            });
+            const float fr = dsum * av.w;
+            W.sfx[q] -= fr * av.x;
+            W.sfy[q] -= fr * av.y;
+            W.sfz[q] -= fr * av.z;
+        }
+    }
+
+    // ---- angular part ------------------------------------------------------------------------
+    const bool g3 = F.hasg3[ei] != 0;
+    const int nrows = cnt - 1, npairs = (g3 && nrows > 0) ? (nrows + 1) / 2 : 0;
+    if (npairs > 0) {
+        for (int k = lane; k < cnt * mw; k += 32) W.mask[k] = mglob[k];
+        __syncwarp();
+        for (int q = lane; q < nrows; q += 32) {
+            int c = 0;
+            for (int w = (q + 1) >> 5; w < mw; ++w) c += __popc(W.mask[q * mw + w]);
+            W.rcnt[q] = c;
+        }
         float Wy[NG][NQ], Wz[NG][NQ], eta[NG];
 #pragma unroll
         for (int m = 0; m < NG; ++m) {
             eta[m] = F.g3eta[ei][m];
 #pragma unroll
             for (int q = 0; q < NQ; ++q) {
-                const int s = F.cell_sf[ei][m][q];
-                const float c = s >= 0 ? W.dG[s] : 0.f;
+                const int sidx = F.cell_sf[ei][m][q];
+                const float c = sidx >= 0 ? dG[sidx] : 0.f;
                 Wy[m][q] = 2.f * c;
                 Wz[m][q] = F.cell_lz[q] * c;
             }
         }
-        int e0, e1, p, pos;
-        share(e0, e1, p, pos);
-        int pc = W.tcnt[p], psp = W.tsplit[p], cq3 = -1;
-        float4 JA = make_float4(0.f, 0.f, 0.f, 0.f), JB = JA, JC = JA;
-        float fjx = 0.f, fjy = 0.f, fjz = 0.f;
-        for (int e = e0; e < e1; ++e) {
-            while (pos >= pc) {
-                ++p;
-                pos = 0;
-                pc = W.tcnt[p];
-                psp = W.tsplit[p];
-            }
-            const int q3 = pos < psp ? p : nrows - 1 - p;
-            const int q4 = W.tq4[(size_t)p * L.maxnb + pos];
-            ++pos;
-            if (q3 != cq3) {
-                if (cq3 >= 0) {
-                    atomicAdd(&W.sfx[cq3], fjx);
-                    atomicAdd(&W.sfy[cq3], fjy);
-                    atomicAdd(&W.sfz[cq3], fjz);
+        __syncwarp();
+        for (int p = lane; p < npairs; p += 32) {
+            const int r1 = nrows - 1 - p;
+            const int ntr = W.rcnt[p] + (r1 != p ? W.rcnt[r1] : 0);
+            RowBits it;
+            it.start(W.mask, mw, p, nrows);
+            int cq3 = -1;
+            float4 JA = make_float4(0.f, 0.f, 0.f, 0.f), JB = JA, JC = JA;
+            float fjx = 0.f, fjy = 0.f, fjz = 0.f;
+            for (int e = 0; e < ntr; ++e) {
+                int q3, q4;
+                it.next(q3, q4);
+                if (q3 != cq3) {
+                    if (cq3 >= 0) {
+                        red_shared(&W.sfx[cq3], fjx);
+                        red_shared(&W.sfy[cq3], fjy);
+                        red_shared(&W.sfz[cq3], fjz);
+                    }
+                    fjx = fjy = fjz = 0.f;
+                    cq3 = q3;
+                    JA = W.ra[q3];
+                    JB = W.rb[q3];
+                    JC = W.rc[q3];
                 }
-                fjx = fjy = fjz = 0.f;
-                cq3 = q3;
-                JA = W.ra[q3];
-                JB = W.rb[q3];
-                JC = W.rc[q3];
-            }
-            const float4 KA = W.ra[q4], KB = W.rb[q4], KC = W.rc[q4];
-            const float jx = JA.x - KA.x, jy = JA.y - KA.y, jz = JA.z - KA.z;
-            const float rjk2 = jx * jx + jy * jy + jz * jz;
-            float fcjk, dfds;
-            fc_of_s_d(fminf(rjk2 * F.inv_rc2, 1.f), fcjk, dfds);
-            const float dfcrjk = 2.f * dfds * F.inv_rc2;
-            const float rr = JA.w * KA.w;
-            const float u = (JA.x * KA.x + JA.y * KA.y + JA.z * KA.z) * rr;
-            const float Ej[4] = {JB.y, JB.z, JB.w, JC.w};
-            const float Ek[4] = {KB.y, KB.z, KB.w, KC.w};
-            float Xm[NG];
+                const float4 KA = W.ra[q4], KB = W.rb[q4], KC = W.rc[q4];
+                const float jx = JA.x - KA.x, jy = JA.y - KA.y, jz = JA.z - KA.z;
+                const float rjk2 = jx * jx + jy * jy + jz * jz;
+                float fcjk, dfds;
+                fc_of_s_d(fminf(rjk2 * F.inv_rc2, 1.f), fcjk, dfds);
+                const float dfcrjk = 2.f * dfds * F.inv_rc2;
+                const float rr = JA.w * KA.w;
+                const float u = (JA.x * KA.x + JA.y * KA.y + JA.z * KA.z) * rr;
+                const float Ej[4] = {JB.y, JB.z, JB.w, JC.w};
+                const float Ek[4] = {KB.y, KB.z, KB.w, KC.w};
+                float Xm[NG];
 #pragma unroll
-            for (int m = 0; m < NG; ++m) Xm[m] = Ej[m] * Ek[m] * exp2f(g3l2[m] * rjk2);
-            float Pp[NZ], Pm[NZ], Qp[NZ], Qm[NZ];
-            zeta_powers<ZM, true>(fmaf(0.5f, u, 0.5f), Pp, Qp);
-            zeta_powers<ZM, true>(fmaf(-0.5f, u, 0.5f), Pm, Qm);
-            float A1 = 0.f, A2 = 0.f, Bs = 0.f;
+                for (int m = 0; m < NG; ++m) Xm[m] = Ej[m] * Ek[m] * exp2f(g3l2[m] * rjk2);
+                float Pp[NZ], Pm[NZ], Qp[NZ], Qm[NZ];
+                zeta_powers<ZM, true>(fmaf(0.5f, u, 0.5f), Pp, Qp);
+                zeta_powers<ZM, true>(fmaf(-0.5f, u, 0.5f), Pm, Qm);
+                float A1 = 0.f, A2 = 0.f, Bs = 0.f;
 #pragma unroll
-            for (int m = 0; m < NG; ++m) {
-                float Y = 0.f, Z = 0.f;
+                for (int m = 0; m < NG; ++m) {
+                    float Y = 0.f, Z = 0.f;
 #pragma unroll
-                for (int k = 0; k < NZ; ++k) {
-                    Y = fmaf(Wy[m][2 * k], Pp[k], Y);
-                    Y = fmaf(Wy[m][2 * k + 1], Pm[k], Y);
-                    Z = fmaf(Wz[m][2 * k], Qp[k], Z);
-                    Z = fmaf(Wz[m][2 * k + 1], Qm[k], Z);
+                    for (int z = 0; z < NZ; ++z) {
+                        Y = fmaf(Wy[m][2 * z], Pp[z], Y);
+                        Y = fmaf(Wy[m][2 * z + 1], Pm[z], Y);
+                        Z = fmaf(Wz[m][2 * z], Qp[z], Z);
+                        Z = fmaf(Wz[m][2 * z + 1], Qm[z], Z);
+                    }
+                    A1 = fmaf(Xm[m], Z, A1);
+                    const float xy = Xm[m] * Y;
+                    Bs += xy;
+                    A2 = fmaf(eta[m], xy, A2);
                 }
-                A1 = fmaf(Xm[m], Z, A1);
-                const float xy = Xm[m] * Y;
-                Bs += xy;
-                A2 = fmaf(eta[m], xy, A2);
+                const float pfc = JB.x * KB.x * fcjk;
+                const float t1 = pfc * A1, t2 = pfc * A2;
+                const float gj = -t1 * u * JA.w * JA.w - 4.f * t2 + Bs * KB.x * fmaf(JC.x, fcjk, JB.x * dfcrjk);
+                const float gk = -t1 * u * KA.w * KA.w - 4.f * t2 + Bs * JB.x * fmaf(KC.x, fcjk, KB.x * dfcrjk);
+                const float gx = t1 * rr + 2.f * t2 - Bs * JB.x * KB.x * dfcrjk;
+                fjx -= gj * JA.x + gx * KA.x;
+                fjy -= gj * JA.y + gx * KA.y;
+                fjz -= gj * JA.z + gx * KA.z;
+                red_shared(&W.sfx[q4], -(gk * KA.x + gx * JA.x));
+                red_shared(&W.sfy[q4], -(gk * KA.y + gx * JA.y));
+                red_shared(&W.sfz[q4], -(gk * KA.z + gx * JA.z));
             }
-            const float pfc = JB.x * KB.x * fcjk;
-            const float t1 = pfc * A1, t2 = pfc * A2;
-            const float gj = -t1 * u * JA.w * JA.w - 4.f * t2 + Bs * KB.x * fmaf(JC.x, fcjk, JB.x * dfcrjk);
-            const float gk = -t1 * u * KA.w * KA.w - 4.f * t2 + Bs * JB.x * fmaf(KC.x, fcjk, KB.x * dfcrjk);
-            const float gx = t1 * rr + 2.f * t2 - Bs * JB.x * KB.x * dfcrjk;
-            fjx -= gj * JA.x + gx * KA.x;
-            fjy -= gj * JA.y + gx * KA.y;
-            fjz -= gj * JA.z + gx * KA.z;
-            atomicAdd(&W.sfx[q4], -(gk * KA.x + gx * JA.x));
-            atomicAdd(&W.sfy[q4], -(gk * KA.y + gx * JA.y));
-            atomicAdd(&W.sfz[q4], -(gk * KA.z + gx * JA.z));
-        }
-        if (cq3 >= 0) {
-            atomicAdd(&W.sfx[cq3], fjx);
-            atomicAdd(&W.sfy[cq3], fjy);
-            atomicAdd(&W.sfz[cq3], fjz);
+            if (cq3 >= 0) {
+                red_shared(&W.sfx[cq3], fjx);
+                red_shared(&W.sfy[cq3], fjy);
+                red_shared(&W.sfz[cq3], fjz);
+            }
         }
     }
     __syncwarp();
 
     // ---- scatter: neighbours get their slot forces, the centre minus their sum ----------
+    float *fwx = S.fw + (size_t)warp * 3 * L.max_atoms, *fwy = fwx + L.max_atoms, *fwz = fwy + L.max_atoms;
     float fix = 0.f, fiy = 0.f, fiz = 0.f;
-    for (int q = lane; q < cnt; q += 32) {
-        const int j = __float_as_int(W.rc[q].z) & 0xFFFF;
-        const float sx = W.sfx[q], sy = W.sfy[q], sz = W.sfz[q];
-        atomicAdd(&S.fx[j], sx);
-        atomicAdd(&S.fy[j], sy);
-        atomicAdd(&S.fz[j], sz);
-        fix -= sx;
-        fiy -= sy;
-        fiz -= sz;
+    for (int q0 = 0; q0 < cnt; q0 += 32) {
+        const int q = q0 + lane;
+        const bool ok = q < cnt;
+        const int j = ok ? (__float_as_int(W.rc[q].z) & 0xFFFF) : -1 - lane;
+        const unsigned same = __match_any_sync(0xffffffffu, j);
+        if (ok) {
+            const float sx = W.sfx[q], sy = W.sfy[q], sz = W.sfz[q];
+            if (same == (1u << lane)) {
+                fwx[j] += sx;
+                fwy[j] += sy;
+                fwz[j] += sz;
+            } else {  // several images of atom j in this block of neighbours
+                atomicAdd(&fwx[j], sx);
+                atomicAdd(&fwy[j], sy);
+                atomicAdd(&fwz[j], sz);
+            }
+            fix -= sx;
+            fiy -= sy;
+            fiz -= sz;
+        }
+        __syncwarp();
     }
     fix = warp_sum(fix);
     fiy = warp_sum(fiy);
     fiz = warp_sum(fiz);
     if (lane == 0) {
-        atomicAdd(&S.fx[i], fix);
-        atomicAdd(&S.fy[i], fiy);
-        atomicAdd(&S.fz[i], fiz);
+        fwx[i] += fix;
+        fwy[i] += fiy;
+        fwz[i] += fiz;
     }
     __syncwarp();
+}
+
+// atoms of the trajectory ordered by element (network groups share an element)
+__device__ void order_by_element(const NNDev &M, const SmemF &S, const FLaunch &L, int N) {
+    if (threadIdx.x == 0) {
+        int *off = S.byel + L.max_atoms;
+        int k = 0;
+        for (int e = 0; e < M.nelem; ++e) {
+            off[e] = k;
+            for (int i = 0; i < N; ++i)
+                if (S.elem[i] == e) S.byel[k++] = i;
+        }
+        off[M.nelem] = k;
+    }
+    __syncthreads();
 }
 
 // ---- one bead ---------------------------------------------------------------------------
@@ -704,13 +970,14 @@ __device__ bool nnf_bead(const Batch &B, const NNDev &M, const FastNN &F, const 
                          const FLaunch &L, int t, int b, bool do_forces, bool skip_if_flagged) {
     const int N = B.natoms[t];
     const int64_t base = B.ba_off[t] + (int64_t)b * N;
-    const int aoff = B.atom_off[t];
     const int tid = threadIdx.x, nt = blockDim.x;
     const int warp = tid >> 5, lane = tid & 31;
     if (tid == 0) {
         acsf_lattice(B.box + 9 * t, S.lat);
         S.misc[0] = 0;
         S.misc[1] = 0;
+        S.misc[2] = 0;
+        S.misc[3] = 0;
     }
     __syncthreads();
     if (tid < 9) {
@@ -735,22 +1002,52 @@ __device__ bool nnf_bead(const Batch &B, const NNDev &M, const FastNN &F, const 
         S.xl[i] = (float)(x - (double)xh);
         S.yl[i] = (float)(y - (double)yh);
         S.zl[i] = (float)(z - (double)zh);
-        S.elem[i] = (int8_t)M.elem_of_type[B.type[aoff + i]];
-        S.fx[i] = 0.f;
-        S.fy[i] = 0.f;
-        S.fz[i] = 0.f;
     }
+    if (do_forces)
+        for (int k = tid; k < kFW * 3 * L.max_atoms; k += nt) S.fw[k] = 0.f;
     __syncthreads();
     const int na[3] = {X.img[3 * t], X.img[3 * t + 1], X.img[3 * t + 2]};
-    const WarpF W = carve_warp(S, L, warp);
+    unsigned *mscr = X.mscr + (size_t)blockIdx.x * X.mcap;
+    const size_t mstride = (size_t)L.maxnb * L.mw;
+    {
+        const WarpF W = carve_warp(S, L, warp);
+        for (;;) {
+            int i = 0;
+            if (lane == 0) i = atomicAdd(&S.misc[1], 1);
+            i = __shfl_sync(0xffffffffu, i, 0);
+            if (i >= N) break;
+            if (S.elem[i] < 0) continue;
+            nnf_descriptors<NG, ZM>(M, F, X, S, W, L, t, base, i, N, na, mscr + (size_t)i * mstride);
+        }
+    }
+    __syncthreads();
+    // network: groups of kNA atoms of one element
     double e_warp = 0.0;
-    for (;;) {
-        int i = 0;
-        if (lane == 0) i = atomicAdd(&S.misc[1], 1);
-        i = __shfl_sync(0xffffffffu, i, 0);
-        if (i >= N) break;
-        if (S.elem[i] < 0) continue;
-        nnf_atom<NG, ZM>(M, F, X, S, W, L, t, i, N, na, do_forces, e_warp);
+    {
+        float *hs = (float *)(S.warp_base + (size_t)warp * S.warp_bytes);
+        float *hv = hs + kNA * (M.nlayers + 1) * L.ls;
+        const int *off = S.byel + L.max_atoms;
+        int ngroups = 0;
+        for (int e = 0; e < M.nelem; ++e) ngroups += (off[e + 1] - off[e] + kNA - 1) / kNA;
+        for (;;) {
+            int g = 0;
+            if (lane == 0) g = atomicAdd(&S.misc[2], 1);
+            g = __shfl_sync(0xffffffffu, g, 0);
+            if (g >= ngroups) break;
+            int e = 0, first = 0;
+            for (int k = 0; k < M.nelem; ++k) {
+                const int ng = (off[k + 1] - off[k] + kNA - 1) / kNA;
+                if (g < ng) {
+                    e = k;
+                    first = off[k] + g * kNA;
+                    break;
+                }
+                g -= ng;
+            }
+            const int n = min(kNA, off[e + 1] - first);
+            const float en = nnf_network4(M, F, S, L, hs, hv, e, S.byel + first, n, do_forces);
+            if (lane == 0) e_warp += (double)en + n * (M.remove_atom_energies ? M.atom_energy[e] : 0.0);
+        }
     }
     const double etot = block_sum(e_warp, S.red);  // contains __syncthreads: flag visible
     const bool flagged = S.misc[0] != 0;
@@ -759,13 +1056,35 @@ __device__ bool nnf_bead(const Batch &B, const NNDev &M, const FastNN &F, const 
         return true;
     }
     if (tid == 0) B.epot[B.bead_off[t] + b] += etot * kHa2eVF;
-    if (do_forces) {
-        const double c = kHa2eVF * kAng2BohrD;
-        for (int i = tid; i < N; i += nt) {
-            B.fx[base + i] += (double)S.fx[i] * c;
-            B.fy[base + i] += (double)S.fy[i] * c;
-            B.fz[base + i] += (double)S.fz[i] * c;
+    if (!do_forces) {
+        __syncthreads();
+        return flagged;
+    }
+    {
+        const WarpF W = carve_warp(S, L, warp);
+        for (;;) {
+            int i = 0;
+            if (lane == 0) i = atomicAdd(&S.misc[3], 1);
+            i = __shfl_sync(0xffffffffu, i, 0);
+            if (i >= N) break;
+            if (S.elem[i] < 0) continue;
+            nnf_forces<NG, ZM>(M, F, X, S, W, L, base, i, mscr + (size_t)i * mstride);
         }
+    }
+    __syncthreads();
+    const double c = kHa2eVF * kAng2BohrD;
+    for (int i = tid; i < N; i += nt) {
+        float fx = 0.f, fy = 0.f, fz = 0.f;
+#pragma unroll
+        for (int w = 0; w < kFW; ++w) {
+            const float *f = S.fw + (size_t)w * 3 * L.max_atoms;
+            fx += f[i];
+            fy += f[L.max_atoms + i];
+            fz += f[2 * L.max_atoms + i];
+        }
+        B.fx[base + i] += (double)fx * c;
+        B.fy[base + i] += (double)fy * c;
+        B.fz[base + i] += (double)fz * c;
     }
     __syncthreads();
     return flagged;
@@ -807,6 +1126,22 @@ __device__ void nnf_calc_force(const Batch &B, const NNDev &M, const FastNN &F, 
     __syncthreads();
 }
 
+// network weights into their padded shared-memory layout; radial-function table
+__device__ void load_model_smem(const NNDev &M, const FastNN &F, const SmemF &S) {
+    for (int e = 0; e < M.nelem; ++e)
+        for (int l = 1; l <= M.nlayers; ++l) {
+            const int nprev = M.nodes[e][l - 1], ncur = M.nodes[e][l], str = F.wstr[e][l];
+            const float *src = M.wf + (size_t)e * M.maxweights + M.woff[e][l];
+            float *dst = S.w + F.wofs[e][l];
+            for (int k = threadIdx.x; k < (nprev + 1) * str; k += blockDim.x) {
+                const int p = k / str, n = k % str;
+                dst[k] = n < ncur ? src[p * ncur + n] : 0.f;
+            }
+        }
+    for (int k = threadIdx.x; k < M.nelem * kFMaxG2; k += blockDim.x) S.g2[k] = F.g2tab[k];
+    __syncthreads();
+}
+
 // mode 0: forces, 1: energies only, 2: nsteps fused MD steps (propagate_1, forces,
 // propagate_2, exit test), as the generic network kernels.
 template <int NG, int ZM>
@@ -815,10 +1150,11 @@ __global__ void __launch_bounds__(kFBlock, 2)
                int *counter, int nsteps, int mode) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int work_slot;
-    const SmemF S = carve_f(smem_raw, L, B.max_beads);
+    const SmemF S = carve_f(smem_raw, L, B.max_beads, F.wtotal, M.nelem, M.nlayers);
     SmemEmt<double> SE = carve_smem<double>(S.warp_base, B.max_atoms, B.max_beads);
     SE.red = S.red;
     SE.cjk = S.cjk;
+    load_model_smem(M, F, S);
     for (;;) {
         if (threadIdx.x == 0) work_slot = atomicAdd(counter, 1);
         __syncthreads();
@@ -828,6 +1164,9 @@ __global__ void __launch_bounds__(kFBlock, 2)
         const int t = order[w];
         const TrajView T = traj_view(B, t);
         load_cjk(B, t, S.cjk);
+        for (int i = threadIdx.x; i < T.N; i += blockDim.x) S.elem[i] = (int8_t)M.elem_of_type[B.type[T.aoff + i]];
+        __syncthreads();
+        order_by_element(M, S, L, T.N);
         if (mode != 2) {
             nnf_calc_force<NG, ZM>(B, M, F, E, X, P, S, SE, L, T, mode == 0);
             continue;
@@ -876,19 +1215,6 @@ int nnf_occupancy_t(size_t sm) {
     return n;
 }
 
-FLaunch flaunch(const Batch &B, const NNDev &M, int surrogate) {
-    FLaunch L;
-    L.max_atoms = B.max_atoms;
-    L.maxnb = M.maxnb;
-    L.npmax = (M.maxnb + 1) / 2;
-    int mx = 1;
-    for (int e = 0; e < M.nelem; ++e)
-        for (int l = 0; l <= M.nlayers; ++l) mx = mx > M.nodes[e][l] ? mx : M.nodes[e][l];
-    L.hsize = (M.nlayers + 1) * mx;
-    L.surrogate = surrogate;
-    return L;
-}
-
 }  // namespace
 
 // Kernels exist for the zeta set {1, 4, 16} (a subset runs with zero-weight cells) and
@@ -901,13 +1227,12 @@ int nnf_zm_supported(int zm) { return (zm & ~0x15) == 0 ? 0x15 : 0; }
         case 4: CALL(4, 0x15); default: break;                               \
     }
 
-size_t nnf_total_smem(const Batch &B, const NNDev &M) {
-    const FLaunch L = flaunch(B, M, 0);
-    return nnf_smem_bytes(B.max_atoms, B.max_beads, L.maxnb, L.npmax, L.hsize);
-}
+size_t nnf_total_smem(const Batch &B, const NNDev &M, const FastNN &F) { return nnf_smem_total(B, M, F); }
+
+int nnf_warps_per_cta() { return kFW; }
 
 int nnf_resident_ctas(const Batch &B, const NNDev &M, const FastNN &F) {
-    const size_t sm = nnf_total_smem(B, M);
+    const size_t sm = nnf_smem_total(B, M, F);
 #define MDT_OCC(NG, ZM) return std::max(1, nnf_occupancy_t<NG, ZM>(sm));
     MDT_NNF_DISPATCH(MDT_OCC)
 #undef MDT_OCC
@@ -917,7 +1242,7 @@ int nnf_resident_ctas(const Batch &B, const NNDev &M, const FastNN &F) {
 cudaError_t launch_nnf(const LaunchCfg &c, const Batch &B, const NNDev &M, const FastNN &F, const EmtConst &E,
                        const NNScratch &X, const PropParams &P, int nsteps, int mode, bool surrogate) {
     const FLaunch L = flaunch(B, M, surrogate ? 1 : 0);
-    const size_t sm = nnf_smem_bytes(B.max_atoms, B.max_beads, L.maxnb, L.npmax, L.hsize);
+    const size_t sm = nnf_smem_total(B, M, F);
 #define MDT_LAUNCH(NG, ZM) return nnf_launch_t<NG, ZM>(c, B, M, F, E, X, P, L, sm, nsteps, mode);
     MDT_NNF_DISPATCH(MDT_LAUNCH)
 #undef MDT_LAUNCH

@@ -297,12 +297,31 @@ def acsf_set(center: str, neighbours: list, rc_ang: float = 6.5) -> list:
     return sort_symfunctions(out)
 
 
-def random_model(elements: list, hidden=(25, 25), act="t", seed: int = 0, neighbours=None) -> NNModel:
+def radial_set(center: str, neighbours: list, rc_ang: float = 6.5) -> list:
+    """24 centred G2 per neighbour element, no angular functions: eta_k = 0.002 *
+    2^(k/3) 1/A^2 (k = 0..23, 0.002-0.41 1/A^2), generated so that eta_{k+3} = 2 eta_k
+    holds exactly (the FP32 kernels then get exp(-eta_{k+3} r^2) by squaring
+    exp(-eta_k r^2)).  Cosine cutoff at rc_ang."""
+    a2b = C.ANG2BOHR
+    rc = rc_ang * a2b
+    etas = [0.002, 0.002 * 2.0 ** (1.0 / 3.0), 0.002 * 2.0 ** (2.0 / 3.0)]
+    while len(etas) < 24:
+        etas.append(2.0 * etas[-3])
+    out = []
+    for z in sorted(Z_OF[n] for n in neighbours):
+        for eta in etas:
+            out.append(SymFunc(2, eta=eta / a2b ** 2, rshift=0.0, rc=rc, e1=z))
+    return sort_symfunctions(out)
+
+
+def random_model(elements: list, hidden=(25, 25), act="t", seed: int = 0, neighbours=None,
+                 descriptor: str = "acsf") -> NNModel:
     """Seeded Glorot-uniform network with the ACSF set above for every element."""
     rng = np.random.default_rng(seed)
     elements = sorted(elements, key=lambda e: Z_OF[e])
     neighbours = neighbours or elements
-    sfs = [acsf_set(e, neighbours) for e in elements]
+    make = {"acsf": acsf_set, "radial": radial_set}[descriptor]
+    sfs = [make(e, neighbours) for e in elements]
     nodes = [[len(s)] + list(hidden) + [1] for s in sfs]
     acts = [[act * n[l + 1] for l in range(len(hidden))] + ["l"] for n in nodes]
     weights = []

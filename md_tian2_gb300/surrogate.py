@@ -61,8 +61,11 @@ def generate_dataset(ntraj: int = 4096, nsamples: int = 8, every: int = 50, seed
     return Dataset(out_u, np.array(out_e), out_f)
 
 
-def surrogate_model(seed: int = 11) -> nene.NNModel:
-    return nene.random_model(["H", "Au"], hidden=(32, 32), act="p", seed=seed, neighbours=["Au"])
+def surrogate_model(seed: int = 11, descriptor: str = "acsf") -> nene.NNModel:
+    """Untrained surrogate network: ``descriptor`` "acsf" = 8 G2 + 16 G3 per element
+    (``nene.acsf_set``), "radial" = 24 G2 (``nene.radial_set``); 24-32-32-1 softplus."""
+    return nene.random_model(["H", "Au"], hidden=(32, 32), act="p", seed=seed, neighbours=["Au"],
+                             descriptor=descriptor)
 
 
 def _opts(lr, w_energy, w_force, precision):

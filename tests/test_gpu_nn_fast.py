@@ -66,6 +66,26 @@ def test_fast_path_qualifies_and_matches_oracle(built_lib, oracle_lib):
         assert abs(out["epot"][t] - E) < 2e-6 * max(1.0, abs(E)), t
 
 
+def test_fast_path_radial_model_matches_oracle(built_lib, oracle_lib):
+    """24 centred G2, no angular functions (the triplet stages are skipped; 21 of the 24
+    exponentials come from squaring, which doubles their relative FP32 error per level,
+    so the bar is 1e-4 of the force RMS)."""
+    from oracle.oracle import NNOracle
+    us = W.config2(5, seed=8)
+    m = surrogate_model(3, descriptor="radial")
+    eng = _engine(us, m)
+    assert eng.nn_fast_path(True)
+    eng.calc_force(SimParams(), precision="fp32")
+    out = eng.download()
+    eng.close()
+    o = NNOracle(m)
+    for t, u in enumerate(us):
+        E, F = o.energy_force(_elems(u), u.r[:, 0, :], u.simbox)
+        f = eng.split(out["f"], t)[:, 0, :]
+        assert np.sqrt(np.mean((f - F) ** 2)) < 1e-4 * np.sqrt(np.mean(F ** 2)), t
+        assert abs(out["epot"][t] - E) < 5e-5 * max(1.0, abs(E)), t
+
+
 def test_fast_path_scaled_model_matches_oracle_like_generic(built_lib, oracle_lib):
     """Scaled descriptors from six configurations: (g - min)/(max - min) amplifies FP32
     rounding of G by |g|/(max - min), for both FP32 paths alike.  The fast path stays
