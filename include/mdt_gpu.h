@@ -143,6 +143,12 @@ int32_t mdt_set_pes(mdt_ctx *ctx, int32_t pes_kind, double range_margin);
    qualifies, else 0 (no replacement in the reference: RuNNer has one code path). */
 int32_t mdt_nn_fast_path(mdt_ctx *ctx, int32_t enable);
 
+/* Verlet skin (A) of the fast kernels' neighbour lists (default 1.0; 0 = build every
+   step).  Lists are rebuilt when an atom of the bead moved more than half the skin
+   since the last build; the per-step list is filtered from it with the same exact
+   cutoff test, so results do not depend on the skin. */
+int32_t mdt_nn_set_skin(mdt_ctx *ctx, double skin_ang);
+
 /* per trajectory: number of bead evaluations that fell back to EMT, and 1 if a
    neighbour list overflowed max_neighbors (either may be NULL) */
 int32_t mdt_nn_stats(mdt_ctx *ctx, int32_t *fallbacks, int32_t *overflow);

@@ -64,6 +64,13 @@ struct mdt_ctx {
     float *d_dscal = nullptr;
     unsigned *mscr = nullptr;  // fast-path mask scratch (grows on demand)
     size_t mscr_n = 0;
+    // fast-path Verlet skin lists (with the batch); skin in A (0: off)
+    int2 *skw = nullptr;
+    int *skcnt = nullptr, *skok = nullptr;
+    double *skref = nullptr;
+    int skcap = 0;
+    double skin_ang = 1.0;
+    bool skin_dirty = true;
 
     // training (buffers live with the batch)
     bool have_labels = false;
@@ -96,6 +103,11 @@ template <typename T> T *dalloc(mdt_ctx *c, size_t n, cudaError_t &e) {
 
 void free_batch(mdt_ctx *c) {
     c->X = NNScratch{};
+    c->skw = nullptr;
+    c->skcnt = c->skok = nullptr;
+    c->skref = nullptr;
+    c->skcap = 0;
+    c->skin_dirty = true;
     c->have_labels = false;
     c->nn_maxnb_alloc = 0;
     for (auto &b : c->bufs) cudaFree(b.p);
@@ -427,6 +439,31 @@ int ensure_mscr(mdt_ctx *c, int grid) {
     }
     c->X.mscr = c->mscr;
     c->X.mcap = (int)per;
+    // skin lists: 2 maxnb entries per bead-atom (the skin adds about 55 % to the list)
+    const int skcap = 2 * c->M.maxnb;
+    cudaError_t e = cudaSuccess;
+    if (!c->skw || c->skcap != skcap) {
+        c->skw = dalloc<int2>(c, (size_t)c->total_ba * skcap, e);
+        c->skcnt = dalloc<int>(c, (size_t)c->total_ba, e);
+        c->skref = dalloc<double>(c, 3 * (size_t)c->total_ba, e);
+        c->skok = dalloc<int>(c, (size_t)c->total_beads, e);
+        if (!c->skw || !c->skcnt || !c->skref || !c->skok) return fail(c, MDT_ERR_NOMEM, "skin-list allocation failed");
+        c->skcap = skcap;
+        c->skin_dirty = true;
+    }
+    if (c->skin_dirty) {
+        e = cudaMemsetAsync(c->skok, 0, sizeof(int) * c->total_beads, c->stream);
+        if (e != cudaSuccess) return cuda_fail(c, e, "skin-list reset");
+        c->skin_dirty = false;
+    }
+    c->X.skw = c->skw;
+    c->X.skcnt = c->skcnt;
+    c->X.skref = c->skref;
+    c->X.skok = c->skok;
+    c->X.skcap = skcap;
+    c->F.skin = (float)(c->skin_ang / kBohr2Ang);
+    const double rs = c->M.maxcut + c->skin_ang / kBohr2Ang;
+    c->F.cut2s = (float)(rs * rs) * 1.0001f;
     return MDT_OK;
 }
 
@@ -1157,6 +1194,7 @@ int32_t mdt_nn_set_model(mdt_ctx *c, const mdt_nn_model *m, int32_t ntypes, cons
     c->have_nn = true;
     c->X = NNScratch{};  // re-allocated for the new neighbour bound on next use
     c->nn_maxnb_alloc = 0;
+    c->skin_dirty = true;
     return upload_fast_scaling(c);
 }
 
@@ -1169,6 +1207,14 @@ int32_t mdt_set_pes(mdt_ctx *c, int32_t pes_kind, double range_margin) {
     c->margin = range_margin;
     c->M.margin = (float)range_margin;
     return c->have_nn ? upload_fast_scaling(c) : MDT_OK;
+}
+
+int32_t mdt_nn_set_skin(mdt_ctx *c, double skin_ang) {
+    if (!c) return MDT_ERR_ARG;
+    if (!(skin_ang >= 0.0) || skin_ang > 5.0) return fail(c, MDT_ERR_ARG, "skin must be in [0, 5] A");
+    c->skin_ang = skin_ang;
+    c->skin_dirty = true;
+    return MDT_OK;
 }
 
 int32_t mdt_nn_fast_path(mdt_ctx *c, int32_t enable) {

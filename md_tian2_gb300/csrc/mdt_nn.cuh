@@ -67,7 +67,7 @@ struct NNDev {
 // and the G3 functions of each element form a grid of eta slots x (lambda = +-1,
 // zeta = 2^b) cells over one neighbour-element pair.
 // ---------------------------------------------------------------------------
-constexpr int kFMaxG2 = 32;  // radial functions per element
+constexpr int kFMaxG2 = 24;  // radial functions per element and neighbour element
 constexpr int kFNQ = 8;      // (lambda, zeta) cells: lambda = +-1 for up to 4 zeta values
 
 struct FastNN {
@@ -76,6 +76,7 @@ struct FastNN {
     int anyg3;                     // some element has G3 functions
     float rc2, inv_rc2;            // bohr^-2
     float cut2_hi, cut2_lo;        // FP32 screen of the neighbour list (bohr^2)
+    float skin, cut2s;             // Verlet skin (bohr, 0: off) and the skin list's squared cutoff
     int hasg3[kMaxElem];
     int pair_a[kMaxElem], pair_b[kMaxElem];  // G3 neighbour-element pair (element indices)
     float g3l2[kMaxElem][4];       // -eta_m log2(e), for exp2
@@ -108,6 +109,13 @@ struct NNScratch {
     double *gout;      // optional: raw symmetry functions [ba][maxsf] (descriptor export)
     unsigned *mscr;    // fast path: triplet masks of a bead, mcap words per CTA
     int mcap;
+    // fast path Verlet skin lists: per bead-atom skcap entries (j, packed unwrapped image),
+    // count (-1: overflow, full build), reference positions, per-bead validity
+    int2 *skw;
+    int *skcnt;
+    double *skref;
+    int *skok;
+    int skcap;
 };
 
 // ---------------------------------------------------------------------------

@@ -141,14 +141,15 @@ struct SmemF {
     double *px, *py, *pz;                // wrapped positions (bohr)
     float *xh, *yh, *zh, *xl, *yl, *zl;  // their FP32 hi/lo split
     int8_t *elem;
+    int *fold;                           // fold counts of the wrapping, 3 x 8 bits (+128)
     int *byel;                           // atoms ordered by element; [max_atoms + kMaxElem + 1] offsets after
     float *fw;                           // [warp][3][max_atoms] force accumulators (Ha/bohr)
     float *sg;                           // [max_atoms][sgs]: descriptors G, then dE/dG
     double *lat;                         // 9 lattice rows + 9 inverse (bohr)
-    float *latf, *ginv, *wk;             // FP32 lattice rows, inverse rows, image half-widths
+    float *latf, *ginv, *wk;             // FP32 lattice rows, inverse rows, image half-widths (cutoff, skin list)
     double *red;                         // block reductions
     double *cjk;                         // ring-polymer transform of the trajectory
-    int *misc;                           // [0] range flag, [1..3] work counters of the three phases
+    int *misc;                           // [0] range flag, [1] group counter, [2] rebuild skin lists, [3] max displacement
     float *w;                            // network weights (FastNN::wofs layout)
     float4 *g2;                          // radial-function table (FastNN::g2tab)
     unsigned char *warp_base;            // per-warp areas
@@ -176,7 +177,8 @@ __host__ __device__ inline size_t warp_bytes_f(int maxnb, int mw, int nlayers, i
 
 __host__ __device__ inline size_t shared_bytes_f(int max_atoms, int max_beads, int wtotal, int nelem, int sgs) {
     return 3 * r16f(8 * (size_t)max_atoms) + 6 * r16f(4 * (size_t)max_atoms) + r16f(max_atoms) +
-           r16f(4 * ((size_t)max_atoms + kMaxElem + 1)) + r16f(4 * (size_t)kFW * 3 * max_atoms) +
+           r16f(4 * (size_t)max_atoms) + r16f(4 * ((size_t)max_atoms + kMaxElem + 1)) +
+           r16f(4 * (size_t)kFW * 3 * max_atoms) +
            r16f(4 * (size_t)max_atoms * sgs) + r16f(8 * 18) + 3 * r16f(4 * 9) + r16f(8 * 64) +
            r16f(8 * (size_t)max_beads * max_beads) + 16 + r16f(4 * (size_t)wtotal) +
            r16f(16 * (size_t)nelem * kFMaxG2);
@@ -227,6 +229,7 @@ __device__ SmemF carve_f(unsigned char *base, const FLaunch &L, int max_beads, i
     s.yl = (float *)take(4 * na);
     s.zl = (float *)take(4 * na);
     s.elem = (int8_t *)take(na);
+    s.fold = (int *)take(4 * (size_t)na);
     s.byel = (int *)take(4 * ((size_t)na + kMaxElem + 1));
     s.fw = (float *)take(4 * (size_t)kFW * 3 * na);
     s.sg = (float *)take(4 * (size_t)na * L.sgs);
@@ -347,6 +350,64 @@ __device__ __forceinline__ int visit_images(const SmemF &S, const FastNN &F, dou
     return c;
 }
 
+// acsf_wrap_one (translate.f90) with the fold counts s_d = floor(f_d) it applied
+__device__ __forceinline__ void wrap_fold(double xa, double ya, double za, const double *lat, double &x, double &y,
+                                          double &z, int &fold) {
+    x = __dmul_rn(xa, kAng2BohrD);
+    y = __dmul_rn(ya, kAng2BohrD);
+    z = __dmul_rn(za, kAng2BohrD);
+    const double *I = lat + 9;
+    double f[3];
+    for (int d = 0; d < 3; ++d)
+        f[d] = __dadd_rn(__dadd_rn(__dmul_rn(I[3 * d], x), __dmul_rn(I[3 * d + 1], y)), __dmul_rn(I[3 * d + 2], z));
+    fold = 0;
+    for (int d = 0; d < 3; ++d) {
+        const double s = floor(f[d]);
+        if (s != 0.0) {
+            x = __dsub_rn(x, __dmul_rn(s, lat[3 * d]));
+            y = __dsub_rn(y, __dmul_rn(s, lat[3 * d + 1]));
+            z = __dsub_rn(z, __dmul_rn(s, lat[3 * d + 2]));
+        }
+        const int si = (int)fmax(-120.0, fmin(120.0, s));
+        fold |= (si + 128) << (8 * d);
+    }
+}
+
+__device__ __forceinline__ int unpack8(int v, int d) { return ((v >> (8 * d)) & 0xFF) - 128; }
+
+// Skin-list images of pair (i, j): every image within the skin-list cutoff (FP32 screen
+// with margin; the exact test is the filter's), stored as (j, image in the unwrapped
+// frame) so that later wrapping changes only shift images by the fold counts.
+template <bool WRITE>
+__device__ __forceinline__ int visit_skin(const SmemF &S, const FastNN &F, int i, int j, float dx, float dy,
+                                          float dz, const int *na, int2 *out, int pos, int cap, int fi, int fj) {
+    int lo[3], hi[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const float f = S.ginv[3 * d] * dx + S.ginv[3 * d + 1] * dy + S.ginv[3 * d + 2] * dz;
+        lo[d] = max(-na[d] - 2, (int)ceilf(-f - S.wk[3 + d]));
+        hi[d] = min(na[d] + 2, (int)floorf(-f + S.wk[3 + d]));
+    }
+    const float *Lf = S.latf;
+    int c = 0;
+    for (int n1 = lo[0]; n1 <= hi[0]; ++n1)
+        for (int n2 = lo[1]; n2 <= hi[1]; ++n2)
+            for (int n3 = lo[2]; n3 <= hi[2]; ++n3) {
+                if (i == j && n1 == 0 && n2 == 0 && n3 == 0) continue;
+                const float ex = dx + (float)n1 * Lf[0] + (float)n2 * Lf[3] + (float)n3 * Lf[6];
+                const float ey = dy + (float)n1 * Lf[1] + (float)n2 * Lf[4] + (float)n3 * Lf[7];
+                const float ez = dz + (float)n1 * Lf[2] + (float)n2 * Lf[5] + (float)n3 * Lf[8];
+                if (ex * ex + ey * ey + ez * ez > F.cut2s) continue;
+                if (WRITE && pos + c < cap) {
+                    const int u0 = n1 - unpack8(fj, 0) + unpack8(fi, 0), u1 = n2 - unpack8(fj, 1) + unpack8(fi, 1),
+                              u2 = n3 - unpack8(fj, 2) + unpack8(fi, 2);
+                    out[pos + c] = make_int2(j, (u0 + 128) | ((u1 + 128) << 8) | ((u2 + 128) << 16));
+                }
+                ++c;
+            }
+    return c;
+}
+
 // Iterator over the set bits of one lane's rows (row pair p: rows p and n-2-p) in
 // row-major order; yields (q3, q4).
 struct RowBits {
@@ -444,7 +505,7 @@ __device__ __forceinline__ void build_rows(const FastNN &F, const SmemF &S, cons
 template <int NG, int ZM>
 __device__ void nnf_descriptors(const NNDev &M, const FastNN &F, const NNScratch &X, const SmemF &S,
                                 const WarpF &W, const FLaunch &L, int t, int64_t base, int i, int N, const int *na,
-                                unsigned *mglob) {
+                                unsigned *mglob, bool rebuild) {
     constexpr int NZ = popc5(ZM), NQ = 2 * NZ;
     static_assert(NG * NQ <= 32, "too many G3 cells");
     const int lane = threadIdx.x & 31;
@@ -454,23 +515,86 @@ __device__ void nnf_descriptors(const NNDev &M, const FastNN &F, const NNScratch
     int *words = X.nbw + (base + i) * (int64_t)M.maxnb;
 
     // ---- neighbour list (RuNNer order) into the global word slot of the bead-atom ------
+    // From the atom's skin list when it is valid: its entries are in RuNNer order (j,
+    // then images; a fold change shifts all images of one j alike), and each gets the
+    // same FP32 screen / exact FP64 test as a full build, so the list is identical.
     int cnt = 0;
     {
         const float xhi = S.xh[i], yhi = S.yh[i], zhi = S.zh[i], xli = S.xl[i], yli = S.yl[i], zli = S.zl[i];
-        for (int j0 = 0; j0 < N; j0 += 32) {
-            const int j = j0 + lane;
-            float dx = 0.f, dy = 0.f, dz = 0.f;
-            int c = 0;
-            if (j < N) {
-                dx = (S.xh[j] - xhi) + (S.xl[j] - xli);
-                dy = (S.yh[j] - yhi) + (S.yl[j] - yli);
-                dz = (S.zh[j] - zhi) + (S.zl[j] - zli);
-                c = visit_images<false>(S, F, cut2, i, j, dx, dy, dz, na, nullptr, 0, 0);
+        const int fi = S.fold[i];
+        int2 *sk = X.skw + (base + i) * (int64_t)X.skcap;
+        int ns = -1;
+        if (F.skin > 0.f) {
+            ns = X.skcnt[base + i];
+            if (rebuild) {
+                ns = 0;
+                for (int j0 = 0; j0 < N; j0 += 32) {
+                    const int j = j0 + lane;
+                    float dx = 0.f, dy = 0.f, dz = 0.f;
+                    int c = 0;
+                    if (j < N) {
+                        dx = (S.xh[j] - xhi) + (S.xl[j] - xli);
+                        dy = (S.yh[j] - yhi) + (S.yl[j] - yli);
+                        dz = (S.zh[j] - zhi) + (S.zl[j] - zli);
+                        c = visit_skin<false>(S, F, i, j, dx, dy, dz, na, nullptr, 0, 0, fi, 0);
+                    }
+                    int tot;
+                    const int ex = warp_excl_scan(c, tot);
+                    if (c > 0) visit_skin<true>(S, F, i, j, dx, dy, dz, na, sk, ns + ex, X.skcap, fi, S.fold[j]);
+                    ns += tot;
+                }
+                if (ns > X.skcap) ns = -1;
+                if (lane == 0) X.skcnt[base + i] = ns;
+                __syncwarp();
             }
-            int tot;
-            const int ex = warp_excl_scan(c, tot);
-            if (c > 0) visit_images<true>(S, F, cut2, i, j, dx, dy, dz, na, words, cnt + ex, L.maxnb);
-            cnt += tot;
+        }
+        if (ns >= 0) {
+            const double *Ld = S.lat;
+            for (int e0 = 0; e0 < ns; e0 += 32) {
+                const int e = e0 + lane;
+                bool in = false;
+                int word = 0;
+                if (e < ns) {
+                    const int2 v = sk[e];
+                    const int j = v.x, fj = S.fold[j];
+                    const int n1 = unpack8(v.y, 0) + unpack8(fj, 0) - unpack8(fi, 0),
+                              n2 = unpack8(v.y, 1) + unpack8(fj, 1) - unpack8(fi, 1),
+                              n3 = unpack8(v.y, 2) + unpack8(fj, 2) - unpack8(fi, 2);
+                    if (abs(n1) <= na[0] && abs(n2) <= na[1] && abs(n3) <= na[2]) {
+                        const float *Lf = S.latf;
+                        const float ex = ((S.xh[j] - xhi) + (S.xl[j] - xli)) + (float)n1 * Lf[0] + (float)n2 * Lf[3] +
+                                         (float)n3 * Lf[6];
+                        const float ey = ((S.yh[j] - yhi) + (S.yl[j] - yli)) + (float)n1 * Lf[1] + (float)n2 * Lf[4] +
+                                         (float)n3 * Lf[7];
+                        const float ez = ((S.zh[j] - zhi) + (S.zl[j] - zli)) + (float)n1 * Lf[2] + (float)n2 * Lf[5] +
+                                         (float)n3 * Lf[8];
+                        const float rf = ex * ex + ey * ey + ez * ez;
+                        in = rf < F.cut2_lo || (rf <= F.cut2_hi && exact_in_cutoff(S, i, j, n1, n2, n3, cut2));
+                        word = pack_nb(j, n1, n2, n3);
+                    }
+                    (void)Ld;
+                }
+                const unsigned bal = __ballot_sync(0xffffffffu, in);
+                const int pos = cnt + __popc(bal & ((1u << lane) - 1u));
+                if (in && pos < L.maxnb) words[pos] = word;
+                cnt += __popc(bal);
+            }
+        } else {
+            for (int j0 = 0; j0 < N; j0 += 32) {
+                const int j = j0 + lane;
+                float dx = 0.f, dy = 0.f, dz = 0.f;
+                int c = 0;
+                if (j < N) {
+                    dx = (S.xh[j] - xhi) + (S.xl[j] - xli);
+                    dy = (S.yh[j] - yhi) + (S.yl[j] - yli);
+                    dz = (S.zh[j] - zhi) + (S.zl[j] - zli);
+                    c = visit_images<false>(S, F, cut2, i, j, dx, dy, dz, na, nullptr, 0, 0);
+                }
+                int tot;
+                const int ex = warp_excl_scan(c, tot);
+                if (c > 0) visit_images<true>(S, F, cut2, i, j, dx, dy, dz, na, words, cnt + ex, L.maxnb);
+                cnt += tot;
+            }
         }
     }
     if (cnt > L.maxnb) {
@@ -492,15 +616,15 @@ __device__ void nnf_descriptors(const NNDev &M, const FastNN &F, const NNScratch
         if (n == 0) continue;
         const float4 *tab = g2e + F.g2beg[ei][a];
         const int chain = F.g2chain[ei][a];
-        float acc[kFMaxG2];
+        float acc[32];
 #pragma unroll
-        for (int k = 0; k < kFMaxG2; ++k) acc[k] = 0.f;
+        for (int k = 0; k < 32; ++k) acc[k] = 0.f;
         for (int q = lane; q < cnt; q += 32) {
             const float4 b = W.rb[q], c = W.rc[q];
             if ((__float_as_int(c.z) >> 16) != a) continue;
             g2_group(tab, n, chain, c.y, c.y * c.y, [&](int k, float e) { acc[k] = fmaf(e, b.x, acc[k]); });
         }
-        reduce_scatter<kFMaxG2>(acc);
+        reduce_scatter<32>(acc);
         if (lane < n) G[__float_as_int(tab[lane].w)] = acc[0];
     }
 
@@ -794,19 +918,28 @@ __device__ void nnf_forces(const NNDev &M, const FastNN &F, const NNScratch &X, 
         if (n == 0) continue;
         const float4 *tab = g2e + F.g2beg[ei][a];
         const int chain = F.g2chain[ei][a];
-        float cw[kFMaxG2];
+        // d/dr sum_k c_k exp(-eta_k (r - rs_k)^2) fc = sum_k c_k e_k (dfc - 2 eta_k (r - rs_k) fc):
+        // A = sum c_k e_k, B = sum (-2 eta_k c_k) e_k, C = sum (-2 eta_k c_k rs_k) e_k,
+        // derivative = A dfc + (B r - C) fc
+        float cw[kFMaxG2], ce[kFMaxG2];
 #pragma unroll
-        for (int k = 0; k < kFMaxG2; ++k) cw[k] = k < n ? dG[__float_as_int(tab[k].w)] : 0.f;
+        for (int k = 0; k < kFMaxG2; ++k) {
+            cw[k] = k < n ? dG[__float_as_int(tab[k].w)] : 0.f;
+            ce[k] = k < n ? cw[k] * tab[k].z : 0.f;
+        }
+        const bool centred = chain > 0;
         for (int q = lane; q < cnt; q += 32) {
             const float4 c = W.rc[q];
             if ((__float_as_int(c.z) >> 16) != a) continue;
             const float4 av = W.ra[q];
             const float fc = W.rb[q].x, dfc = c.x * c.y, r = c.y;
-            float dsum = 0.f;
+            float A = 0.f, Bv = 0.f, Cv = 0.f;
             g2_group(tab, n, chain, r, r * r, [&](int k, float e) {
-                dsum = fmaf(cw[k] * e, fmaf(tab[k].z * (r - tab[k].y), fc, dfc), dsum);
+                A = fmaf(cw[k], e, A);
+                Bv = fmaf(ce[k], e, Bv);
+                if (!centred) Cv = fmaf(ce[k] * tab[k].y, e, Cv);
             });
-            const float fr = dsum * av.w;
+            const float fr = fmaf(A, dfc, fmaf(Bv, r, -Cv) * fc) * av.w;
             W.sfx[q] -= fr * av.x;
             W.sfy[q] -= fr * av.y;
             W.sfz[q] -= fr * av.z;
@@ -965,6 +1098,8 @@ __device__ void order_by_element(const NNDev &M, const SmemF &S, const FLaunch &
 }
 
 // ---- one bead ---------------------------------------------------------------------------
+// Warps take groups of kNA atoms of one element: descriptors of each atom, the group's
+// network, forces of each atom; no CTA barrier between the stages.
 template <int NG, int ZM>
 __device__ bool nnf_bead(const Batch &B, const NNDev &M, const FastNN &F, const NNScratch &X, const SmemF &S,
                          const FLaunch &L, int t, int b, bool do_forces, bool skip_if_flagged) {
@@ -972,11 +1107,11 @@ __device__ bool nnf_bead(const Batch &B, const NNDev &M, const FastNN &F, const 
     const int64_t base = B.ba_off[t] + (int64_t)b * N;
     const int tid = threadIdx.x, nt = blockDim.x;
     const int warp = tid >> 5, lane = tid & 31;
+    const int bead = B.bead_off[t] + b;
     if (tid == 0) {
         acsf_lattice(B.box + 9 * t, S.lat);
         S.misc[0] = 0;
         S.misc[1] = 0;
-        S.misc[2] = 0;
         S.misc[3] = 0;
     }
     __syncthreads();
@@ -984,17 +1119,23 @@ __device__ bool nnf_bead(const Batch &B, const NNDev &M, const FastNN &F, const 
         S.latf[tid] = (float)S.lat[tid];
         S.ginv[tid] = (float)S.lat[9 + tid];
     }
-    if (tid < 3) {
-        const double *I = S.lat + 9 + 3 * tid;
+    if (tid < 6) {  // image half-widths: list cutoff (0..2), skin-list cutoff (3..5)
+        const int d = tid % 3;
+        const double *I = S.lat + 9 + 3 * d;
         const double bn = sqrt(I[0] * I[0] + I[1] * I[1] + I[2] * I[2]);
-        S.wk[tid] = (float)(M.maxcut * bn * (1.0 + 1e-4) + 1e-4);
+        const double rc = tid < 3 ? M.maxcut : M.maxcut + (double)F.skin;
+        S.wk[tid] = (float)(rc * bn * (1.0 + 1e-4) + 1e-4);
     }
+    float d2max = 0.f;
     for (int i = tid; i < N; i += nt) {
         double x, y, z;
-        acsf_wrap_one(B.rx[base + i], B.ry[base + i], B.rz[base + i], S.lat, x, y, z);
+        int fold;
+        const double rx = B.rx[base + i], ry = B.ry[base + i], rz = B.rz[base + i];
+        wrap_fold(rx, ry, rz, S.lat, x, y, z, fold);
         S.px[i] = x;
         S.py[i] = y;
         S.pz[i] = z;
+        S.fold[i] = fold;
         const float xh = (float)x, yh = (float)y, zh = (float)z;
         S.xh[i] = xh;
         S.yh[i] = yh;
@@ -1002,76 +1143,88 @@ __device__ bool nnf_bead(const Batch &B, const NNDev &M, const FastNN &F, const 
         S.xl[i] = (float)(x - (double)xh);
         S.yl[i] = (float)(y - (double)yh);
         S.zl[i] = (float)(z - (double)zh);
+        if (F.skin > 0.f) {
+            const double *r0 = X.skref + 3 * (base + i);
+            const float ddx = (float)(rx - r0[0]), ddy = (float)(ry - r0[1]), ddz = (float)(rz - r0[2]);
+            d2max = fmaxf(d2max, ddx * ddx + ddy * ddy + ddz * ddz);
+        }
     }
     if (do_forces)
         for (int k = tid; k < kFW * 3 * L.max_atoms; k += nt) S.fw[k] = 0.f;
+    if (F.skin > 0.f) atomicMax(&S.misc[3], __float_as_int(d2max));  // non-negative floats order as ints
     __syncthreads();
+    // skin lists are rebuilt when invalid or when some atom moved more than half the skin
+    // (positions in A; the skin is in bohr)
+    if (tid == 0) {
+        const float half = 0.5f * F.skin * (float)kBohr2Ang;
+        S.misc[2] = F.skin > 0.f && (X.skok[bead] == 0 || __int_as_float(S.misc[3]) > half * half) ? 1 : 0;
+    }
+    __syncthreads();
+    const bool rebuild = S.misc[2] != 0;
+    if (F.skin > 0.f) {
+        if (rebuild) {
+            for (int i = tid; i < N; i += nt) {
+                double *r0 = X.skref + 3 * (base + i);
+                r0[0] = B.rx[base + i];
+                r0[1] = B.ry[base + i];
+                r0[2] = B.rz[base + i];
+            }
+            if (tid == 0) X.skok[bead] = 1;
+        }
+    }
     const int na[3] = {X.img[3 * t], X.img[3 * t + 1], X.img[3 * t + 2]};
     unsigned *mscr = X.mscr + (size_t)blockIdx.x * X.mcap;
     const size_t mstride = (size_t)L.maxnb * L.mw;
-    {
-        const WarpF W = carve_warp(S, L, warp);
-        for (;;) {
-            int i = 0;
-            if (lane == 0) i = atomicAdd(&S.misc[1], 1);
-            i = __shfl_sync(0xffffffffu, i, 0);
-            if (i >= N) break;
-            if (S.elem[i] < 0) continue;
-            nnf_descriptors<NG, ZM>(M, F, X, S, W, L, t, base, i, N, na, mscr + (size_t)i * mstride);
-        }
-    }
-    __syncthreads();
-    // network: groups of kNA atoms of one element
+    const int *off = S.byel + L.max_atoms;
+    int ngroups = 0;
+    for (int e = 0; e < M.nelem; ++e) ngroups += (off[e + 1] - off[e] + kNA - 1) / kNA;
     double e_warp = 0.0;
-    {
-        float *hs = (float *)(S.warp_base + (size_t)warp * S.warp_bytes);
-        float *hv = hs + kNA * (M.nlayers + 1) * L.ls;
-        const int *off = S.byel + L.max_atoms;
-        int ngroups = 0;
-        for (int e = 0; e < M.nelem; ++e) ngroups += (off[e + 1] - off[e] + kNA - 1) / kNA;
-        for (;;) {
-            int g = 0;
-            if (lane == 0) g = atomicAdd(&S.misc[2], 1);
-            g = __shfl_sync(0xffffffffu, g, 0);
-            if (g >= ngroups) break;
-            int e = 0, first = 0;
-            for (int k = 0; k < M.nelem; ++k) {
-                const int ng = (off[k + 1] - off[k] + kNA - 1) / kNA;
-                if (g < ng) {
-                    e = k;
-                    first = off[k] + g * kNA;
-                    break;
-                }
-                g -= ng;
+    float *hs = (float *)(S.warp_base + (size_t)warp * S.warp_bytes);
+    float *hv = hs + kNA * (M.nlayers + 1) * L.ls;
+    const WarpF W = carve_warp(S, L, warp);
+    for (;;) {
+        int g = 0;
+        if (lane == 0) g = atomicAdd(&S.misc[1], 1);
+        g = __shfl_sync(0xffffffffu, g, 0);
+        if (g >= ngroups) break;
+        int e = 0, first = 0;
+        for (int k = 0; k < M.nelem; ++k) {
+            const int ng = (off[k + 1] - off[k] + kNA - 1) / kNA;
+            if (g < ng) {
+                e = k;
+                first = off[k] + g * kNA;
+                break;
             }
-            const int n = min(kNA, off[e + 1] - first);
-            const float en = nnf_network4(M, F, S, L, hs, hv, e, S.byel + first, n, do_forces);
-            if (lane == 0) e_warp += (double)en + n * (M.remove_atom_energies ? M.atom_energy[e] : 0.0);
+            g -= ng;
         }
+        const int n = min(kNA, off[e + 1] - first);
+        const int *atoms = S.byel + first;
+        for (int a = 0; a < n; ++a)
+            nnf_descriptors<NG, ZM>(M, F, X, S, W, L, t, base, atoms[a], N, na, mscr + (size_t)atoms[a] * mstride,
+                                    rebuild);
+        __syncwarp();
+        const float en = nnf_network4(M, F, S, L, hs, hv, e, atoms, n, do_forces);
+        if (lane == 0) e_warp += (double)en + n * (M.remove_atom_energies ? M.atom_energy[e] : 0.0);
+        if (do_forces)
+            for (int a = 0; a < n; ++a)
+                nnf_forces<NG, ZM>(M, F, X, S, W, L, base, atoms[a], mscr + (size_t)atoms[a] * mstride);
     }
     const double etot = block_sum(e_warp, S.red);  // contains __syncthreads: flag visible
+    if (F.skin > 0.f && rebuild) {
+        // an overflowing skin list invalidates the bead's lists: rebuilt on the next step
+        for (int k = tid; k < N; k += nt)
+            if (X.skcnt[base + k] < 0) X.skok[bead] = 0;
+    }
     const bool flagged = S.misc[0] != 0;
     if (skip_if_flagged && flagged) {
         __syncthreads();
         return true;
     }
-    if (tid == 0) B.epot[B.bead_off[t] + b] += etot * kHa2eVF;
+    if (tid == 0) B.epot[bead] += etot * kHa2eVF;
     if (!do_forces) {
         __syncthreads();
         return flagged;
     }
-    {
-        const WarpF W = carve_warp(S, L, warp);
-        for (;;) {
-            int i = 0;
-            if (lane == 0) i = atomicAdd(&S.misc[3], 1);
-            i = __shfl_sync(0xffffffffu, i, 0);
-            if (i >= N) break;
-            if (S.elem[i] < 0) continue;
-            nnf_forces<NG, ZM>(M, F, X, S, W, L, base, i, mscr + (size_t)i * mstride);
-        }
-    }
-    __syncthreads();
     const double c = kHa2eVF * kAng2BohrD;
     for (int i = tid; i < N; i += nt) {
         float fx = 0.f, fy = 0.f, fz = 0.f;

@@ -120,6 +120,10 @@ class Engine:
             self._check(r, "mdt_nn_fast_path")
         return bool(r)
 
+    def nn_set_skin(self, skin_ang: float) -> None:
+        """Verlet skin (A) of the fast kernels' neighbour lists; 0 rebuilds every step."""
+        self._check(self.lib.mdt_nn_set_skin(self.h, skin_ang), "mdt_nn_set_skin")
+
     def nn_stats(self):
         fb = np.zeros(self.T, np.int32)
         ov = np.zeros(self.T, np.int32)

@@ -75,19 +75,20 @@ def _opts(lr, w_energy, w_force, precision):
 class Trainer:
     """Holds a training set on the GPU (one configuration per batch trajectory)."""
 
-    def __init__(self, data: Dataset, model: nene.NNModel, device: int = 0, scale_margin: float = 0.0):
+    def __init__(self, data: Dataset, model: nene.NNModel, device: int = 0, scale_margin: float = 0.0,
+                 max_neighbors: int = 0):
         self.data = data
         self.model = model
         self.eng = Engine(device)
         self.eng.define(data.universes)
         self.eng.upload()
         # scaling.data from the training set's own descriptors (RuNNer's scaling mode)
-        self.eng.read_nene(model, data.universes[0].names)
+        self.eng.read_nene(model, data.universes[0].names, max_neighbors=max_neighbors)
         self.eng.set_pes(PES_NENE, 0.0)
         G = self.eng.nn_descriptors()
         elem = np.concatenate([[model.elements.index(u.names[i - 1]) for i in u.idx] for u in data.universes])
         nene.set_scaling(model, G, elem, margin=scale_margin)
-        self.eng.read_nene(model, data.universes[0].names)
+        self.eng.read_nene(model, data.universes[0].names, max_neighbors=max_neighbors)
         self.eng.set_pes(PES_NENE, 0.0)
         forces = np.concatenate([f.reshape(-1) for f in data.forces])
         self.eng._check(self.eng.lib.mdt_train_set_labels(self.eng.h, np.ascontiguousarray(data.energy).ctypes.data,
@@ -144,12 +145,13 @@ class Trainer:
         self.eng.close()
 
 
-def force_rmse(model: nene.NNModel, data: Dataset, device: int = 0, precision: str = "fp32") -> tuple:
+def force_rmse(model: nene.NNModel, data: Dataset, device: int = 0, precision: str = "fp32",
+               max_neighbors: int = 0) -> tuple:
     """Force RMSE (eV/A) and per-atom energy RMSE (eV) of the network on a dataset."""
     eng = Engine(device)
     eng.define(data.universes)
     eng.upload()
-    eng.read_nene(model, data.universes[0].names)
+    eng.read_nene(model, data.universes[0].names, max_neighbors=max_neighbors)
     eng.set_pes(PES_NENE, 0.0)
     eng.calc_force(SimParams(), precision=precision)
     out = eng.download()

@@ -34,27 +34,30 @@ def main(argv=None):
     ap.add_argument("--w-force", type=float, default=1.0)
     ap.add_argument("--time-budget", type=float, default=None)
     ap.add_argument("--scale-margin", type=float, default=0.02)
+    ap.add_argument("--descriptor", choices=("acsf", "radial"), default="acsf")
+    ap.add_argument("--max-neighbors", type=int, default=80)
+    ap.add_argument("--seed", type=int, default=11)
     a = ap.parse_args(argv)
     log = lambda m: print(m, file=sys.stderr, flush=True)  # noqa: E731
     t0 = time.perf_counter()
     data = generate_dataset(a.ntraj, a.nsamples, a.every, seed=7)
     t_data = time.perf_counter() - t0
     log(f"dataset: {len(data.universes)} configurations, {sum(u.natoms for u in data.universes)} atoms, {t_data:.1f} s")
-    model = surrogate_model()
+    model = surrogate_model(a.seed, descriptor=a.descriptor)
     t1 = time.perf_counter()
-    tr = Trainer(data, model, scale_margin=a.scale_margin)
+    tr = Trainer(data, model, scale_margin=a.scale_margin, max_neighbors=a.max_neighbors)
     t_setup = time.perf_counter() - t1
     hist = tr.train(epochs=a.epochs, batch=a.batch, lr=a.lr, lr_final=a.lr_final, w_energy=a.w_energy,
                     w_force=a.w_force, time_budget=a.time_budget, log=log)
-    report = {"configs": len(data.universes), "atoms": int(sum(u.natoms for u in data.universes)),
+    report = {"descriptor": a.descriptor, "max_neighbors": a.max_neighbors, "configs": len(data.universes), "atoms": int(sum(u.natoms for u in data.universes)),
               "dataset_s": t_data, "setup_s": t_setup, "train_s": tr.seconds, "steps": tr.steps,
               "atoms_per_s": tr.atoms_trained / tr.seconds, "train_force_rmse_last": hist[-1][2],
               "train_energy_rmse_last": hist[-1][1]}
     tr.close()
     del data
     held = generate_dataset(512, 8, a.every, seed=1234)
-    f32, e32 = force_rmse(model, held, precision="fp32")
-    f64, e64 = force_rmse(model, held, precision="fp64")
+    f32, e32 = force_rmse(model, held, precision="fp32", max_neighbors=a.max_neighbors)
+    f64, e64 = force_rmse(model, held, precision="fp64", max_neighbors=a.max_neighbors)
     report.update({"heldout_configs": len(held.universes), "heldout_force_rmse_fp32": f32,
                    "heldout_force_rmse_fp64": f64, "heldout_energy_rmse_per_atom_fp64": e64})
     Path(a.out).parent.mkdir(parents=True, exist_ok=True)

@@ -175,3 +175,41 @@ def test_fast_neighbour_overflow_is_reported(built_lib):
     _, ov = eng.nn_stats()
     assert ov.all()
     eng.close()
+
+
+def test_skin_lists_do_not_change_results(built_lib, oracle_lib):
+    """30 fused MD steps with the default 1 A skin (lists rebuilt when an atom moved more
+    than 0.5 A) against lists built every step; then positions displaced by 0.4 A (no
+    rebuild) and by 2 A (rebuild) through the state upload, both checked against the
+    oracle.  Only FP32 summation order differs between the runs."""
+    from oracle.oracle import NNOracle
+    us = W.config2(6, seed=12)
+    m = surrogate_model(5, descriptor="radial")
+    sp = SimParams(step=0.5, gamma_const=1e-3, seed=3)
+    res = {}
+    for skin in (1.0, 0.0):
+        eng = _engine(us, m)
+        eng.nn_set_skin(skin)
+        eng.calc_force(sp, precision="fp32")
+        eng.md_steps(30, sp, precision="fp32")
+        res[skin] = eng.download()
+        eng.close()
+    assert np.abs(res[1.0]["r"] - res[0.0]["r"]).max() < 1e-6
+    o = NNOracle(m)
+    eng = _engine(us, m)
+    eng.calc_force(sp, precision="fp32")
+    rng = np.random.default_rng(0)
+    for amp in (0.4, 2.0):
+        moved = []
+        for u in us:
+            d = rng.normal(size=u.r.shape)
+            d *= amp / np.linalg.norm(d, axis=-1, keepdims=True) / np.sqrt(3.0)
+            moved.append(u.r + d)
+        eng.upload(r=np.concatenate([r.reshape(-1, 3) for r in moved]))
+        eng.calc_force(sp, precision="fp32")
+        out = eng.download()
+        for t, u in enumerate(us):
+            E, F = o.energy_force(_elems(u), moved[t][:, 0, :], u.simbox)
+            f = eng.split(out["f"], t)[:, 0, :]
+            assert np.sqrt(np.mean((f - F) ** 2)) < 1e-4 * np.sqrt(np.mean(F ** 2)), (amp, t)
+    eng.close()
