@@ -383,6 +383,22 @@ FastNN build_fast(const NNDev &M, const mdt_nn_model *m, const std::vector<int> 
                     ok = m->eta[e * ms + idx[q]] == 2.0 * m->eta[e * ms + idx[q - S]];
                 if (ok) chain = S;
             }
+            // uniformly shifted: one eta, r_s,k = r_s,0 + k D
+            if (chain == 0 && idx.size() >= 3) {
+                const double eta = m->eta[e * ms + idx[0]], r0 = m->rshift[e * ms + idx[0]];
+                const double D = m->rshift[e * ms + idx[1]] - r0;
+                bool ok = D > 0.0;
+                for (size_t q = 0; q < idx.size() && ok; ++q) {
+                    const double rs = m->rshift[e * ms + idx[q]];
+                    ok = m->eta[e * ms + idx[q]] == eta && std::fabs(rs - (r0 + q * D)) <= 1e-9 * std::max(1.0, rs);
+                }
+                if (ok) {
+                    chain = -1;
+                    F.g2sh[e][a][0] = (float)(2.0 * eta * D * log2e);
+                    F.g2sh[e][a][1] = (float)(-eta * D * D * log2e);
+                    F.g2sh[e][a][2] = (float)std::exp2(-2.0 * eta * D * D * log2e);
+                }
+            }
             F.g2chain[e][a] = chain;
             for (int s : idx) {
                 const int k = e * ms + s;

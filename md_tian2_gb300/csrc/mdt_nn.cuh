@@ -88,7 +88,12 @@ struct FastNN {
     // g2tab[e*kFMaxG2 + g2beg[e][a] ...) with g2cnt[e][a] entries, ascending eta.  With
     // g2chain[e][a] = S > 0 the group is centred (r_s = 0) and eta_{k+S} = 2 eta_k, so
     // exp(-eta_{k+S} r^2) = exp(-eta_k r^2)^2: S exponentials, the rest by squaring.
+    // g2chain[e][a] = -1: one eta and r_s,k = r_s,0 + k D; then with t = r - r_s,m at the
+    // middle centre m, e_m and the ratios e_{m+-1}/e_m = exp2(+-a t + b) start recurrences
+    // whose ratios change by the factor c = exp2(2 b) per centre: g2sh[e][a] = (a, b, c),
+    // a = 2 eta D log2 e, b = -eta D^2 log2 e (three exponentials per neighbour).
     int g2beg[kMaxElem][kMaxElem], g2cnt[kMaxElem][kMaxElem], g2chain[kMaxElem][kMaxElem];
+    float g2sh[kMaxElem][kMaxElem][3];
     const float4 *g2tab;           // [e*kFMaxG2 + s]: (-eta log2 e, r_s, -2 eta, sf index)
     // network weights as the fast kernels keep them in shared memory: layer l of element
     // e is a row-major (n_{l-1} + 1) x stride matrix (last row: biases) at wofs[e][l]

@@ -164,14 +164,14 @@ struct WarpF {
     float *sfx, *sfy, *sfz;
 };
 
-constexpr int kNA = 4;  // atoms per warp in the network phase
+constexpr int kNAmax = 4;  // atoms per warp in the network phase
 
 __host__ __device__ inline size_t r16f(size_t b) { return (b + 15) & ~size_t(15); }
 
 __host__ __device__ inline size_t warp_bytes_f(int maxnb, int mw, int nlayers, int ls) {
     const size_t rows = 3 * r16f(16 * (size_t)maxnb) + r16f(maxnb) + r16f(4 * (size_t)maxnb * mw) +
                         r16f(4 * ((size_t)maxnb + 1)) + 3 * r16f(4 * (size_t)maxnb);
-    const size_t net = 2 * r16f(4 * (size_t)kNA * (nlayers + 1) * ls);
+    const size_t net = 2 * r16f(4 * (size_t)kNAmax * (nlayers + 1) * ls);
     return rows > net ? rows : net;
 }
 
@@ -457,8 +457,40 @@ __device__ __forceinline__ void g2_chain(const float4 *tab, int n, float r, floa
     }
 }
 
+// Uniformly shifted group (one eta, centres r_s,0 + k D): recurrences up and down from
+// the middle centre, where no value can underflow (|t| <= half the centre span).
 template <typename Fn>
-__device__ __forceinline__ void g2_group(const float4 *tab, int n, int S, float r, float r2, Fn &&f) {
+__device__ __forceinline__ void g2_shifted(const float4 *tab, int n, float r, const float *sh, Fn &&f) {
+    const int km = n >> 1;
+    const float t = r - tab[km].y;
+    const float em = exp2f(tab[km].x * t * t);
+    const float c = sh[2];
+    float eu = em, ru = exp2f(fmaf(sh[0], t, sh[1]));
+#pragma unroll
+    for (int k = 0; k < kFMaxG2; ++k) {
+        if (k >= n) break;
+        if (k < km) continue;
+        f(k, eu);
+        eu *= ru;
+        ru *= c;
+    }
+    float ed = em, rd = exp2f(fmaf(-sh[0], t, sh[1]));
+#pragma unroll
+    for (int k = kFMaxG2 - 1; k >= 0; --k) {
+        if (k >= km) continue;
+        ed *= rd;
+        rd *= c;
+        f(k, ed);
+    }
+}
+
+template <typename Fn>
+__device__ __forceinline__ void g2_group(const float4 *tab, int n, int S, float r, float r2, const float *sh,
+                                         Fn &&f) {
+    if (S < 0) {
+        g2_shifted(tab, n, r, sh, f);
+        return;
+    }
     switch (S) {
         case 1: g2_chain<1>(tab, n, r, r2, f); break;
         case 2: g2_chain<2>(tab, n, r, r2, f); break;
@@ -622,7 +654,8 @@ __device__ void nnf_descriptors(const NNDev &M, const FastNN &F, const NNScratch
         for (int q = lane; q < cnt; q += 32) {
             const float4 b = W.rb[q], c = W.rc[q];
             if ((__float_as_int(c.z) >> 16) != a) continue;
-            g2_group(tab, n, chain, c.y, c.y * c.y, [&](int k, float e) { acc[k] = fmaf(e, b.x, acc[k]); });
+            g2_group(tab, n, chain, c.y, c.y * c.y, F.g2sh[ei][a],
+                     [&](int k, float e) { acc[k] = fmaf(e, b.x, acc[k]); });
         }
         reduce_scatter<32>(acc);
         if (lane < n) G[__float_as_int(tab[lane].w)] = acc[0];
@@ -730,12 +763,13 @@ __device__ void nnf_descriptors(const NNDev &M, const FastNN &F, const NNScratch
     }
 }
 
-// ---- phase 2: network for up to kNA atoms of element e (lanes = nodes) -----------------
+// ---- network for up to kNA atoms of element e (lanes = nodes) --------------------------
 // calconenn.f90:83-153 forward, getdnodes_values.f90 + getshortatomic.f90:263-291 back;
 // scaling and range check of getshortatomic.f90:174-236.  Replaces the descriptors of
 // the atoms in S.sg by dE/dG (raw G); returns the energy sum of the group (lane 0).
-__device__ float nnf_network4(const NNDev &M, const FastNN &F, const SmemF &S, const FLaunch &L, float *hs,
-                              float *hv, int ei, const int *atoms, int na, bool do_forces) {
+template <int kNA>
+__device__ float nnf_network(const NNDev &M, const FastNN &F, const SmemF &S, const FLaunch &L, float *hs,
+                             float *hv, int ei, const int *atoms, int na, bool do_forces) {
     const int lane = threadIdx.x & 31;
     const int ls = L.ls, lstr = (M.nlayers + 1) * ls;  // per-atom stride in hs/hv
     const int nsf = M.nsf[ei], sfb = ei * M.maxsf;
@@ -921,12 +955,9 @@ __device__ void nnf_forces(const NNDev &M, const FastNN &F, const NNScratch &X, 
         // d/dr sum_k c_k exp(-eta_k (r - rs_k)^2) fc = sum_k c_k e_k (dfc - 2 eta_k (r - rs_k) fc):
         // A = sum c_k e_k, B = sum (-2 eta_k c_k) e_k, C = sum (-2 eta_k c_k rs_k) e_k,
         // derivative = A dfc + (B r - C) fc
-        float cw[kFMaxG2], ce[kFMaxG2];
+        float cw[kFMaxG2];
 #pragma unroll
-        for (int k = 0; k < kFMaxG2; ++k) {
-            cw[k] = k < n ? dG[__float_as_int(tab[k].w)] : 0.f;
-            ce[k] = k < n ? cw[k] * tab[k].z : 0.f;
-        }
+        for (int k = 0; k < kFMaxG2; ++k) cw[k] = k < n ? dG[__float_as_int(tab[k].w)] : 0.f;
         const bool centred = chain > 0;
         for (int q = lane; q < cnt; q += 32) {
             const float4 c = W.rc[q];
@@ -934,10 +965,11 @@ __device__ void nnf_forces(const NNDev &M, const FastNN &F, const NNScratch &X, 
             const float4 av = W.ra[q];
             const float fc = W.rb[q].x, dfc = c.x * c.y, r = c.y;
             float A = 0.f, Bv = 0.f, Cv = 0.f;
-            g2_group(tab, n, chain, r, r * r, [&](int k, float e) {
+            g2_group(tab, n, chain, r, r * r, F.g2sh[ei][a], [&](int k, float e) {
+                const float ce = cw[k] * tab[k].z;
                 A = fmaf(cw[k], e, A);
-                Bv = fmaf(ce[k], e, Bv);
-                if (!centred) Cv = fmaf(ce[k] * tab[k].y, e, Cv);
+                Bv = fmaf(ce, e, Bv);
+                if (!centred) Cv = fmaf(ce * tab[k].y, e, Cv);
             });
             const float fr = fmaf(A, dfc, fmaf(Bv, r, -Cv) * fc) * av.w;
             W.sfx[q] -= fr * av.x;
@@ -1098,7 +1130,7 @@ __device__ void order_by_element(const NNDev &M, const SmemF &S, const FLaunch &
 }
 
 // ---- one bead ---------------------------------------------------------------------------
-// Warps take groups of kNA atoms of one element: descriptors of each atom, the group's
+// Warps take groups of 2-4 atoms of one element: descriptors of each atom, the group's
 // network, forces of each atom; no CTA barrier between the stages.
 template <int NG, int ZM>
 __device__ bool nnf_bead(const Batch &B, const NNDev &M, const FastNN &F, const NNScratch &X, const SmemF &S,
@@ -1176,11 +1208,13 @@ __device__ bool nnf_bead(const Batch &B, const NNDev &M, const FastNN &F, const 
     unsigned *mscr = X.mscr + (size_t)blockIdx.x * X.mcap;
     const size_t mstride = (size_t)L.maxnb * L.mw;
     const int *off = S.byel + L.max_atoms;
+    // groups of 4 atoms (network ILP) on large beads, of 2 on small ones (tail balance)
+    const int gsz = N >= 96 ? 4 : 2;
     int ngroups = 0;
-    for (int e = 0; e < M.nelem; ++e) ngroups += (off[e + 1] - off[e] + kNA - 1) / kNA;
+    for (int e = 0; e < M.nelem; ++e) ngroups += (off[e + 1] - off[e] + gsz - 1) / gsz;
     double e_warp = 0.0;
     float *hs = (float *)(S.warp_base + (size_t)warp * S.warp_bytes);
-    float *hv = hs + kNA * (M.nlayers + 1) * L.ls;
+    float *hv = hs + gsz * (M.nlayers + 1) * L.ls;
     const WarpF W = carve_warp(S, L, warp);
     for (;;) {
         int g = 0;
@@ -1189,21 +1223,22 @@ __device__ bool nnf_bead(const Batch &B, const NNDev &M, const FastNN &F, const 
         if (g >= ngroups) break;
         int e = 0, first = 0;
         for (int k = 0; k < M.nelem; ++k) {
-            const int ng = (off[k + 1] - off[k] + kNA - 1) / kNA;
+            const int ng = (off[k + 1] - off[k] + gsz - 1) / gsz;
             if (g < ng) {
                 e = k;
-                first = off[k] + g * kNA;
+                first = off[k] + g * gsz;
                 break;
             }
             g -= ng;
         }
-        const int n = min(kNA, off[e + 1] - first);
+        const int n = min(gsz, off[e + 1] - first);
         const int *atoms = S.byel + first;
         for (int a = 0; a < n; ++a)
             nnf_descriptors<NG, ZM>(M, F, X, S, W, L, t, base, atoms[a], N, na, mscr + (size_t)atoms[a] * mstride,
                                     rebuild);
         __syncwarp();
-        const float en = nnf_network4(M, F, S, L, hs, hv, e, atoms, n, do_forces);
+        const float en = gsz == 4 ? nnf_network<4>(M, F, S, L, hs, hv, e, atoms, n, do_forces)
+                                  : nnf_network<2>(M, F, S, L, hs, hv, e, atoms, n, do_forces);
         if (lane == 0) e_warp += (double)en + n * (M.remove_atom_energies ? M.atom_energy[e] : 0.0);
         if (do_forces)
             for (int a = 0; a < n; ++a)
