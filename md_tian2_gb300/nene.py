@@ -298,19 +298,21 @@ def acsf_set(center: str, neighbours: list, rc_ang: float = 6.5) -> list:
 
 
 def radial_set(center: str, neighbours: list, rc_ang: float = 6.5) -> list:
-    """24 centred G2 per neighbour element, no angular functions: eta_k = 0.002 *
-    2^(k/3) 1/A^2 (k = 0..23, 0.002-0.41 1/A^2), generated so that eta_{k+3} = 2 eta_k
-    holds exactly (the FP32 kernels then get exp(-eta_{k+3} r^2) by squaring
-    exp(-eta_k r^2)).  Cosine cutoff at rc_ang."""
+    """24 radial functions per centre element, no angular ones: for metal neighbours 20
+    shifted Gaussians (r_s = 0.8 ... 6.5 A every 0.3 A, eta = 4 1/A^2), for H neighbours
+    4 (r_s = 1, 2, 3, 4 A, eta = 1 1/A^2).  The 0.3 A grid resolves the neighbour shells
+    and the region of EMT's cutoff; equal spacing lets the FP32 kernels evaluate a group
+    with three exponentials.  Cosine cutoff at rc_ang."""
     a2b = C.ANG2BOHR
     rc = rc_ang * a2b
-    etas = [0.002, 0.002 * 2.0 ** (1.0 / 3.0), 0.002 * 2.0 ** (2.0 / 3.0)]
-    while len(etas) < 24:
-        etas.append(2.0 * etas[-3])
     out = []
     for z in sorted(Z_OF[n] for n in neighbours):
-        for eta in etas:
-            out.append(SymFunc(2, eta=eta / a2b ** 2, rshift=0.0, rc=rc, e1=z))
+        if z == Z_OF["H"]:
+            grid, eta = [1.0 + 1.0 * k for k in range(4)], 1.0
+        else:
+            grid, eta = [0.8 + 0.3 * k for k in range(20)], 4.0
+        for rs in grid:
+            out.append(SymFunc(2, eta=eta / a2b ** 2, rshift=rs * a2b, rc=rc, e1=z))
     return sort_symfunctions(out)
 
 

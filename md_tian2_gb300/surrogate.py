@@ -62,9 +62,11 @@ def generate_dataset(ntraj: int = 4096, nsamples: int = 8, every: int = 50, seed
 
 
 def surrogate_model(seed: int = 11, descriptor: str = "acsf") -> nene.NNModel:
-    """Untrained surrogate network: ``descriptor`` "acsf" = 8 G2 + 16 G3 per element
-    (``nene.acsf_set``), "radial" = 24 G2 (``nene.radial_set``); 24-32-32-1 softplus."""
-    return nene.random_model(["H", "Au"], hidden=(32, 32), act="p", seed=seed, neighbours=["Au"],
+    """Untrained surrogate network: ``descriptor`` "acsf" = 8 G2 + 16 G3 per element over
+    Au neighbours (``nene.acsf_set``), "radial" = 24 G2 over Au and H neighbours
+    (``nene.radial_set``); 24-32-32-1 softplus."""
+    nbr = ["Au"] if descriptor == "acsf" else ["H", "Au"]
+    return nene.random_model(["H", "Au"], hidden=(32, 32), act="p", seed=seed, neighbours=nbr,
                              descriptor=descriptor)
 
 
