@@ -1,19 +1,25 @@
 #!/usr/bin/env python
-"""Throughput benchmark of the md_tian2 GB300 engine.
+"""Throughput benchmark of the md_tian2 GB300 engine: NN surrogate vs plain FP64 EMT.
 
 Workload (per GPU): 4096 H/Au(111) trajectories, slabs of 4 layers x {3x3,4x4,5x5,6x6}
 (37-145 atoms) drawn from a seed, Einc ~ U(0.5,5) eV, polar ~ U(0,60), azimuth ~
 U(0,360), Tsurf = 300 K, constant-friction Langevin on Au and velocity Verlet on H,
-dt = 0.1 fs.  One bench step = one MD step (propagate_1 -> calc_force ->
-propagate_2) of every trajectory.  Metric: atom-steps/s = sum over trajectories of
-natoms x completed steps / time.
+dt = 0.1 fs.  One bench step = one MD step (propagate_1 -> calc_force -> propagate_2)
+of every trajectory.  Metric: atom-steps/s = sum over trajectories of natoms x
+completed steps / time.
+
+The headline ``value`` is the learned surrogate (FP32 fast kernels, trained on the GPU
+from FP64 EMT labels; FP64 EMT recomputes any bead whose descriptors leave the training
+range); ``emt_fp64`` is the plain FP64 EMT kernel on the same trajectories, and
+``accuracy`` holds the surrogate's force RMSE against FP64 EMT on held-out
+configurations the bench generates with FP64 EMT.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 N > 1 runs under torchrun as independent replicas (weak scaling): trajectories are
 independent, the path has no exchange step.  ``--impl reference`` times the CPU
-restatement of the reference's Fortran (oracle/, the same loops and dense arrays) on
-the host cores, on a bounded sample of the same workload.
+restatement of the reference's Fortran EMT path (oracle/) on the host cores, on a
+bounded sample of the same workload.
 """
 from __future__ import annotations
 
@@ -49,7 +55,10 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--ntraj", type=int, default=4096)
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"], help="EMT arm precision")
+    ap.add_argument("--model", default=str(ROOT / "md_tian2_gb300" / "data" / "surrogate_radial.npz"))
+    ap.add_argument("--margin", type=float, default=0.1, help="descriptor range margin before the EMT fallback")
+    ap.add_argument("--rmse-traj", type=int, default=256)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     return ap.parse_args()
@@ -234,8 +243,38 @@ def run_reference(args):
 
 
 # ---------------------------------------------------------------------------
-# GPU arm
+# GPU arms
 # ---------------------------------------------------------------------------
+# Algorithmic FLOP convention of the surrogate (radial descriptor: 24 shifted Gaussians
+# in two uniformly spaced groups, exp = 20, sqrt/div = 10): per neighbour entry: row
+# (sqrt, div, cutoff polynomial and derivative) 70, radial forward (3 exp + 2 mul + 1
+# FMA per function) 60 + 4 x 24 = 156, radial backward (3 exp + 2 mul + 3 FMA per
+# function) 60 + 8 x 24 = 252, slot force 14 -> 492; per atom: network forward
+# 2*(24*32+32*32+32) + 64 softplus x 40, backward 2*(32+32*32+24*32) + 64 derivative x 20.
+FLOP_SURR_ENTRY = 70 + 156 + 252 + 14
+FLOP_SURR_ATOM = 2 * (24 * 32 + 32 * 32 + 32) + 64 * 40 + 2 * (32 + 32 * 32 + 24 * 32) + 64 * 20
+
+
+def timed_steps(eng, sp, precision, steps, stream, torch, dist=None, clock_index=None):
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clk = ClockSampler(clock_index) if clock_index is not None else None
+    if clk:
+        clk.__enter__()
+    ev0.record(stream)
+    for _ in range(steps):
+        eng.md_steps(1, sp, precision=precision)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    if clk:
+        clk.__exit__()
+    if dist:
+        dist.barrier()
+    return ev0.elapsed_time(ev1), (clk.summary() if clk else None)
+
+
 def run_ours(args):
     import ctypes as ct
 
@@ -253,49 +292,46 @@ def run_ours(args):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(args.cpu_seconds)  # before the first GPU call of this process's pool
 
+    from md_tian2_gb300 import nene
     from md_tian2_gb300._lib import load
-    from md_tian2_gb300.engine import Engine
+    from md_tian2_gb300.engine import PES_EMT, PES_SURROGATE, Engine
+    from md_tian2_gb300.surrogate import force_rmse, generate_dataset
     lib = load()
     universes, emt = workload(args.ntraj, seed=7 + rank)
     sp = sim_params()
+    model = nene.load_npz(args.model)
     eng = Engine(local)
     stream = torch.cuda.Stream()  # a real stream handle: the library and the events share it
     eng.lib.mdt_set_stream(eng.h, ct.c_void_p(stream.cuda_stream))
     eng.read_emt(emt)
     eng.define(universes)
-    eng.upload()
-    eng.calc_force(sp, precision=args.precision)
+    eng.read_nene(model, ["H", "Au"], max_neighbors=80)
     natoms = np.array([u.natoms * u.nbeads for u in universes], np.int64)
 
     def atom_steps_now():
         return int(np.sum(natoms * eng.query(sp)["steps_done"]))
 
-    same, mixed, nat = count_pairs(universes, emt_cut(emt))
-    flop_per_step = FLOP_SAME_PAIR * same + FLOP_MIXED_PAIR * mixed + FLOP_ATOM * nat
-
+    # ---- surrogate (headline) -------------------------------------------------------
+    eng.set_pes(PES_SURROGATE, args.margin)
+    fast = eng.nn_fast_path(True)
+    eng.upload()
+    eng.calc_force(sp, precision="fp32")
     for _ in range(args.warmup):
-        eng.md_steps(1, sp, precision=args.precision)
+        eng.md_steps(1, sp, precision="fp32")
     torch.cuda.synchronize()
     s0 = atom_steps_now()
     launches0 = eng.launch_count()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    with ClockSampler(local) as clk:
-        ev0.record(stream)
-        for _ in range(args.steps):
-            eng.md_steps(1, sp, precision=args.precision)
-        ev1.record(stream)
-        torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
-    ms = ev0.elapsed_time(ev1)
+    fb0 = int(eng.nn_stats()[0].sum())
+    ms, clocks = timed_steps(eng, sp, "fp32", args.steps, stream, torch, dist, local)
     launches = eng.launch_count() - launches0
-    s1 = atom_steps_now()
-    done = s1 - s0
+    done = atom_steps_now() - s0
+    fb_count = int(eng.nn_stats()[0].sum()) - fb0
+    bead_evals = int(np.sum([u.nbeads for u in universes])) * args.steps
+    counts, _ = eng.nn_neighbors()
+    entries = int(np.sum(counts))
+    surr_flop = FLOP_SURR_ENTRY * entries + FLOP_SURR_ATOM * int(np.sum(natoms))
 
-    # end-to-end through the C ABI with pinned host buffers
+    # end-to-end through the C ABI with pinned host buffers (surrogate)
     nslots = eng.nslots
     h_r = torch.empty(3 * nslots, dtype=torch.float64).pin_memory()
     h_v = torch.empty(3 * nslots, dtype=torch.float64).pin_memory()
@@ -304,72 +340,106 @@ def run_ours(args):
     e2e_steps = max(3, args.steps // 2)
     for w in range(2):
         eng.upload_ptr(h_r.data_ptr(), h_v.data_ptr())
-        eng.md_steps(1, sp, precision=args.precision)
+        eng.md_steps(1, sp, precision="fp32")
         lib.mdt_state_download(eng.h, h_r.data_ptr(), h_v.data_ptr(), None, None, h_e.data_ptr(), None)
     torch.cuda.synchronize()
-    e_atoms = 0
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         eng.upload_ptr(h_r.data_ptr(), h_v.data_ptr())
-        eng.md_steps(1, sp, precision=args.precision)
+        eng.md_steps(1, sp, precision="fp32")
         rc = lib.mdt_state_download(eng.h, h_r.data_ptr(), h_v.data_ptr(), None, None, h_e.data_ptr(), None)
         if rc != 0:
             raise RuntimeError("download failed")
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
-    # upload resets status, so every trajectory runs every e2e step
-    e_atoms = int(natoms.sum()) * e2e_steps
+    e_atoms = int(natoms.sum()) * e2e_steps  # upload resets status: every trajectory runs every e2e step
     h2d = 2 * 3 * nslots * 8
     d2h = 2 * 3 * nslots * 8 + 8 * int(eng.bead_off[-1])
 
-    # roofline: FP64 (or FP32) FMA peak measured on this GPU
+    # ---- plain FP64 EMT on the same trajectories ------------------------------------------
+    eng.set_pes(PES_EMT, 0.0)
+    eng.upload()
+    eng.calc_force(sp, precision=args.precision)
+    for _ in range(args.warmup):
+        eng.md_steps(1, sp, precision=args.precision)
+    torch.cuda.synchronize()
+    s0 = atom_steps_now()
+    ms_emt, clocks_emt = timed_steps(eng, sp, args.precision, args.steps, stream, torch, dist, local)
+    done_emt = atom_steps_now() - s0
+    same, mixed, nat = count_pairs(universes, emt_cut(emt))
+    emt_flop = FLOP_SAME_PAIR * same + FLOP_MIXED_PAIR * mixed + FLOP_ATOM * nat
+    eng.close()
+
+    # ---- accuracy against FP64 EMT on held-out configurations ------------------------------
+    acc = None
+    if rank == 0 and args.rmse_traj > 0:
+        held = generate_dataset(args.rmse_traj, 8, 50, seed=4242 + rank, device=local)
+        f32, e32 = force_rmse(model, held, device=local, precision="fp32", max_neighbors=80)
+        acc = {"force_rmse_meV_per_A": 1e3 * f32, "energy_rmse_meV_per_atom": 1e3 * e32,
+               "configs": len(held.universes),
+               "sample": f"{args.rmse_traj} config-2 trajectories (seed {4242 + rank}) propagated with FP64 EMT, "
+                         "sampled every 50 steps x 8; network forces (no fallback) vs FP64 EMT forces"}
+
     peak = ct.c_double()
-    lib.mdt_peak_fma(1 if args.precision == "fp32" else 0, 2000 if args.precision == "fp64" else 20000,
-                     ct.byref(peak))
-    achieved = flop_per_step / (ms / args.steps * 1e-3)
+    lib.mdt_peak_fma(1, 20000, ct.byref(peak))
+    peak64 = ct.c_double()
+    lib.mdt_peak_fma(0, 2000, ct.byref(peak64))
     traffic = None
-    prof = ROOT / "profiles" / "emt_fused_traffic.json"
+    prof = ROOT / "profiles" / "nnf_surrogate_traffic.json"
     if prof.exists():
         try:
-            traffic = json.loads(prof.read_text()).get(args.precision)
+            traffic = json.loads(prof.read_text()).get("bytes_per_launch")
         except Exception:
             traffic = None
 
-    elapsed = ms * 1e-3
+    elapsed, elapsed_emt = ms * 1e-3, ms_emt * 1e-3
     if dist:
-        t = torch.tensor([elapsed, float(done), e2e_s, float(e_atoms)], device="cuda")
+        t = torch.tensor([elapsed, float(done), e2e_s, float(e_atoms), elapsed_emt, float(done_emt)], device="cuda")
         mx = t.clone()
         dist.all_reduce(mx, op=dist.ReduceOp.MAX)
         sm = t.clone()
         dist.all_reduce(sm, op=dist.ReduceOp.SUM)
-        elapsed, done_all, e2e_s, e_atoms_all = mx[0].item(), sm[1].item(), mx[2].item(), sm[3].item()
+        elapsed, e2e_s, elapsed_emt = mx[0].item(), mx[2].item(), mx[4].item()
+        done_all, e_atoms_all, done_emt_all = sm[1].item(), sm[3].item(), sm[5].item()
     else:
-        done_all, e_atoms_all = done, e_atoms
+        done_all, e_atoms_all, done_emt_all = done, e_atoms, done_emt
     if rank == 0:
+        value = done_all / elapsed
+        emt_value = done_emt_all / elapsed_emt
+        achieved = surr_flop / (elapsed / args.steps)
         line = {
-            "metric": METRIC, "value": done_all / elapsed, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32",
-            "data": "synthetic (seeded H/Au(111) slabs, see workloads.py)",
-            "config": {"workload": f"plain {args.precision.upper()} EMT, {args.ntraj} ragged H/Au(111) trajectories "
-                                   "(37-145 atoms), Verlet H + constant-friction Langevin Au, dt 0.1 fs; "
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded H/Au(111) slabs, see workloads.py); surrogate weights trained on the GPU "
+                    "from FP64 EMT labels (md_tian2_gb300/data)",
+            "config": {"workload": f"NN surrogate (FP32 fast kernels, EMT fallback), {args.ntraj} ragged H/Au(111) "
+                                   "trajectories (37-145 atoms), Verlet H + constant-friction Langevin Au, dt 0.1 fs; "
                                    "one bench step = one MD step of every trajectory",
-                       "ntraj_per_gpu": args.ntraj, "parallelism": f"replicas x{world}",
-                       "l2": "pair scratch (>0.7 GB) rewritten every step: inputs larger than L2",
-                       "surrogate": "not built yet; value is the plain EMT path"},
-            "clocks": clk.summary(),
+                       "model": Path(args.model).name, "fast_path": bool(fast), "ntraj_per_gpu": args.ntraj,
+                       "parallelism": f"replicas x{world}", "range_margin": args.margin,
+                       "l2": "per-step state, skin lists and neighbour words of all trajectories (>0.5 GB) exceed L2"},
+            "emt_fp64": {"value": emt_value, "unit": UNIT, "ms_per_step": 1e3 * elapsed_emt / args.steps,
+                         "dtype": args.precision, "clocks": clocks_emt,
+                         "roofline": {"bound": args.precision, "achieved": emt_flop / (elapsed_emt / args.steps) / 1e12,
+                                      "peak": (peak64.value if args.precision == "fp64" else peak.value) / 1e12,
+                                      "unit": "TFLOP/s"}},
+            "speedup_vs_fp64_emt": value / emt_value,
+            "accuracy": acc,
+            "fallback": {"bead_evaluations": bead_evals, "emt_fallbacks": fb_count,
+                         "fraction": fb_count / max(1, bead_evals)},
+            "clocks": clocks,
             "e2e": {"value": e_atoms_all / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": int(launches),
-            "roofline": {"bound": "fp64" if args.precision == "fp64" else "fp32",
+            "roofline": {"bound": "fp32", "kernel": "nnf_kernel (fused MD step, surrogate)",
                          "achieved": achieved / 1e12, "peak": peak.value / 1e12, "unit": "TFLOP/s",
                          "frac": achieved / peak.value if peak.value > 0 else None, "traffic": traffic,
-                         "peak_source": "measured FMA microbenchmark (mdt_peak_fma), MEASURED_PEAKS.json has no "
-                                        "FP64/FP32 entry",
-                         "flop_per_step": flop_per_step, "pairs_same": same, "pairs_mixed": mixed},
+                         "peak_source": "measured FP32 FMA microbenchmark (mdt_peak_fma); MEASURED_PEAKS.json has "
+                                        "no FP32/FP64 CUDA-core entry",
+                         "flop_per_step": surr_flop, "neighbour_entries": entries},
             "cpu_baseline": cpu,
         }
         print(json.dumps(line), flush=True)
-    eng.close()
     if dist:
         dist.destroy_process_group()
 
