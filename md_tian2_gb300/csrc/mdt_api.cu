@@ -372,38 +372,11 @@ FastNN build_fast(const NNDev &M, const mdt_nn_model *m, const std::vector<int> 
                 const double ex = m->eta[e * ms + x], ey = m->eta[e * ms + y];
                 return ex != ey ? ex < ey : m->rshift[e * ms + x] < m->rshift[e * ms + y];
             });
-            F.g2beg[e][a] = pos;
-            F.g2cnt[e][a] = (int)idx.size();
-            int chain = 0;
-            bool centred = true;
-            for (int s : idx) centred = centred && m->rshift[e * ms + s] == 0.0;
-            for (int S = 1; S <= 4 && centred && chain == 0; ++S) {
-                bool ok = (int)idx.size() > S;
-                for (size_t q = S; q < idx.size() && ok; ++q)
-                    ok = m->eta[e * ms + idx[q]] == 2.0 * m->eta[e * ms + idx[q - S]];
-                if (ok) chain = S;
-            }
-            // uniformly shifted: one eta, r_s,k = r_s,0 + k D
-            if (chain == 0 && idx.size() >= 3) {
-                const double eta = m->eta[e * ms + idx[0]], r0 = m->rshift[e * ms + idx[0]];
-                const double D = m->rshift[e * ms + idx[1]] - r0;
-                bool ok = D > 0.0;
-                for (size_t q = 0; q < idx.size() && ok; ++q) {
-                    const double rs = m->rshift[e * ms + idx[q]];
-                    ok = m->eta[e * ms + idx[q]] == eta && std::fabs(rs - (r0 + q * D)) <= 1e-9 * std::max(1.0, rs);
-                }
-                if (ok) {
-                    chain = -1;
-                    F.g2sh[e][a][0] = (float)(2.0 * eta * D * log2e);
-                    F.g2sh[e][a][1] = (float)(-eta * D * D * log2e);
-                    F.g2sh[e][a][2] = (float)std::exp2(-2.0 * eta * D * D * log2e);
-                }
-            }
-            F.g2chain[e][a] = chain;
             for (int s : idx) {
                 const int k = e * ms + s;
                 float4 v = make_float4((float)(-m->eta[k] * log2e), (float)m->rshift[k], (float)(-2.0 * m->eta[k]), 0.f);
-                std::memcpy(&v.w, &s, 4);
+                const int bits = s | (a << 8);
+                std::memcpy(&v.w, &bits, 4);
                 g2tab[e * kFMaxG2 + pos++] = v;
             }
         }

@@ -67,7 +67,7 @@ struct NNDev {
 // and the G3 functions of each element form a grid of eta slots x (lambda = +-1,
 // zeta = 2^b) cells over one neighbour-element pair.
 // ---------------------------------------------------------------------------
-constexpr int kFMaxG2 = 24;  // radial functions per element and neighbour element
+constexpr int kFMaxG2 = 24;  // radial functions per element
 constexpr int kFNQ = 8;      // (lambda, zeta) cells: lambda = +-1 for up to 4 zeta values
 
 struct FastNN {
@@ -84,17 +84,8 @@ struct FastNN {
     int8_t cell_sf[kMaxElem][4][kFNQ];  // SF index of cell (m, 2k + [lambda < 0]), -1 if none
     float cell_lz[kFNQ];           // lambda zeta of cell q
     int ng2[kMaxElem];
-    // radial functions of element e grouped by neighbour element: group (e, a) is
-    // g2tab[e*kFMaxG2 + g2beg[e][a] ...) with g2cnt[e][a] entries, ascending eta.  With
-    // g2chain[e][a] = S > 0 the group is centred (r_s = 0) and eta_{k+S} = 2 eta_k, so
-    // exp(-eta_{k+S} r^2) = exp(-eta_k r^2)^2: S exponentials, the rest by squaring.
-    // g2chain[e][a] = -1: one eta and r_s,k = r_s,0 + k D; then with t = r - r_s,m at the
-    // middle centre m, e_m and the ratios e_{m+-1}/e_m = exp2(+-a t + b) start recurrences
-    // whose ratios change by the factor c = exp2(2 b) per centre: g2sh[e][a] = (a, b, c),
-    // a = 2 eta D log2 e, b = -eta D^2 log2 e (three exponentials per neighbour).
-    int g2beg[kMaxElem][kMaxElem], g2cnt[kMaxElem][kMaxElem], g2chain[kMaxElem][kMaxElem];
-    float g2sh[kMaxElem][kMaxElem][3];
-    const float4 *g2tab;           // [e*kFMaxG2 + s]: (-eta log2 e, r_s, -2 eta, sf index)
+    // radial functions of element e: g2tab[e*kFMaxG2 + k], k < ng2[e], ordered by neighbour element
+    const float4 *g2tab;           // (-eta log2 e, r_s, -2 eta, sf index | neighbour element << 8)
     // network weights as the fast kernels keep them in shared memory: layer l of element
     // e is a row-major (n_{l-1} + 1) x stride matrix (last row: biases) at wofs[e][l]
     int wofs[kMaxElem][kMaxLayers + 1], wstr[kMaxElem][kMaxLayers + 1], wtotal;

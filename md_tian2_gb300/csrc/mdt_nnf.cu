@@ -19,9 +19,9 @@
 //    Distances are screened in FP32 from a hi/lo split of the wrapped positions; within
 //    1e-4 (relative) of the cutoff the exact FP64 test of mdt_acsf.cuh decides.
 //  * Neighbour rows (d, 1/r, fc, (dfc/dr)/r, exp(-eta_m r^2)) are computed once per pair.
-//  * Radial functions per neighbour-element group; when the group is centred with
-//    eta_{k+S} = 2 eta_k, S exponentials and squarings give all of them.  Per-lane
-//    partial sums are combined by one reduce-scatter (31 shuffles for 32 values).
+//  * Radial functions in one pass over the neighbours (each function predicated on the
+//    neighbour's element), per-lane partial sums combined by one reduce-scatter (31
+//    shuffles for 32 values).
 //  * Triplets (q3 < q4) with r_jk <= rc and the G3 element pair: lane p owns the row
 //    pair (p, n-2-p) of the upper triangle (n candidates together) and marks the valid
 //    second neighbours of both rows in bit masks; the forward and the force walk visit
@@ -438,66 +438,12 @@ struct RowBits {
     }
 };
 
-// Radial functions of one neighbour-element group at distance r: calls f(k, exp(-eta_k
-// (r - r_s,k)^2)) for k < n.  S > 0: centred group with eta_{k+S} = 2 eta_k.
-template <int S, typename Fn>
-__device__ __forceinline__ void g2_chain(const float4 *tab, int n, float r, float r2, Fn &&f) {
-    float ev[kFMaxG2];
-#pragma unroll
-    for (int k = 0; k < kFMaxG2; ++k) {
-        if (k >= n) break;
-        if (S > 0 && k >= S) {
-            ev[k] = ev[k - S] * ev[k - S];
-        } else {
-            const float4 g = tab[k];
-            const float u = S > 0 ? r : r - g.y;
-            ev[k] = exp2f(g.x * (S > 0 ? r2 : u * u));
-        }
-        f(k, ev[k]);
-    }
-}
-
-// Uniformly shifted group (one eta, centres r_s,0 + k D): recurrences up and down from
-// the middle centre, where no value can underflow (|t| <= half the centre span).
-template <typename Fn>
-__device__ __forceinline__ void g2_shifted(const float4 *tab, int n, float r, const float *sh, Fn &&f) {
-    const int km = n >> 1;
-    const float t = r - tab[km].y;
-    const float em = exp2f(tab[km].x * t * t);
-    const float c = sh[2];
-    float eu = em, ru = exp2f(fmaf(sh[0], t, sh[1]));
-#pragma unroll
-    for (int k = 0; k < kFMaxG2; ++k) {
-        if (k >= n) break;
-        if (k < km) continue;
-        f(k, eu);
-        eu *= ru;
-        ru *= c;
-    }
-    float ed = em, rd = exp2f(fmaf(-sh[0], t, sh[1]));
-#pragma unroll
-    for (int k = kFMaxG2 - 1; k >= 0; --k) {
-        if (k >= km) continue;
-        ed *= rd;
-        rd *= c;
-        f(k, ed);
-    }
-}
-
-template <typename Fn>
-__device__ __forceinline__ void g2_group(const float4 *tab, int n, int S, float r, float r2, const float *sh,
-                                         Fn &&f) {
-    if (S < 0) {
-        g2_shifted(tab, n, r, sh, f);
-        return;
-    }
-    switch (S) {
-        case 1: g2_chain<1>(tab, n, r, r2, f); break;
-        case 2: g2_chain<2>(tab, n, r, r2, f); break;
-        case 3: g2_chain<3>(tab, n, r, r2, f); break;
-        case 4: g2_chain<4>(tab, n, r, r2, f); break;
-        default: g2_chain<0>(tab, n, r, r2, f); break;
-    }
+// 2^x for x <= 0 (hardware approximation, relative error about 2^-22; results below the
+// FP32 normal range flush to zero, far below any radial function that matters)
+__device__ __forceinline__ float ex2a(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
 }
 
 // Neighbour rows of atom i from its packed words (global scratch), elements codes.
@@ -640,25 +586,30 @@ __device__ void nnf_descriptors(const NNDev &M, const FastNN &F, const NNScratch
     for (int m = 0; m < NG; ++m) g3l2[m] = F.g3l2[ei][m];
     build_rows<NG>(F, S, W, words, cnt, i, ei, g3l2);
 
-    // ---- radial functions, per neighbour-element group -----------------------------------
+    // ---- radial functions: one pass over the neighbours, each function predicated on the
+    // neighbour's element, one reduce-scatter ---------------------------------------------
     float *G = S.sg + (size_t)i * L.sgs;
     const float4 *g2e = S.g2 + ei * kFMaxG2;
-    for (int a = 0; a < M.nelem; ++a) {
-        const int n = F.g2cnt[ei][a];
-        if (n == 0) continue;
-        const float4 *tab = g2e + F.g2beg[ei][a];
-        const int chain = F.g2chain[ei][a];
+    const int ng2 = F.ng2[ei];
+    {
         float acc[32];
 #pragma unroll
         for (int k = 0; k < 32; ++k) acc[k] = 0.f;
         for (int q = lane; q < cnt; q += 32) {
-            const float4 b = W.rb[q], c = W.rc[q];
-            if ((__float_as_int(c.z) >> 16) != a) continue;
-            g2_group(tab, n, chain, c.y, c.y * c.y, F.g2sh[ei][a],
-                     [&](int k, float e) { acc[k] = fmaf(e, b.x, acc[k]); });
+            const float fc = W.rb[q].x;
+            const float4 c = W.rc[q];
+            const int el = __float_as_int(c.z) >> 16;
+#pragma unroll
+            for (int k = 0; k < kFMaxG2; ++k) {
+                if (k >= ng2) break;
+                const float4 g = g2e[k];
+                if ((__float_as_int(g.w) >> 8) != el) continue;
+                const float u = c.y - g.y;
+                acc[k] = fmaf(ex2a(g.x * u * u), fc, acc[k]);
+            }
         }
         reduce_scatter<32>(acc);
-        if (lane < n) G[__float_as_int(tab[lane].w)] = acc[0];
+        if (lane < ng2) G[__float_as_int(g2e[lane].w) & 0xFF] = acc[0];
     }
 
     // ---- triplet masks and G3 ----------------------------------------------------------------
@@ -946,36 +897,29 @@ __device__ void nnf_forces(const NNDev &M, const FastNN &F, const NNScratch &X, 
         W.sfy[q] = 0.f;
         W.sfz[q] = 0.f;
     }
+    // d/dr sum_k c_k exp(-eta_k (r - rs_k)^2) fc = sum_k c_k e_k (dfc - 2 eta_k (r - rs_k) fc)
     const float4 *g2e = S.g2 + ei * kFMaxG2;
-    for (int a = 0; a < M.nelem; ++a) {
-        const int n = F.g2cnt[ei][a];
-        if (n == 0) continue;
-        const float4 *tab = g2e + F.g2beg[ei][a];
-        const int chain = F.g2chain[ei][a];
-        // d/dr sum_k c_k exp(-eta_k (r - rs_k)^2) fc = sum_k c_k e_k (dfc - 2 eta_k (r - rs_k) fc):
-        // A = sum c_k e_k, B = sum (-2 eta_k c_k) e_k, C = sum (-2 eta_k c_k rs_k) e_k,
-        // derivative = A dfc + (B r - C) fc
-        float cw[kFMaxG2];
+    const int ng2 = F.ng2[ei];
+    float cw[kFMaxG2];
 #pragma unroll
-        for (int k = 0; k < kFMaxG2; ++k) cw[k] = k < n ? dG[__float_as_int(tab[k].w)] : 0.f;
-        const bool centred = chain > 0;
-        for (int q = lane; q < cnt; q += 32) {
-            const float4 c = W.rc[q];
-            if ((__float_as_int(c.z) >> 16) != a) continue;
-            const float4 av = W.ra[q];
-            const float fc = W.rb[q].x, dfc = c.x * c.y, r = c.y;
-            float A = 0.f, Bv = 0.f, Cv = 0.f;
-            g2_group(tab, n, chain, r, r * r, F.g2sh[ei][a], [&](int k, float e) {
-                const float ce = cw[k] * tab[k].z;
-                A = fmaf(cw[k], e, A);
-                Bv = fmaf(ce, e, Bv);
-                if (!centred) Cv = fmaf(ce * tab[k].y, e, Cv);
-            });
-            const float fr = fmaf(A, dfc, fmaf(Bv, r, -Cv) * fc) * av.w;
-            W.sfx[q] -= fr * av.x;
-            W.sfy[q] -= fr * av.y;
-            W.sfz[q] -= fr * av.z;
+    for (int k = 0; k < kFMaxG2; ++k) cw[k] = k < ng2 ? dG[__float_as_int(g2e[k].w) & 0xFF] : 0.f;
+    for (int q = lane; q < cnt; q += 32) {
+        const float4 c = W.rc[q], av = W.ra[q];
+        const int el = __float_as_int(c.z) >> 16;
+        const float fc = W.rb[q].x, dfc = c.x * c.y, r = c.y;
+        float dsum = 0.f;
+#pragma unroll
+        for (int k = 0; k < kFMaxG2; ++k) {
+            if (k >= ng2) break;
+            const float4 g = g2e[k];
+            if ((__float_as_int(g.w) >> 8) != el) continue;
+            const float u = r - g.y;
+            dsum = fmaf(cw[k] * ex2a(g.x * u * u), fmaf(g.z * u, fc, dfc), dsum);
         }
+        const float fr = dsum * av.w;
+        W.sfx[q] -= fr * av.x;
+        W.sfy[q] -= fr * av.y;
+        W.sfz[q] -= fr * av.z;
     }
 
     // ---- angular part ------------------------------------------------------------------------

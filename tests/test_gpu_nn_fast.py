@@ -68,9 +68,8 @@ def test_fast_path_qualifies_and_matches_oracle(built_lib, oracle_lib):
 
 def test_fast_path_radial_model_matches_oracle(built_lib, oracle_lib):
     """24 shifted G2 over Au and H neighbours, no angular functions (the triplet stages are
-    skipped; each uniformly spaced group is evaluated by recurrences from its middle
-    centre, whose relative FP32 error grows with the distance from it, so the bar is
-    1e-4 of the force RMS)."""
+    skipped; the exponentials use the hardware 2^x approximation, so the bar is 1e-4 of
+    the force RMS)."""
     from oracle.oracle import NNOracle
     us = W.config2(5, seed=8)
     m = surrogate_model(3, descriptor="radial")
