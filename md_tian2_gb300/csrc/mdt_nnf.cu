@@ -586,30 +586,31 @@ __device__ void nnf_descriptors(const NNDev &M, const FastNN &F, const NNScratch
     for (int m = 0; m < NG; ++m) g3l2[m] = F.g3l2[ei][m];
     build_rows<NG>(F, S, W, words, cnt, i, ei, g3l2);
 
-    // ---- radial functions: one pass over the neighbours, each function predicated on the
-    // neighbour's element, one reduce-scatter ---------------------------------------------
+    // ---- radial functions: lane k owns function k and loops over the neighbours (row data
+    // are broadcast reads), so no cross-lane reduction and little code ------------------
     float *G = S.sg + (size_t)i * L.sgs;
     const float4 *g2e = S.g2 + ei * kFMaxG2;
     const int ng2 = F.ng2[ei];
     {
-        float acc[32];
-#pragma unroll
-        for (int k = 0; k < 32; ++k) acc[k] = 0.f;
-        for (int q = lane; q < cnt; q += 32) {
-            const float fc = W.rb[q].x;
-            const float4 c = W.rc[q];
-            const int el = __float_as_int(c.z) >> 16;
-#pragma unroll
-            for (int k = 0; k < kFMaxG2; ++k) {
-                if (k >= ng2) break;
-                const float4 g = g2e[k];
-                if ((__float_as_int(g.w) >> 8) != el) continue;
-                const float u = c.y - g.y;
-                acc[k] = fmaf(ex2a(g.x * u * u), fc, acc[k]);
-            }
+        const bool own = lane < ng2;
+        const float4 g = own ? g2e[lane] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const int gel = own ? (__float_as_int(g.w) >> 8) : -2;
+        float a0 = 0.f, a1 = 0.f;
+        int q = 0;
+        for (; q + 2 <= cnt; q += 2) {
+            const float4 c0 = W.rc[q], c1 = W.rc[q + 1];
+            const float f0 = W.rb[q].x, f1 = W.rb[q + 1].x;
+            const float u0 = c0.y - g.y, u1 = c1.y - g.y;
+            const float e0 = ex2a(g.x * u0 * u0), e1 = ex2a(g.x * u1 * u1);
+            if ((__float_as_int(c0.z) >> 16) == gel) a0 = fmaf(e0, f0, a0);
+            if ((__float_as_int(c1.z) >> 16) == gel) a1 = fmaf(e1, f1, a1);
         }
-        reduce_scatter<32>(acc);
-        if (lane < ng2) G[__float_as_int(g2e[lane].w) & 0xFF] = acc[0];
+        if (q < cnt) {
+            const float4 c0 = W.rc[q];
+            const float u0 = c0.y - g.y;
+            if ((__float_as_int(c0.z) >> 16) == gel) a0 = fmaf(ex2a(g.x * u0 * u0), W.rb[q].x, a0);
+        }
+        if (own) G[__float_as_int(g.w) & 0xFF] = a0 + a1;
     }
 
     // ---- triplet masks and G3 ----------------------------------------------------------------
@@ -897,24 +898,22 @@ __device__ void nnf_forces(const NNDev &M, const FastNN &F, const NNScratch &X, 
         W.sfy[q] = 0.f;
         W.sfz[q] = 0.f;
     }
-    // d/dr sum_k c_k exp(-eta_k (r - rs_k)^2) fc = sum_k c_k e_k (dfc - 2 eta_k (r - rs_k) fc)
+    // d/dr sum_k c_k exp(-eta_k (r - rs_k)^2) fc = sum_k c_k e_k (dfc - 2 eta_k (r - rs_k) fc);
+    // lanes = neighbours, a short loop over the functions (table and c_k broadcast)
     const float4 *g2e = S.g2 + ei * kFMaxG2;
     const int ng2 = F.ng2[ei];
-    float cw[kFMaxG2];
-#pragma unroll
-    for (int k = 0; k < kFMaxG2; ++k) cw[k] = k < ng2 ? dG[__float_as_int(g2e[k].w) & 0xFF] : 0.f;
     for (int q = lane; q < cnt; q += 32) {
         const float4 c = W.rc[q], av = W.ra[q];
         const int el = __float_as_int(c.z) >> 16;
         const float fc = W.rb[q].x, dfc = c.x * c.y, r = c.y;
         float dsum = 0.f;
-#pragma unroll
-        for (int k = 0; k < kFMaxG2; ++k) {
-            if (k >= ng2) break;
+#pragma unroll 2
+        for (int k = 0; k < ng2; ++k) {
             const float4 g = g2e[k];
-            if ((__float_as_int(g.w) >> 8) != el) continue;
+            const int gw = __float_as_int(g.w);
             const float u = r - g.y;
-            dsum = fmaf(cw[k] * ex2a(g.x * u * u), fmaf(g.z * u, fc, dfc), dsum);
+            const float t = dG[gw & 0xFF] * ex2a(g.x * u * u) * fmaf(g.z * u, fc, dfc);
+            if ((gw >> 8) == el) dsum += t;
         }
         const float fr = dsum * av.w;
         W.sfx[q] -= fr * av.x;
