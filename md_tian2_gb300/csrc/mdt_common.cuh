@@ -122,12 +122,15 @@ __device__ __forceinline__ double u01_53(uint32_t a, uint32_t b) {
 }
 
 // One N(0,1) deviate per (key, counter) by the Box-Muller form the reference uses
-// (useful_things.f90:121-173: sqrt(-2 ln u1) cos(2 pi u2)).
+// (useful_things.f90:121-173: sqrt(-2 ln u1) cos(2 pi u2)), evaluated in FP32: on this
+// GPU FP64 runs at 1/64 of FP32, and the thermostat noise needs no more than 24-bit
+// uniforms (u1 in (0, 1]: tails end at sqrt(2 ln 2^24) = 5.77 sigma).
 __device__ __forceinline__ double normal_deviate(uint64_t seed, uint32_t traj, uint32_t step,
                                                  uint32_t slot, uint32_t stream) {
     U4 r = philox4x32_10(U4{step, slot, stream, traj}, (uint32_t)seed, (uint32_t)(seed >> 32));
-    const double u1 = u01_53(r.x, r.y), u2 = u01_53(r.z, r.w);
-    return sqrt(-2.0 * log(u1)) * cospi(2.0 * u2);
+    const float u1 = (float)((r.x >> 8) + 1u) * (1.0f / 16777216.0f);
+    const float u2 = (float)(r.z >> 8) * (1.0f / 16777216.0f);
+    return (double)(sqrtf(-2.0f * logf(u1)) * cospif(2.0f * u2));
 }
 
 __device__ __forceinline__ double uniform_deviate(uint64_t seed, uint32_t traj, uint32_t step,

@@ -1057,6 +1057,26 @@ __device__ void nnf_forces(const NNDev &M, const FastNN &F, const NNScratch &X, 
     __syncwarp();
 }
 
+// lattice rows and inverse (bohr), their FP32 copies and the image half-widths of the
+// list cutoff (0..2) and the skin-list cutoff (3..5) of trajectory t
+__device__ void cell_setup(const Batch &B, const NNDev &M, const FastNN &F, const SmemF &S, int t) {
+    const int tid = threadIdx.x;
+    if (tid == 0) acsf_lattice(B.box + 9 * t, S.lat);
+    __syncthreads();
+    if (tid < 9) {
+        S.latf[tid] = (float)S.lat[tid];
+        S.ginv[tid] = (float)S.lat[9 + tid];
+    }
+    if (tid < 6) {
+        const int d = tid % 3;
+        const double *I = S.lat + 9 + 3 * d;
+        const double bn = sqrt(I[0] * I[0] + I[1] * I[1] + I[2] * I[2]);
+        const double rc = tid < 3 ? M.maxcut : M.maxcut + (double)F.skin;
+        S.wk[tid] = (float)(rc * bn * (1.0 + 1e-4) + 1e-4);
+    }
+    __syncthreads();
+}
+
 // atoms of the trajectory ordered by element (network groups share an element)
 __device__ void order_by_element(const NNDev &M, const SmemF &S, const FLaunch &L, int N) {
     if (threadIdx.x == 0) {
@@ -1073,8 +1093,9 @@ __device__ void order_by_element(const NNDev &M, const SmemF &S, const FLaunch &
 }
 
 // ---- one bead ---------------------------------------------------------------------------
-// Warps take groups of 2-4 atoms of one element: descriptors of each atom, the group's
-// network, forces of each atom; no CTA barrier between the stages.
+// Warps take 1-4 atoms at a time: descriptors of each atom, the network of each run of
+// one element, forces of each atom; no CTA barrier between the stages.  The lattice
+// tables (S.lat, latf, ginv, wk) are set once per trajectory by cell_setup.
 template <int NG, int ZM>
 __device__ bool nnf_bead(const Batch &B, const NNDev &M, const FastNN &F, const NNScratch &X, const SmemF &S,
                          const FLaunch &L, int t, int b, bool do_forces, bool skip_if_flagged) {
@@ -1084,23 +1105,11 @@ __device__ bool nnf_bead(const Batch &B, const NNDev &M, const FastNN &F, const 
     const int warp = tid >> 5, lane = tid & 31;
     const int bead = B.bead_off[t] + b;
     if (tid == 0) {
-        acsf_lattice(B.box + 9 * t, S.lat);
         S.misc[0] = 0;
         S.misc[1] = 0;
         S.misc[3] = 0;
     }
     __syncthreads();
-    if (tid < 9) {
-        S.latf[tid] = (float)S.lat[tid];
-        S.ginv[tid] = (float)S.lat[9 + tid];
-    }
-    if (tid < 6) {  // image half-widths: list cutoff (0..2), skin-list cutoff (3..5)
-        const int d = tid % 3;
-        const double *I = S.lat + 9 + 3 * d;
-        const double bn = sqrt(I[0] * I[0] + I[1] * I[1] + I[2] * I[2]);
-        const double rc = tid < 3 ? M.maxcut : M.maxcut + (double)F.skin;
-        S.wk[tid] = (float)(rc * bn * (1.0 + 1e-4) + 1e-4);
-    }
     float d2max = 0.f;
     for (int i = tid; i < N; i += nt) {
         double x, y, z;
@@ -1151,38 +1160,39 @@ __device__ bool nnf_bead(const Batch &B, const NNDev &M, const FastNN &F, const 
     unsigned *mscr = X.mscr + (size_t)blockIdx.x * X.mcap;
     const size_t mstride = (size_t)L.maxnb * L.mw;
     const int *off = S.byel + L.max_atoms;
-    // groups of 4 atoms (network ILP) on large beads, of 2 on small ones (tail balance)
-    const int gsz = N >= 96 ? 4 : 2;
-    int ngroups = 0;
-    for (int e = 0; e < M.nelem; ++e) ngroups += (off[e + 1] - off[e] + gsz - 1) / gsz;
+    const int nnn = off[M.nelem];  // network atoms, ordered by element
     double e_warp = 0.0;
     float *hs = (float *)(S.warp_base + (size_t)warp * S.warp_bytes);
-    float *hv = hs + gsz * (M.nlayers + 1) * L.ls;
+    float *hv = hs + kNAmax * (M.nlayers + 1) * L.ls;
     const WarpF W = carve_warp(S, L, warp);
+    // guided split: 4 atoms per grab while many remain (network ILP), then 2, then 1
+    // (the bead's last atoms spread over all warps)
     for (;;) {
-        int g = 0;
-        if (lane == 0) g = atomicAdd(&S.misc[1], 1);
-        g = __shfl_sync(0xffffffffu, g, 0);
-        if (g >= ngroups) break;
-        int e = 0, first = 0;
-        for (int k = 0; k < M.nelem; ++k) {
-            const int ng = (off[k + 1] - off[k] + gsz - 1) / gsz;
-            if (g < ng) {
-                e = k;
-                first = off[k] + g * gsz;
-                break;
-            }
-            g -= ng;
+        int st = 0, n = 0;
+        if (lane == 0) {
+            const int rem = nnn - *(volatile int *)&S.misc[1];
+            const int k = rem > 8 * kFW ? 4 : rem > 2 * kFW ? 2 : 1;
+            st = atomicAdd(&S.misc[1], k);
+            n = min(k, nnn - st);
         }
-        const int n = min(gsz, off[e + 1] - first);
-        const int *atoms = S.byel + first;
+        st = __shfl_sync(0xffffffffu, st, 0);
+        n = __shfl_sync(0xffffffffu, n, 0);
+        if (n <= 0) break;
+        const int *atoms = S.byel + st;
         for (int a = 0; a < n; ++a)
             nnf_descriptors<NG, ZM>(M, F, X, S, W, L, t, base, atoms[a], N, na, mscr + (size_t)atoms[a] * mstride,
                                     rebuild);
         __syncwarp();
-        const float en = gsz == 4 ? nnf_network<4>(M, F, S, L, hs, hv, e, atoms, n, do_forces)
-                                  : nnf_network<2>(M, F, S, L, hs, hv, e, atoms, n, do_forces);
-        if (lane == 0) e_warp += (double)en + n * (M.remove_atom_energies ? M.atom_energy[e] : 0.0);
+        for (int r0 = 0; r0 < n;) {  // runs of one element
+            const int e = S.elem[atoms[r0]];
+            int r1 = r0 + 1;
+            while (r1 < n && S.elem[atoms[r1]] == e) ++r1;
+            const int m = r1 - r0;
+            const float en = m > 2 ? nnf_network<4>(M, F, S, L, hs, hv, e, atoms + r0, m, do_forces)
+                                   : nnf_network<2>(M, F, S, L, hs, hv, e, atoms + r0, m, do_forces);
+            if (lane == 0) e_warp += (double)en + m * (M.remove_atom_energies ? M.atom_energy[e] : 0.0);
+            r0 = r1;
+        }
         if (do_forces)
             for (int a = 0; a < n; ++a)
                 nnf_forces<NG, ZM>(M, F, X, S, W, L, base, atoms[a], mscr + (size_t)atoms[a] * mstride);
@@ -1298,6 +1308,7 @@ __global__ void __launch_bounds__(kFBlock, 2)
         for (int i = threadIdx.x; i < T.N; i += blockDim.x) S.elem[i] = (int8_t)M.elem_of_type[B.type[T.aoff + i]];
         __syncthreads();
         order_by_element(M, S, L, T.N);
+        cell_setup(B, M, F, S, t);
         if (mode != 2) {
             nnf_calc_force<NG, ZM>(B, M, F, E, X, P, S, SE, L, T, mode == 0);
             continue;
