@@ -720,7 +720,7 @@ __device__ void nnf_descriptors(const NNDev &M, const FastNN &F, const NNScratch
 // scaling and range check of getshortatomic.f90:174-236.  Replaces the descriptors of
 // the atoms in S.sg by dE/dG (raw G); returns the energy sum of the group (lane 0).
 template <int kNA>
-__device__ float nnf_network(const NNDev &M, const FastNN &F, const SmemF &S, const FLaunch &L, float *hs,
+__device__ double nnf_network(const NNDev &M, const FastNN &F, const SmemF &S, const FLaunch &L, float *hs,
                              float *hv, int ei, const int *atoms, int na, bool do_forces) {
     const int lane = threadIdx.x & 31;
     const int ls = L.ls, lstr = (M.nlayers + 1) * ls;  // per-atom stride in hs/hv
@@ -742,7 +742,7 @@ __device__ float nnf_network(const NNDev &M, const FastNN &F, const SmemF &S, co
 #pragma unroll
         for (int a = 0; a < kNA; ++a) hv[a * lstr + s] = 0.f;
     __syncwarp();
-    float eout = 0.f;
+    double eout = 0.0;  // per-atom outputs summed in FP64: independent of the grouping
     for (int l = 1; l <= M.nlayers; ++l) {
         const int nprev = M.nodes[ei][l - 1], ncur = M.nodes[ei][l];
         const float *Wl = S.w + F.wofs[ei][l];
@@ -767,7 +767,7 @@ __device__ float nnf_network(const NNDev &M, const FastNN &F, const SmemF &S, co
                     hs[a * lstr + l * ls] = zz;
                     hv[a * lstr + l * ls] = v;
                 }
-                if (l == M.nlayers && a < na) eout += v;
+                if (l == M.nlayers && a < na) eout += (double)v;
             }
         } else {
             for (int n = lane; n < ncur; n += 32) {
@@ -1093,7 +1093,7 @@ __device__ void order_by_element(const NNDev &M, const SmemF &S, const FLaunch &
 }
 
 // ---- one bead ---------------------------------------------------------------------------
-// Warps take 1-4 atoms at a time: descriptors of each atom, the network of each run of
+// Warps take 2 or 4 atoms at a time: descriptors of each atom, the network of each run of
 // one element, forces of each atom; no CTA barrier between the stages.  The lattice
 // tables (S.lat, latf, ginv, wk) are set once per trajectory by cell_setup.
 template <int NG, int ZM>
@@ -1165,15 +1165,14 @@ __device__ bool nnf_bead(const Batch &B, const NNDev &M, const FastNN &F, const 
     float *hs = (float *)(S.warp_base + (size_t)warp * S.warp_bytes);
     float *hv = hs + kNAmax * (M.nlayers + 1) * L.ls;
     const WarpF W = carve_warp(S, L, warp);
-    // guided split: 4 atoms per grab while many remain (network ILP), then 2, then 1
-    // (the bead's last atoms spread over all warps)
+    // grabs of 4 atoms (network ILP) on large beads, of 2 on small ones (tail balance);
+    // a grab that spans two elements runs the network once per element
+    const int gsz = N >= 96 ? 4 : 2;
     for (;;) {
         int st = 0, n = 0;
         if (lane == 0) {
-            const int rem = nnn - *(volatile int *)&S.misc[1];
-            const int k = rem > 8 * kFW ? 4 : rem > 2 * kFW ? 2 : 1;
-            st = atomicAdd(&S.misc[1], k);
-            n = min(k, nnn - st);
+            st = atomicAdd(&S.misc[1], gsz);
+            n = min(gsz, nnn - st);
         }
         st = __shfl_sync(0xffffffffu, st, 0);
         n = __shfl_sync(0xffffffffu, n, 0);
@@ -1188,9 +1187,9 @@ __device__ bool nnf_bead(const Batch &B, const NNDev &M, const FastNN &F, const 
             int r1 = r0 + 1;
             while (r1 < n && S.elem[atoms[r1]] == e) ++r1;
             const int m = r1 - r0;
-            const float en = m > 2 ? nnf_network<4>(M, F, S, L, hs, hv, e, atoms + r0, m, do_forces)
-                                   : nnf_network<2>(M, F, S, L, hs, hv, e, atoms + r0, m, do_forces);
-            if (lane == 0) e_warp += (double)en + m * (M.remove_atom_energies ? M.atom_energy[e] : 0.0);
+            const double en = m > 2 ? nnf_network<4>(M, F, S, L, hs, hv, e, atoms + r0, m, do_forces)
+                                    : nnf_network<2>(M, F, S, L, hs, hv, e, atoms + r0, m, do_forces);
+            if (lane == 0) e_warp += en + m * (M.remove_atom_energies ? M.atom_energy[e] : 0.0);
             r0 = r1;
         }
         if (do_forces)
