@@ -131,7 +131,7 @@ __device__ __forceinline__ void zeta_powers(float h, float *P, float *Q) {
 }
 
 struct FLaunch {
-    int max_atoms, maxnb, mw, ls, sgs;  // mw: mask words per row; ls: node stride; sgs: descriptor stride
+    int max_atoms, maxnb, mw, ls, sgs;  // mw: mask words per row (0 without G3); ls: node stride; sgs: descriptor stride
     int surrogate, netshape;            // netshape: all layers fit the 4-atom network kernel
 };
 
@@ -143,8 +143,7 @@ struct SmemF {
     int8_t *elem;
     int *fold;                           // fold counts of the wrapping, 3 x 8 bits (+128)
     int *byel;                           // atoms ordered by element; [max_atoms + kMaxElem + 1] offsets after
-    float *fw;                           // [warp][3][max_atoms] force accumulators (Ha/bohr)
-    float *sg;                           // [max_atoms][sgs]: descriptors G, then dE/dG
+    float *f3;                           // [3][max_atoms] bead force accumulators (Ha/bohr)
     double *lat;                         // 9 lattice rows + 9 inverse (bohr)
     float *latf, *ginv, *wk;             // FP32 lattice rows, inverse rows, image half-widths (cutoff, skin list)
     double *red;                         // block reductions
@@ -162,24 +161,24 @@ struct WarpF {
     unsigned *mask;        // [q][mw]: valid second neighbours q4 > q of row q
     int *rcnt;             // [q]: valid triplets of row q
     float *sfx, *sfy, *sfz;
+    float *gb;             // [kNAmax][sgs]: descriptors G, then dE/dG, of the atoms in flight
 };
 
 constexpr int kNAmax = 4;  // atoms per warp in the network phase
 
 __host__ __device__ inline size_t r16f(size_t b) { return (b + 15) & ~size_t(15); }
 
-__host__ __device__ inline size_t warp_bytes_f(int maxnb, int mw, int nlayers, int ls) {
+__host__ __device__ inline size_t warp_bytes_f(int maxnb, int mw, int nlayers, int ls, int sgs) {
     const size_t rows = 3 * r16f(16 * (size_t)maxnb) + r16f(maxnb) + r16f(4 * (size_t)maxnb * mw) +
                         r16f(4 * ((size_t)maxnb + 1)) + 3 * r16f(4 * (size_t)maxnb);
     const size_t net = 2 * r16f(4 * (size_t)kNAmax * (nlayers + 1) * ls);
-    return rows > net ? rows : net;
+    return (rows > net ? rows : net) + r16f(4 * (size_t)kNAmax * sgs);
 }
 
-__host__ __device__ inline size_t shared_bytes_f(int max_atoms, int max_beads, int wtotal, int nelem, int sgs) {
+__host__ __device__ inline size_t shared_bytes_f(int max_atoms, int max_beads, int wtotal, int nelem) {
     return 3 * r16f(8 * (size_t)max_atoms) + 6 * r16f(4 * (size_t)max_atoms) + r16f(max_atoms) +
            r16f(4 * (size_t)max_atoms) + r16f(4 * ((size_t)max_atoms + kMaxElem + 1)) +
-           r16f(4 * (size_t)kFW * 3 * max_atoms) +
-           r16f(4 * (size_t)max_atoms * sgs) + r16f(8 * 18) + 3 * r16f(4 * 9) + r16f(8 * 64) +
+           3 * r16f(4 * (size_t)max_atoms) + r16f(8 * 18) + 3 * r16f(4 * 9) + r16f(8 * 64) +
            r16f(8 * (size_t)max_beads * max_beads) + 16 + r16f(4 * (size_t)wtotal) +
            r16f(16 * (size_t)nelem * kFMaxG2);
 }
@@ -188,7 +187,9 @@ FLaunch flaunch(const Batch &B, const NNDev &M, int surrogate) {
     FLaunch L;
     L.max_atoms = B.max_atoms;
     L.maxnb = M.maxnb;
-    L.mw = (M.maxnb + 31) / 32;
+    L.mw = 0;
+    for (int e = 0; e < M.nelem; ++e)
+        if (M.g3fast[e]) L.mw = (M.maxnb + 31) / 32;
     int mx = 1;
     for (int e = 0; e < M.nelem; ++e)
         for (int l = 0; l <= M.nlayers; ++l) mx = mx > M.nodes[e][l] ? mx : M.nodes[e][l];
@@ -204,9 +205,9 @@ FLaunch flaunch(const Batch &B, const NNDev &M, int surrogate) {
 
 size_t nnf_smem_total(const Batch &B, const NNDev &M, const FastNN &F) {
     const FLaunch L = flaunch(B, M, 0);
-    const size_t wb = kFW * warp_bytes_f(L.maxnb, L.mw, M.nlayers, L.ls);
+    const size_t wb = kFW * warp_bytes_f(L.maxnb, L.mw, M.nlayers, L.ls, L.sgs);
     const size_t emt = smem_bytes(B.max_atoms, B.max_beads, 8);
-    return shared_bytes_f(B.max_atoms, B.max_beads, F.wtotal, M.nelem, L.sgs) + (wb > emt ? wb : emt);
+    return shared_bytes_f(B.max_atoms, B.max_beads, F.wtotal, M.nelem) + (wb > emt ? wb : emt);
 }
 
 __device__ SmemF carve_f(unsigned char *base, const FLaunch &L, int max_beads, int wtotal, int nelem,
@@ -231,8 +232,7 @@ __device__ SmemF carve_f(unsigned char *base, const FLaunch &L, int max_beads, i
     s.elem = (int8_t *)take(na);
     s.fold = (int *)take(4 * (size_t)na);
     s.byel = (int *)take(4 * ((size_t)na + kMaxElem + 1));
-    s.fw = (float *)take(4 * (size_t)kFW * 3 * na);
-    s.sg = (float *)take(4 * (size_t)na * L.sgs);
+    s.f3 = (float *)take(4 * 3 * (size_t)na);
     s.lat = (double *)take(8 * 18);
     s.latf = (float *)take(4 * 9);
     s.ginv = (float *)take(4 * 9);
@@ -243,7 +243,7 @@ __device__ SmemF carve_f(unsigned char *base, const FLaunch &L, int max_beads, i
     s.w = (float *)take(4 * (size_t)wtotal);
     s.g2 = (float4 *)take(16 * (size_t)nelem * kFMaxG2);
     s.warp_base = base + off;
-    s.warp_bytes = warp_bytes_f(L.maxnb, L.mw, nlayers, L.ls);
+    s.warp_bytes = warp_bytes_f(L.maxnb, L.mw, nlayers, L.ls, L.sgs);
     return s;
 }
 
@@ -266,6 +266,7 @@ __device__ WarpF carve_warp(const SmemF &S, const FLaunch &L, int warp) {
     w.sfx = (float *)take(4 * (size_t)nb);
     w.sfy = (float *)take(4 * (size_t)nb);
     w.sfz = (float *)take(4 * (size_t)nb);
+    w.gb = (float *)(base + S.warp_bytes - r16f(4 * (size_t)kNAmax * L.sgs));
     return w;
 }
 
@@ -483,7 +484,7 @@ __device__ __forceinline__ void build_rows(const FastNN &F, const SmemF &S, cons
 template <int NG, int ZM>
 __device__ void nnf_descriptors(const NNDev &M, const FastNN &F, const NNScratch &X, const SmemF &S,
                                 const WarpF &W, const FLaunch &L, int t, int64_t base, int i, int N, const int *na,
-                                unsigned *mglob, bool rebuild) {
+                                unsigned *mglob, bool rebuild, float *G) {
     constexpr int NZ = popc5(ZM), NQ = 2 * NZ;
     static_assert(NG * NQ <= 32, "too many G3 cells");
     const int lane = threadIdx.x & 31;
@@ -588,7 +589,6 @@ __device__ void nnf_descriptors(const NNDev &M, const FastNN &F, const NNScratch
 
     // ---- radial functions: lane k owns function k and loops over the neighbours (row data
     // are broadcast reads), so no cross-lane reduction and little code ------------------
-    float *G = S.sg + (size_t)i * L.sgs;
     const float4 *g2e = S.g2 + ei * kFMaxG2;
     const int ng2 = F.ng2[ei];
     {
@@ -718,10 +718,10 @@ __device__ void nnf_descriptors(const NNDev &M, const FastNN &F, const NNScratch
 // ---- network for up to kNA atoms of element e (lanes = nodes) --------------------------
 // calconenn.f90:83-153 forward, getdnodes_values.f90 + getshortatomic.f90:263-291 back;
 // scaling and range check of getshortatomic.f90:174-236.  Replaces the descriptors of
-// the atoms in S.sg by dE/dG (raw G); returns the energy sum of the group (lane 0).
+// the descriptors in gb by dE/dG (raw G); returns the energy sum of the group (lane 0).
 template <int kNA>
 __device__ double nnf_network(const NNDev &M, const FastNN &F, const SmemF &S, const FLaunch &L, float *hs,
-                             float *hv, int ei, const int *atoms, int na, bool do_forces) {
+                              float *hv, int ei, float *gb, int na, bool do_forces) {
     const int lane = threadIdx.x & 31;
     const int ls = L.ls, lstr = (M.nlayers + 1) * ls;  // per-atom stride in hs/hv
     const int nsf = M.nsf[ei], sfb = ei * M.maxsf;
@@ -731,7 +731,7 @@ __device__ double nnf_network(const NNDev &M, const FastNN &F, const SmemF &S, c
         for (int a = 0; a < kNA; ++a) {
             float v = 0.f;
             if (a < na) {
-                const float g = S.sg[(size_t)atoms[a] * L.sgs + s];
+                const float g = gb[a * L.sgs + s];
                 if (g < sc.z || g > sc.w) S.misc[0] = 1;
                 v = fmaf(sc.x, g, sc.y);
             }
@@ -869,7 +869,7 @@ __device__ double nnf_network(const NNDev &M, const FastNN &F, const SmemF &S, c
             const float dsc = F.dscal[sfb + s];
 #pragma unroll
             for (int a = 0; a < kNA; ++a)
-                if (a < na) S.sg[(size_t)atoms[a] * L.sgs + s] = u[a] * dsc;
+                if (a < na) gb[a * L.sgs + s] = u[a] * dsc;
         }
     }
     __syncwarp();
@@ -879,7 +879,7 @@ __device__ double nnf_network(const NNDev &M, const FastNN &F, const SmemF &S, c
 // ---- phase 3: forces of one central atom ---------------------------------------------
 template <int NG, int ZM>
 __device__ void nnf_forces(const NNDev &M, const FastNN &F, const NNScratch &X, const SmemF &S, const WarpF &W,
-                           const FLaunch &L, int64_t base, int i, const unsigned *mglob) {
+                           const FLaunch &L, int64_t base, int i, const unsigned *mglob, const float *dG) {
     constexpr int NZ = popc5(ZM), NQ = 2 * NZ;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int ei = S.elem[i];
@@ -890,7 +890,6 @@ __device__ void nnf_forces(const NNDev &M, const FastNN &F, const NNScratch &X, 
 #pragma unroll
     for (int m = 0; m < NG; ++m) g3l2[m] = F.g3l2[ei][m];
     build_rows<NG>(F, S, W, words, cnt, i, ei, g3l2);
-    const float *dG = S.sg + (size_t)i * L.sgs;
 
     // ---- radial part: slot forces start here -----------------------------------------------
     for (int q = lane; q < cnt; q += 32) {
@@ -1022,37 +1021,25 @@ __device__ void nnf_forces(const NNDev &M, const FastNN &F, const NNScratch &X, 
     __syncwarp();
 
     // ---- scatter: neighbours get their slot forces, the centre minus their sum ----------
-    float *fwx = S.fw + (size_t)warp * 3 * L.max_atoms, *fwy = fwx + L.max_atoms, *fwz = fwy + L.max_atoms;
+    float *fx = S.f3, *fy = fx + L.max_atoms, *fz = fy + L.max_atoms;
     float fix = 0.f, fiy = 0.f, fiz = 0.f;
-    for (int q0 = 0; q0 < cnt; q0 += 32) {
-        const int q = q0 + lane;
-        const bool ok = q < cnt;
-        const int j = ok ? (__float_as_int(W.rc[q].z) & 0xFFFF) : -1 - lane;
-        const unsigned same = __match_any_sync(0xffffffffu, j);
-        if (ok) {
-            const float sx = W.sfx[q], sy = W.sfy[q], sz = W.sfz[q];
-            if (same == (1u << lane)) {
-                fwx[j] += sx;
-                fwy[j] += sy;
-                fwz[j] += sz;
-            } else {  // several images of atom j in this block of neighbours
-                atomicAdd(&fwx[j], sx);
-                atomicAdd(&fwy[j], sy);
-                atomicAdd(&fwz[j], sz);
-            }
-            fix -= sx;
-            fiy -= sy;
-            fiz -= sz;
-        }
-        __syncwarp();
+    for (int q = lane; q < cnt; q += 32) {
+        const int j = __float_as_int(W.rc[q].z) & 0xFFFF;
+        const float sx = W.sfx[q], sy = W.sfy[q], sz = W.sfz[q];
+        red_shared(&fx[j], sx);
+        red_shared(&fy[j], sy);
+        red_shared(&fz[j], sz);
+        fix -= sx;
+        fiy -= sy;
+        fiz -= sz;
     }
     fix = warp_sum(fix);
     fiy = warp_sum(fiy);
     fiz = warp_sum(fiz);
     if (lane == 0) {
-        fwx[i] += fix;
-        fwy[i] += fiy;
-        fwz[i] += fiz;
+        red_shared(&fx[i], fix);
+        red_shared(&fy[i], fiy);
+        red_shared(&fz[i], fiz);
     }
     __syncwarp();
 }
@@ -1134,7 +1121,7 @@ __device__ bool nnf_bead(const Batch &B, const NNDev &M, const FastNN &F, const 
         }
     }
     if (do_forces)
-        for (int k = tid; k < kFW * 3 * L.max_atoms; k += nt) S.fw[k] = 0.f;
+        for (int k = tid; k < 3 * L.max_atoms; k += nt) S.f3[k] = 0.f;
     if (F.skin > 0.f) atomicMax(&S.misc[3], __float_as_int(d2max));  // non-negative floats order as ints
     __syncthreads();
     // skin lists are rebuilt when invalid or when some atom moved more than half the skin
@@ -1180,21 +1167,23 @@ __device__ bool nnf_bead(const Batch &B, const NNDev &M, const FastNN &F, const 
         const int *atoms = S.byel + st;
         for (int a = 0; a < n; ++a)
             nnf_descriptors<NG, ZM>(M, F, X, S, W, L, t, base, atoms[a], N, na, mscr + (size_t)atoms[a] * mstride,
-                                    rebuild);
+                                    rebuild, W.gb + a * L.sgs);
         __syncwarp();
         for (int r0 = 0; r0 < n;) {  // runs of one element
             const int e = S.elem[atoms[r0]];
             int r1 = r0 + 1;
             while (r1 < n && S.elem[atoms[r1]] == e) ++r1;
             const int m = r1 - r0;
-            const double en = m > 2 ? nnf_network<4>(M, F, S, L, hs, hv, e, atoms + r0, m, do_forces)
-                                    : nnf_network<2>(M, F, S, L, hs, hv, e, atoms + r0, m, do_forces);
+            float *gb = W.gb + r0 * L.sgs;
+            const double en = m > 2 ? nnf_network<4>(M, F, S, L, hs, hv, e, gb, m, do_forces)
+                                    : nnf_network<2>(M, F, S, L, hs, hv, e, gb, m, do_forces);
             if (lane == 0) e_warp += en + m * (M.remove_atom_energies ? M.atom_energy[e] : 0.0);
             r0 = r1;
         }
         if (do_forces)
             for (int a = 0; a < n; ++a)
-                nnf_forces<NG, ZM>(M, F, X, S, W, L, base, atoms[a], mscr + (size_t)atoms[a] * mstride);
+                nnf_forces<NG, ZM>(M, F, X, S, W, L, base, atoms[a], mscr + (size_t)atoms[a] * mstride,
+                                   W.gb + a * L.sgs);
     }
     const double etot = block_sum(e_warp, S.red);  // contains __syncthreads: flag visible
     if (F.skin > 0.f && rebuild) {
@@ -1214,14 +1203,7 @@ __device__ bool nnf_bead(const Batch &B, const NNDev &M, const FastNN &F, const 
     }
     const double c = kHa2eVF * kAng2BohrD;
     for (int i = tid; i < N; i += nt) {
-        float fx = 0.f, fy = 0.f, fz = 0.f;
-#pragma unroll
-        for (int w = 0; w < kFW; ++w) {
-            const float *f = S.fw + (size_t)w * 3 * L.max_atoms;
-            fx += f[i];
-            fy += f[L.max_atoms + i];
-            fz += f[2 * L.max_atoms + i];
-        }
+        const float fx = S.f3[i], fy = S.f3[L.max_atoms + i], fz = S.f3[2 * L.max_atoms + i];
         B.fx[base + i] += (double)fx * c;
         B.fy[base + i] += (double)fy * c;
         B.fz[base + i] += (double)fz * c;
@@ -1285,7 +1267,7 @@ __device__ void load_model_smem(const NNDev &M, const FastNN &F, const SmemF &S)
 // mode 0: forces, 1: energies only, 2: nsteps fused MD steps (propagate_1, forces,
 // propagate_2, exit test), as the generic network kernels.
 template <int NG, int ZM>
-__global__ void __launch_bounds__(kFBlock, 2)
+__global__ void __launch_bounds__(kFBlock, 3)
     nnf_kernel(Batch B, NNDev M, FastNN F, EmtConst E, NNScratch X, PropParams P, FLaunch L, const int *order,
                int *counter, int nsteps, int mode) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
