@@ -481,7 +481,7 @@ __device__ __forceinline__ void build_rows(const FastNN &F, const SmemF &S, cons
 }
 
 // ---- phase 1: neighbour list, rows, descriptors of one central atom ---------------------
-template <int NG, int ZM>
+template <int NG, int ZM, bool G3ON>
 __device__ void nnf_descriptors(const NNDev &M, const FastNN &F, const NNScratch &X, const SmemF &S,
                                 const WarpF &W, const FLaunch &L, int t, int64_t base, int i, int N, const int *na,
                                 unsigned *mglob, bool rebuild, float *G) {
@@ -614,7 +614,7 @@ __device__ void nnf_descriptors(const NNDev &M, const FastNN &F, const NNScratch
     }
 
     // ---- triplet masks and G3 ----------------------------------------------------------------
-    const bool g3 = F.hasg3[ei] != 0;
+    const bool g3 = G3ON && F.hasg3[ei] != 0;
     const int nrows = cnt - 1, npairs = (g3 && nrows > 0) ? (nrows + 1) / 2 : 0;
     if (g3 && npairs == 0) {
         for (int q = lane; q < NG * NQ; q += 32) {
@@ -877,7 +877,7 @@ __device__ double nnf_network(const NNDev &M, const FastNN &F, const SmemF &S, c
 }
 
 // ---- phase 3: forces of one central atom ---------------------------------------------
-template <int NG, int ZM>
+template <int NG, int ZM, bool G3ON>
 __device__ void nnf_forces(const NNDev &M, const FastNN &F, const NNScratch &X, const SmemF &S, const WarpF &W,
                            const FLaunch &L, int64_t base, int i, const unsigned *mglob, const float *dG) {
     constexpr int NZ = popc5(ZM), NQ = 2 * NZ;
@@ -921,7 +921,7 @@ __device__ void nnf_forces(const NNDev &M, const FastNN &F, const NNScratch &X, 
     }
 
     // ---- angular part ------------------------------------------------------------------------
-    const bool g3 = F.hasg3[ei] != 0;
+    const bool g3 = G3ON && F.hasg3[ei] != 0;
     const int nrows = cnt - 1, npairs = (g3 && nrows > 0) ? (nrows + 1) / 2 : 0;
     if (npairs > 0) {
         for (int k = lane; k < cnt * mw; k += 32) W.mask[k] = mglob[k];
@@ -1083,7 +1083,7 @@ __device__ void order_by_element(const NNDev &M, const SmemF &S, const FLaunch &
 // Warps take 2 or 4 atoms at a time: descriptors of each atom, the network of each run of
 // one element, forces of each atom; no CTA barrier between the stages.  The lattice
 // tables (S.lat, latf, ginv, wk) are set once per trajectory by cell_setup.
-template <int NG, int ZM>
+template <int NG, int ZM, bool G3ON>
 __device__ bool nnf_bead(const Batch &B, const NNDev &M, const FastNN &F, const NNScratch &X, const SmemF &S,
                          const FLaunch &L, int t, int b, bool do_forces, bool skip_if_flagged) {
     const int N = B.natoms[t];
@@ -1166,7 +1166,7 @@ __device__ bool nnf_bead(const Batch &B, const NNDev &M, const FastNN &F, const 
         if (n <= 0) break;
         const int *atoms = S.byel + st;
         for (int a = 0; a < n; ++a)
-            nnf_descriptors<NG, ZM>(M, F, X, S, W, L, t, base, atoms[a], N, na, mscr + (size_t)atoms[a] * mstride,
+            nnf_descriptors<NG, ZM, G3ON>(M, F, X, S, W, L, t, base, atoms[a], N, na, mscr + (size_t)atoms[a] * mstride,
                                     rebuild, W.gb + a * L.sgs);
         __syncwarp();
         for (int r0 = 0; r0 < n;) {  // runs of one element
@@ -1182,7 +1182,7 @@ __device__ bool nnf_bead(const Batch &B, const NNDev &M, const FastNN &F, const 
         }
         if (do_forces)
             for (int a = 0; a < n; ++a)
-                nnf_forces<NG, ZM>(M, F, X, S, W, L, base, atoms[a], mscr + (size_t)atoms[a] * mstride,
+                nnf_forces<NG, ZM, G3ON>(M, F, X, S, W, L, base, atoms[a], mscr + (size_t)atoms[a] * mstride,
                                    W.gb + a * L.sgs);
     }
     const double etot = block_sum(e_warp, S.red);  // contains __syncthreads: flag visible
@@ -1214,7 +1214,7 @@ __device__ bool nnf_bead(const Batch &B, const NNDev &M, const FastNN &F, const 
 
 // calc_force (force.f90:40-86) with the network: zero, free ring-polymer step, per-bead
 // prediction (EMT for a flagged bead of the surrogate), accelerations.
-template <int NG, int ZM>
+template <int NG, int ZM, bool G3ON>
 __device__ void nnf_calc_force(const Batch &B, const NNDev &M, const FastNN &F, const EmtConst &E,
                                const NNScratch &X, const PropParams &P, const SmemF &S, const SmemEmt<double> &SE,
                                const FLaunch &L, const TrajView &T, bool do_forces) {
@@ -1228,7 +1228,7 @@ __device__ void nnf_calc_force(const Batch &B, const NNDev &M, const FastNN &F, 
     __syncthreads();
     if (T.nb > 1) ring_polymer_step(B, P, T, S.cjk);
     for (int b = 0; b < T.nb; ++b) {
-        const bool flagged = nnf_bead<NG, ZM>(B, M, F, X, S, L, T.t, b, do_forces, L.surrogate != 0);
+        const bool flagged = nnf_bead<NG, ZM, G3ON>(B, M, F, X, S, L, T.t, b, do_forces, L.surrogate != 0);
         if (L.surrogate && flagged) {
             emt_bead<double>(B, E, SE, T.t, b, do_forces);
             if (threadIdx.x == 0) X.fallback[T.t] += 1;
@@ -1266,7 +1266,7 @@ __device__ void load_model_smem(const NNDev &M, const FastNN &F, const SmemF &S)
 
 // mode 0: forces, 1: energies only, 2: nsteps fused MD steps (propagate_1, forces,
 // propagate_2, exit test), as the generic network kernels.
-template <int NG, int ZM>
+template <int NG, int ZM, bool G3ON>
 __global__ void __launch_bounds__(kFBlock, 3)
     nnf_kernel(Batch B, NNDev M, FastNN F, EmtConst E, NNScratch X, PropParams P, FLaunch L, const int *order,
                int *counter, int nsteps, int mode) {
@@ -1291,7 +1291,7 @@ __global__ void __launch_bounds__(kFBlock, 3)
         order_by_element(M, S, L, T.N);
         cell_setup(B, M, F, S, t);
         if (mode != 2) {
-            nnf_calc_force<NG, ZM>(B, M, F, E, X, P, S, SE, L, T, mode == 0);
+            nnf_calc_force<NG, ZM, G3ON>(B, M, F, E, X, P, S, SE, L, T, mode == 0);
             continue;
         }
         const int ty0 = B.type[T.aoff];
@@ -1299,7 +1299,7 @@ __global__ void __launch_bounds__(kFBlock, 3)
             if (B.status[t] != kStatusRunning) break;
             const int step = B.steps_done[t] + 1;
             propagate_1(B, P, T, S.cjk, step, S.red);
-            nnf_calc_force<NG, ZM>(B, M, F, E, X, P, S, SE, L, T, true);
+            nnf_calc_force<NG, ZM, G3ON>(B, M, F, E, X, P, S, SE, L, T, true);
             propagate_2(B, P, T, step);
             if (threadIdx.x == 0) {
                 B.steps_done[t] = step;
@@ -1319,22 +1319,22 @@ __global__ void __launch_bounds__(kFBlock, 3)
     }
 }
 
-template <int NG, int ZM>
+template <int NG, int ZM, bool G3ON>
 cudaError_t nnf_launch_t(const LaunchCfg &c, const Batch &B, const NNDev &M, const FastNN &F, const EmtConst &E,
                          const NNScratch &X, const PropParams &P, const FLaunch &L, size_t sm, int nsteps, int mode) {
     cudaError_t e = cudaMemsetAsync(c.counter, 0, sizeof(int), c.stream);
     if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(nnf_kernel<NG, ZM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    e = cudaFuncSetAttribute(nnf_kernel<NG, ZM, G3ON>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
-    nnf_kernel<NG, ZM><<<c.grid, kFBlock, sm, c.stream>>>(B, M, F, E, X, P, L, c.order, c.counter, nsteps, mode);
+    nnf_kernel<NG, ZM, G3ON><<<c.grid, kFBlock, sm, c.stream>>>(B, M, F, E, X, P, L, c.order, c.counter, nsteps, mode);
     return cudaGetLastError();
 }
 
-template <int NG, int ZM>
+template <int NG, int ZM, bool G3ON>
 int nnf_occupancy_t(size_t sm) {
     int n = 0;
-    cudaFuncSetAttribute(nnf_kernel<NG, ZM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, nnf_kernel<NG, ZM>, kFBlock, sm);
+    cudaFuncSetAttribute(nnf_kernel<NG, ZM, G3ON>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, nnf_kernel<NG, ZM, G3ON>, kFBlock, sm);
     return n;
 }
 
@@ -1344,10 +1344,15 @@ int nnf_occupancy_t(size_t sm) {
 // 1..4 eta slots.
 int nnf_zm_supported(int zm) { return (zm & ~0x15) == 0 ? 0x15 : 0; }
 
-#define MDT_NNF_DISPATCH(CALL)                                               \
-    switch (F.ng) {                                                          \
-        case 1: CALL(1, 0x15); case 2: CALL(2, 0x15); case 3: CALL(3, 0x15); \
-        case 4: CALL(4, 0x15); default: break;                               \
+// radial-only models (no G3 anywhere) get a kernel without the angular stages
+#define MDT_NNF_DISPATCH(CALL)                                                                       \
+    if (!F.anyg3) {                                                                                  \
+        CALL(1, 0x15, false);                                                                        \
+    } else {                                                                                         \
+        switch (F.ng) {                                                                              \
+            case 1: CALL(1, 0x15, true); case 2: CALL(2, 0x15, true); case 3: CALL(3, 0x15, true);   \
+            case 4: CALL(4, 0x15, true); default: break;                                             \
+        }                                                                                            \
     }
 
 size_t nnf_total_smem(const Batch &B, const NNDev &M, const FastNN &F) { return nnf_smem_total(B, M, F); }
@@ -1356,7 +1361,7 @@ int nnf_warps_per_cta() { return kFW; }
 
 int nnf_resident_ctas(const Batch &B, const NNDev &M, const FastNN &F) {
     const size_t sm = nnf_smem_total(B, M, F);
-#define MDT_OCC(NG, ZM) return std::max(1, nnf_occupancy_t<NG, ZM>(sm));
+#define MDT_OCC(NG, ZM, G3ON) return std::max(1, nnf_occupancy_t<NG, ZM, G3ON>(sm));
     MDT_NNF_DISPATCH(MDT_OCC)
 #undef MDT_OCC
     return 1;
@@ -1366,7 +1371,7 @@ cudaError_t launch_nnf(const LaunchCfg &c, const Batch &B, const NNDev &M, const
                        const NNScratch &X, const PropParams &P, int nsteps, int mode, bool surrogate) {
     const FLaunch L = flaunch(B, M, surrogate ? 1 : 0);
     const size_t sm = nnf_smem_total(B, M, F);
-#define MDT_LAUNCH(NG, ZM) return nnf_launch_t<NG, ZM>(c, B, M, F, E, X, P, L, sm, nsteps, mode);
+#define MDT_LAUNCH(NG, ZM, G3ON) return nnf_launch_t<NG, ZM, G3ON>(c, B, M, F, E, X, P, L, sm, nsteps, mode);
     MDT_NNF_DISPATCH(MDT_LAUNCH)
 #undef MDT_LAUNCH
     return cudaErrorInvalidValue;
