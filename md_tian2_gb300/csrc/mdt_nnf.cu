@@ -1175,8 +1175,7 @@ __device__ bool nnf_bead(const Batch &B, const NNDev &M, const FastNN &F, const 
             while (r1 < n && S.elem[atoms[r1]] == e) ++r1;
             const int m = r1 - r0;
             float *gb = W.gb + r0 * L.sgs;
-            const double en = m > 2 ? nnf_network<4>(M, F, S, L, hs, hv, e, gb, m, do_forces)
-                                    : nnf_network<2>(M, F, S, L, hs, hv, e, gb, m, do_forces);
+            const double en = nnf_network<4>(M, F, S, L, hs, hv, e, gb, m, do_forces);
             if (lane == 0) e_warp += en + m * (M.remove_atom_energies ? M.atom_energy[e] : 0.0);
             r0 = r1;
         }
