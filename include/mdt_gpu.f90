@@ -132,6 +132,12 @@ module mdt_gpu
             integer(c_int32_t), value :: enable
         end function
 
+        integer(c_int32_t) function mdt_nn_radial_kernel(ctx, enable) bind(C, name="mdt_nn_radial_kernel")
+            import :: c_int32_t, c_ptr
+            type(c_ptr), value :: ctx
+            integer(c_int32_t), value :: enable
+        end function
+
         integer(c_int32_t) function mdt_nn_set_skin(ctx, skin_ang) bind(C, name="mdt_nn_set_skin")
             import :: c_int32_t, c_ptr, c_double
             type(c_ptr), value :: ctx

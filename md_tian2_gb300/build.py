@@ -18,7 +18,7 @@ CSRC = PKG / "csrc"
 OUT_DIR = PKG / "_build"
 LIB = PKG / "libmdt_gpu.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["mdt_api.cu", "mdt_md.cu", "mdt_peak.cu", "mdt_nn.cu", "mdt_noalloc.cu", "mdt_train.cu", "mdt_nnf.cu"]
+SOURCES = ["mdt_api.cu", "mdt_md.cu", "mdt_peak.cu", "mdt_nn.cu", "mdt_noalloc.cu", "mdt_train.cu", "mdt_nnf.cu", "mdt_nnr.cu"]
 
 
 def nvcc() -> str:

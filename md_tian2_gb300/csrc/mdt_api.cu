@@ -71,6 +71,13 @@ struct mdt_ctx {
     int skcap = 0;
     double skin_ang = 1.0;
     bool skin_dirty = true;
+    int sk_layout = -1;        // 0: warp-per-atom lists, 1: thread-per-atom lists (entry-major)
+    // thread-per-atom kernel of radial-only models (mdt_nnr.cu): tables, switch, pack plan
+    RadialNN R{};
+    bool radial_enabled = true;
+    int2 *rpacks = nullptr;    // (offset into rptraj, count) per pack
+    int *rptraj = nullptr;     // trajectories of the packs
+    int rnpack = 0, rblock = 0;
 
     // training (buffers live with the batch)
     bool have_labels = false;
@@ -108,6 +115,10 @@ void free_batch(mdt_ctx *c) {
     c->skref = nullptr;
     c->skcap = 0;
     c->skin_dirty = true;
+    c->sk_layout = -1;
+    c->rpacks = nullptr;
+    c->rptraj = nullptr;
+    c->rnpack = c->rblock = 0;
     c->have_labels = false;
     c->nn_maxnb_alloc = 0;
     for (auto &b : c->bufs) cudaFree(b.p);
@@ -398,6 +409,92 @@ FastNN build_fast(const NNDev &M, const mdt_nn_model *m, const std::vector<int> 
     return F;
 }
 
+// RadialNN tables of a model (RadialNN::ok = 0 when it does not qualify; see mdt_nn.cuh).
+RadialNN build_radial(const NNDev &M, const mdt_nn_model *m, const FastNN &F, const std::vector<int> &e1) {
+    RadialNN R{};
+    R.ok = 0;
+    if (!F.ok || F.anyg3 || M.nelem > 2 || (M.nlayers != 2 && M.nlayers != 3)) return R;
+    const int ne = M.nelem, ms = M.maxsf, nh = M.nlayers - 1;
+    for (int e = 0; e < ne; ++e) {
+        for (int l = 1; l <= nh; ++l)
+            if (M.nodes[e][l] > 32) return R;
+        if (M.nodes[e][M.nlayers] != 1) return R;
+        if (M.normnodes)
+            for (int l = 0; l <= M.nlayers; ++l)
+                if (M.nodes[e][l] != M.nodes[0][l]) return R;
+    }
+    // one activation per layer over nodes and elements, of the kinds the kernel has
+    for (int l = 0; l < M.nlayers; ++l) {
+        const uint8_t a = m->act[((size_t)0 * m->nlayers + l) * m->maxnodes];
+        if (!std::strchr("ptsl", (int)a) || a == 0) return R;
+        for (int e = 0; e < ne; ++e)
+            for (int n = 0; n < M.nodes[e][l + 1]; ++n)
+                if (m->act[((size_t)e * m->nlayers + l) * m->maxnodes + n] != a) return R;
+        R.act[l] = a;
+        R.rn[l] = M.normnodes ? (float)(1.0 / M.nodes[0][l]) : 1.f;
+    }
+    // (eta, r_s) list per neighbour element, identical for every centre element
+    std::vector<int> idx[kMaxElem][2];
+    for (int e = 0; e < ne; ++e)
+        for (int g = 0; g < 2; ++g) {
+            for (int s = 0; s < M.nsf[e]; ++s)
+                if (m->sftype[e * ms + s] == 2 && e1[e * ms + s] == g) idx[e][g].push_back(s);
+            std::stable_sort(idx[e][g].begin(), idx[e][g].end(), [&](int x, int y) {
+                const double ex = m->eta[e * ms + x], ey = m->eta[e * ms + y];
+                return ex != ey ? ex < ey : m->rshift[e * ms + x] < m->rshift[e * ms + y];
+            });
+        }
+    for (int e = 0; e < ne; ++e) {
+        int n2 = 0;
+        for (int s = 0; s < M.nsf[e]; ++s) n2 += m->sftype[e * ms + s] == 2 && (e1[e * ms + s] == 0 || e1[e * ms + s] == 1);
+        if (n2 != M.nsf[e]) return R;  // every function over an element of the model
+        for (int g = 0; g < 2; ++g) {
+            if (idx[e][g].size() != idx[0][g].size() || idx[e][g].size() > (size_t)kRMaxK) return R;
+            for (size_t k = 0; k < idx[e][g].size(); ++k) {
+                const int a = e * ms + idx[e][g][k], b = idx[0][g][k];
+                if (m->eta[a] != m->eta[b] || m->rshift[a] != m->rshift[b]) return R;
+            }
+        }
+    }
+    const int cnt0 = (int)idx[0][0].size(), cnt1 = (int)idx[0][1].size();
+    int ka, kb;
+    if (!nnr_shape(cnt0, cnt1, nh, ka, kb)) return R;
+    R.ka = ka;
+    R.kb = kb;
+    R.nh = nh;
+    R.nelem = ne;
+    R.nin = ka + kb;
+    const double log2e = 1.4426950408889634;
+    for (int g = 0; g < 2; ++g)
+        for (int k = 0; k < kRMaxK; ++k) {
+            const bool on = k < (int)idx[0][g].size();
+            R.c[g][k] = on ? (float)(-m->eta[idx[0][g][k]] * log2e) : 0.f;
+            R.rs[g][k] = on ? (float)m->rshift[idx[0][g][k]] : 0.f;
+        }
+    for (int e = 0; e < 2; ++e)
+        for (int q = 0; q < 2 * kRMaxK; ++q) R.qsrc[e][q] = -1;
+    for (int e = 0; e < ne; ++e) {
+        for (int k = 0; k < cnt0; ++k) R.qsrc[e][k] = (int8_t)idx[e][0][k];
+        for (int k = 0; k < cnt1; ++k) R.qsrc[e][ka + k] = (int8_t)idx[e][1][k];
+    }
+    const double rc = M.maxcut;
+    R.rc2 = (float)(rc * rc);
+    R.inv_rc2 = (float)(1.0 / (rc * rc));
+    R.rc_b = (float)rc;
+    R.maxnb = M.maxnb;
+    for (int t = 0; t < kMaxTypes; ++t) R.elem_of_type[t] = M.elem_of_type[t];
+    for (int e = 0; e < 2; ++e) R.atom_energy[e] = e < ne ? M.atom_energy[e] : 0.0;
+    R.maxweights = M.maxweights;
+    R.maxsf = M.maxsf;
+    for (int e = 0; e < 2; ++e)
+        for (int l = 0; l <= kMaxLayers; ++l) {
+            R.woff[e][l] = e < ne && l <= M.nlayers ? M.woff[e][l] : 0;
+            R.nodes[e][l] = e < ne && l <= M.nlayers ? M.nodes[e][l] : 0;
+        }
+    R.ok = 1;
+    return R;
+}
+
 bool use_fast(mdt_ctx *c, int precision) {
     if (precision != MDT_PREC_FP32 || !c->F.ok || !c->fast_enabled) return false;
     int dev = 0, optin = 0;
@@ -412,9 +509,132 @@ LaunchCfg nnf_cfg(mdt_ctx *c) {
     return LaunchCfg{c->stream, grid, c->order, c->counter};
 }
 
+int ensure_mscr(mdt_ctx *c, int grid, int layout);
+
+// Pack plan of the thread-per-atom kernel for the batch.  A pack is a set of whole
+// trajectories run by one CTA (thread = atom).  For w waves of the resident CTAs the
+// trajectories are dealt largest first to the pack with the fewest atoms (at most
+// kRMaxTraj per pack); the block is the largest pack rounded up to a warp, and the plan
+// with the smallest w * block (CTA time is set by the fullest pack of a wave) wins.
+bool radial_plan(mdt_ctx *c) {
+    if (c->rnpack > 0) return true;
+    if (c->max_beads != 1 || c->max_atoms > kRBlockMax) return false;
+    for (int t = 0; t < c->ntypes; ++t)
+        if (c->R.elem_of_type[t] < 0) return false;
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (nnr_smem(c->R) > (size_t)optin ||
+        nnr_emt_smem(c->max_atoms) > 4 * (size_t)nnr_hbw(c->R.nin, c->R.nh) * kRBlockMax)
+        return false;
+    c->R.block = kRBlockMax;
+    const int slots = c->num_sms * std::max(1, nnr_resident_ctas(c->R));
+    std::vector<int> order(c->T);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return c->natoms[a] > c->natoms[b]; });
+    const int64_t total = c->total_atoms;
+    const int w0 = (int)std::max<int64_t>(1, (total + (int64_t)slots * kRBlockMax - 1) / ((int64_t)slots * kRBlockMax));
+    int64_t best = -1;
+    std::vector<std::vector<int>> bestp;
+    int bestb = 0;
+    for (int w = w0; w <= w0 + 4; ++w) {
+        const int np = std::min<int64_t>((int64_t)w * slots, c->T);
+        std::vector<std::vector<int>> packs(np);
+        std::vector<int> load(np, 0);
+        // min-heap of (atoms, pack) over packs that still take trajectories
+        std::vector<std::pair<int, int>> heap;
+        for (int k = 0; k < np; ++k) heap.emplace_back(0, k);
+        auto cmp = [](const std::pair<int, int> &a, const std::pair<int, int> &b) { return a > b; };
+        std::make_heap(heap.begin(), heap.end(), cmp);
+        bool ok = true;
+        for (int t : order) {
+            if (heap.empty()) {
+                ok = false;
+                break;
+            }
+            std::pop_heap(heap.begin(), heap.end(), cmp);
+            const int k = heap.back().second;
+            heap.pop_back();
+            packs[k].push_back(t);
+            load[k] += c->natoms[t];
+            if ((int)packs[k].size() < kRMaxTraj) {
+                heap.emplace_back(load[k], k);
+                std::push_heap(heap.begin(), heap.end(), cmp);
+            }
+        }
+        if (!ok) continue;
+        const int mx = *std::max_element(load.begin(), load.end());
+        const int block = (mx + 31) & ~31;
+        if (block > kRBlockMax) continue;
+        const int64_t cost = (int64_t)((np + slots - 1) / slots) * block;
+        if (best < 0 || cost < best) {
+            best = cost;
+            bestp = std::move(packs);
+            bestb = block;
+        }
+    }
+    if (bestp.empty()) return false;
+    // packs largest first (the work queue hands them out in order)
+    std::stable_sort(bestp.begin(), bestp.end(), [&](const std::vector<int> &a, const std::vector<int> &b) {
+        int la = 0, lb = 0;
+        for (int t : a) la += c->natoms[t];
+        for (int t : b) lb += c->natoms[t];
+        return la > lb;
+    });
+    std::vector<int2> hp;
+    std::vector<int> ht;
+    for (auto &p : bestp) {
+        if (p.empty()) continue;
+        std::sort(p.begin(), p.end());
+        hp.push_back(make_int2((int)ht.size(), (int)p.size()));
+        ht.insert(ht.end(), p.begin(), p.end());
+    }
+    cudaError_t e = cudaSuccess;
+    int2 *d = dalloc<int2>(c, hp.size(), e);
+    int *dt = dalloc<int>(c, ht.size(), e);
+    if (!d || !dt) return false;
+    if (cudaMemcpy(d, hp.data(), sizeof(int2) * hp.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(dt, ht.data(), sizeof(int) * ht.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+        return false;
+    c->rpacks = d;
+    c->rptraj = dt;
+    c->rnpack = (int)hp.size();
+    c->rblock = bestb;
+    return true;
+}
+
+// The thread-per-atom kernel runs FP32 forces of an admitted model; the fused MD step also
+// needs single-bead trajectories with Verlet or constant-friction Langevin propagators.
+bool use_radial(mdt_ctx *c, int precision, bool md) {
+    if (precision != MDT_PREC_FP32 || !c->R.ok || !c->radial_enabled || !c->fast_enabled) return false;
+    if (md)
+        for (int t = 0; t < c->ntypes; ++t)
+            if (c->B.algo[t] != kPropVerlet && c->B.algo[t] != kPropLangevinConst) return false;
+    return radial_plan(c);
+}
+
+int run_radial(mdt_ctx *c, const PropParams &P, int nsteps, int mode, bool surr) {
+    RadialNN &R = c->R;
+    R.block = c->rblock;
+    const int per_sm = std::max(1, nnr_resident_ctas(R));
+    const int grid = std::max(1, std::min(c->rnpack, c->num_sms * per_sm));
+    int rc = ensure_mscr(c, grid, 1);
+    if (rc) return rc;
+    R.skin = c->F.skin;
+    R.cut2s = c->F.cut2s;
+    R.rcs = (float)(c->M.maxcut + c->skin_ang / kBohr2Ang);
+    R.surrogate = surr ? 1 : 0;
+    R.fscal = c->F.scal;
+    R.fdscal = c->F.dscal;
+    const cudaError_t e = launch_nnr(LaunchCfg{c->stream, grid, c->order, c->counter}, c->B, R, c->E, c->X, P,
+                                     c->rpacks, c->rptraj, c->rnpack, nsteps, mode);
+    c->launches++;
+    return e == cudaSuccess ? MDT_OK : cuda_fail(c, e, "network kernel (thread per atom)");
+}
+
 // mask scratch of the fast path: the triplet masks of one bead per CTA (maxnb rows of
 // mw words per atom), written by the descriptor phase and read by the force phase
-int ensure_mscr(mdt_ctx *c, int grid) {
+int ensure_mscr(mdt_ctx *c, int grid, int layout) {
     const int mw = (c->M.maxnb + 31) / 32;
     const size_t per = c->F.anyg3 ? (size_t)c->max_atoms * c->M.maxnb * mw : 4;
     const size_t n = (size_t)grid * per;
@@ -440,10 +660,11 @@ int ensure_mscr(mdt_ctx *c, int grid) {
         c->skcap = skcap;
         c->skin_dirty = true;
     }
-    if (c->skin_dirty) {
+    if (c->skin_dirty || c->sk_layout != layout) {
         e = cudaMemsetAsync(c->skok, 0, sizeof(int) * c->total_beads, c->stream);
         if (e != cudaSuccess) return cuda_fail(c, e, "skin-list reset");
         c->skin_dirty = false;
+        c->sk_layout = layout;
     }
     c->X.skw = c->skw;
     c->X.skcnt = c->skcnt;
@@ -895,9 +1116,10 @@ int32_t mdt_calc_force(mdt_ctx *c, int32_t flag, int32_t precision, const mdt_pr
         if (c->pes_kind == MDT_PES_SURROGATE && (rc = ensure_scratch(c, MDT_PREC_FP64))) return rc;
         const PropParams P = to_dev(c, p);
         const bool surr = c->pes_kind == MDT_PES_SURROGATE;
+        if (use_radial(c, precision, false)) return run_radial(c, P, 0, flag == MDT_ENERGY_ONLY ? 1 : 0, surr);
         const bool fast = use_fast(c, precision);
         const LaunchCfg fcfg = fast ? nnf_cfg(c) : LaunchCfg{};
-        if (fast && (rc = ensure_mscr(c, fcfg.grid))) return rc;
+        if (fast && (rc = ensure_mscr(c, fcfg.grid, 0))) return rc;
         cudaError_t e = fast
                             ? launch_nnf(fcfg, c->B, c->M, c->F, c->E, c->X, P, 0,
                                          flag == MDT_ENERGY_ONLY ? 1 : 0, surr)
@@ -947,9 +1169,10 @@ int32_t mdt_md_steps(mdt_ctx *c, int32_t nsteps, int32_t precision, const mdt_pr
         if (nsteps == 0) return MDT_OK;
         const PropParams P = to_dev(c, p);
         const bool surr = c->pes_kind == MDT_PES_SURROGATE;
+        if (use_radial(c, precision, true)) return run_radial(c, P, nsteps, 2, surr);
         const bool fast = use_fast(c, precision);
         const LaunchCfg fcfg = fast ? nnf_cfg(c) : LaunchCfg{};
-        if (fast && (rc = ensure_mscr(c, fcfg.grid))) return rc;
+        if (fast && (rc = ensure_mscr(c, fcfg.grid, 0))) return rc;
         cudaError_t e = fast
                             ? launch_nnf(fcfg, c->B, c->M, c->F, c->E, c->X, P, nsteps, 2, surr)
                             : launch_nn(nn_cfg(c, precision), c->B, c->M, c->E, c->X, P, c->ngeta_max, nsteps, 2,
@@ -1173,6 +1396,11 @@ int32_t mdt_nn_set_model(mdt_ctx *c, const mdt_nn_model *m, int32_t ntypes, cons
     }
     if (e != cudaSuccess) return cuda_fail(c, e, "mdt_nn_set_model upload");
     c->F = F;
+    c->R = build_radial(M, m, F, e1);
+    c->R.wf = M.wf;
+    c->R.fscal = F.scal;
+    c->R.fdscal = F.dscal;
+    c->rnpack = c->rblock = 0;
     c->d_scal = (float4 *)F.scal;
     c->d_dscal = (float *)F.dscal;
     c->h_smin.assign(m->smin, m->smin + nk);
@@ -1204,6 +1432,12 @@ int32_t mdt_nn_set_skin(mdt_ctx *c, double skin_ang) {
     c->skin_ang = skin_ang;
     c->skin_dirty = true;
     return MDT_OK;
+}
+
+int32_t mdt_nn_radial_kernel(mdt_ctx *c, int32_t enable) {
+    if (!c) return MDT_ERR_ARG;
+    c->radial_enabled = enable != 0;
+    return c->have_nn && c->R.ok ? 1 : 0;
 }
 
 int32_t mdt_nn_fast_path(mdt_ctx *c, int32_t enable) {

@@ -39,6 +39,14 @@ int nnf_resident_ctas(const Batch &B, const NNDev &M, const FastNN &F);
 cudaError_t launch_nnf(const LaunchCfg &c, const Batch &B, const NNDev &M, const FastNN &F, const EmtConst &E,
                        const NNScratch &X, const PropParams &P, int nsteps, int mode, bool surrogate);
 
+// FP32 thread-per-atom kernel of radial-only models (mdt_nnr.cu)
+bool nnr_shape(int cnt0, int cnt1, int nh, int &ka, int &kb);
+size_t nnr_smem(const RadialNN &R);
+size_t nnr_emt_smem(int max_atoms);  // EMT fallback area (aliases the network buffers)
+int nnr_resident_ctas(const RadialNN &R);
+cudaError_t launch_nnr(const LaunchCfg &c, const Batch &B, const RadialNN &R, const EmtConst &E, const NNScratch &X,
+                       const PropParams &P, const int2 *packs, const int *ptraj, int npack, int nsteps, int mode);
+
 struct TrainArgs {
     const double *E_ref;
     const double *fx_ref, *fy_ref, *fz_ref;

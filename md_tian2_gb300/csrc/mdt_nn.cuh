@@ -94,6 +94,56 @@ struct FastNN {
 };
 
 // ---------------------------------------------------------------------------
+// FP32 thread-per-atom kernel of radial-only models (mdt_nnr.cu).  Applies when every
+// symmetry function is a G2 under one cosine cutoff, there are at most two elements,
+// every centre element has the same (eta, r_s) list per neighbour element, and the
+// network has one or two hidden layers of at most 32 nodes with one activation per
+// layer.  Descriptors live in a padded grouped order: slots [0, ka) are the functions
+// over neighbour element 0, [ka, ka + kb) those over element 1.
+// ---------------------------------------------------------------------------
+constexpr int kRBlockMax = 512;  // threads per CTA (atoms of a pack)
+constexpr int kRMaxTraj = 32;    // trajectories per pack
+constexpr int kRMaxK = 24;       // functions per neighbour element
+
+// Shared-memory layout constants of a shape (nin = functions per atom, nh = hidden
+// layers): weight block of one element (W1 + b1, then W2, b2, W2T, w3, b3 + 3 pad or
+// w2, b2 + 3 pad), offset of element 1's block (64 bytes off the 128-byte grid), both
+// blocks, per-thread buffer floats (two hidden layers: layer-1 values and delta2 side by
+// side).
+__host__ __device__ constexpr int nnr_wblock(int nin, int nh) {
+    return 32 * (nin + 1) + (nh == 2 ? 2 * 32 * 32 + 2 * 32 + 4 : 32 + 4);
+}
+__host__ __device__ constexpr int nnr_wofs1(int nin, int nh) { return ((nnr_wblock(nin, nh) + 31) & ~31) + 16; }
+__host__ __device__ constexpr int nnr_wtotal(int nin, int nh) { return nnr_wofs1(nin, nh) + nnr_wblock(nin, nh); }
+__host__ __device__ constexpr int nnr_hbw(int nin, int nh) {
+    return nin > (nh == 2 ? 64 : 32) ? nin : (nh == 2 ? 64 : 32);
+}
+
+struct RadialNN {
+    int ok;
+    int ka, kb, nh;                 // kernel shape: padded functions per group, hidden layers
+    int nelem, nin;                 // elements, ka + kb
+    int block;                      // threads per CTA (batch plan)
+    int surrogate, maxnb;
+    int elem_of_type[kMaxTypes];
+    float rc2, inv_rc2, rc_b, rcs;  // cutoff^2, 1/cutoff^2, cutoff, skin-list cutoff (bohr)
+    float skin, cut2s;              // Verlet skin (bohr, 0: off), skin-list cutoff^2 (bohr^2)
+    float c[2][kRMaxK];             // -eta log2(e) (bohr^-2); 0 on padded slots
+    float rs[2][kRMaxK];            // r_s (bohr)
+    uint8_t act[3];                 // activation of hidden layers 1..nh, then of the output
+    float rn[3];                    // 1/n_(l-1) per layer with normnodes, else 1
+    double atom_energy[2];          // Ha (0 unless remove_atom_energies)
+    // weight blocks in shared memory (nnr_wblock layout), built from the model's FP32
+    // weights at kernel start
+    const float *wf;                // model weights (NNDev::wf layout)
+    int maxweights, woff[2][kMaxLayers + 1], nodes[2][kMaxLayers + 1];
+    int8_t qsrc[2][2 * kRMaxK];     // model descriptor index of padded slot q (-1: none)
+    const float4 *fscal;            // FastNN::scal / dscal (model order), permuted at kernel start
+    const float *fdscal;
+    int maxsf;
+};
+
+// ---------------------------------------------------------------------------
 // Host-visible launch parameters of the NN kernels
 // ---------------------------------------------------------------------------
 struct NNScratch {

@@ -43,6 +43,7 @@
 
 #include "mdt_common.cuh"
 #include "mdt_emt.cuh"
+#include "mdt_fastmath.cuh"
 #include "mdt_internal.h"
 #include "mdt_nn.cuh"
 #include "mdt_acsf.cuh"
@@ -55,45 +56,6 @@ namespace {
 constexpr int kFW = 8;
 constexpr int kFBlock = 32 * kFW;
 constexpr double kHa2eVF = 27.21138602;
-
-// Cosine cutoff fc = (cos(pi r/rc) + 1)/2 = c^2 with c = cos(pi sqrt(s)/2), s = r^2/rc^2.
-// c is the Taylor series sum_n (-pi^2 s/4)^n / (2n)! truncated after n = 7 (remainder
-// below 1e-10 on [0, 1], alternating terms no larger than 1.24, so FP32 Horner loses
-// little), and fc = c^2 keeps the absolute error vanishing at the cutoff.
-constexpr double half_cos_sqrt_coef(int n) {
-    double c = 1.0;
-    for (int k = 1; k <= n; ++k) c *= -(kPi * kPi / 4.0) / ((2.0 * k - 1.0) * (2.0 * k));
-    return c;
-}
-constexpr float kCs0 = (float)half_cos_sqrt_coef(0), kCs1 = (float)half_cos_sqrt_coef(1),
-                kCs2 = (float)half_cos_sqrt_coef(2), kCs3 = (float)half_cos_sqrt_coef(3),
-                kCs4 = (float)half_cos_sqrt_coef(4), kCs5 = (float)half_cos_sqrt_coef(5),
-                kCs6 = (float)half_cos_sqrt_coef(6), kCs7 = (float)half_cos_sqrt_coef(7);
-
-// fc(s)
-__device__ __forceinline__ float fc_of_s(float s) {
-    float c = kCs7;
-    c = fmaf(c, s, kCs6);
-    c = fmaf(c, s, kCs5);
-    c = fmaf(c, s, kCs4);
-    c = fmaf(c, s, kCs3);
-    c = fmaf(c, s, kCs2);
-    c = fmaf(c, s, kCs1);
-    c = fmaf(c, s, kCs0);
-    return c * c;
-}
-
-// fc(s) and dfc/ds = 2 c c'(s) (Horner with derivative)
-__device__ __forceinline__ void fc_of_s_d(float s, float &fc, float &dfds) {
-    float c = kCs7, d = 0.f;
-#define MDT_STEP(k)        \
-    d = fmaf(d, s, c);     \
-    c = fmaf(c, s, k);
-    MDT_STEP(kCs6) MDT_STEP(kCs5) MDT_STEP(kCs4) MDT_STEP(kCs3) MDT_STEP(kCs2) MDT_STEP(kCs1) MDT_STEP(kCs0)
-#undef MDT_STEP
-    fc = c * c;
-    dfds = 2.f * c * d;
-}
 
 // Activations in FP32.  Softplus in the form that cannot overflow (identical to
 // log(exp(x) + 1) and (exp(v) - 1)/exp(v) of calconenn.f90 / getdnodes_values.f90 to
@@ -302,11 +264,6 @@ __device__ __forceinline__ void reduce_scatter(float (&v)[NV]) {
     }
 }
 
-__device__ __forceinline__ void red_shared(float *p, float v) {
-    const unsigned a = (unsigned)__cvta_generic_to_shared(p);
-    asm volatile("red.shared.add.f32 [%0], %1;" ::"r"(a), "f"(v) : "memory");
-}
-
 // exact FP64 cutoff test of one image (the oracle's operation order, no fused operations)
 __device__ __forceinline__ bool exact_in_cutoff(const SmemF &S, int i, int j, int n1, int n2, int n3, double cut2) {
     const double *L = S.lat;
@@ -438,14 +395,6 @@ struct RowBits {
         q4 = (w << 5) + b;
     }
 };
-
-// 2^x for x <= 0 (hardware approximation, relative error about 2^-22; results below the
-// FP32 normal range flush to zero, far below any radial function that matters)
-__device__ __forceinline__ float ex2a(float x) {
-    float y;
-    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-    return y;
-}
 
 // Neighbour rows of atom i from its packed words (global scratch), elements codes.
 template <int NG>

@@ -1,0 +1,825 @@
+// mdt_nnr.cu -- FP32 thread-per-atom force evaluation and MD step for radial-only HDNNP /
+// EMT-surrogate models (every symmetry function a G2 shifted Gaussian under one cosine
+// cutoff, at most two elements, one or two hidden layers of at most 32 nodes).
+//
+// Same prediction as the generic and warp-per-atom kernels (RuNNer's short-range
+// network, src/pes_nene_mod.f90:7145-7368 with RuNNer_src/atomsymfunction2.f90 and
+// calconenn.f90 / getdnodes_values.f90 / getshortatomic.f90), organised so that a
+// thread owns one atom from its neighbour list to its force:
+//
+//  * CTA = a pack of whole trajectories (host-planned, atoms of all of them <= block):
+//    thread k is atom k of the pack; positions, forces and per-thread network buffers
+//    in shared memory; CTA barriers only around the propagator half-steps and the
+//    per-trajectory reductions.
+//  * Verlet skin lists per bead-atom, entry-major per bead (entry e of atom i at
+//    e*N + i, so a warp's loads coalesce), entries grouped by neighbour element, each
+//    (j, image in the unwrapped frame): distances come from unwrapped positions, so the
+//    lists survive wrapping.  Rebuilt when some atom of the trajectory moved more than
+//    half the skin.
+//  * Radial functions: every centre element carries the same (eta, r_s) list per
+//    neighbour element (the admission test), so the Gaussian loop is uniform across
+//    lanes and its parameters are constant-bank operands; descriptors accumulate in
+//    registers (template group sizes KA, KB).
+//  * Network: lane = atom; the weights of both elements sit in shared memory (element 1
+//    shifted by 64 bytes so a warp with both elements reads two rows in one pass), rows
+//    broadcast with 128-bit loads against 32 register accumulators; hidden layers padded
+//    to 32 nodes with zero weights (exact).  The backward pass keeps the activation
+//    derivatives of the forward pass, so dE/dG costs three matrix-vector products.
+//  * Forces: reverse mode; the neighbour's share by a shared-memory reduction, the
+//    centre's in registers.
+//  * A trajectory whose descriptors leave the training range is recomputed by FP64 EMT
+//    (surrogate) with the whole CTA, before the second propagator half-step.
+#include <cstdio>
+
+#include "mdt_common.cuh"
+#include "mdt_emt.cuh"
+#include "mdt_fastmath.cuh"
+#include "mdt_internal.h"
+#include "mdt_nn.cuh"
+#include "mdt_acsf.cuh"
+#include "mdt_prop.cuh"
+
+namespace mdt {
+
+namespace {
+
+constexpr int kRW = 32;          // padded hidden width
+constexpr double kHa2eVR = 27.21138602;
+
+struct SmemR {
+    float *xh, *yh, *zh, *xl, *yl, *zl;  // [slot] unwrapped positions (bohr), FP32 hi/lo split
+    float *f3;                           // [3][bs] neighbour force accumulators (Ha/bohr)
+    double *ea;                          // [slot] atomic energies (Ha)
+    int8_t *elem;                        // [slot]
+    float *hb;                           // [hbw][bs] per-thread network buffer
+    float *w;                            // weight blocks of the elements
+    float4 *scal;                        // [e][q]: scaled = x g + y, range [z, w]
+    float *dscal;                        // [e][q]
+    int *tr_t, *tr_st, *tr_n, *tr_flag, *tr_rebuild, *tr_d2, *tr_over;
+    float *tr_lat;                       // [s][24]: lattice rows (9), inverse rows (9), skin half-widths (3)
+    double *red;
+    int *misc;                           // [0] pack, [1] trajectories, [2] running trajectories
+    unsigned char *emt;                  // EMT fallback area (aliases hb)
+};
+
+__host__ __device__ constexpr size_t r16r(size_t b) { return (b + 15) & ~size_t(15); }
+
+// Shared memory of a CTA, laid out for kRS threads whatever the block (every offset a
+// compile-time constant of the shape, so no shared-memory address occupies a register)
+constexpr int kRS = kRBlockMax;
+
+__host__ __device__ constexpr size_t smem_r(int nin, int nh) {
+    return 6 * r16r(4 * (size_t)kRS) + r16r(12 * (size_t)kRS) + r16r(8 * (size_t)kRS) + r16r(kRS) +
+           r16r(4 * (size_t)nnr_hbw(nin, nh) * kRS) + r16r(4 * (size_t)nnr_wtotal(nin, nh)) + r16r(16 * 2 * (size_t)nin) +
+           r16r(4 * 2 * (size_t)nin) + 7 * r16r(4 * kRMaxTraj) + r16r(4 * 24 * kRMaxTraj) + r16r(8 * 64) + r16r(16);
+}
+
+template <int NIN, int NH>
+__device__ __forceinline__ SmemR carve_r(unsigned char *base) {
+    SmemR s;
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        unsigned char *p = base + off;
+        off += r16r(bytes);
+        return p;
+    };
+    s.xh = (float *)take(4 * (size_t)kRS);
+    s.yh = (float *)take(4 * (size_t)kRS);
+    s.zh = (float *)take(4 * (size_t)kRS);
+    s.xl = (float *)take(4 * (size_t)kRS);
+    s.yl = (float *)take(4 * (size_t)kRS);
+    s.zl = (float *)take(4 * (size_t)kRS);
+    s.f3 = (float *)take(12 * (size_t)kRS);
+    s.ea = (double *)take(8 * (size_t)kRS);
+    s.elem = (int8_t *)take(kRS);
+    s.hb = (float *)take(4 * (size_t)nnr_hbw(NIN, NH) * kRS);
+    s.emt = (unsigned char *)s.hb;
+    s.w = (float *)take(4 * (size_t)nnr_wtotal(NIN, NH));
+    s.scal = (float4 *)take(16 * 2 * (size_t)NIN);
+    s.dscal = (float *)take(4 * 2 * (size_t)NIN);
+    s.tr_t = (int *)take(4 * kRMaxTraj);
+    s.tr_st = (int *)take(4 * kRMaxTraj);
+    s.tr_n = (int *)take(4 * kRMaxTraj);
+    s.tr_flag = (int *)take(4 * kRMaxTraj);
+    s.tr_rebuild = (int *)take(4 * kRMaxTraj);
+    s.tr_d2 = (int *)take(4 * kRMaxTraj);
+    s.tr_over = (int *)take(4 * kRMaxTraj);
+    s.tr_lat = (float *)take(4 * 24 * kRMaxTraj);
+    s.red = (double *)take(8 * 64);
+    s.misc = (int *)take(16);
+    return s;
+}
+
+// small non-negative integer b (< 2^23) to float by the exponent trick (two full-rate
+// instructions instead of a conversion)
+__device__ __forceinline__ float small_to_float(unsigned b) {
+    return __int_as_float(0x4B000000 | b) - 8388608.f;
+}
+
+// One thread's view of its atom.
+struct AtomR {
+    int slot, s, i, st, N, ei;
+    int64_t base;                 // bead-atom slot of atom 0 of the bead
+    float xhi, yhi, zhi, xli, yli, zli;
+    float L[9];                   // lattice rows (bohr)
+};
+
+__device__ __forceinline__ void rel_pos(const SmemR &S, const AtomR &A, int js, float &dx, float &dy, float &dz) {
+    dx = (S.xh[js] - A.xhi) + (S.xl[js] - A.xli);
+    dy = (S.yh[js] - A.yhi) + (S.yl[js] - A.yli);
+    dz = (S.zh[js] - A.zhi) + (S.zl[js] - A.zli);
+}
+
+// Calls fn(group g as integral constant, pack slot of j, d, r^2) for every neighbour of
+// the atom inside the cutoff: from the skin list when it is valid (cnt >= 0), else by a
+// full image scan of the trajectory.
+template <int G> struct GC { static constexpr int value = G; };
+
+template <class Fn>
+__device__ __forceinline__ void for_neighbours(const RadialNN &R, const SmemR &S, const AtomR &A, const int2 *sk,
+                                               int cnt, Fn &&fn) {
+    if (cnt >= 0) {
+        const int n0 = cnt & 0xFFFF, n1 = cnt >> 16;
+        auto walk = [&](auto gc, int e0, int e1) {
+            for (int e = e0; e < e1; ++e) {
+                const int2 v = sk[(size_t)e * A.N + A.i];
+                const int js = A.st + v.x;
+                const float m1 = small_to_float((unsigned)v.y & 255u) - 128.f;
+                const float m2 = small_to_float(((unsigned)v.y >> 8) & 255u) - 128.f;
+                const float m3 = small_to_float(((unsigned)v.y >> 16) & 255u) - 128.f;
+                float dx, dy, dz;
+                rel_pos(S, A, js, dx, dy, dz);
+                dx += fmaf(m1, A.L[0], fmaf(m2, A.L[3], m3 * A.L[6]));
+                dy += fmaf(m1, A.L[1], fmaf(m2, A.L[4], m3 * A.L[7]));
+                dz += fmaf(m1, A.L[2], fmaf(m2, A.L[5], m3 * A.L[8]));
+                const float r2 = dx * dx + dy * dy + dz * dz;
+                if (r2 < R.rc2) fn(gc, js, dx, dy, dz, r2);
+            }
+        };
+        walk(GC<0>{}, 0, n0);
+        walk(GC<1>{}, n0, n0 + n1);
+        return;
+    }
+    // full scan (skin list overflowed or skin off): images with |f + n| <= rc |b_d|
+    const float *T = S.tr_lat + 24 * A.s;
+    for (int j = 0; j < A.N; ++j) {
+        const int js = A.st + j;
+        const int ej = S.elem[js];
+        float dx0, dy0, dz0;
+        rel_pos(S, A, js, dx0, dy0, dz0);
+        int lo[3], hi[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const float f = T[9 + 3 * d] * dx0 + T[9 + 3 * d + 1] * dy0 + T[9 + 3 * d + 2] * dz0;
+            const float wk = R.rc_b * T[21 + d] + 1e-4f;
+            lo[d] = max(-120, (int)ceilf(-f - wk));
+            hi[d] = min(120, (int)floorf(-f + wk));
+        }
+        for (int n1 = lo[0]; n1 <= hi[0]; ++n1)
+            for (int n2 = lo[1]; n2 <= hi[1]; ++n2)
+                for (int n3 = lo[2]; n3 <= hi[2]; ++n3) {
+                    if (j == A.i && n1 == 0 && n2 == 0 && n3 == 0) continue;
+                    const float m1 = (float)n1, m2 = (float)n2, m3 = (float)n3;
+                    const float dx = dx0 + fmaf(m1, A.L[0], fmaf(m2, A.L[3], m3 * A.L[6]));
+                    const float dy = dy0 + fmaf(m1, A.L[1], fmaf(m2, A.L[4], m3 * A.L[7]));
+                    const float dz = dz0 + fmaf(m1, A.L[2], fmaf(m2, A.L[5], m3 * A.L[8]));
+                    const float r2 = dx * dx + dy * dy + dz * dz;
+                    if (!(r2 < R.rc2)) continue;
+                    if (ej == 0) fn(GC<0>{}, js, dx, dy, dz, r2);
+                    else if (ej == 1) fn(GC<1>{}, js, dx, dy, dz, r2);
+                }
+    }
+}
+
+// Skin list of one atom: every image of every atom of the trajectory within the skin
+// cutoff, element 0 first, as (j, image + 128 per byte).  Returns the packed count
+// (n0 | n1 << 16), or -1 when the list does not fit.
+__device__ int build_skin(const RadialNN &R, const SmemR &S, const AtomR &A, int2 *sk, int skcap) {
+    const float *T = S.tr_lat + 24 * A.s;
+    int tot = 0, n0 = 0;
+    bool over = false;
+    for (int g = 0; g < 2; ++g) {
+        for (int j = 0; j < A.N; ++j) {
+            const int js = A.st + j;
+            if (S.elem[js] != g) continue;
+            float dx0, dy0, dz0;
+            rel_pos(S, A, js, dx0, dy0, dz0);
+            int lo[3], hi[3];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                const float f = T[9 + 3 * d] * dx0 + T[9 + 3 * d + 1] * dy0 + T[9 + 3 * d + 2] * dz0;
+                const float wk = T[18 + d];
+                lo[d] = max(-120, (int)ceilf(-f - wk));
+                hi[d] = min(120, (int)floorf(-f + wk));
+            }
+            for (int n1 = lo[0]; n1 <= hi[0]; ++n1)
+                for (int n2 = lo[1]; n2 <= hi[1]; ++n2)
+                    for (int n3 = lo[2]; n3 <= hi[2]; ++n3) {
+                        if (j == A.i && n1 == 0 && n2 == 0 && n3 == 0) continue;
+                        const float m1 = (float)n1, m2 = (float)n2, m3 = (float)n3;
+                        const float dx = dx0 + fmaf(m1, A.L[0], fmaf(m2, A.L[3], m3 * A.L[6]));
+                        const float dy = dy0 + fmaf(m1, A.L[1], fmaf(m2, A.L[4], m3 * A.L[7]));
+                        const float dz = dz0 + fmaf(m1, A.L[2], fmaf(m2, A.L[5], m3 * A.L[8]));
+                        if (dx * dx + dy * dy + dz * dz > R.cut2s) continue;
+                        if (tot < skcap)
+                            sk[(size_t)tot * A.N + A.i] =
+                                make_int2(j, (n1 + 128) | ((n2 + 128) << 8) | ((n3 + 128) << 16));
+                        else
+                            over = true;
+                        ++tot;
+                        if (g == 0) ++n0;
+                    }
+        }
+    }
+    return over ? -1 : (n0 | ((tot - n0) << 16));
+}
+
+// Activations ('p' softplus, 't' tanh, 's' sigmoid, 'l' linear): the value, and the
+// derivative from the value as getdnodes_values.f90 forms it ((e^v - 1)/e^v = 1 - e^-v for
+// softplus, 1 - v^2, v (1 - v), 1), so a layer's derivatives need no stored pre-activations.
+template <char A> __device__ __forceinline__ float act_v(float z) {
+    if (A == 'p') {
+        const float e = ex2a(-fabsf(z) * kLog2eF);
+        return fmaf(lg2a(1.f + e), kLn2F, fmaxf(z, 0.f));
+    } else if (A == 't') {
+        return tanhf(z);
+    } else if (A == 's') {
+        return rcpa(1.f + ex2a(-z * kLog2eF));
+    }
+    return z;
+}
+template <char A> __device__ __forceinline__ float act_dv(float v) {
+    if (A == 'p') return 1.f - ex2a(-v * kLog2eF);
+    if (A == 't') return fmaf(-v, v, 1.f);
+    if (A == 's') return v * (1.f - v);
+    return 1.f;
+}
+__device__ __forceinline__ void act_d(uint8_t a, float z, float &v, float &dv) {
+    if (a == 'p') {
+        softplus_d(z, v, dv);
+    } else if (a == 't') {
+        v = act_v<'t'>(z);
+        dv = act_dv<'t'>(v);
+    } else if (a == 's') {
+        v = act_v<'s'>(z);
+        dv = act_dv<'s'>(v);
+    } else {
+        v = z;
+        dv = 1.f;
+    }
+}
+// z[n] <- act(z[n] rn) for a whole layer (kind uniform per layer)
+template <char A> __device__ __forceinline__ void act_layer_k(float (&z)[kRW], float rn) {
+#pragma unroll
+    for (int n = 0; n < kRW; ++n) z[n] = act_v<A>(z[n] * rn);
+}
+__device__ __forceinline__ void act_layer(uint8_t a, float (&z)[kRW], float rn) {
+    if (a == 'p') act_layer_k<'p'>(z, rn);
+    else if (a == 't') act_layer_k<'t'>(z, rn);
+    else if (a == 's') act_layer_k<'s'>(z, rn);
+    else act_layer_k<'l'>(z, rn);
+}
+// d[n] <- act'(v[n]) c[n] from the layer's values
+template <char A> __device__ __forceinline__ void act_dv_layer_k(const float (&v)[kRW], float (&d)[kRW]) {
+#pragma unroll
+    for (int n = 0; n < kRW; ++n) d[n] *= act_dv<A>(v[n]);
+}
+__device__ __forceinline__ void act_dv_layer(uint8_t a, const float (&v)[kRW], float (&d)[kRW]) {
+    if (a == 'p') act_dv_layer_k<'p'>(v, d);
+    else if (a == 't') act_dv_layer_k<'t'>(v, d);
+    else if (a == 's') act_dv_layer_k<'s'>(v, d);
+}
+
+// z[0..32) += x[p] W[p][0..32) over p < np, x from the per-thread buffer (stride bs),
+// W rows of 32 floats broadcast from shared memory
+template <int NP>
+__device__ __forceinline__ void rowmv(float (&z)[kRW], const float *W, const float *x) {
+#pragma unroll 2
+    for (int p = 0; p < NP; ++p) {
+        const float xv = x[p * kRS];
+        const float4 *row = reinterpret_cast<const float4 *>(W + p * kRW);
+#pragma unroll
+        for (int n4 = 0; n4 < kRW / 4; ++n4) {
+            const float4 w = row[n4];
+            z[4 * n4] = fmaf(w.x, xv, z[4 * n4]);
+            z[4 * n4 + 1] = fmaf(w.y, xv, z[4 * n4 + 1]);
+            z[4 * n4 + 2] = fmaf(w.z, xv, z[4 * n4 + 2]);
+            z[4 * n4 + 3] = fmaf(w.w, xv, z[4 * n4 + 3]);
+        }
+    }
+}
+__device__ __forceinline__ void load_row(float (&z)[kRW], const float *b) {
+    const float4 *b4 = reinterpret_cast<const float4 *>(b);
+#pragma unroll
+    for (int n4 = 0; n4 < kRW / 4; ++n4) {
+        const float4 v = b4[n4];
+        z[4 * n4] = v.x;
+        z[4 * n4 + 1] = v.y;
+        z[4 * n4 + 2] = v.z;
+        z[4 * n4 + 3] = v.w;
+    }
+}
+
+// ---- network of one atom (lane = atom) ---------------------------------------------------
+// Inputs x[q] = scaled descriptors in the per-thread buffer; returns the atomic energy
+// (output node, Ha) and leaves dE/dG (raw descriptors, padded grouped order) in the
+// buffer when do_forces.  Weight block of an element (floats, rows of 32):
+//   W1 [nin][32], b1 [32], then NH = 2: W2 [32][32], b2 [32], W2T [32][32], w3 [32], b3
+//                               NH = 1: w2 [32], b2
+// Padded hidden nodes have zero weights in and out, so they change nothing.
+template <int NIN, int NH>
+__device__ __forceinline__ float nnr_network(const RadialNN &R, const SmemR &S, int ei, int tid, bool do_forces) {
+    constexpr int nin = NIN, bs = kRS;
+    const float *wb = S.w + (ei == 0 ? 0 : nnr_wofs1(NIN, NH));
+    float *hb = S.hb + tid;
+    const float rn1 = R.rn[0];
+    float z[kRW];
+    load_row(z, wb + nin * kRW);
+    rowmv<nin>(z, wb, hb);
+    act_layer(R.act[0], z, rn1);  // z = layer-1 values
+    float d1[kRW];                // becomes dE/d(layer-1 sum) times rn1
+    float out;
+    if (NH == 2) {
+#pragma unroll
+        for (int n = 0; n < kRW; ++n) hb[n * bs] = z[n];
+        const float *w2 = wb + (nin + 1) * kRW;
+        const float *w3 = w2 + 2 * kRW * kRW + kRW;
+        load_row(z, w2 + kRW * kRW);
+        rowmv<kRW>(z, w2, hb);
+        const float rn2 = R.rn[1];
+        const uint8_t a2 = R.act[1];
+        float o[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+        for (int n = 0; n < kRW; ++n) {
+            float v, dv;
+            act_d(a2, z[n] * rn2, v, dv);
+            const float w = w3[n];
+            o[n & 3] = fmaf(w, v, o[n & 3]);
+            z[n] = w * dv;  // d(output sum)/d(layer-2 sum), before rn2
+        }
+        float vo, dvo;
+        act_d(R.act[2], ((o[0] + o[1]) + (o[2] + o[3]) + w3[kRW]) * R.rn[2], vo, dvo);
+        out = vo;
+        if (!do_forces) return out;
+        // delta2 = dE/d(layer-2 sum) rn2 beside the layer-1 values in the buffer
+        const float g2 = R.rn[2] * dvo * rn2;
+        float *hd = hb + kRW * bs;
+#pragma unroll
+        for (int n = 0; n < kRW; ++n) hd[n * bs] = z[n] * g2;
+#pragma unroll
+        for (int p = 0; p < kRW; ++p) d1[p] = 0.f;
+        rowmv<kRW>(d1, w2 + kRW * kRW + kRW, hd);  // sum_n W2[p][n] delta2[n]
+        const uint8_t a1 = R.act[0];
+#pragma unroll
+        for (int p = 0; p < kRW; ++p) {
+            z[p] = hb[p * bs];
+            d1[p] *= rn1;
+        }
+        act_dv_layer(a1, z, d1);
+    } else {
+        const float *w2 = wb + (nin + 1) * kRW;
+        float o[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+        for (int n = 0; n < kRW; ++n) o[n & 3] = fmaf(w2[n], z[n], o[n & 3]);
+        float vo, dvo;
+        act_d(R.act[1], ((o[0] + o[1]) + (o[2] + o[3]) + w2[kRW]) * R.rn[1], vo, dvo);
+        out = vo;
+        if (!do_forces) return out;
+        const float g1 = R.rn[1] * dvo * rn1;
+#pragma unroll
+        for (int p = 0; p < kRW; ++p) d1[p] = w2[p] * g1;
+        act_dv_layer(R.act[0], z, d1);
+    }
+    // dE/dG_q = dscal_q sum_p W1[q][p] d1[p]
+    const float *ds = S.dscal + ei * nin;
+#pragma unroll 2
+    for (int q = 0; q < nin; ++q) {
+        const float4 *row = reinterpret_cast<const float4 *>(wb + q * kRW);
+        float a[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+        for (int p4 = 0; p4 < kRW / 4; ++p4) {
+            const float4 w = row[p4];
+            a[p4 & 3] = fmaf(w.x, d1[4 * p4], a[p4 & 3]);
+            a[p4 & 3] = fmaf(w.y, d1[4 * p4 + 1], a[p4 & 3]);
+            a[p4 & 3] = fmaf(w.z, d1[4 * p4 + 2], a[p4 & 3]);
+            a[p4 & 3] = fmaf(w.w, d1[4 * p4 + 3], a[p4 & 3]);
+        }
+        hb[q * bs] = ((a[0] + a[1]) + (a[2] + a[3])) * ds[q];
+    }
+    return out;
+}
+
+// ---- one force evaluation of the atom: descriptors, network, forces ------------------
+template <int KA, int KB, int NH>
+__device__ __forceinline__ double nnr_atom(const RadialNN &R, const NNScratch &X, const SmemR &S, const AtomR &A,
+                                           int tid, bool do_forces, float &fix, float &fiy, float &fiz) {
+    constexpr int KT = KA + KB, bs = kRS;
+    const int2 *sk = X.skw + A.base * X.skcap;
+    const int cnt = R.skin > 0.f ? X.skcnt[A.base + A.i] : -1;
+    float G[KT];
+#pragma unroll
+    for (int k = 0; k < KT; ++k) G[k] = 0.f;
+    int nn = 0;
+    for_neighbours(R, S, A, sk, cnt, [&](auto gc, int js, float dx, float dy, float dz, float r2) {
+        constexpr int g = decltype(gc)::value;
+        constexpr int K = g == 0 ? KA : KB, off = g == 0 ? 0 : KA;
+        ++nn;
+        const float r = r2 * rsqrtf(r2);
+        const float fc = fc_of_s(fminf(r2 * R.inv_rc2, 1.f));
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const float u = r - R.rs[g][k];
+            const float t = u * R.c[g][k];
+            G[off + k] = fmaf(ex2a(t * u), fc, G[off + k]);
+        }
+    });
+    if (nn > R.maxnb) X.nnstatus[S.tr_t[A.s]] = 1;
+    // scaling and range test (padded grouped order)
+    {
+        const float4 *sc = S.scal + A.ei * KT;
+        bool out = false;
+#pragma unroll
+        for (int q = 0; q < KT; ++q) {
+            const float4 c = sc[q];
+            out |= G[q] < c.z || G[q] > c.w;
+            S.hb[q * bs + tid] = fmaf(c.x, G[q], c.y);
+        }
+        if (out) S.tr_flag[A.s] = 1;
+    }
+    const float e = nnr_network<KT, NH>(R, S, A.ei, tid, do_forces);
+    const double ea = (double)e + R.atom_energy[A.ei];
+    if (!do_forces) return ea;
+    float dG[KT];
+#pragma unroll
+    for (int q = 0; q < KT; ++q) dG[q] = S.hb[q * bs + tid];
+    float fx = 0.f, fy = 0.f, fz = 0.f;
+    for_neighbours(R, S, A, sk, cnt, [&](auto gc, int js, float dx, float dy, float dz, float r2) {
+        constexpr int g = decltype(gc)::value;
+        constexpr int K = g == 0 ? KA : KB, off = g == 0 ? 0 : KA;
+        const float ri = rsqrtf(r2);
+        const float r = r2 * ri;
+        float fc, dfds;
+        fc_of_s_d(fminf(r2 * R.inv_rc2, 1.f), fc, dfds);
+        float s0 = 0.f, s1 = 0.f;
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const float u = r - R.rs[g][k];
+            const float t = u * R.c[g][k];
+            const float w = dG[off + k] * ex2a(t * u);
+            s0 += w;
+            s1 = fmaf(w, t, s1);
+        }
+        // dE/dr = fc sum_k dG_k de_k/dr + dfc/dr sum_k dG_k e_k, de_k/dr = 2 ln2 t_k e_k
+        const float dEdr = fmaf(fc * (2.f * kLn2F), s1, (2.f * R.inv_rc2) * r * dfds * s0);
+        const float f = dEdr * ri;
+        fx = fmaf(f, dx, fx);
+        fy = fmaf(f, dy, fy);
+        fz = fmaf(f, dz, fz);
+        red_shared(&S.f3[js], -f * dx);
+        red_shared(&S.f3[bs + js], -f * dy);
+        red_shared(&S.f3[2 * bs + js], -f * dz);
+    });
+    fix = fx;
+    fiy = fy;
+    fiz = fz;
+    return ea;
+}
+
+// Weight blocks and scaling tables in shared memory from the model's current FP32 weights
+// (calconenn.f90 layout: layer l of element e is an n_(l-1) x n_l row-major matrix plus
+// n_l biases at woff[e][l]); hidden layers padded to 32 nodes with zeros, inputs in the
+// padded grouped order.
+template <int NIN, int NH>
+__device__ void load_weights_r(const RadialNN &R, const SmemR &S) {
+    const int tid = threadIdx.x, bs = blockDim.x, nin = NIN;
+    for (int e = 0; e < R.nelem; ++e) {
+        const float *src = R.wf + (size_t)e * R.maxweights;
+        float *dst = S.w + (e == 0 ? 0 : nnr_wofs1(NIN, NH));
+        const int n1 = R.nodes[e][1];
+        const float *l1 = src + R.woff[e][1];
+        for (int k = tid; k < (nin + 1) * kRW; k += bs) {
+            const int q = k / kRW, n = k % kRW;
+            float v = 0.f;
+            if (n < n1) {
+                if (q < nin) {
+                    const int s = R.qsrc[e][q];
+                    if (s >= 0) v = l1[s * n1 + n];
+                } else {
+                    v = l1[R.nodes[e][0] * n1 + n];
+                }
+            }
+            dst[k] = v;
+        }
+        const int o2 = (nin + 1) * kRW;
+        const float *l2 = src + R.woff[e][2];
+        if (NH == 2) {
+            const int n2 = R.nodes[e][2];
+            const float *l3 = src + R.woff[e][3];
+            for (int k = tid; k < kRW * kRW; k += bs) {
+                const int p = k / kRW, n = k % kRW;
+                const float v = (p < n1 && n < n2) ? l2[p * n2 + n] : 0.f;
+                dst[o2 + k] = v;                                  // W2 [p][n]
+                dst[o2 + kRW * kRW + kRW + n * kRW + p] = v;      // W2T [n][p]
+            }
+            for (int n = tid; n < kRW; n += bs) {
+                dst[o2 + kRW * kRW + n] = n < n2 ? l2[n1 * n2 + n] : 0.f;          // b2
+                dst[o2 + 2 * kRW * kRW + kRW + n] = n < n2 ? l3[n] : 0.f;          // w3
+            }
+            if (tid < 4) dst[o2 + 2 * kRW * kRW + 2 * kRW + tid] = tid == 0 ? l3[n2] : 0.f;  // b3
+        } else {
+            for (int n = tid; n < kRW; n += bs) dst[o2 + n] = n < n1 ? l2[n] : 0.f;       // w2
+            if (tid < 4) dst[o2 + kRW + tid] = tid == 0 ? l2[n1] : 0.f;                  // b2
+        }
+        for (int q = tid; q < nin; q += bs) {
+            const int s = R.qsrc[e][q];
+            S.scal[e * nin + q] =
+                s >= 0 ? R.fscal[e * R.maxsf + s] : make_float4(1.f, 0.f, -INFINITY, INFINITY);
+            S.dscal[e * nin + q] = s >= 0 ? R.fdscal[e * R.maxsf + s] : 0.f;
+        }
+    }
+}
+
+// mode 0: forces, 1: energies only, 2: nsteps fused MD steps (propagate_1, forces,
+// propagate_2, exit test), as the other network kernels.
+template <int KA, int KB, int NH>
+__global__ void __launch_bounds__(kRBlockMax, 1)
+    nnr_kernel(Batch B, RadialNN R, EmtConst E, NNScratch X, PropParams P, const int2 *packs, const int *ptraj, int npack,
+               int *counter, int nsteps, int mode) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int KT = KA + KB, bs = kRS;
+    const int tid = threadIdx.x;
+    const SmemR S = carve_r<KT, NH>(smem_raw);
+    SmemEmt<double> SE = carve_smem<double>(S.emt, B.max_atoms, B.max_beads);
+    SE.red = S.red;
+    SE.cjk = S.red;  // single-bead trajectories only: the ring-polymer table is never read
+    load_weights_r<KT, NH>(R, S);
+    __syncthreads();
+    const bool do_forces = mode != 1;
+    for (;;) {
+        __syncthreads();
+        if (tid == 0) S.misc[0] = atomicAdd(counter, 1);
+        __syncthreads();
+        const int pk = S.misc[0];
+        if (pk >= npack) break;
+        const int2 pd = packs[pk];
+        if (tid < pd.y) {
+            const int t = ptraj[pd.x + tid];
+            S.tr_t[tid] = t;
+            S.tr_n[tid] = B.natoms[t];
+            S.tr_over[tid] = 0;
+            double lat[18];
+            acsf_lattice(B.box + 9 * t, lat);
+            float *T = S.tr_lat + 24 * tid;
+            for (int k = 0; k < 18; ++k) T[k] = (float)lat[k];
+            for (int d = 0; d < 3; ++d) {
+                const double *I = lat + 9 + 3 * d;
+                const double bn = sqrt(I[0] * I[0] + I[1] * I[1] + I[2] * I[2]);
+                T[18 + d] = (float)(R.rcs * bn * (1.0 + 1e-4) + 1e-4);
+                T[21 + d] = (float)(bn * (1.0 + 1e-4));
+            }
+        }
+        __syncthreads();
+        if (tid == 0) {
+            int st = 0;
+            for (int s = 0; s < pd.y; ++s) {
+                S.tr_st[s] = st;
+                st += S.tr_n[s];
+            }
+            S.misc[1] = pd.y;
+        }
+        __syncthreads();
+        AtomR A;
+        A.slot = tid;
+        A.s = -1;
+        for (int s = 0; s < pd.y; ++s)
+            if (tid >= S.tr_st[s] && tid < S.tr_st[s] + S.tr_n[s]) A.s = s;
+        TrajView T{};
+        if (A.s >= 0) {
+            const int t = S.tr_t[A.s];
+            T = traj_view(B, t);
+            A.st = S.tr_st[A.s];
+            A.N = T.N;
+            A.i = tid - A.st;
+            A.base = T.base;
+            A.ei = R.elem_of_type[B.type[T.aoff + A.i]];
+            S.elem[tid] = (int8_t)A.ei;
+            const float *TL = S.tr_lat + 24 * A.s;
+#pragma unroll
+            for (int k = 0; k < 9; ++k) A.L[k] = TL[k];
+        }
+        const int steps = mode == 2 ? nsteps : 1;
+        for (int step_i = 0; step_i < steps; ++step_i) {
+            __syncthreads();  // status and step counters of the previous step are visible
+            // ---- first half-step and positions --------------------------------------
+            bool active = A.s >= 0;
+            int step = 0;
+            if (active && mode == 2) {
+                active = B.status[T.t] == kStatusRunning;
+                step = B.steps_done[T.t] + 1;
+            }
+            if (tid < pd.y) {
+                S.tr_flag[tid] = 0;
+                S.tr_d2[tid] = 0;
+            }
+            if (tid == 0) S.misc[2] = 0;
+            __syncthreads();
+            if (active) {
+                S.misc[2] = 1;
+                if (mode == 2) {
+                    const int algo = B.algo[B.type[T.aoff + A.i]];
+                    if (algo == kPropVerlet) verlet_half(B, P, T, A.i, true);
+                    else langevin_1(B, P, T, A.i, step, algo);
+                }
+                const int64_t k = A.base + A.i;
+                const double rx = B.rx[k], ry = B.ry[k], rz = B.rz[k];
+                const double x = rx * kAng2BohrD, y = ry * kAng2BohrD, z = rz * kAng2BohrD;
+                A.xhi = (float)x;
+                A.yhi = (float)y;
+                A.zhi = (float)z;
+                A.xli = (float)(x - (double)A.xhi);
+                A.yli = (float)(y - (double)A.yhi);
+                A.zli = (float)(z - (double)A.zhi);
+                S.xh[tid] = A.xhi;
+                S.yh[tid] = A.yhi;
+                S.zh[tid] = A.zhi;
+                S.xl[tid] = A.xli;
+                S.yl[tid] = A.yli;
+                S.zl[tid] = A.zli;
+                if (R.skin > 0.f) {
+                    const double *r0 = X.skref + 3 * k;
+                    const float ddx = (float)(rx - r0[0]), ddy = (float)(ry - r0[1]), ddz = (float)(rz - r0[2]);
+                    atomicMax(&S.tr_d2[A.s], __float_as_int(ddx * ddx + ddy * ddy + ddz * ddz));
+                }
+            }
+            S.f3[tid] = 0.f;
+            S.f3[bs + tid] = 0.f;
+            S.f3[2 * bs + tid] = 0.f;
+            __syncthreads();
+            if (S.misc[2] == 0) break;  // every trajectory of the pack has stopped
+            // skin lists rebuilt when invalid or when some atom moved more than half the skin
+            // (positions in A; the skin is in bohr)
+            if (tid < pd.y) {
+                const int bead = B.bead_off[S.tr_t[tid]];
+                const float half = 0.5f * R.skin * (float)kBohr2Ang;
+                S.tr_rebuild[tid] =
+                    R.skin > 0.f && (X.skok[bead] == 0 || __int_as_float(S.tr_d2[tid]) > half * half) ? 1 : 0;
+            }
+            __syncthreads();
+            // ---- forces ------------------------------------------------------------------
+            float fix = 0.f, fiy = 0.f, fiz = 0.f;
+            double ea = 0.0;
+            if (active) {
+                if (S.tr_rebuild[A.s]) {
+                    const int64_t k = A.base + A.i;
+                    const int c = build_skin(R, S, A, X.skw + A.base * X.skcap, X.skcap);
+                    X.skcnt[k] = c;
+                    if (c < 0) S.tr_over[A.s] = 1;
+                    double *r0 = X.skref + 3 * k;
+                    r0[0] = B.rx[k];
+                    r0[1] = B.ry[k];
+                    r0[2] = B.rz[k];
+                }
+                ea = nnr_atom<KA, KB, NH>(R, X, S, A, tid, do_forces, fix, fiy, fiz);
+                S.ea[tid] = ea;
+            }
+            __syncthreads();
+            if (tid < pd.y && (mode != 2 || B.status[S.tr_t[tid]] == kStatusRunning)) {
+                const int t = S.tr_t[tid];
+                const int bead = B.bead_off[t];
+                if (S.tr_rebuild[tid]) X.skok[bead] = S.tr_over[tid] ? 0 : 1;
+                S.tr_over[tid] = 0;
+                const bool fb = R.surrogate && S.tr_flag[tid];
+                if (!fb) {
+                    double e = 0.0;
+                    for (int k = 0; k < S.tr_n[tid]; ++k) e += S.ea[S.tr_st[tid] + k];
+                    B.epot[bead] = e * kHa2eVR;
+                } else {
+                    B.epot[bead] = 0.0;
+                }
+            }
+            if (active) {
+                const int64_t k = A.base + A.i;
+                const bool fb = R.surrogate && S.tr_flag[A.s];
+                const double c = kHa2eVR * kAng2BohrD;
+                double fx = 0.0, fy = 0.0, fz = 0.0;
+                if (do_forces && !fb) {
+                    fx = (double)(S.f3[tid] + fix) * c;
+                    fy = (double)(S.f3[bs + tid] + fiy) * c;
+                    fz = (double)(S.f3[2 * bs + tid] + fiz) * c;
+                }
+                B.fx[k] = fx;
+                B.fy[k] = fy;
+                B.fz[k] = fz;
+                const double m = B.mass[T.aoff + A.i];
+                const uint8_t fxd = B.fixed[k];
+                B.ax[k] = (do_forces && !(fxd & 1)) ? fx / m : 0.0;
+                B.ay[k] = (do_forces && !(fxd & 2)) ? fy / m : 0.0;
+                B.az[k] = (do_forces && !(fxd & 4)) ? fz / m : 0.0;
+            }
+            // ---- EMT for the trajectories whose descriptors left the training range ----------
+            if (R.surrogate) {
+                __syncthreads();
+                for (int s = 0; s < pd.y; ++s) {
+                    const int t = S.tr_t[s];
+                    if (!S.tr_flag[s] || (mode == 2 && B.status[t] != kStatusRunning)) continue;
+                    __syncthreads();
+                    emt_bead<double>(B, E, SE, t, 0, do_forces);
+                    if (tid == 0) X.fallback[t] += 1;
+                    if (A.s == s && do_forces) {
+                        const int64_t k = A.base + A.i;
+                        const double m = B.mass[T.aoff + A.i];
+                        const uint8_t fxd = B.fixed[k];
+                        if (!(fxd & 1)) B.ax[k] = B.fx[k] / m;
+                        if (!(fxd & 2)) B.ay[k] = B.fy[k] / m;
+                        if (!(fxd & 4)) B.az[k] = B.fz[k] / m;
+                    }
+                    __syncthreads();
+                }
+            }
+            // ---- second half-step and exit test ---------------------------------------------
+            if (active && mode == 2) {
+                const int algo = B.algo[B.type[T.aoff + A.i]];
+                if (algo == kPropVerlet) verlet_half(B, P, T, A.i, false);
+                else langevin_2(B, P, T, A.i, step, algo);
+            }
+            __syncthreads();
+            if (mode == 2 && tid < pd.y) {
+                const int t = S.tr_t[tid];
+                if (B.status[t] == kStatusRunning) {
+                    const TrajView V = traj_view(B, t);
+                    B.steps_done[t] = B.steps_done[t] + 1;
+                    const int ty0 = B.type[V.aoff];
+                    if (P.use_exit && B.is_proj[ty0]) {
+                        const double z = B.rz[V.base];
+                        if (z > P.pul) B.status[t] = kStatusExitUpper;
+                        else if (z < P.pll) B.status[t] = kStatusExitLower;
+                    }
+                }
+            }
+        }
+    }
+}
+
+template <int KA, int KB, int NH>
+cudaError_t nnr_launch_t(const LaunchCfg &c, const Batch &B, const RadialNN &R, const EmtConst &E,
+                         const NNScratch &X, const PropParams &P, const int2 *packs, const int *ptraj, int npack,
+                         size_t sm, int nsteps, int mode) {
+    cudaError_t e = cudaMemsetAsync(c.counter, 0, sizeof(int), c.stream);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(nnr_kernel<KA, KB, NH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    nnr_kernel<KA, KB, NH><<<c.grid, R.block, sm, c.stream>>>(B, R, E, X, P, packs, ptraj, npack, c.counter, nsteps, mode);
+    return cudaGetLastError();
+}
+
+template <int KA, int KB, int NH>
+int nnr_occupancy_t(int block, size_t sm) {
+    int n = 0;
+    cudaFuncSetAttribute(nnr_kernel<KA, KB, NH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, nnr_kernel<KA, KB, NH>, block, sm);
+    return n;
+}
+
+}  // namespace
+
+// Instantiated shapes (functions over neighbour element 0 and 1, hidden layers): exact
+// sizes for the shipped H/Au surrogate layout, and padded kernels for any other radial
+// model within the limits (unused slots carry zero weights).
+#define MDT_NNR_SHAPES(X) X(4, 20, 2) X(24, 24, 2) X(24, 24, 1)
+
+bool nnr_shape(int cnt0, int cnt1, int nh, int &ka, int &kb) {
+#define MDT_TRY(A_, B_, H_)                                                 \
+    if (nh == H_ && cnt0 <= A_ && cnt1 <= B_ && (ka < 0 || A_ + B_ < ka + kb)) { \
+        ka = A_;                                                            \
+        kb = B_;                                                            \
+    }
+    ka = kb = -1;
+    MDT_NNR_SHAPES(MDT_TRY)
+#undef MDT_TRY
+    return ka >= 0;
+}
+
+size_t nnr_smem(const RadialNN &R) { return smem_r(R.nin, R.nh); }
+
+size_t nnr_emt_smem(int max_atoms) { return smem_bytes(max_atoms, 1, 8); }
+
+int nnr_resident_ctas(const RadialNN &R) {
+    const size_t sm = nnr_smem(R);
+#define MDT_OCC(A_, B_, H_) \
+    if (R.ka == A_ && R.kb == B_ && R.nh == H_) return nnr_occupancy_t<A_, B_, H_>(R.block, sm);
+    MDT_NNR_SHAPES(MDT_OCC)
+#undef MDT_OCC
+    return 0;
+}
+
+cudaError_t launch_nnr(const LaunchCfg &c, const Batch &B, const RadialNN &R, const EmtConst &E, const NNScratch &X,
+                       const PropParams &P, const int2 *packs, const int *ptraj, int npack, int nsteps, int mode) {
+    const size_t sm = nnr_smem(R);
+#define MDT_LAUNCH(A_, B_, H_) \
+    if (R.ka == A_ && R.kb == B_ && R.nh == H_) return nnr_launch_t<A_, B_, H_>(c, B, R, E, X, P, packs, ptraj, npack, sm, nsteps, mode);
+    MDT_NNR_SHAPES(MDT_LAUNCH)
+#undef MDT_LAUNCH
+    return cudaErrorInvalidValue;
+}
+
+}  // namespace mdt

@@ -120,6 +120,14 @@ class Engine:
             self._check(r, "mdt_nn_fast_path")
         return bool(r)
 
+    def nn_radial_kernel(self, enable: bool = True) -> bool:
+        """Allow (default) or forbid the thread-per-atom kernel of radial-only models;
+        True if the installed model qualifies."""
+        r = self.lib.mdt_nn_radial_kernel(self.h, 1 if enable else 0)
+        if r < 0:
+            self._check(r, "mdt_nn_radial_kernel")
+        return bool(r)
+
     def nn_set_skin(self, skin_ang: float) -> None:
         """Verlet skin (A) of the fast kernels' neighbour lists; 0 rebuilds every step."""
         self._check(self.lib.mdt_nn_set_skin(self.h, skin_ang), "mdt_nn_set_skin")

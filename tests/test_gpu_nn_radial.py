@@ -1,0 +1,164 @@
+"""GPU parity of the thread-per-atom kernel of radial-only models (mdt_nnr.cu): shifted
+G2 functions over H and Au neighbours, 24-32-32-1 softplus networks (the layout of the
+shipped H/Au surrogate) and one-hidden-layer variants.
+
+Bars: unscaled descriptors against the FP64 oracle, force RMSE below 1e-4 of the force
+RMS and energies within 5e-5 relative (the exponentials use the hardware 2^x
+approximation, as on the warp-per-atom fast kernel); against the warp-per-atom kernel on
+the same batch the same bars; fused MD steps stay within 1e-6 A of the FP64 generic
+kernels; the surrogate's EMT fallback is FP64-exact (1e-10 eV/A)."""
+import numpy as np
+import pytest
+
+from md_tian2_gb300 import constants as C
+from md_tian2_gb300 import nene
+from md_tian2_gb300 import workloads as W
+from md_tian2_gb300.engine import PES_NENE, PES_SURROGATE, Engine, SimParams
+from md_tian2_gb300.surrogate import surrogate_model
+
+pytestmark = pytest.mark.gpu
+MAXNB = 120
+
+
+def _engine(us, m, kind=PES_NENE, emt=None, margin=0.1, maxnb=MAXNB, radial=True, fast=True):
+    eng = Engine(0)
+    if emt is not None:
+        eng.read_emt(emt)
+    eng.define(us)
+    eng.read_nene(m, ["H", "Au"], max_neighbors=maxnb)
+    eng.set_pes(kind, margin)
+    eng.nn_fast_path(fast)
+    eng.nn_radial_kernel(radial)
+    eng.upload()
+    return eng
+
+
+def _elems(u):
+    return np.array([0] + [1] * (u.natoms - 1))
+
+
+def _radial_model(seed, hidden=(32, 32)):
+    return nene.random_model(["H", "Au"], hidden=hidden, act="p", seed=seed, neighbours=["H", "Au"],
+                             descriptor="radial")
+
+
+def _scaled(us, m):
+    eng = _engine(us, m, radial=False)
+    G = eng.nn_descriptors()
+    eng.close()
+    nene.set_scaling(m, G, np.concatenate([_elems(u) for u in us]))
+    return m
+
+
+@pytest.mark.parametrize("hidden", [(32, 32), (32,), (20, 25)])
+def test_radial_kernel_matches_oracle(built_lib, oracle_lib, hidden):
+    from oracle.oracle import NNOracle
+    us = W.config2(7, seed=21)
+    m = _radial_model(4, hidden)
+    eng = _engine(us, m)
+    assert eng.nn_radial_kernel(True)
+    eng.calc_force(SimParams(), precision="fp32")
+    out = eng.download()
+    _, ov = eng.nn_stats()
+    assert not ov.any()
+    eng.close()
+    o = NNOracle(m)
+    for t, u in enumerate(us):
+        E, F = o.energy_force(_elems(u), u.r[:, 0, :], u.simbox)
+        f = eng.split(out["f"], t)[:, 0, :]
+        assert np.sqrt(np.mean((f - F) ** 2)) < 1e-4 * np.sqrt(np.mean(F ** 2)), (hidden, t)
+        assert abs(out["epot"][t] - E) < 5e-5 * max(1.0, abs(E)), (hidden, t)
+
+
+def test_radial_kernel_matches_warp_kernel_scaled_and_energy_only(built_lib, oracle_lib):
+    """A scaled model on a ragged batch larger than one pack: thread-per-atom against
+    warp-per-atom, forces and energies, then the energy-only evaluation."""
+    us = W.config2(40, seed=22)
+    m = _scaled(us[:8], _radial_model(6))
+    outs = {}
+    for radial in (True, False):
+        eng = _engine(us, m, radial=radial)
+        eng.calc_force(SimParams(), precision="fp32")
+        o = eng.download()
+        eng.calc_force(SimParams(), flag=C.ENERGY_ONLY, precision="fp32")
+        o["epot_only"] = eng.download()["epot"]
+        outs[radial] = o
+        eng.close()
+    a, b = outs[True], outs[False]
+    frms = np.sqrt(np.mean(b["f"] ** 2))
+    assert np.sqrt(np.mean((a["f"] - b["f"]) ** 2)) < 1e-4 * frms
+    assert np.abs(a["epot"] - b["epot"]).max() < 5e-5 * max(1.0, np.abs(b["epot"]).max())
+    assert np.allclose(a["epot_only"], a["epot"], rtol=0, atol=1e-9)
+
+
+def test_radial_md_steps_track_fp64(built_lib, oracle_lib):
+    """Ten fused MD steps (constant-friction Langevin slab, Verlet projectile, same
+    deviates on both sides) in FP32 forces stay within 1e-6 A of the FP64 kernels."""
+    us = W.config2(6, seed=23)
+    m = _radial_model(8)
+    sp = SimParams(step=0.1, gamma_const=1e-3, seed=5)
+    res = {}
+    for prec in ("fp32", "fp64"):
+        eng = _engine(us, m)
+        eng.calc_force(sp, precision=prec)
+        eng.md_steps(10, sp, precision=prec)
+        res[prec] = eng.download()
+        eng.close()
+    assert np.abs(res["fp32"]["r"] - res["fp64"]["r"]).max() < 1e-6
+    assert np.abs(res["fp32"]["v"] - res["fp64"]["v"]).max() < 1e-6
+
+
+def test_radial_md_exit_and_skin(built_lib, oracle_lib):
+    """Projectiles that leave through pul stop (status and step count as the warp
+    kernel gives them); 40 steps with the 1 A skin equal 40 steps built every step."""
+    us = W.config2(12, seed=24)
+    m = _radial_model(9)
+    sp = SimParams(step=0.5, gamma_const=1e-3, seed=7, pul=6.05, use_exit=True)
+    res = {}
+    for radial, skin in ((True, 1.0), (True, 0.0), (False, 1.0)):
+        eng = _engine(us, m, radial=radial)
+        eng.nn_set_skin(skin)
+        eng.calc_force(sp, precision="fp32")
+        eng.md_steps(40, sp, precision="fp32")
+        out = eng.download()
+        q = eng.query(sp)
+        res[(radial, skin)] = (out, q)
+        eng.close()
+    a, qa = res[(True, 1.0)]
+    b, qb = res[(True, 0.0)]
+    c, qc = res[(False, 1.0)]
+    assert np.abs(a["r"] - b["r"]).max() < 1e-6
+    assert np.abs(a["r"] - c["r"]).max() < 1e-5
+    assert (qa["status"] == qc["status"]).all() and (qa["steps_done"] == qc["steps_done"]).all()
+
+
+def test_radial_surrogate_fallback_is_fp64_emt(built_lib, oracle_lib):
+    from oracle.oracle import OracleUniverse
+    rng = np.random.default_rng(4)
+    train = [W.h_on_metal(rng, "Au", 3, 1.0, 0.0, 0.0, 300.0, z0=5.0)]
+    far = [W.h_on_metal(rng, "Au", 4, 1.0, 0.0, 0.0, 300.0, z0=0.8)]
+    emt = W.emt_params()
+    m = _scaled(train, _radial_model(10))
+    sp = SimParams()
+    eng = _engine(train + far, m, kind=PES_SURROGATE, emt=emt, margin=0.01)
+    assert eng.nn_radial_kernel(True)
+    eng.calc_force(sp, precision="fp32")
+    out = eng.download()
+    fb, ov = eng.nn_stats()
+    assert fb[0] == 0 and fb[1] == 1 and not ov.any()
+    o = OracleUniverse(far[0], emt)
+    o.calc_force(sp)
+    assert np.abs(eng.split(out["f"], 1) - o.f).max() < 1e-10
+    assert abs(out["epot"][1] - o.epot[0]) < 1e-9
+    eng.close()
+
+
+def test_radial_neighbour_overflow_is_reported(built_lib):
+    us = W.config2(3, seed=25)
+    eng = _engine(us, _radial_model(2), maxnb=30)
+    assert eng.nn_radial_kernel(True)
+    eng.calc_force(SimParams(), precision="fp32")
+    eng.download()
+    _, ov = eng.nn_stats()
+    assert ov.all()
+    eng.close()
