@@ -51,7 +51,9 @@ FLOP_ATOM = 4 * 20 + 20
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--steps-per-launch", type=int, default=10,
+                    help="MD steps fused into one kernel launch (mdt_md_steps), both arms alike")
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--ntraj", type=int, default=4096)
@@ -120,8 +122,11 @@ class ClockSampler:
     def __enter__(self):
         try:
             self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
-                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                       "--format=csv,noheader,nounits", "-lms", "100"],
                                       stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            # nvidia-smi's start-up (driver queries) stalls CUDA launches of this process for a
+            # few ms: the timed region opens only after its first sample
+            self.p.stdout.readline()
         except OSError:
             self.p = None
         return self
@@ -255,7 +260,15 @@ FLOP_SURR_ENTRY = 70 + 156 + 252 + 14
 FLOP_SURR_ATOM = 2 * (24 * 32 + 32 * 32 + 32) + 64 * 40 + 2 * (32 + 32 * 32 + 24 * 32) + 64 * 20
 
 
-def timed_steps(eng, sp, precision, steps, stream, torch, dist=None, clock_index=None):
+def steps_per_launch(steps, want):
+    """Largest divisor of the timed step count not above the requested steps per launch."""
+    want = max(1, min(want, steps))
+    while steps % want:
+        want -= 1
+    return want
+
+
+def timed_steps(eng, sp, precision, steps, stream, torch, dist=None, clock_index=None, per_launch=1):
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     if dist:
         dist.barrier()
@@ -264,8 +277,8 @@ def timed_steps(eng, sp, precision, steps, stream, torch, dist=None, clock_index
     if clk:
         clk.__enter__()
     ev0.record(stream)
-    for _ in range(steps):
-        eng.md_steps(1, sp, precision=precision)
+    for _ in range(steps // per_launch):
+        eng.md_steps(per_launch, sp, precision=precision)
     ev1.record(stream)
     torch.cuda.synchronize()
     if clk:
@@ -314,6 +327,9 @@ def run_ours(args):
     # ---- surrogate (headline) -------------------------------------------------------
     eng.set_pes(PES_SURROGATE, args.margin)
     fast = eng.nn_fast_path(True)
+    radial = eng.nn_radial_kernel(True)
+    kname = ("nnr_kernel (thread per atom, fused MD step, surrogate)" if radial
+             else "nnf_kernel (warp per atom, fused MD step, surrogate)")
     eng.upload()
     eng.calc_force(sp, precision="fp32")
     for _ in range(args.warmup):
@@ -322,12 +338,17 @@ def run_ours(args):
     s0 = atom_steps_now()
     launches0 = eng.launch_count()
     fb0 = int(eng.nn_stats()[0].sum())
-    ms, clocks = timed_steps(eng, sp, "fp32", args.steps, stream, torch, dist, local)
+    per_launch = steps_per_launch(args.steps, args.steps_per_launch)
+    ms, clocks = timed_steps(eng, sp, "fp32", args.steps, stream, torch, dist, local, per_launch)
     launches = eng.launch_count() - launches0
     done = atom_steps_now() - s0
     fb_count = int(eng.nn_stats()[0].sum()) - fb0
     bead_evals = int(np.sum([u.nbeads for u in universes])) * args.steps
+    # neighbour entries of the step (the warp-per-atom kernel writes the per-atom lists)
+    eng.nn_radial_kernel(False)
+    eng.calc_force(sp, precision="fp32")
     counts, _ = eng.nn_neighbors()
+    eng.nn_radial_kernel(True)
     entries = int(np.sum(counts))
     surr_flop = FLOP_SURR_ENTRY * entries + FLOP_SURR_ATOM * int(np.sum(natoms))
 
@@ -364,7 +385,7 @@ def run_ours(args):
         eng.md_steps(1, sp, precision=args.precision)
     torch.cuda.synchronize()
     s0 = atom_steps_now()
-    ms_emt, clocks_emt = timed_steps(eng, sp, args.precision, args.steps, stream, torch, dist, local)
+    ms_emt, clocks_emt = timed_steps(eng, sp, args.precision, args.steps, stream, torch, dist, local, per_launch)
     done_emt = atom_steps_now() - s0
     same, mixed, nat = count_pairs(universes, emt_cut(emt))
     emt_flop = FLOP_SAME_PAIR * same + FLOP_MIXED_PAIR * mixed + FLOP_ATOM * nat
@@ -385,7 +406,7 @@ def run_ours(args):
     peak64 = ct.c_double()
     lib.mdt_peak_fma(0, 2000, ct.byref(peak64))
     traffic = None
-    prof = ROOT / "profiles" / "nnf_surrogate_traffic.json"
+    prof = ROOT / "profiles" / ("nnr_surrogate_traffic.json" if radial else "nnf_surrogate_traffic.json")
     if prof.exists():
         try:
             traffic = json.loads(prof.read_text()).get("bytes_per_launch")
@@ -416,7 +437,9 @@ def run_ours(args):
             "config": {"workload": f"NN surrogate (FP32 fast kernels, EMT fallback), {args.ntraj} ragged H/Au(111) "
                                    "trajectories (37-145 atoms), Verlet H + constant-friction Langevin Au, dt 0.1 fs; "
                                    "one bench step = one MD step of every trajectory",
-                       "model": Path(args.model).name, "fast_path": bool(fast), "ntraj_per_gpu": args.ntraj,
+                       "steps_per_launch": per_launch,
+                       "model": Path(args.model).name, "fast_path": bool(fast), "radial_kernel": bool(radial),
+                       "ntraj_per_gpu": args.ntraj,
                        "parallelism": f"replicas x{world}", "range_margin": args.margin,
                        "l2": "per-step state, skin lists and neighbour words of all trajectories (>0.5 GB) exceed L2"},
             "emt_fp64": {"value": emt_value, "unit": UNIT, "ms_per_step": 1e3 * elapsed_emt / args.steps,
@@ -431,7 +454,7 @@ def run_ours(args):
             "clocks": clocks,
             "e2e": {"value": e_atoms_all / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": int(launches),
-            "roofline": {"bound": "fp32", "kernel": "nnf_kernel (fused MD step, surrogate)",
+            "roofline": {"bound": "fp32", "kernel": kname,
                          "achieved": achieved / 1e12, "peak": peak.value / 1e12, "unit": "TFLOP/s",
                          "frac": achieved / peak.value if peak.value > 0 else None, "traffic": traffic,
                          "peak_source": "measured FP32 FMA microbenchmark (mdt_peak_fma); MEASURED_PEAKS.json has "

@@ -138,6 +138,12 @@ module mdt_gpu
             integer(c_int32_t), value :: enable
         end function
 
+        integer(c_int32_t) function mdt_nn_radial_block(ctx, max_block) bind(C, name="mdt_nn_radial_block")
+            import :: c_int32_t, c_ptr
+            type(c_ptr), value :: ctx
+            integer(c_int32_t), value :: max_block
+        end function
+
         integer(c_int32_t) function mdt_nn_set_skin(ctx, skin_ang) bind(C, name="mdt_nn_set_skin")
             import :: c_int32_t, c_ptr, c_double
             type(c_ptr), value :: ctx

@@ -152,6 +152,11 @@ int32_t mdt_nn_fast_path(mdt_ctx *ctx, int32_t enable);
    else 0 (no replacement in the reference: src/pes_nene_mod.f90:7145 has one path). */
 int32_t mdt_nn_radial_kernel(mdt_ctx *ctx, int32_t enable);
 
+/* Largest CTA (atoms of the trajectories packed into one CTA, 32..512, default 512) the
+   thread-per-atom kernel's pack plan may use; batches whose largest trajectory exceeds
+   it stay on the warp-per-atom kernel (no replacement in the reference). */
+int32_t mdt_nn_radial_block(mdt_ctx *ctx, int32_t max_block);
+
 /* Verlet skin (A) of the fast kernels' neighbour lists (default 1.0; 0 = build every
    step).  Lists are rebuilt when an atom of the bead moved more than half the skin
    since the last build; the per-step list is filtered from it with the same exact

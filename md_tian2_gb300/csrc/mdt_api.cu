@@ -78,6 +78,7 @@ struct mdt_ctx {
     int2 *rpacks = nullptr;    // (offset into rptraj, count) per pack
     int *rptraj = nullptr;     // trajectories of the packs
     int rnpack = 0, rblock = 0;
+    int rmaxblock = kRBlockMax; // largest block the pack plan may use
 
     // training (buffers live with the batch)
     bool have_labels = false;
@@ -457,10 +458,35 @@ RadialNN build_radial(const NNDev &M, const mdt_nn_model *m, const FastNN &F, co
         }
     }
     const int cnt0 = (int)idx[0][0].size(), cnt1 = (int)idx[0][1].size();
-    int ka, kb;
-    if (!nnr_shape(cnt0, cnt1, nh, ka, kb)) return R;
-    R.ka = ka;
-    R.kb = kb;
+    // recurrence admission per neighbour group: one eta, r_s evenly spaced (within 1e-9
+    // bohr), and blocks short enough that a block start below the FP32 range (2^-126,
+    // flushed to zero) hides only functions below 2^-40: (L - 1) delta <= 4.9 / sqrt(|c|)
+    // with c = -eta log2(e) (sqrt(126) - sqrt(40) = 4.9)
+    int maxbl[2] = {0, 0};
+    double dl[2] = {0.0, 0.0};
+    for (int g = 0; g < 2; ++g) {
+        const std::vector<int> &v = idx[0][g];
+        if (v.size() < 2) continue;
+        const double eta0 = m->eta[v[0]];
+        const double d = (m->rshift[v.back()] - m->rshift[v[0]]) / (double)(v.size() - 1);
+        bool uni = eta0 > 0.0 && d > 0.0;
+        for (size_t k = 0; k < v.size() && uni; ++k) {
+            uni = m->eta[v[k]] == eta0 && std::fabs(m->rshift[v[k]] - (m->rshift[v[0]] + d * (double)k)) <= 1e-9;
+        }
+        if (!uni) continue;
+        const double c = eta0 * 1.4426950408889634;
+        maxbl[g] = 1 + (int)std::floor(4.9 / std::sqrt(c) / d);
+        dl[g] = d;
+    }
+    if (!nnr_shape(cnt0, cnt1, nh, maxbl, R)) return R;
+    const int ka = R.ka, kb = R.kb;
+    for (int g = 0; g < 2; ++g) {
+        const double c = -m->eta[idx[0][g].empty() ? 0 : idx[0][g][0]] * 1.4426950408889634;
+        R.dl[g] = (float)dl[g];
+        R.gq[g] = (float)(-2.0 * c * dl[g]);
+        R.gc[g] = (float)(c * dl[g] * dl[g]);
+        R.gam[g] = (float)std::exp2(2.0 * c * dl[g] * dl[g]);
+    }
     R.nh = nh;
     R.nelem = ne;
     R.nin = ka + kb;
@@ -527,13 +553,39 @@ bool radial_plan(mdt_ctx *c) {
     if (nnr_smem(c->R) > (size_t)optin ||
         nnr_emt_smem(c->max_atoms) > 4 * (size_t)nnr_hbw(c->R.nin, c->R.nh) * kRBlockMax)
         return false;
+    // the kernel's image loops span at most 65 cells per direction: every cell must be wider
+    // than the skin-list cutoff / 32 in each direction
+    {
+        std::vector<double> box(9 * (size_t)c->T);
+        if (cudaMemcpy(box.data(), c->B.box, sizeof(double) * box.size(), cudaMemcpyDeviceToHost) != cudaSuccess)
+            return false;
+        const double rcs = c->M.maxcut * kBohr2Ang + c->skin_ang;  // A
+        for (int t = 0; t < c->T; ++t) {
+            const double *a = box.data() + 9 * (size_t)t;  // cell vectors a[0..2], a[3..5], a[6..8]
+            auto cross = [&](int p, int q, double *o) {
+                o[0] = a[3 * p + 1] * a[3 * q + 2] - a[3 * p + 2] * a[3 * q + 1];
+                o[1] = a[3 * p + 2] * a[3 * q] - a[3 * p] * a[3 * q + 2];
+                o[2] = a[3 * p] * a[3 * q + 1] - a[3 * p + 1] * a[3 * q];
+            };
+            double x[3];
+            cross(1, 2, x);
+            const double vol = std::fabs(a[0] * x[0] + a[1] * x[1] + a[2] * x[2]);
+            for (int d = 0; d < 3; ++d) {
+                cross((d + 1) % 3, (d + 2) % 3, x);
+                const double area = std::sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
+                if (!(vol > 0.0) || !(area > 0.0) || !(32.0 * vol / area > rcs)) return false;
+            }
+        }
+    }
     c->R.block = kRBlockMax;
     const int slots = c->num_sms * std::max(1, nnr_resident_ctas(c->R));
     std::vector<int> order(c->T);
     std::iota(order.begin(), order.end(), 0);
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return c->natoms[a] > c->natoms[b]; });
     const int64_t total = c->total_atoms;
-    const int w0 = (int)std::max<int64_t>(1, (total + (int64_t)slots * kRBlockMax - 1) / ((int64_t)slots * kRBlockMax));
+    const int bmax = std::max(32, std::min(kRBlockMax, c->rmaxblock));
+    if (c->max_atoms > bmax) return false;
+    const int w0 = (int)std::max<int64_t>(1, (total + (int64_t)slots * bmax - 1) / ((int64_t)slots * bmax));
     int64_t best = -1;
     std::vector<std::vector<int>> bestp;
     int bestb = 0;
@@ -565,7 +617,7 @@ bool radial_plan(mdt_ctx *c) {
         if (!ok) continue;
         const int mx = *std::max_element(load.begin(), load.end());
         const int block = (mx + 31) & ~31;
-        if (block > kRBlockMax) continue;
+        if (block > bmax) continue;
         const int64_t cost = (int64_t)((np + slots - 1) / slots) * block;
         if (best < 0 || cost < best) {
             best = cost;
@@ -1431,6 +1483,7 @@ int32_t mdt_nn_set_skin(mdt_ctx *c, double skin_ang) {
     if (!(skin_ang >= 0.0) || skin_ang > 5.0) return fail(c, MDT_ERR_ARG, "skin must be in [0, 5] A");
     c->skin_ang = skin_ang;
     c->skin_dirty = true;
+    c->rnpack = 0;  // the thread-per-atom plan checks cell widths against the skin cutoff
     return MDT_OK;
 }
 
@@ -1438,6 +1491,14 @@ int32_t mdt_nn_radial_kernel(mdt_ctx *c, int32_t enable) {
     if (!c) return MDT_ERR_ARG;
     c->radial_enabled = enable != 0;
     return c->have_nn && c->R.ok ? 1 : 0;
+}
+
+int32_t mdt_nn_radial_block(mdt_ctx *c, int32_t max_block) {
+    if (!c) return MDT_ERR_ARG;
+    if (max_block < 32 || max_block > kRBlockMax) return fail(c, MDT_ERR_ARG, "max_block outside [32, 512]");
+    c->rmaxblock = max_block;
+    c->rnpack = 0;  // re-plan on the next evaluation
+    return MDT_OK;
 }
 
 int32_t mdt_nn_fast_path(mdt_ctx *c, int32_t enable) {

@@ -40,7 +40,9 @@ cudaError_t launch_nnf(const LaunchCfg &c, const Batch &B, const NNDev &M, const
                        const NNScratch &X, const PropParams &P, int nsteps, int mode, bool surrogate);
 
 // FP32 thread-per-atom kernel of radial-only models (mdt_nnr.cu)
-bool nnr_shape(int cnt0, int cnt1, int nh, int &ka, int &kb);
+// shape of a model (group counts, hidden layers; maxbl[g] = longest recurrence block group g
+// admits, 0 = none): sets R.ka, R.kb, R.bla, R.blb
+bool nnr_shape(int cnt0, int cnt1, int nh, const int *maxbl, RadialNN &R);
 size_t nnr_smem(const RadialNN &R);
 size_t nnr_emt_smem(int max_atoms);  // EMT fallback area (aliases the network buffers)
 int nnr_resident_ctas(const RadialNN &R);

@@ -122,6 +122,7 @@ __host__ __device__ constexpr int nnr_hbw(int nin, int nh) {
 struct RadialNN {
     int ok;
     int ka, kb, nh;                 // kernel shape: padded functions per group, hidden layers
+    int bla, blb;                   // recurrence block length per group (0: one 2^x per function)
     int nelem, nin;                 // elements, ka + kb
     int block;                      // threads per CTA (batch plan)
     int surrogate, maxnb;
@@ -130,6 +131,9 @@ struct RadialNN {
     float skin, cut2s;              // Verlet skin (bohr, 0: off), skin-list cutoff^2 (bohr^2)
     float c[2][kRMaxK];             // -eta log2(e) (bohr^-2); 0 on padded slots
     float rs[2][kRMaxK];            // r_s (bohr)
+    // recurrence of a group with one eta and r_s spaced by delta: the ratio of consecutive
+    // functions is q = 2^(gq u + gc) (u = r - r_s), and consecutive q differ by gam
+    float gq[2], gc[2], gam[2], dl[2];
     uint8_t act[3];                 // activation of hidden layers 1..nh, then of the output
     float rn[3];                    // 1/n_(l-1) per layer with normnodes, else 1
     double atom_energy[2];          // Ha (0 unless remove_atom_energies)

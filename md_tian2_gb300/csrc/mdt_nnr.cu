@@ -50,6 +50,8 @@ struct SmemR {
     float *xh, *yh, *zh, *xl, *yl, *zl;  // [slot] unwrapped positions (bohr), FP32 hi/lo split
     float *f3;                           // [3][bs] neighbour force accumulators (Ha/bohr)
     double *ea;                          // [slot] atomic energies (Ha)
+    double *lc;                          // [8][slot] Langevin coefficients of the atom (see LcR)
+    double *im;                          // [slot] 1 / mass
     int8_t *elem;                        // [slot]
     float *hb;                           // [hbw][bs] per-thread network buffer
     float *w;                            // weight blocks of the elements
@@ -69,7 +71,8 @@ __host__ __device__ constexpr size_t r16r(size_t b) { return (b + 15) & ~size_t(
 constexpr int kRS = kRBlockMax;
 
 __host__ __device__ constexpr size_t smem_r(int nin, int nh) {
-    return 6 * r16r(4 * (size_t)kRS) + r16r(12 * (size_t)kRS) + r16r(8 * (size_t)kRS) + r16r(kRS) +
+    return 6 * r16r(4 * (size_t)kRS) + r16r(12 * (size_t)kRS) + r16r(8 * (size_t)kRS) + r16r(64 * (size_t)kRS) +
+           r16r(8 * (size_t)kRS) + r16r(kRS) +
            r16r(4 * (size_t)nnr_hbw(nin, nh) * kRS) + r16r(4 * (size_t)nnr_wtotal(nin, nh)) + r16r(16 * 2 * (size_t)nin) +
            r16r(4 * 2 * (size_t)nin) + 7 * r16r(4 * kRMaxTraj) + r16r(4 * 24 * kRMaxTraj) + r16r(8 * 64) + r16r(16);
 }
@@ -91,6 +94,8 @@ __device__ __forceinline__ SmemR carve_r(unsigned char *base) {
     s.zl = (float *)take(4 * (size_t)kRS);
     s.f3 = (float *)take(12 * (size_t)kRS);
     s.ea = (double *)take(8 * (size_t)kRS);
+    s.lc = (double *)take(64 * (size_t)kRS);
+    s.im = (double *)take(8 * (size_t)kRS);
     s.elem = (int8_t *)take(kRS);
     s.hb = (float *)take(4 * (size_t)nnr_hbw(NIN, NH) * kRS);
     s.emt = (unsigned char *)s.hb;
@@ -118,7 +123,7 @@ __device__ __forceinline__ float small_to_float(unsigned b) {
 
 // One thread's view of its atom.
 struct AtomR {
-    int slot, s, i, st, N, ei;
+    int slot, s, i, st, N, ei, algo;
     int64_t base;                 // bead-atom slot of atom 0 of the bead
     float xhi, yhi, zhi, xli, yli, zli;
     float L[9];                   // lattice rows (bohr)
@@ -130,23 +135,50 @@ __device__ __forceinline__ void rel_pos(const SmemR &S, const AtomR &A, int js, 
     dz = (S.zh[js] - A.zhi) + (S.zl[js] - A.zli);
 }
 
+// Skin-list entry: j (bits 0-9) and the image (n1, n2, n3) in the unwrapped frame, each
+// + 64 in 7 bits (bits 10-16, 17-23, 24-30).  An image outside [-63, 63] (atoms that
+// drifted more than 63 cells apart) does not fit: the list overflows and the atom takes
+// the full scan.
+constexpr int kImgBias = 64;
+__device__ __forceinline__ unsigned pack_entry(int j, int n1, int n2, int n3) {
+    return (unsigned)j | (unsigned)(n1 + kImgBias) << 10 | (unsigned)(n2 + kImgBias) << 17 |
+           (unsigned)(n3 + kImgBias) << 24;
+}
+__device__ __forceinline__ bool image_fits(int n) { return n >= -63 && n <= 63; }
+
+// Image range of dimension d for the displacement with fractional coordinate f: the n
+// with |f + n| <= w.  Returns false for a non-finite or absurd displacement; the range
+// holds at most 65 images.
+__device__ __forceinline__ bool image_range(float f, float w, int &lo, int &hi) {
+    if (!(fabsf(f) < 1e6f) || !(w < 64.f)) return false;
+    lo = (int)ceilf(-f - w);
+    hi = (int)floorf(-f + w);
+    return true;
+}
+
 // Calls fn(group g as integral constant, pack slot of j, d, r^2) for every neighbour of
 // the atom inside the cutoff: from the skin list when it is valid (cnt >= 0), else by a
 // full image scan of the trajectory.
 template <int G> struct GC { static constexpr int value = G; };
 
 template <class Fn>
-__device__ __forceinline__ void for_neighbours(const RadialNN &R, const SmemR &S, const AtomR &A, const int2 *sk,
+__device__ __forceinline__ void for_neighbours(const RadialNN &R, const SmemR &S, const AtomR &A, const unsigned *sk,
                                                int cnt, Fn &&fn) {
     if (cnt >= 0) {
         const int n0 = cnt & 0xFFFF, n1 = cnt >> 16;
+        // entries two iterations ahead are in flight while one is processed
         auto walk = [&](auto gc, int e0, int e1) {
+            const unsigned *p = sk + (size_t)e0 * A.N + A.i;
+            unsigned w0 = e0 < e1 ? p[0] : 0u;
+            unsigned w1 = e0 + 1 < e1 ? p[A.N] : 0u;
             for (int e = e0; e < e1; ++e) {
-                const int2 v = sk[(size_t)e * A.N + A.i];
-                const int js = A.st + v.x;
-                const float m1 = small_to_float((unsigned)v.y & 255u) - 128.f;
-                const float m2 = small_to_float(((unsigned)v.y >> 8) & 255u) - 128.f;
-                const float m3 = small_to_float(((unsigned)v.y >> 16) & 255u) - 128.f;
+                const unsigned v = w0;
+                w0 = w1;
+                if (e + 2 < e1) w1 = p[(size_t)(e - e0 + 2) * A.N];
+                const int js = A.st + (int)(v & 1023u);
+                const float m1 = small_to_float((v >> 10) & 127u) - (float)kImgBias;
+                const float m2 = small_to_float((v >> 17) & 127u) - (float)kImgBias;
+                const float m3 = small_to_float((v >> 24) & 127u) - (float)kImgBias;
                 float dx, dy, dz;
                 rel_pos(S, A, js, dx, dy, dz);
                 dx += fmaf(m1, A.L[0], fmaf(m2, A.L[3], m3 * A.L[6]));
@@ -168,13 +200,13 @@ __device__ __forceinline__ void for_neighbours(const RadialNN &R, const SmemR &S
         float dx0, dy0, dz0;
         rel_pos(S, A, js, dx0, dy0, dz0);
         int lo[3], hi[3];
+        bool ok = true;
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
             const float f = T[9 + 3 * d] * dx0 + T[9 + 3 * d + 1] * dy0 + T[9 + 3 * d + 2] * dz0;
-            const float wk = R.rc_b * T[21 + d] + 1e-4f;
-            lo[d] = max(-120, (int)ceilf(-f - wk));
-            hi[d] = min(120, (int)floorf(-f + wk));
+            ok &= image_range(f, R.rc_b * T[21 + d] + 1e-4f, lo[d], hi[d]);
         }
+        if (!ok) continue;
         for (int n1 = lo[0]; n1 <= hi[0]; ++n1)
             for (int n2 = lo[1]; n2 <= hi[1]; ++n2)
                 for (int n3 = lo[2]; n3 <= hi[2]; ++n3) {
@@ -192,9 +224,9 @@ __device__ __forceinline__ void for_neighbours(const RadialNN &R, const SmemR &S
 }
 
 // Skin list of one atom: every image of every atom of the trajectory within the skin
-// cutoff, element 0 first, as (j, image + 128 per byte).  Returns the packed count
-// (n0 | n1 << 16), or -1 when the list does not fit.
-__device__ int build_skin(const RadialNN &R, const SmemR &S, const AtomR &A, int2 *sk, int skcap) {
+// cutoff, element 0 first.  Returns the packed count (n0 | n1 << 16), or -1 when the list
+// does not fit (more than skcap entries, or an image outside the entry's range).
+__device__ int build_skin(const RadialNN &R, const SmemR &S, const AtomR &A, unsigned *sk, int skcap) {
     const float *T = S.tr_lat + 24 * A.s;
     int tot = 0, n0 = 0;
     bool over = false;
@@ -205,12 +237,15 @@ __device__ int build_skin(const RadialNN &R, const SmemR &S, const AtomR &A, int
             float dx0, dy0, dz0;
             rel_pos(S, A, js, dx0, dy0, dz0);
             int lo[3], hi[3];
+            bool ok = true;
 #pragma unroll
             for (int d = 0; d < 3; ++d) {
                 const float f = T[9 + 3 * d] * dx0 + T[9 + 3 * d + 1] * dy0 + T[9 + 3 * d + 2] * dz0;
-                const float wk = T[18 + d];
-                lo[d] = max(-120, (int)ceilf(-f - wk));
-                hi[d] = min(120, (int)floorf(-f + wk));
+                ok &= image_range(f, T[18 + d], lo[d], hi[d]);
+            }
+            if (!ok) {
+                over = true;
+                continue;
             }
             for (int n1 = lo[0]; n1 <= hi[0]; ++n1)
                 for (int n2 = lo[1]; n2 <= hi[1]; ++n2)
@@ -221,9 +256,8 @@ __device__ int build_skin(const RadialNN &R, const SmemR &S, const AtomR &A, int
                         const float dy = dy0 + fmaf(m1, A.L[1], fmaf(m2, A.L[4], m3 * A.L[7]));
                         const float dz = dz0 + fmaf(m1, A.L[2], fmaf(m2, A.L[5], m3 * A.L[8]));
                         if (dx * dx + dy * dy + dz * dz > R.cut2s) continue;
-                        if (tot < skcap)
-                            sk[(size_t)tot * A.N + A.i] =
-                                make_int2(j, (n1 + 128) | ((n2 + 128) << 8) | ((n3 + 128) << 16));
+                        if (tot < skcap && image_fits(n1) && image_fits(n2) && image_fits(n3))
+                            sk[(size_t)tot * A.N + A.i] = pack_entry(j, n1, n2, n3);
                         else
                             over = true;
                         ++tot;
@@ -410,11 +444,13 @@ __device__ __forceinline__ float nnr_network(const RadialNN &R, const SmemR &S, 
 }
 
 // ---- one force evaluation of the atom: descriptors, network, forces ------------------
-template <int KA, int KB, int NH>
+// BLA / BLB: block length of the shifted-Gaussian recurrence of group 0 / 1 (0: one 2^x
+// per function)
+template <int KA, int KB, int NH, int BLA, int BLB>
 __device__ __forceinline__ double nnr_atom(const RadialNN &R, const NNScratch &X, const SmemR &S, const AtomR &A,
                                            int tid, bool do_forces, float &fix, float &fiy, float &fiz) {
     constexpr int KT = KA + KB, bs = kRS;
-    const int2 *sk = X.skw + A.base * X.skcap;
+    const unsigned *sk = reinterpret_cast<const unsigned *>(X.skw) + A.base * X.skcap;
     const int cnt = R.skin > 0.f ? X.skcnt[A.base + A.i] : -1;
     float G[KT];
 #pragma unroll
@@ -422,15 +458,33 @@ __device__ __forceinline__ double nnr_atom(const RadialNN &R, const NNScratch &X
     int nn = 0;
     for_neighbours(R, S, A, sk, cnt, [&](auto gc, int js, float dx, float dy, float dz, float r2) {
         constexpr int g = decltype(gc)::value;
-        constexpr int K = g == 0 ? KA : KB, off = g == 0 ? 0 : KA;
+        constexpr int K = g == 0 ? KA : KB, off = g == 0 ? 0 : KA, BL = g == 0 ? BLA : BLB;
         ++nn;
         const float r = r2 * rsqrtf(r2);
         const float fc = fc_of_s(fminf(r2 * R.inv_rc2, 1.f));
+        if constexpr (BL > 0) {
+            // e_(k+1) = e_k q_k, q_(k+1) = q_k gamma; a fresh 2^x at every block start
 #pragma unroll
-        for (int k = 0; k < K; ++k) {
-            const float u = r - R.rs[g][k];
-            const float t = u * R.c[g][k];
-            G[off + k] = fmaf(ex2a(t * u), fc, G[off + k]);
+            for (int b = 0; b < K; b += BL) {
+                const float u = r - R.rs[g][b];
+                float e = ex2a(u * R.c[g][b] * u);
+                float q = ex2a(fmaf(R.gq[g], u, R.gc[g]));
+#pragma unroll
+                for (int m = 0; m < BL && b + m < K; ++m) {
+                    G[off + b + m] = fmaf(e, fc, G[off + b + m]);
+                    if (m + 1 < BL && b + m + 1 < K) {
+                        e *= q;
+                        q *= R.gam[g];
+                    }
+                }
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                const float u = r - R.rs[g][k];
+                const float t = u * R.c[g][k];
+                G[off + k] = fmaf(ex2a(t * u), fc, G[off + k]);
+            }
         }
     });
     if (nn > R.maxnb) X.nnstatus[S.tr_t[A.s]] = 1;
@@ -455,22 +509,47 @@ __device__ __forceinline__ double nnr_atom(const RadialNN &R, const NNScratch &X
     float fx = 0.f, fy = 0.f, fz = 0.f;
     for_neighbours(R, S, A, sk, cnt, [&](auto gc, int js, float dx, float dy, float dz, float r2) {
         constexpr int g = decltype(gc)::value;
-        constexpr int K = g == 0 ? KA : KB, off = g == 0 ? 0 : KA;
+        constexpr int K = g == 0 ? KA : KB, off = g == 0 ? 0 : KA, BL = g == 0 ? BLA : BLB;
         const float ri = rsqrtf(r2);
         const float r = r2 * ri;
         float fc, dfds;
         fc_of_s_d(fminf(r2 * R.inv_rc2, 1.f), fc, dfds);
-        float s0 = 0.f, s1 = 0.f;
+        float s0 = 0.f, s1 = 0.f, dEdr;
+        if constexpr (BL > 0) {
+            // s1 = sum_k w_k u_k, u_k = u_b - (k - b) delta within a block; dE/dr needs c s1
 #pragma unroll
-        for (int k = 0; k < K; ++k) {
-            const float u = r - R.rs[g][k];
-            const float t = u * R.c[g][k];
-            const float w = dG[off + k] * ex2a(t * u);
-            s0 += w;
-            s1 = fmaf(w, t, s1);
+            for (int b = 0; b < K; b += BL) {
+                const float u = r - R.rs[g][b];
+                float e = ex2a(u * R.c[g][b] * u);
+                float q = ex2a(fmaf(R.gq[g], u, R.gc[g]));
+                float sb = 0.f, sm = 0.f;
+#pragma unroll
+                for (int m = 0; m < BL && b + m < K; ++m) {
+                    const float w = dG[off + b + m] * e;
+                    sb += w;
+                    sm = fmaf(w, (float)m, sm);
+                    if (m + 1 < BL && b + m + 1 < K) {
+                        e *= q;
+                        q *= R.gam[g];
+                    }
+                }
+                s0 += sb;
+                s1 = fmaf(u, sb, s1);
+                s1 = fmaf(-R.dl[g], sm, s1);
+            }
+            dEdr = fmaf(fc * (2.f * kLn2F) * R.c[g][0], s1, (2.f * R.inv_rc2) * r * dfds * s0);
+        } else {
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                const float u = r - R.rs[g][k];
+                const float t = u * R.c[g][k];
+                const float w = dG[off + k] * ex2a(t * u);
+                s0 += w;
+                s1 = fmaf(w, t, s1);
+            }
+            // dE/dr = fc sum_k dG_k de_k/dr + dfc/dr sum_k dG_k e_k, de_k/dr = 2 ln2 t_k e_k
+            dEdr = fmaf(fc * (2.f * kLn2F), s1, (2.f * R.inv_rc2) * r * dfds * s0);
         }
-        // dE/dr = fc sum_k dG_k de_k/dr + dfc/dr sum_k dG_k e_k, de_k/dr = 2 ln2 t_k e_k
-        const float dEdr = fmaf(fc * (2.f * kLn2F), s1, (2.f * R.inv_rc2) * r * dfds * s0);
         const float f = dEdr * ri;
         fx = fmaf(f, dx, fx);
         fy = fmaf(f, dy, fy);
@@ -539,9 +618,71 @@ __device__ void load_weights_r(const RadialNN &R, const SmemR &S) {
     }
 }
 
+// Propagators of the fused step for single-bead atoms.  The constant-friction Langevin
+// coefficients (langevin_coef of md_algo.f90:165-198 / 253-285: exp, sqrt and divisions in
+// FP64, the slowest pipe of the GPU) depend only on the atom, so they are formed once per
+// pack by the same FP64 expressions as langevin_1 / langevin_2 and the per-step updates
+// apply them exactly as those functions do.
+enum { kLcC0, kLcC1, kLcC2S, kLcC1mC2, kLcSr, kLcSvr, kLcC2, kLcSv2, kLcN };
+
+__device__ __forceinline__ void lc_setup(const Batch &B, const PropParams &P, const TrajView &T, int i, double *lc,
+                                         int stride) {
+    const int ty = B.type[T.aoff + i];
+    const double temp = kBoltz * T.nb * temp_of(B, P, ty) / B.mass[T.aoff + i];
+    const bool all_big = all_xidt_big(B, P, T, i, kPropLangevinConst);
+    LangCoef a, b;
+    langevin_coef(P.gamma_const, P.step, temp, all_big, false, a);
+    langevin_coef(P.gamma_const, P.step, temp, all_big, true, b);
+    lc[kLcC0 * stride] = a.c0;
+    lc[kLcC1 * stride] = a.c1;
+    lc[kLcC2S * stride] = a.c2 * P.step;
+    lc[kLcC1mC2 * stride] = a.c1 - a.c2;
+    lc[kLcSr * stride] = a.sigma_r;
+    lc[kLcSvr * stride] = a.sigma_v * a.c_rv;
+    lc[kLcC2 * stride] = b.c2;
+    lc[kLcSv2 * stride] = b.sigma_v * sqrt(1 - b.c_rv * b.c_rv);
+}
+
+// langevin_1 (md_algo.f90:146-232) for one single-bead atom with its coefficients
+__device__ __forceinline__ void lc_half1(const Batch &B, const PropParams &P, const TrajView &T, int i, int step,
+                                         const double *lc, int stride) {
+    const int64_t k = T.base + i;
+    const uint8_t fx = B.fixed[k];
+    const double c0 = lc[kLcC0 * stride], c1 = lc[kLcC1 * stride], c2s = lc[kLcC2S * stride],
+                 c1mc2 = lc[kLcC1mC2 * stride], sr = lc[kLcSr * stride], svr = lc[kLcSvr * stride];
+    for (int d = 0; d < 3; ++d) {
+        double &v = comp(B.vx, B.vy, B.vz, d, k);
+        if (!(fx >> d & 1)) {
+            const double rnd = rand_normal(P, T, step, 0, i, d, kStreamLangevin, P.randy);
+            const double a = comp(B.ax, B.ay, B.az, d, k);
+            comp(B.rx, B.ry, B.rz, d, k) += c1 * v + c2s * a + sr * rnd;
+            v = c0 * v + c1mc2 * a + svr * rnd;
+        } else {
+            v = 0.0;
+        }
+    }
+}
+
+// langevin_2 (md_algo.f90:236-300) for one single-bead atom with its coefficients
+__device__ __forceinline__ void lc_half2(const Batch &B, const PropParams &P, const TrajView &T, int i, int step,
+                                         const double *lc, int stride) {
+    const int64_t k = T.base + i;
+    const uint8_t fx = B.fixed[k];
+    const double c2 = lc[kLcC2 * stride], sv = lc[kLcSv2 * stride];
+    for (int d = 0; d < 3; ++d) {
+        double &v = comp(B.vx, B.vy, B.vz, d, k);
+        if (!(fx >> d & 1)) {
+            const double rnd = rand_normal(P, T, step, 0, i, d, kStreamLangevin, P.randy);
+            v = v + c2 * comp(B.ax, B.ay, B.az, d, k) + sv * rnd;
+        } else {
+            v = 0.0;
+        }
+    }
+}
+
 // mode 0: forces, 1: energies only, 2: nsteps fused MD steps (propagate_1, forces,
 // propagate_2, exit test), as the other network kernels.
-template <int KA, int KB, int NH>
+template <int KA, int KB, int NH, int BLA, int BLB>
 __global__ void __launch_bounds__(kRBlockMax, 1)
     nnr_kernel(Batch B, RadialNN R, EmtConst E, NNScratch X, PropParams P, const int2 *packs, const int *ptraj, int npack,
                int *counter, int nsteps, int mode) {
@@ -606,6 +747,10 @@ __global__ void __launch_bounds__(kRBlockMax, 1)
             const float *TL = S.tr_lat + 24 * A.s;
 #pragma unroll
             for (int k = 0; k < 9; ++k) A.L[k] = TL[k];
+            const int ty = B.type[T.aoff + A.i];
+            A.algo = B.algo[ty];
+            S.im[tid] = 1.0 / B.mass[T.aoff + A.i];
+            if (mode == 2 && A.algo == kPropLangevinConst) lc_setup(B, P, T, A.i, S.lc + tid, bs);
         }
         const int steps = mode == 2 ? nsteps : 1;
         for (int step_i = 0; step_i < steps; ++step_i) {
@@ -626,9 +771,8 @@ __global__ void __launch_bounds__(kRBlockMax, 1)
             if (active) {
                 S.misc[2] = 1;
                 if (mode == 2) {
-                    const int algo = B.algo[B.type[T.aoff + A.i]];
-                    if (algo == kPropVerlet) verlet_half(B, P, T, A.i, true);
-                    else langevin_1(B, P, T, A.i, step, algo);
+                    if (A.algo == kPropVerlet) verlet_half(B, P, T, A.i, true);
+                    else lc_half1(B, P, T, A.i, step, S.lc + tid, bs);
                 }
                 const int64_t k = A.base + A.i;
                 const double rx = B.rx[k], ry = B.ry[k], rz = B.rz[k];
@@ -671,7 +815,7 @@ __global__ void __launch_bounds__(kRBlockMax, 1)
             if (active) {
                 if (S.tr_rebuild[A.s]) {
                     const int64_t k = A.base + A.i;
-                    const int c = build_skin(R, S, A, X.skw + A.base * X.skcap, X.skcap);
+                    const int c = build_skin(R, S, A, reinterpret_cast<unsigned *>(X.skw) + A.base * X.skcap, X.skcap);
                     X.skcnt[k] = c;
                     if (c < 0) S.tr_over[A.s] = 1;
                     double *r0 = X.skref + 3 * k;
@@ -679,7 +823,7 @@ __global__ void __launch_bounds__(kRBlockMax, 1)
                     r0[1] = B.ry[k];
                     r0[2] = B.rz[k];
                 }
-                ea = nnr_atom<KA, KB, NH>(R, X, S, A, tid, do_forces, fix, fiy, fiz);
+                ea = nnr_atom<KA, KB, NH, BLA, BLB>(R, X, S, A, tid, do_forces, fix, fiy, fiz);
                 S.ea[tid] = ea;
             }
             __syncthreads();
@@ -710,11 +854,11 @@ __global__ void __launch_bounds__(kRBlockMax, 1)
                 B.fx[k] = fx;
                 B.fy[k] = fy;
                 B.fz[k] = fz;
-                const double m = B.mass[T.aoff + A.i];
+                const double im = S.im[tid];
                 const uint8_t fxd = B.fixed[k];
-                B.ax[k] = (do_forces && !(fxd & 1)) ? fx / m : 0.0;
-                B.ay[k] = (do_forces && !(fxd & 2)) ? fy / m : 0.0;
-                B.az[k] = (do_forces && !(fxd & 4)) ? fz / m : 0.0;
+                B.ax[k] = (do_forces && !(fxd & 1)) ? fx * im : 0.0;
+                B.ay[k] = (do_forces && !(fxd & 2)) ? fy * im : 0.0;
+                B.az[k] = (do_forces && !(fxd & 4)) ? fz * im : 0.0;
             }
             // ---- EMT for the trajectories whose descriptors left the training range ----------
             if (R.surrogate) {
@@ -738,9 +882,8 @@ __global__ void __launch_bounds__(kRBlockMax, 1)
             }
             // ---- second half-step and exit test ---------------------------------------------
             if (active && mode == 2) {
-                const int algo = B.algo[B.type[T.aoff + A.i]];
-                if (algo == kPropVerlet) verlet_half(B, P, T, A.i, false);
-                else langevin_2(B, P, T, A.i, step, algo);
+                if (A.algo == kPropVerlet) verlet_half(B, P, T, A.i, false);
+                else lc_half2(B, P, T, A.i, step, S.lc + tid, bs);
             }
             __syncthreads();
             if (mode == 2 && tid < pd.y) {
@@ -760,43 +903,49 @@ __global__ void __launch_bounds__(kRBlockMax, 1)
     }
 }
 
-template <int KA, int KB, int NH>
+template <int KA, int KB, int NH, int BLA, int BLB>
 cudaError_t nnr_launch_t(const LaunchCfg &c, const Batch &B, const RadialNN &R, const EmtConst &E,
                          const NNScratch &X, const PropParams &P, const int2 *packs, const int *ptraj, int npack,
                          size_t sm, int nsteps, int mode) {
     cudaError_t e = cudaMemsetAsync(c.counter, 0, sizeof(int), c.stream);
     if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(nnr_kernel<KA, KB, NH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    e = cudaFuncSetAttribute(nnr_kernel<KA, KB, NH, BLA, BLB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
-    nnr_kernel<KA, KB, NH><<<c.grid, R.block, sm, c.stream>>>(B, R, E, X, P, packs, ptraj, npack, c.counter, nsteps, mode);
+    nnr_kernel<KA, KB, NH, BLA, BLB><<<c.grid, R.block, sm, c.stream>>>(B, R, E, X, P, packs, ptraj, npack,
+                                                                        c.counter, nsteps, mode);
     return cudaGetLastError();
 }
 
-template <int KA, int KB, int NH>
+template <int KA, int KB, int NH, int BLA, int BLB>
 int nnr_occupancy_t(int block, size_t sm) {
     int n = 0;
-    cudaFuncSetAttribute(nnr_kernel<KA, KB, NH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, nnr_kernel<KA, KB, NH>, block, sm);
+    cudaFuncSetAttribute(nnr_kernel<KA, KB, NH, BLA, BLB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, nnr_kernel<KA, KB, NH, BLA, BLB>, block, sm);
     return n;
 }
 
 }  // namespace
 
-// Instantiated shapes (functions over neighbour element 0 and 1, hidden layers): exact
-// sizes for the shipped H/Au surrogate layout, and padded kernels for any other radial
-// model within the limits (unused slots carry zero weights).
-#define MDT_NNR_SHAPES(X) X(4, 20, 2) X(24, 24, 2) X(24, 24, 1)
+// Instantiated shapes (functions over neighbour element 0 and 1, hidden layers, recurrence
+// block lengths): exact sizes for the shipped H/Au surrogate layout (4 + 20 shifted
+// Gaussians, recurrences of 4 and 5), and padded kernels with one 2^x per function for any
+// other radial model within the limits (unused slots carry zero weights).
+#define MDT_NNR_SHAPES(X) X(4, 20, 2, 4, 5) X(24, 24, 2, 0, 0) X(24, 24, 1, 0, 0)
 
-bool nnr_shape(int cnt0, int cnt1, int nh, int &ka, int &kb) {
-#define MDT_TRY(A_, B_, H_)                                                 \
-    if (nh == H_ && cnt0 <= A_ && cnt1 <= B_ && (ka < 0 || A_ + B_ < ka + kb)) { \
-        ka = A_;                                                            \
-        kb = B_;                                                            \
+bool nnr_shape(int cnt0, int cnt1, int nh, const int *maxbl, RadialNN &R) {
+    bool found = false;
+#define MDT_TRY(A_, B_, H_, LA_, LB_)                                                                   \
+    if (!found && nh == H_ && cnt0 <= A_ && cnt1 <= B_ && (LA_ == 0 || (cnt0 == A_ && LA_ <= maxbl[0])) && \
+        (LB_ == 0 || (cnt1 == B_ && LB_ <= maxbl[1]))) {                                                 \
+        R.ka = A_;                                                                                      \
+        R.kb = B_;                                                                                      \
+        R.bla = LA_;                                                                                    \
+        R.blb = LB_;                                                                                    \
+        found = true;                                                                                   \
     }
-    ka = kb = -1;
     MDT_NNR_SHAPES(MDT_TRY)
 #undef MDT_TRY
-    return ka >= 0;
+    return found;
 }
 
 size_t nnr_smem(const RadialNN &R) { return smem_r(R.nin, R.nh); }
@@ -805,8 +954,9 @@ size_t nnr_emt_smem(int max_atoms) { return smem_bytes(max_atoms, 1, 8); }
 
 int nnr_resident_ctas(const RadialNN &R) {
     const size_t sm = nnr_smem(R);
-#define MDT_OCC(A_, B_, H_) \
-    if (R.ka == A_ && R.kb == B_ && R.nh == H_) return nnr_occupancy_t<A_, B_, H_>(R.block, sm);
+#define MDT_OCC(A_, B_, H_, LA_, LB_)                                                   \
+    if (R.ka == A_ && R.kb == B_ && R.nh == H_ && R.bla == LA_ && R.blb == LB_) \
+        return nnr_occupancy_t<A_, B_, H_, LA_, LB_>(R.block, sm);
     MDT_NNR_SHAPES(MDT_OCC)
 #undef MDT_OCC
     return 0;
@@ -815,8 +965,9 @@ int nnr_resident_ctas(const RadialNN &R) {
 cudaError_t launch_nnr(const LaunchCfg &c, const Batch &B, const RadialNN &R, const EmtConst &E, const NNScratch &X,
                        const PropParams &P, const int2 *packs, const int *ptraj, int npack, int nsteps, int mode) {
     const size_t sm = nnr_smem(R);
-#define MDT_LAUNCH(A_, B_, H_) \
-    if (R.ka == A_ && R.kb == B_ && R.nh == H_) return nnr_launch_t<A_, B_, H_>(c, B, R, E, X, P, packs, ptraj, npack, sm, nsteps, mode);
+#define MDT_LAUNCH(A_, B_, H_, LA_, LB_)                                                                      \
+    if (R.ka == A_ && R.kb == B_ && R.nh == H_ && R.bla == LA_ && R.blb == LB_)                       \
+        return nnr_launch_t<A_, B_, H_, LA_, LB_>(c, B, R, E, X, P, packs, ptraj, npack, sm, nsteps, mode);
     MDT_NNR_SHAPES(MDT_LAUNCH)
 #undef MDT_LAUNCH
     return cudaErrorInvalidValue;

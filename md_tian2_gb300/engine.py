@@ -128,6 +128,10 @@ class Engine:
             self._check(r, "mdt_nn_radial_kernel")
         return bool(r)
 
+    def nn_radial_block(self, max_block: int = 512) -> None:
+        """Largest CTA (atoms per pack) the thread-per-atom kernel's plan may use."""
+        self._check(self.lib.mdt_nn_radial_block(self.h, max_block), "mdt_nn_radial_block")
+
     def nn_set_skin(self, skin_ang: float) -> None:
         """Verlet skin (A) of the fast kernels' neighbour lists; 0 rebuilds every step."""
         self._check(self.lib.mdt_nn_set_skin(self.h, skin_ang), "mdt_nn_set_skin")
