@@ -540,8 +540,10 @@ int ensure_mscr(mdt_ctx *c, int grid, int layout);
 // Pack plan of the thread-per-atom kernel for the batch.  A pack is a set of whole
 // trajectories run by one CTA (thread = atom).  For w waves of the resident CTAs the
 // trajectories are dealt largest first to the pack with the fewest atoms (at most
-// kRMaxTraj per pack); the block is the largest pack rounded up to a warp, and the plan
-// with the smallest w * block (CTA time is set by the fullest pack of a wave) wins.
+// kRMaxTraj per pack); the block is the largest pack rounded up to a warp, and the
+// smallest w whose block fits the cap wins (one CTA per SM is resident, so the largest
+// CTAs keep the most warps in flight; the latency-bound kernel gains more from them than
+// it loses to the emptier last wave).
 bool radial_plan(mdt_ctx *c) {
     if (c->rnpack > 0) return true;
     if (c->max_beads != 1 || c->max_atoms > kRBlockMax) return false;
@@ -618,12 +620,11 @@ bool radial_plan(mdt_ctx *c) {
         const int mx = *std::max_element(load.begin(), load.end());
         const int block = (mx + 31) & ~31;
         if (block > bmax) continue;
-        const int64_t cost = (int64_t)((np + slots - 1) / slots) * block;
-        if (best < 0 || cost < best) {
-            best = cost;
-            bestp = std::move(packs);
-            bestb = block;
-        }
+        // fewest waves first: the largest CTAs keep the most warps per SM in flight
+        best = (int64_t)((np + slots - 1) / slots) * block;
+        bestp = std::move(packs);
+        bestb = block;
+        break;
     }
     if (bestp.empty()) return false;
     // packs largest first (the work queue hands them out in order)

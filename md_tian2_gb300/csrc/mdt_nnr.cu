@@ -157,8 +157,9 @@ __device__ __forceinline__ bool image_range(float f, float w, int &lo, int &hi) 
 }
 
 // Calls fn(group g as integral constant, pack slot of j, d, r^2) for every neighbour of
-// the atom inside the cutoff: from the skin list when it is valid (cnt >= 0), else by a
-// full image scan of the trajectory.
+// the atom inside the cutoff: from the skin list when it is valid (cnt >= 0; the skin
+// shell's entries beyond the cutoff are passed too and fn masks them), else by a full image
+// scan of the trajectory.
 template <int G> struct GC { static constexpr int value = G; };
 
 template <class Fn>
@@ -171,6 +172,7 @@ __device__ __forceinline__ void for_neighbours(const RadialNN &R, const SmemR &S
             const unsigned *p = sk + (size_t)e0 * A.N + A.i;
             unsigned w0 = e0 < e1 ? p[0] : 0u;
             unsigned w1 = e0 + 1 < e1 ? p[A.N] : 0u;
+#pragma unroll 2
             for (int e = e0; e < e1; ++e) {
                 const unsigned v = w0;
                 w0 = w1;
@@ -184,8 +186,9 @@ __device__ __forceinline__ void for_neighbours(const RadialNN &R, const SmemR &S
                 dx += fmaf(m1, A.L[0], fmaf(m2, A.L[3], m3 * A.L[6]));
                 dy += fmaf(m1, A.L[1], fmaf(m2, A.L[4], m3 * A.L[7]));
                 dz += fmaf(m1, A.L[2], fmaf(m2, A.L[5], m3 * A.L[8]));
-                const float r2 = dx * dx + dy * dy + dz * dz;
-                if (r2 < R.rc2) fn(gc, js, dx, dy, dz, r2);
+                // entries of the skin shell (r >= rc) go through the same arithmetic with the
+                // cutoff function masked to zero: no divergent branch in the walk
+                fn(gc, js, dx, dy, dz, dx * dx + dy * dy + dz * dz);
             }
         };
         walk(GC<0>{}, 0, n0);
@@ -459,9 +462,10 @@ __device__ __forceinline__ double nnr_atom(const RadialNN &R, const NNScratch &X
     for_neighbours(R, S, A, sk, cnt, [&](auto gc, int js, float dx, float dy, float dz, float r2) {
         constexpr int g = decltype(gc)::value;
         constexpr int K = g == 0 ? KA : KB, off = g == 0 ? 0 : KA, BL = g == 0 ? BLA : BLB;
-        ++nn;
+        const bool inside = r2 < R.rc2;
+        nn += inside ? 1 : 0;
         const float r = r2 * rsqrtf(r2);
-        const float fc = fc_of_s(fminf(r2 * R.inv_rc2, 1.f));
+        const float fc = inside ? fc_of_s(r2 * R.inv_rc2) : 0.f;
         if constexpr (BL > 0) {
             // e_(k+1) = e_k q_k, q_(k+1) = q_k gamma; a fresh 2^x at every block start
 #pragma unroll
@@ -514,6 +518,10 @@ __device__ __forceinline__ double nnr_atom(const RadialNN &R, const NNScratch &X
         const float r = r2 * ri;
         float fc, dfds;
         fc_of_s_d(fminf(r2 * R.inv_rc2, 1.f), fc, dfds);
+        if (!(r2 < R.rc2)) {
+            fc = 0.f;
+            dfds = 0.f;
+        }
         float s0 = 0.f, s1 = 0.f, dEdr;
         if constexpr (BL > 0) {
             // s1 = sum_k w_k u_k, u_k = u_b - (k - b) delta within a block; dE/dr needs c s1
@@ -827,18 +835,23 @@ __global__ void __launch_bounds__(kRBlockMax, 1)
                 S.ea[tid] = ea;
             }
             __syncthreads();
-            if (tid < pd.y && (mode != 2 || B.status[S.tr_t[tid]] == kStatusRunning)) {
-                const int t = S.tr_t[tid];
-                const int bead = B.bead_off[t];
-                if (S.tr_rebuild[tid]) X.skok[bead] = S.tr_over[tid] ? 0 : 1;
-                S.tr_over[tid] = 0;
-                const bool fb = R.surrogate && S.tr_flag[tid];
-                if (!fb) {
+            // per-trajectory energy: one warp per trajectory, strided partial sums and a
+            // butterfly (FP64, fixed order)
+            {
+                const int warp = tid >> 5, lane = tid & 31, nw = blockDim.x >> 5;
+                for (int s = warp; s < pd.y; s += nw) {
+                    const int t = S.tr_t[s];
+                    if (mode == 2 && B.status[t] != kStatusRunning) continue;
                     double e = 0.0;
-                    for (int k = 0; k < S.tr_n[tid]; ++k) e += S.ea[S.tr_st[tid] + k];
-                    B.epot[bead] = e * kHa2eVR;
-                } else {
-                    B.epot[bead] = 0.0;
+                    for (int k = lane; k < S.tr_n[s]; k += 32) e += S.ea[S.tr_st[s] + k];
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
+                    if (lane == 0) {
+                        const int bead = B.bead_off[t];
+                        if (S.tr_rebuild[s]) X.skok[bead] = S.tr_over[s] ? 0 : 1;
+                        S.tr_over[s] = 0;
+                        B.epot[bead] = (R.surrogate && S.tr_flag[s]) ? 0.0 : e * kHa2eVR;
+                    }
                 }
             }
             if (active) {
