@@ -61,6 +61,9 @@ def parse():
     ap.add_argument("--model", default=str(ROOT / "md_tian2_gb300" / "data" / "surrogate_radial.npz"))
     ap.add_argument("--margin", type=float, default=0.1, help="descriptor range margin before the EMT fallback")
     ap.add_argument("--rmse-traj", type=int, default=256)
+    ap.add_argument("--scatter-traj", type=int, default=4096,
+                    help="trajectories of the whole-run scattering comparison (0: skip)")
+    ap.add_argument("--scatter-steps", type=int, default=10000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     return ap.parse_args()
@@ -288,6 +291,45 @@ def timed_steps(eng, sp, precision, steps, stream, torch, dist=None, clock_index
     return ev0.elapsed_time(ev1), (clk.summary() if clk else None)
 
 
+def scattering_comparison(args, model, device):
+    """Config-2 trajectories from identical initial states run to their exit (pul) or the
+    step limit with the surrogate (FP32 kernels, EMT fallback) and with plain FP64 EMT:
+    the analysis script's observables, their two-sample comparison and the wall time of
+    each whole run (time to solution)."""
+    import time as _time
+
+    from md_tian2_gb300 import workloads as W
+    from md_tian2_gb300.engine import PES_EMT, PES_SURROGATE, Engine, SimParams
+    from md_tian2_gb300.scatter import compare, run_to_exit
+    us = W.config2(args.scatter_traj, seed=7)
+    sp = SimParams(step=0.1, gamma_const=1e-3, Tsurf=300.0, Tproj=300.0, seed=2024, pul=6.05, use_exit=True)
+    res, wall, fb = {}, {}, 0
+    for kind, prec in ((PES_SURROGATE, "fp32"), (PES_EMT, "fp64")):
+        eng = Engine(device)
+        eng.read_emt(W.emt_params())
+        eng.define(us)
+        eng.read_nene(model, ["H", "Au"], max_neighbors=80)
+        eng.set_pes(kind, args.margin)
+        eng.upload()
+        eng.synchronize()
+        t0 = _time.perf_counter()
+        res[kind] = run_to_exit(eng, sp, precision=prec, max_steps=args.scatter_steps, chunk=1000)
+        eng.synchronize()
+        wall[kind] = _time.perf_counter() - t0
+        if kind == PES_SURROGATE:
+            fb = int(eng.nn_stats()[0].sum())
+        eng.close()
+    s, e = res[PES_SURROGATE], res[PES_EMT]
+    return {"trajectories": args.scatter_traj, "max_steps": args.scatter_steps,
+            "surrogate": s.summary(), "emt_fp64": e.summary(), "compare": compare(s, e),
+            "wall_s": {"surrogate": wall[PES_SURROGATE], "emt_fp64": wall[PES_EMT]},
+            "time_to_solution_speedup": wall[PES_EMT] / wall[PES_SURROGATE],
+            "surrogate_emt_fallbacks": fb, "surrogate_bead_steps": int(s.steps.sum()),
+            "definitions": "scripts/analysis/2_AnalyzePESTrajectory2.12.py:171-183 (eloss, scattered, transmitted "
+                           "below -7.276 A, adsorbed = sticking); mean eloss over scattered; z = difference / "
+                           "combined standard error; two-sample KS on scattered eloss"}
+
+
 def run_ours(args):
     import ctypes as ct
 
@@ -401,6 +443,11 @@ def run_ours(args):
                "sample": f"{args.rmse_traj} config-2 trajectories (seed {4242 + rank}) propagated with FP64 EMT, "
                          "sampled every 50 steps x 8; network forces (no fallback) vs FP64 EMT forces"}
 
+    # ---- scattering observables: whole trajectories to exit, surrogate vs FP64 EMT ----------
+    obs = None
+    if rank == 0 and args.scatter_traj > 0:
+        obs = scattering_comparison(args, model, local)
+
     peak = ct.c_double()
     lib.mdt_peak_fma(1, 20000, ct.byref(peak))
     peak64 = ct.c_double()
@@ -451,6 +498,7 @@ def run_ours(args):
             "accuracy": acc,
             "fallback": {"bead_evaluations": bead_evals, "emt_fallbacks": fb_count,
                          "fraction": fb_count / max(1, bead_evals)},
+            "scattering": obs,
             "clocks": clocks,
             "e2e": {"value": e_atoms_all / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": int(launches),

@@ -373,6 +373,30 @@ def load_npz(path) -> NNModel:
                    normnodes=bool(o[2]), atom_energy=ae, eshort=(float(fo[3]), float(fo[4])))
 
 
+def rescale_first_layer(model: NNModel, old_smin: list, old_smax: list) -> None:
+    """After the scaling columns of a scaled network changed from (old_smin, old_smax) to
+    the model's current ones, change its first-layer weights and biases so that the
+    network computes the same function of the raw symmetry functions: with scaled
+    x = a G + b (scale_symmetry_functions, no centring), x_old = k x_new + c with
+    k = a_old / a_new and c = b_old - k b_new, folded into W1 and b1."""
+    if model.centersym or not model.scalesym:
+        raise ValueError("rescale_first_layer needs scale_symmetry_functions without centring")
+    span = model.scmax - model.scmin
+    for e in range(model.nelem):
+        n0, n1 = model.nodes[e][0], model.nodes[e][1]
+        a_o = span / (np.asarray(old_smax[e]) - np.asarray(old_smin[e]))
+        b_o = model.scmin - a_o * np.asarray(old_smin[e])
+        a_n = span / (np.asarray(model.smax[e]) - np.asarray(model.smin[e]))
+        b_n = model.scmin - a_n * np.asarray(model.smin[e])
+        k = a_o / a_n
+        c = b_o - k * b_n
+        w = np.asarray(model.weights[e], dtype=np.float64).copy()
+        W = w[:n0 * n1].reshape(n0, n1)
+        w[n0 * n1:n0 * n1 + n1] += c @ W
+        w[:n0 * n1] = (W * k[:, None]).reshape(-1)
+        model.weights[e] = w
+
+
 def set_scaling(model: NNModel, G: np.ndarray, elem: np.ndarray, margin: float = 0.0) -> None:
     """Fill scaling.data columns (min, max, average per element and function) from raw
     descriptors G (rows = atoms) the way RuNNer's scaling mode does, and switch on

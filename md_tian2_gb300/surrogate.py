@@ -78,7 +78,9 @@ class Trainer:
     """Holds a training set on the GPU (one configuration per batch trajectory)."""
 
     def __init__(self, data: Dataset, model: nene.NNModel, device: int = 0, scale_margin: float = 0.0,
-                 max_neighbors: int = 0):
+                 max_neighbors: int = 0, keep_function: bool = False):
+        """keep_function: the model is already trained (warm start); its first layer is
+        changed with the new scaling so that it starts from the same function."""
         self.data = data
         self.model = model
         self.eng = Engine(device)
@@ -89,7 +91,10 @@ class Trainer:
         self.eng.set_pes(PES_NENE, 0.0)
         G = self.eng.nn_descriptors()
         elem = np.concatenate([[model.elements.index(u.names[i - 1]) for i in u.idx] for u in data.universes])
+        old = ([np.array(x) for x in model.smin], [np.array(x) for x in model.smax]) if keep_function else None
         nene.set_scaling(model, G, elem, margin=scale_margin)
+        if old is not None:
+            nene.rescale_first_layer(model, *old)
         self.eng.read_nene(model, data.universes[0].names, max_neighbors=max_neighbors)
         self.eng.set_pes(PES_NENE, 0.0)
         forces = np.concatenate([f.reshape(-1) for f in data.forces])

@@ -17,7 +17,7 @@ from pathlib import Path
 import numpy as np
 
 from . import nene
-from .surrogate import Trainer, force_rmse, generate_dataset, surrogate_model
+from .surrogate import Dataset, Trainer, force_rmse, generate_dataset, surrogate_model
 
 
 def main(argv=None):
@@ -37,19 +37,29 @@ def main(argv=None):
     ap.add_argument("--descriptor", choices=("acsf", "radial"), default="acsf")
     ap.add_argument("--max-neighbors", type=int, default=80)
     ap.add_argument("--seed", type=int, default=11)
+    ap.add_argument("--long-samples", type=int, default=0,
+                    help="extra samples per trajectory taken every --long-every steps (late-time coverage)")
+    ap.add_argument("--long-every", type=int, default=400)
+    ap.add_argument("--init", default=None, help="warm start from this .npz model (same descriptor)")
     a = ap.parse_args(argv)
     log = lambda m: print(m, file=sys.stderr, flush=True)  # noqa: E731
     t0 = time.perf_counter()
     data = generate_dataset(a.ntraj, a.nsamples, a.every, seed=7)
+    if a.long_samples > 0:
+        late = generate_dataset(a.ntraj, a.long_samples, a.long_every, seed=8)
+        data = Dataset(data.universes + late.universes, np.concatenate([data.energy, late.energy]),
+                       data.forces + late.forces)
     t_data = time.perf_counter() - t0
     log(f"dataset: {len(data.universes)} configurations, {sum(u.natoms for u in data.universes)} atoms, {t_data:.1f} s")
-    model = surrogate_model(a.seed, descriptor=a.descriptor)
+    model = nene.load_npz(a.init) if a.init else surrogate_model(a.seed, descriptor=a.descriptor)
     t1 = time.perf_counter()
-    tr = Trainer(data, model, scale_margin=a.scale_margin, max_neighbors=a.max_neighbors)
+    tr = Trainer(data, model, scale_margin=a.scale_margin, max_neighbors=a.max_neighbors, keep_function=bool(a.init))
     t_setup = time.perf_counter() - t1
     hist = tr.train(epochs=a.epochs, batch=a.batch, lr=a.lr, lr_final=a.lr_final, w_energy=a.w_energy,
                     w_force=a.w_force, time_budget=a.time_budget, log=log)
-    report = {"descriptor": a.descriptor, "max_neighbors": a.max_neighbors, "configs": len(data.universes), "atoms": int(sum(u.natoms for u in data.universes)),
+    report = {"descriptor": a.descriptor, "init": Path(a.init).name if a.init else None,
+              "samples": {"every": a.every, "nsamples": a.nsamples, "long_every": a.long_every,
+                          "long_samples": a.long_samples}, "max_neighbors": a.max_neighbors, "configs": len(data.universes), "atoms": int(sum(u.natoms for u in data.universes)),
               "dataset_s": t_data, "setup_s": t_setup, "train_s": tr.seconds, "steps": tr.steps,
               "atoms_per_s": tr.atoms_trained / tr.seconds, "train_force_rmse_last": hist[-1][2],
               "train_energy_rmse_last": hist[-1][1]}
