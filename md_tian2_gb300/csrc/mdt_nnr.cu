@@ -57,7 +57,10 @@ struct SmemR {
     float *w;                            // weight blocks of the elements
     float4 *scal;                        // [e][q]: scaled = x g + y, range [z, w]
     float *dscal;                        // [e][q]
-    int *tr_t, *tr_st, *tr_n, *tr_flag, *tr_rebuild, *tr_d2, *tr_over;
+    int *tr_t, *tr_st, *tr_n;
+    // per-step flags, buffered by step (step & 1; tr_stat by step % 3): descriptors out of
+    // range, largest squared displacement, skin-list overflow, running during the step
+    int *tr_flag, *tr_d2, *tr_over, *tr_stat;
     float *tr_lat;                       // [s][24]: lattice rows (9), inverse rows (9), skin half-widths (3)
     double *red;
     int *misc;                           // [0] pack, [1] trajectories, [2] running trajectories
@@ -74,7 +77,7 @@ __host__ __device__ constexpr size_t smem_r(int nin, int nh) {
     return 6 * r16r(4 * (size_t)kRS) + r16r(12 * (size_t)kRS) + r16r(8 * (size_t)kRS) + r16r(64 * (size_t)kRS) +
            r16r(8 * (size_t)kRS) + r16r(kRS) +
            r16r(4 * (size_t)nnr_hbw(nin, nh) * kRS) + r16r(4 * (size_t)nnr_wtotal(nin, nh)) + r16r(16 * 2 * (size_t)nin) +
-           r16r(4 * 2 * (size_t)nin) + 7 * r16r(4 * kRMaxTraj) + r16r(4 * 24 * kRMaxTraj) + r16r(8 * 64) + r16r(16);
+           r16r(4 * 2 * (size_t)nin) + 3 * r16r(4 * kRMaxTraj) + 3 * r16r(8 * kRMaxTraj) + r16r(12 * kRMaxTraj) + r16r(4 * 24 * kRMaxTraj) + r16r(8 * 64) + r16r(16);
 }
 
 template <int NIN, int NH>
@@ -105,10 +108,10 @@ __device__ __forceinline__ SmemR carve_r(unsigned char *base) {
     s.tr_t = (int *)take(4 * kRMaxTraj);
     s.tr_st = (int *)take(4 * kRMaxTraj);
     s.tr_n = (int *)take(4 * kRMaxTraj);
-    s.tr_flag = (int *)take(4 * kRMaxTraj);
-    s.tr_rebuild = (int *)take(4 * kRMaxTraj);
-    s.tr_d2 = (int *)take(4 * kRMaxTraj);
-    s.tr_over = (int *)take(4 * kRMaxTraj);
+    s.tr_flag = (int *)take(8 * kRMaxTraj);
+    s.tr_d2 = (int *)take(8 * kRMaxTraj);
+    s.tr_over = (int *)take(8 * kRMaxTraj);
+    s.tr_stat = (int *)take(12 * kRMaxTraj);
     s.tr_lat = (float *)take(4 * 24 * kRMaxTraj);
     s.red = (double *)take(8 * 64);
     s.misc = (int *)take(16);
@@ -451,7 +454,7 @@ __device__ __forceinline__ float nnr_network(const RadialNN &R, const SmemR &S, 
 // per function)
 template <int KA, int KB, int NH, int BLA, int BLB>
 __device__ __forceinline__ double nnr_atom(const RadialNN &R, const NNScratch &X, const SmemR &S, const AtomR &A,
-                                           int tid, bool do_forces, float &fix, float &fiy, float &fiz) {
+                                           int tid, bool do_forces, int *flag, float &fix, float &fiy, float &fiz) {
     constexpr int KT = KA + KB, bs = kRS;
     const unsigned *sk = reinterpret_cast<const unsigned *>(X.skw) + A.base * X.skcap;
     const int cnt = R.skin > 0.f ? X.skcnt[A.base + A.i] : -1;
@@ -502,7 +505,7 @@ __device__ __forceinline__ double nnr_atom(const RadialNN &R, const NNScratch &X
             out |= G[q] < c.z || G[q] > c.w;
             S.hb[q * bs + tid] = fmaf(c.x, G[q], c.y);
         }
-        if (out) S.tr_flag[A.s] = 1;
+        if (out) flag[A.s] = 1;
     }
     const float e = nnr_network<KT, NH>(R, S, A.ei, tid, do_forces);
     const double ea = (double)e + R.atom_energy[A.ei];
@@ -715,7 +718,13 @@ __global__ void __launch_bounds__(kRBlockMax, 1)
             const int t = ptraj[pd.x + tid];
             S.tr_t[tid] = t;
             S.tr_n[tid] = B.natoms[t];
-            S.tr_over[tid] = 0;
+            const int run = (mode != 2 || B.status[t] == kStatusRunning) ? 1 : 0;
+            for (int b = 0; b < 2; ++b) {
+                S.tr_over[b * kRMaxTraj + tid] = 0;
+                S.tr_flag[b * kRMaxTraj + tid] = 0;
+                S.tr_d2[b * kRMaxTraj + tid] = 0;
+            }
+            for (int b = 0; b < 3; ++b) S.tr_stat[b * kRMaxTraj + tid] = run;
             double lat[18];
             acsf_lattice(B.box + 9 * t, lat);
             float *T = S.tr_lat + 24 * tid;
@@ -760,24 +769,26 @@ __global__ void __launch_bounds__(kRBlockMax, 1)
             S.im[tid] = 1.0 / B.mass[T.aoff + A.i];
             if (mode == 2 && A.algo == kPropLangevinConst) lc_setup(B, P, T, A.i, S.lc + tid, bs);
         }
+        const int steps0 = A.s >= 0 ? B.steps_done[T.t] : 0;
+        __syncthreads();  // pack set-up read before any thread of the pack writes state
+        // Two CTA barriers per MD step: (A) positions and this step's flags written, before
+        // neighbours read them; (B) forces accumulated, before they are read.  The exit test
+        // needs only the positions after the first half-step, so the projectile's thread
+        // decides whether its trajectory runs the next step before (A).
         const int steps = mode == 2 ? nsteps : 1;
         for (int step_i = 0; step_i < steps; ++step_i) {
-            __syncthreads();  // status and step counters of the previous step are visible
-            // ---- first half-step and positions --------------------------------------
-            bool active = A.s >= 0;
-            int step = 0;
-            if (active && mode == 2) {
-                active = B.status[T.t] == kStatusRunning;
-                step = B.steps_done[T.t] + 1;
-            }
-            if (tid < pd.y) {
-                S.tr_flag[tid] = 0;
-                S.tr_d2[tid] = 0;
-            }
-            if (tid == 0) S.misc[2] = 0;
-            __syncthreads();
+            const int cur = step_i & 1, nxt = cur ^ 1;
+            const int *stat = S.tr_stat + (step_i % 3) * kRMaxTraj;
+            bool any = false;
+            for (int s = 0; s < pd.y; ++s) any |= stat[s] != 0;
+            if (!any) break;  // every trajectory of the pack has stopped (uniform: flags are stable)
+            const bool active = A.s >= 0 && stat[A.s] != 0;
+            const int step = steps0 + step_i + 1;
+            int *flag = S.tr_flag + cur * kRMaxTraj;
+            int *d2 = S.tr_d2 + cur * kRMaxTraj;
+            int *over = S.tr_over + cur * kRMaxTraj;
+            // ---- first half-step, positions, exit decision ------------------------------
             if (active) {
-                S.misc[2] = 1;
                 if (mode == 2) {
                     if (A.algo == kPropVerlet) verlet_half(B, P, T, A.i, true);
                     else lc_half1(B, P, T, A.i, step, S.lc + tid, bs);
@@ -800,63 +811,78 @@ __global__ void __launch_bounds__(kRBlockMax, 1)
                 if (R.skin > 0.f) {
                     const double *r0 = X.skref + 3 * k;
                     const float ddx = (float)(rx - r0[0]), ddy = (float)(ry - r0[1]), ddz = (float)(rz - r0[2]);
-                    atomicMax(&S.tr_d2[A.s], __float_as_int(ddx * ddx + ddy * ddy + ddz * ddz));
+                    atomicMax(&d2[A.s], __float_as_int(ddx * ddx + ddy * ddy + ddz * ddz));
                 }
+            }
+            if (A.s >= 0 && A.i == 0) {
+                // the exit test of md_tian2.f90:88-92 on the projectile (atom 0); positions do
+                // not change in the second half-step
+                int run_next = active ? 1 : 0;
+                if (active && mode == 2) {
+                    B.steps_done[T.t] = step;
+                    if (P.use_exit && B.is_proj[B.type[T.aoff]]) {
+                        const double z = B.rz[T.base];
+                        if (z > P.pul) {
+                            B.status[T.t] = kStatusExitUpper;
+                            run_next = 0;
+                        } else if (z < P.pll) {
+                            B.status[T.t] = kStatusExitLower;
+                            run_next = 0;
+                        }
+                    }
+                }
+                S.tr_stat[((step_i + 1) % 3) * kRMaxTraj + A.s] = run_next;
             }
             S.f3[tid] = 0.f;
             S.f3[bs + tid] = 0.f;
             S.f3[2 * bs + tid] = 0.f;
-            __syncthreads();
-            if (S.misc[2] == 0) break;  // every trajectory of the pack has stopped
-            // skin lists rebuilt when invalid or when some atom moved more than half the skin
-            // (positions in A; the skin is in bohr)
+            __syncthreads();  // (A)
             if (tid < pd.y) {
-                const int bead = B.bead_off[S.tr_t[tid]];
-                const float half = 0.5f * R.skin * (float)kBohr2Ang;
-                S.tr_rebuild[tid] =
-                    R.skin > 0.f && (X.skok[bead] == 0 || __int_as_float(S.tr_d2[tid]) > half * half) ? 1 : 0;
+                S.tr_flag[nxt * kRMaxTraj + tid] = 0;
+                S.tr_d2[nxt * kRMaxTraj + tid] = 0;
+                S.tr_over[nxt * kRMaxTraj + tid] = 0;
             }
-            __syncthreads();
-            // ---- forces ------------------------------------------------------------------
+            // ---- forces; skin lists rebuilt when invalid or when some atom of the
+            // trajectory moved more than half the skin (displacements in A, skin in bohr) ----
+            const float half = 0.5f * R.skin * (float)kBohr2Ang;
             float fix = 0.f, fiy = 0.f, fiz = 0.f;
-            double ea = 0.0;
             if (active) {
-                if (S.tr_rebuild[A.s]) {
-                    const int64_t k = A.base + A.i;
+                const int64_t k = A.base + A.i;
+                const int bead = B.bead_off[T.t];
+                if (R.skin > 0.f && (X.skok[bead] == 0 || __int_as_float(d2[A.s]) > half * half)) {
                     const int c = build_skin(R, S, A, reinterpret_cast<unsigned *>(X.skw) + A.base * X.skcap, X.skcap);
                     X.skcnt[k] = c;
-                    if (c < 0) S.tr_over[A.s] = 1;
+                    if (c < 0) over[A.s] = 1;
                     double *r0 = X.skref + 3 * k;
                     r0[0] = B.rx[k];
                     r0[1] = B.ry[k];
                     r0[2] = B.rz[k];
                 }
-                ea = nnr_atom<KA, KB, NH, BLA, BLB>(R, X, S, A, tid, do_forces, fix, fiy, fiz);
-                S.ea[tid] = ea;
+                S.ea[tid] = nnr_atom<KA, KB, NH, BLA, BLB>(R, X, S, A, tid, do_forces, flag, fix, fiy, fiz);
             }
-            __syncthreads();
-            // per-trajectory energy: one warp per trajectory, strided partial sums and a
-            // butterfly (FP64, fixed order)
+            __syncthreads();  // (B)
+            // per-trajectory energy and skin-list state: one warp per trajectory, strided FP64
+            // partial sums and a butterfly (fixed order)
             {
                 const int warp = tid >> 5, lane = tid & 31, nw = blockDim.x >> 5;
                 for (int s = warp; s < pd.y; s += nw) {
+                    if (!stat[s]) continue;
                     const int t = S.tr_t[s];
-                    if (mode == 2 && B.status[t] != kStatusRunning) continue;
                     double e = 0.0;
                     for (int k = lane; k < S.tr_n[s]; k += 32) e += S.ea[S.tr_st[s] + k];
 #pragma unroll
                     for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
                     if (lane == 0) {
                         const int bead = B.bead_off[t];
-                        if (S.tr_rebuild[s]) X.skok[bead] = S.tr_over[s] ? 0 : 1;
-                        S.tr_over[s] = 0;
-                        B.epot[bead] = (R.surrogate && S.tr_flag[s]) ? 0.0 : e * kHa2eVR;
+                        if (R.skin > 0.f && (X.skok[bead] == 0 || __int_as_float(d2[s]) > half * half))
+                            X.skok[bead] = over[s] ? 0 : 1;
+                        B.epot[bead] = (R.surrogate && flag[s]) ? 0.0 : e * kHa2eVR;
                     }
                 }
             }
             if (active) {
                 const int64_t k = A.base + A.i;
-                const bool fb = R.surrogate && S.tr_flag[A.s];
+                const bool fb = R.surrogate && flag[A.s];
                 const double c = kHa2eVR * kAng2BohrD;
                 double fx = 0.0, fy = 0.0, fz = 0.0;
                 if (do_forces && !fb) {
@@ -875,42 +901,32 @@ __global__ void __launch_bounds__(kRBlockMax, 1)
             }
             // ---- EMT for the trajectories whose descriptors left the training range ----------
             if (R.surrogate) {
-                __syncthreads();
-                for (int s = 0; s < pd.y; ++s) {
-                    const int t = S.tr_t[s];
-                    if (!S.tr_flag[s] || (mode == 2 && B.status[t] != kStatusRunning)) continue;
+                bool anyfb = false;
+                for (int s = 0; s < pd.y; ++s) anyfb |= stat[s] && flag[s];
+                if (anyfb) {  // uniform over the CTA
                     __syncthreads();
-                    emt_bead<double>(B, E, SE, t, 0, do_forces);
-                    if (tid == 0) X.fallback[t] += 1;
-                    if (A.s == s && do_forces) {
-                        const int64_t k = A.base + A.i;
-                        const double m = B.mass[T.aoff + A.i];
-                        const uint8_t fxd = B.fixed[k];
-                        if (!(fxd & 1)) B.ax[k] = B.fx[k] / m;
-                        if (!(fxd & 2)) B.ay[k] = B.fy[k] / m;
-                        if (!(fxd & 4)) B.az[k] = B.fz[k] / m;
+                    for (int s = 0; s < pd.y; ++s) {
+                        if (!stat[s] || !flag[s]) continue;
+                        const int t = S.tr_t[s];
+                        __syncthreads();
+                        emt_bead<double>(B, E, SE, t, 0, do_forces);
+                        if (tid == 0) X.fallback[t] += 1;
+                        if (A.s == s && do_forces) {
+                            const int64_t k = A.base + A.i;
+                            const double m = B.mass[T.aoff + A.i];
+                            const uint8_t fxd = B.fixed[k];
+                            if (!(fxd & 1)) B.ax[k] = B.fx[k] / m;
+                            if (!(fxd & 2)) B.ay[k] = B.fy[k] / m;
+                            if (!(fxd & 4)) B.az[k] = B.fz[k] / m;
+                        }
+                        __syncthreads();
                     }
-                    __syncthreads();
                 }
             }
-            // ---- second half-step and exit test ---------------------------------------------
+            // ---- second half-step ------------------------------------------------------------
             if (active && mode == 2) {
                 if (A.algo == kPropVerlet) verlet_half(B, P, T, A.i, false);
                 else lc_half2(B, P, T, A.i, step, S.lc + tid, bs);
-            }
-            __syncthreads();
-            if (mode == 2 && tid < pd.y) {
-                const int t = S.tr_t[tid];
-                if (B.status[t] == kStatusRunning) {
-                    const TrajView V = traj_view(B, t);
-                    B.steps_done[t] = B.steps_done[t] + 1;
-                    const int ty0 = B.type[V.aoff];
-                    if (P.use_exit && B.is_proj[ty0]) {
-                        const double z = B.rz[V.base];
-                        if (z > P.pul) B.status[t] = kStatusExitUpper;
-                        else if (z < P.pll) B.status[t] = kStatusExitLower;
-                    }
-                }
             }
         }
     }
