@@ -119,6 +119,14 @@ module mdt_gpu
             type(mdt_traj_summary), intent(out) :: out(*)
         end function
 
+        integer(c_int32_t) function mdt_traj_observables(ctx, turn_pnts, cl_appr, cl_appr_step, r_min_p) &
+                bind(C, name="mdt_traj_observables")
+            import :: c_int32_t, c_ptr, c_double
+            type(c_ptr), value :: ctx
+            integer(c_int32_t), intent(out) :: turn_pnts(*), cl_appr_step(*)
+            real(c_double), intent(out) :: cl_appr(*), r_min_p(*)
+        end function
+
         integer(c_int32_t) function mdt_set_pes(ctx, pes_kind, range_margin) bind(C, name="mdt_set_pes")
             import :: c_int32_t, c_ptr, c_double
             type(c_ptr), value :: ctx

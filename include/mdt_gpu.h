@@ -243,6 +243,18 @@ int32_t mdt_md_steps(mdt_ctx *ctx, int32_t nsteps, int32_t precision, const mdt_
 int32_t mdt_set_random_arrays(mdt_ctx *ctx, const double *randy, const double *zeta, const double *andersen_v,
                               const double *andersen_u);
 
+/* Trajectory observables of collect_trajectory_characteristics (src/trajectory_info.f90:
+   47-75, 92-132, 243-250), tracked on the device by the fused MD steps (mdt_md_steps) after
+   every step and reset by mdt_state_upload: per trajectory the turning points of the
+   projectile centroid's z velocity, the closest approach (A) of the projectile (atom 0) to
+   any other atom (minimum image of the centroids; the FP32 radial kernel takes the nearest
+   entry of its neighbour list, within cutoff + skin) and the step at which it was first
+   reached, and the lowest projectile centroid position r_min_p[3*t .. 3*t+2].  Any output
+   may be NULL.  The reference's closest-approach time (the step times `step` once per
+   later collect) follows from cl_appr_step on the host. */
+int32_t mdt_traj_observables(mdt_ctx *ctx, int32_t *turn_pnts, double *cl_appr, int32_t *cl_appr_step,
+                             double *r_min_p);
+
 /* per-trajectory status, steps and energies (output_mod.f90:658-697 fields) */
 int32_t mdt_query(mdt_ctx *ctx, const mdt_prop_params *p, mdt_traj_summary *out);
 

@@ -76,6 +76,7 @@ SIGNATURES = {
     "mdt_nn_fast_path": (ct.c_int32, [ct.c_void_p, ct.c_int32]),
     "mdt_nn_radial_kernel": (ct.c_int32, [ct.c_void_p, ct.c_int32]),
     "mdt_nn_radial_block": (ct.c_int32, [ct.c_void_p, ct.c_int32]),
+    "mdt_traj_observables": (ct.c_int32, [ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p]),
     "mdt_nn_set_skin": (ct.c_int32, [ct.c_void_p, ct.c_double]),
     "mdt_nn_stats": (ct.c_int32, [ct.c_void_p, ct.c_void_p, ct.c_void_p]),
     "mdt_nn_neighbors": (ct.c_int32, [ct.c_void_p, ct.c_void_p, ct.c_void_p]),

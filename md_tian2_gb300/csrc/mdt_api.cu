@@ -1003,6 +1003,10 @@ int32_t mdt_batch_define(mdt_ctx *c, int32_t ntraj, const int32_t *natoms, const
     ALLOC(d_cjk_off, int, ntraj);
     ALLOC(d_status, int, ntraj);
     ALLOC(d_steps, int, ntraj);
+    int *d_obs_i;
+    double *d_obs_d;
+    ALLOC(d_obs_i, int, 3 * (size_t)ntraj);
+    ALLOC(d_obs_d, double, 4 * (size_t)ntraj);
     ALLOC(d_ba_off, int64_t, ntraj);
     ALLOC(d_pair_off, int64_t, ntraj);
     ALLOC(d_mass, double, at);
@@ -1066,10 +1070,20 @@ int32_t mdt_batch_define(mdt_ctx *c, int32_t ntraj, const int32_t *natoms, const
     B.ibox = d_ibox;
     B.status = d_status;
     B.steps_done = d_steps;
+    B.obs_turn = d_obs_i;
+    B.obs_up = d_obs_i + ntraj;
+    B.obs_clstep = d_obs_i + 2 * (size_t)ntraj;
+    B.obs_cl = d_obs_d;
+    B.obs_low = d_obs_d + ntraj;
     B.cjk_off = d_cjk_off;
     B.cjk = d_cjk;
     B.pair_scratch = nullptr;
     c->scratch_prec_bytes = 0;
+    e = launch_obs_reset(c->stream, B);
+    if (e != cudaSuccess) {
+        free_batch(c);
+        return cuda_fail(c, e, "mdt_batch_define observables");
+    }
     c->have_batch = true;
     return MDT_OK;
 }
@@ -1092,6 +1106,7 @@ int32_t mdt_state_upload(mdt_ctx *c, const double *r, const double *v) {
     }
     if (e == cudaSuccess) e = cudaMemsetAsync(B.status, 0, sizeof(int) * c->T, c->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(B.steps_done, 0, sizeof(int) * c->T, c->stream);
+    if (e == cudaSuccess) e = launch_obs_reset(c->stream, B);
     return e == cudaSuccess ? MDT_OK : cuda_fail(c, e, "mdt_state_upload");
 }
 
@@ -1239,6 +1254,21 @@ int32_t mdt_md_steps(mdt_ctx *c, int32_t nsteps, int32_t precision, const mdt_pr
     cudaError_t e = launch_md_steps(cfg(c, precision), c->B, c->E, P, nsteps, precision);
     c->launches++;
     return e == cudaSuccess ? MDT_OK : cuda_fail(c, e, "mdt_md_steps");
+}
+
+int32_t mdt_traj_observables(mdt_ctx *c, int32_t *turn_pnts, double *cl_appr, int32_t *cl_appr_step,
+                             double *r_min_p) {
+    int rc = check_ready(c, false);
+    if (rc) return rc;
+    const Batch &B = c->B;
+    const size_t T = (size_t)c->T;
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e == cudaSuccess && turn_pnts) e = cudaMemcpy(turn_pnts, B.obs_turn, sizeof(int) * T, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && cl_appr) e = cudaMemcpy(cl_appr, B.obs_cl, sizeof(double) * T, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && cl_appr_step)
+        e = cudaMemcpy(cl_appr_step, B.obs_clstep, sizeof(int) * T, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && r_min_p) e = cudaMemcpy(r_min_p, B.obs_low, sizeof(double) * 3 * T, cudaMemcpyDeviceToHost);
+    return e == cudaSuccess ? MDT_OK : cuda_fail(c, e, "mdt_traj_observables");
 }
 
 int32_t mdt_query(mdt_ctx *c, const mdt_prop_params *p, mdt_traj_summary *out) {

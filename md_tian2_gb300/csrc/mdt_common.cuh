@@ -24,6 +24,7 @@ constexpr double kHbar = 0.6582119514467406;  // eV fs
 constexpr double kTwelfth = 1.0 / 12.0;
 constexpr double kTolerance = 1.0e-9;
 constexpr double kBohr2Ang = 0.529177211;
+constexpr double kDefaultReal = 1.7976931348623157e308;  // huge(0_dp), constants.f90:101
 constexpr double kAmu2Mass = 103.638239276;
 
 // propagator ids, src/constants.f90:107-112; 1007 = constant-friction Langevin
@@ -79,6 +80,12 @@ struct Batch {
     const int *cjk_off;        // per trajectory: offset of its nbeads x nbeads table
     const double *cjk;         // normal-mode tables, column major cjk(j,k)
     void *pair_scratch;        // per pair slot: dx, dy, dz, Q_ij, Q_ji, F_V (FP64 or FP32)
+    // trajectory observables of trajectory_info.f90 (projectile = atom 0), updated by the
+    // fused MD kernels after every step: turning points of the centroid's z velocity, 1
+    // while it moves up, closest approach to any other atom (A, minimum image of the
+    // centroids) with the step it was first reached, lowest centroid position (3 per traj)
+    int *obs_turn, *obs_up, *obs_clstep;
+    double *obs_cl, *obs_low;
     int max_atoms, max_beads;
     int algo[kMaxTypes];       // propagator per type
     int is_proj[kMaxTypes];

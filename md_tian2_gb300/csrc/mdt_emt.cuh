@@ -106,6 +106,19 @@ static __device__ __noinline__ double block_sum(double v, double *red) {
     return t;
 }
 
+// Block-wide minimum of a double; every thread gets the result.
+static __device__ __noinline__ double block_min(double v, double *red) {
+    for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    __syncthreads();
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    double m = red[0];
+    for (int w = 1; w < nw; ++w) m = fmin(m, red[w]);
+    __syncthreads();
+    return m;
+}
+
 // Cell of one trajectory: FP64 matrix for applying image shifts, FP32 inverse for
 // choosing them.  Column major (cell vectors as columns).
 struct Cell {

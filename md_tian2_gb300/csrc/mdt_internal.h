@@ -39,6 +39,8 @@ int nnf_resident_ctas(const Batch &B, const NNDev &M, const FastNN &F);
 cudaError_t launch_nnf(const LaunchCfg &c, const Batch &B, const NNDev &M, const FastNN &F, const EmtConst &E,
                        const NNScratch &X, const PropParams &P, int nsteps, int mode, bool surrogate);
 
+cudaError_t launch_obs_reset(cudaStream_t s, const Batch &B);
+
 // FP32 thread-per-atom kernel of radial-only models (mdt_nnr.cu)
 // shape of a model (group counts, hidden layers; maxbl[g] = longest recurrence block group g
 // admits, 0 = none): sets R.ka, R.kb, R.bla, R.blb

@@ -110,6 +110,10 @@ __global__ void __launch_bounds__(kBlock, 4) md_steps_kernel(Batch B, EmtConst E
             propagate_1(B, P, T, S.cjk, step, S.red);
             calc_force<R>(B, E, P, S, T, true);
             propagate_2(B, P, T, step);
+            {
+                const double dmin = closest_approach_step(B, T, S.cell, S.red);
+                if (threadIdx.x == 0) observe_step(B, T, step, dmin);
+            }
             if (threadIdx.x == 0) {
                 B.steps_done[t] = step;
                 if (P.use_exit && B.is_proj[ty0] && B.status[t] == kStatusRunning) {
@@ -126,6 +130,24 @@ __global__ void __launch_bounds__(kBlock, 4) md_steps_kernel(Batch B, EmtConst E
             __syncthreads();
         }
     }
+}
+
+// trajectory observables at their initial values (trajectory_info.f90:55-70)
+__global__ void obs_reset_kernel(Batch B) {
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < B.ntraj; t += gridDim.x * blockDim.x) {
+        B.obs_turn[t] = 0;
+        B.obs_up[t] = 0;
+        B.obs_clstep[t] = 0;
+        B.obs_cl[t] = kDefaultReal;
+        B.obs_low[3 * t] = kDefaultReal;
+        B.obs_low[3 * t + 1] = kDefaultReal;
+        B.obs_low[3 * t + 2] = kDefaultReal;
+    }
+}
+
+cudaError_t launch_obs_reset(cudaStream_t s, const Batch &B) {
+    obs_reset_kernel<<<(B.ntraj + 255) / 256, 256, 0, s>>>(B);
+    return cudaGetLastError();
 }
 
 // Fortran-order host layout (3, nb, N) per trajectory <-> SoA device layout.

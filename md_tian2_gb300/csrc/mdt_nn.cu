@@ -331,6 +331,10 @@ __global__ void __launch_bounds__(kNNBlock) nn_md_steps_kernel(Batch B, NNDev M,
             propagate_1(B, P, T, SE.cjk, step, SE.red);
             nn_calc_force<R, SURR>(B, M, E, X, P, S, SE, T, true);
             propagate_2(B, P, T, step);
+            {
+                const double dmin = closest_approach_step(B, T, SE.cell, SE.red);
+                if (threadIdx.x == 0) observe_step(B, T, step, dmin);
+            }
             if (threadIdx.x == 0) {
                 B.steps_done[t] = step;
                 if (P.use_exit && B.is_proj[ty0] && B.status[t] == kStatusRunning) {

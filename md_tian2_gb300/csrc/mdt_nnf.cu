@@ -1249,6 +1249,10 @@ __global__ void __launch_bounds__(kFBlock, 3)
             propagate_1(B, P, T, S.cjk, step, S.red);
             nnf_calc_force<NG, ZM, G3ON>(B, M, F, E, X, P, S, SE, L, T, true);
             propagate_2(B, P, T, step);
+            {
+                const double dmin = closest_approach_step(B, T, SE.cell, SE.red);
+                if (threadIdx.x == 0) observe_step(B, T, step, dmin);
+            }
             if (threadIdx.x == 0) {
                 B.steps_done[t] = step;
                 if (P.use_exit && B.is_proj[ty0] && B.status[t] == kStatusRunning) {

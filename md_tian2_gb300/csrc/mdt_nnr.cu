@@ -454,7 +454,8 @@ __device__ __forceinline__ float nnr_network(const RadialNN &R, const SmemR &S, 
 // per function)
 template <int KA, int KB, int NH, int BLA, int BLB>
 __device__ __forceinline__ double nnr_atom(const RadialNN &R, const NNScratch &X, const SmemR &S, const AtomR &A,
-                                           int tid, bool do_forces, int *flag, float &fix, float &fiy, float &fiz) {
+                                           int tid, bool do_forces, int *flag, float &rmin2, float &fix, float &fiy,
+                                           float &fiz) {
     constexpr int KT = KA + KB, bs = kRS;
     const unsigned *sk = reinterpret_cast<const unsigned *>(X.skw) + A.base * X.skcap;
     const int cnt = R.skin > 0.f ? X.skcnt[A.base + A.i] : -1;
@@ -467,6 +468,7 @@ __device__ __forceinline__ double nnr_atom(const RadialNN &R, const NNScratch &X
         constexpr int K = g == 0 ? KA : KB, off = g == 0 ? 0 : KA, BL = g == 0 ? BLA : BLB;
         const bool inside = r2 < R.rc2;
         nn += inside ? 1 : 0;
+        rmin2 = fminf(rmin2, r2);
         const float r = r2 * rsqrtf(r2);
         const float fc = inside ? fc_of_s(r2 * R.inv_rc2) : 0.f;
         if constexpr (BL > 0) {
@@ -846,6 +848,7 @@ __global__ void __launch_bounds__(kRBlockMax, 1)
             // trajectory moved more than half the skin (displacements in A, skin in bohr) ----
             const float half = 0.5f * R.skin * (float)kBohr2Ang;
             float fix = 0.f, fiy = 0.f, fiz = 0.f;
+            float rmin2 = INFINITY;  // nearest neighbour entry (bohr^2): the closest approach of atom 0
             if (active) {
                 const int64_t k = A.base + A.i;
                 const int bead = B.bead_off[T.t];
@@ -858,7 +861,7 @@ __global__ void __launch_bounds__(kRBlockMax, 1)
                     r0[1] = B.ry[k];
                     r0[2] = B.rz[k];
                 }
-                S.ea[tid] = nnr_atom<KA, KB, NH, BLA, BLB>(R, X, S, A, tid, do_forces, flag, fix, fiy, fiz);
+                S.ea[tid] = nnr_atom<KA, KB, NH, BLA, BLB>(R, X, S, A, tid, do_forces, flag, rmin2, fix, fiy, fiz);
             }
             __syncthreads();  // (B)
             // per-trajectory energy and skin-list state: one warp per trajectory, strided FP64
@@ -927,6 +930,9 @@ __global__ void __launch_bounds__(kRBlockMax, 1)
             if (active && mode == 2) {
                 if (A.algo == kPropVerlet) verlet_half(B, P, T, A.i, false);
                 else lc_half2(B, P, T, A.i, step, S.lc + tid, bs);
+                // trajectory observables by the projectile's thread; the closest approach is
+                // the nearest entry of its skin list (every image within the cutoff + skin)
+                if (A.i == 0) observe_step(B, T, step, rmin2 < INFINITY ? (double)sqrtf(rmin2) * kBohr2Ang : kDefaultReal);
             }
         }
     }

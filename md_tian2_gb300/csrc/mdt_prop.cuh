@@ -35,6 +35,72 @@ static __device__ __forceinline__ double &comp(double *x, double *y, double *z, 
     return d == 0 ? x[k] : (d == 1 ? y[k] : z[k]);
 }
 
+// collect_trajectory_characteristics after a step (trajectory_info.f90:47-75, 113-132,
+// 243-250), by one thread: the lowest projectile centroid position, the closest approach
+// `dmin` of this step (computed by the caller) with the step at which it was first
+// reached, and a turning point whenever the sign of the centroid's z velocity changes.
+static __device__ void observe_step(const Batch &B, const TrajView &T, int step, double dmin) {
+    const int t = T.t;
+    double x = 0.0, y = 0.0, z = 0.0, vz = 0.0;
+    for (int b = 0; b < T.nb; ++b) {
+        const int64_t k = T.base + (int64_t)b * T.N;
+        x += B.rx[k];
+        y += B.ry[k];
+        z += B.rz[k];
+        vz += B.vz[k];
+    }
+    x /= T.nb;
+    y /= T.nb;
+    z /= T.nb;
+    if (z < B.obs_low[3 * t + 2]) {
+        B.obs_low[3 * t] = x;
+        B.obs_low[3 * t + 1] = y;
+        B.obs_low[3 * t + 2] = z;
+    }
+    if (dmin < B.obs_cl[t]) {
+        B.obs_cl[t] = dmin;
+        B.obs_clstep[t] = step;
+    }
+    const int down = vz / T.nb < 0.0 ? 1 : 0;
+    if (down == B.obs_up[t]) {  // moving down now and up before, or the reverse
+        B.obs_turn[t] += 1;
+        B.obs_up[t] = 1 - down;
+    }
+}
+
+// Closest approach of the projectile (atom 0) after a step: the minimum image of the
+// centroids of atom 0 and atom i over i >= 1 (trajectory_info.f90:92-105), CTA-wide
+// (every thread gets the result; `cell` and `red` are shared-memory scratch).
+static __device__ double closest_approach_step(const Batch &B, const TrajView &T, Cell *cell, double *red) {
+    __syncthreads();
+    if (threadIdx.x == 0) load_cell(B, T.t, *cell);
+    __syncthreads();
+    double c0x = 0.0, c0y = 0.0, c0z = 0.0;
+    for (int b = 0; b < T.nb; ++b) {
+        const int64_t k = T.base + (int64_t)b * T.N;
+        c0x += B.rx[k];
+        c0y += B.ry[k];
+        c0z += B.rz[k];
+    }
+    c0x /= T.nb;
+    c0y /= T.nb;
+    c0z /= T.nb;
+    double dmin = kDefaultReal;
+    for (int i = 1 + threadIdx.x; i < T.N; i += blockDim.x) {
+        double cx = 0.0, cy = 0.0, cz = 0.0;
+        for (int b = 0; b < T.nb; ++b) {
+            const int64_t k = T.base + (int64_t)b * T.N + i;
+            cx += B.rx[k];
+            cy += B.ry[k];
+            cz += B.rz[k];
+        }
+        double dx, dy, dz;
+        min_image(*cell, c0x - cx / T.nb, c0y - cy / T.nb, c0z - cz / T.nb, dx, dy, dz);
+        dmin = fmin(dmin, sqrt(dx * dx + dy * dy + dz * dz));
+    }
+    return block_min(dmin, red);
+}
+
 // verlet_1 / verlet_2, md_algo.f90:110-142
 static __device__ void verlet_half(const Batch &B, const PropParams &P, const TrajView &T, int i, bool move_r) {
     for (int b = 0; b < T.nb; ++b) {

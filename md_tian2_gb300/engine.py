@@ -250,5 +250,16 @@ class Engine:
                         dtype=[("status", "i4"), ("steps_done", "i4"), ("epot", "f8"), ("ekin_p", "f8"),
                                ("ekin_l", "f8"), ("ebead", "f8")])
 
+    def observables(self) -> dict:
+        """Per-trajectory observables of the fused MD steps (trajectory_info.f90): turning
+        points, closest approach (A) and its step, lowest projectile position (T, 3)."""
+        turn = np.zeros(self.T, np.int32)
+        cl = np.zeros(self.T)
+        clstep = np.zeros(self.T, np.int32)
+        low = np.zeros((self.T, 3))
+        self._check(self.lib.mdt_traj_observables(self.h, turn.ctypes.data, cl.ctypes.data, clstep.ctypes.data,
+                                                  low.ctypes.data), "mdt_traj_observables")
+        return {"turn_pnts": turn, "cl_appr": cl, "cl_appr_step": clstep, "r_min_p": low}
+
     def launch_count(self) -> int:
         return int(self.lib.mdt_launch_count(self.h))

@@ -14,7 +14,10 @@ over [min, max] and density normalisation, as the analysis script does (:357-411
 
 ``run_to_exit`` propagates a batch with ``mdt_md_steps`` in chunks until every
 trajectory has left through ``pul``/``pll`` or the step limit is reached (the reference's
-nsteps loop with its exit test, src/md_tian2.f90:78-92).
+nsteps loop with its exit test, src/md_tian2.f90:78-98), and collects the fields of the
+reference's per-trajectory scatter record; ``write_mxt_fin`` writes them as the
+reference's ``traj/mxt_fin%08d.dat`` files (output_scatter, src/output_mod.f90:634-697),
+which its summary scripts (scripts/analysis/1_CreateMXTSummary2.02.py) read unchanged.
 """
 from __future__ import annotations
 
@@ -41,6 +44,8 @@ class ScatterResult:
     steps: np.ndarray    # MD steps run per trajectory
     status: np.ndarray   # engine status (0 running = stopped by the step limit)
     shot_thru: float
+    # the rest of the reference's scatter record (None when not collected)
+    record: dict | None = None
 
     @property
     def eloss(self) -> np.ndarray:
@@ -96,10 +101,10 @@ def run_to_exit(eng, sp, precision: str = "fp64", max_steps: int = 10000, chunk:
     if not sp.use_exit:
         raise ValueError("run_to_exit needs SimParams.use_exit (the pul/pll exit test)")
     T = eng.T
+    eng.calc_force(sp, precision=precision)  # epot_i: output follows calc_force (md_tian2.f90:69-73)
     q0 = eng.query(sp)
-    r0 = eng.download()["r"]
-    z_i = np.array([eng.split(r0, t)[0, 0, 2] for t in range(T)])
-    eng.calc_force(sp, precision=precision)
+    o0 = eng.download()
+    z_i = np.array([eng.split(o0["r"], t)[0, 0, 2] for t in range(T)])
     done = 0
     while done < max_steps:
         n = min(chunk, max_steps - done)
@@ -108,11 +113,131 @@ def run_to_exit(eng, sp, precision: str = "fp64", max_steps: int = 10000, chunk:
         if not np.any(eng.query(sp)["status"] == 0):
             break
     q = eng.query(sp)
-    r = eng.download()["r"]
-    z_f = np.array([eng.split(r, t)[0, 0, 2] for t in range(T)])
+    o = eng.download()
+    z_f = np.array([eng.split(o["r"], t)[0, 0, 2] for t in range(T)])
+
+    def centroid(flat, t):  # projectile centroid over beads
+        return eng.split(flat, t)[0].mean(axis=0)
+
+    obs = eng.observables()
+    record = {"ekin_l_i": q0["ekin_l"].copy(), "epot_i": q0["epot"].copy(),
+              "etotal_i": q0["ekin_p"] + q0["ekin_l"] + q0["epot"] + q0["ebead"],
+              "r_i": np.array([centroid(o0["r"], t) for t in range(T)]),
+              "v_i": np.array([centroid(o0["v"], t) for t in range(T)]),
+              "ekin_l_f": q["ekin_l"].copy(), "epot_f": q["epot"].copy(),
+              "etotal_f": q["ekin_p"] + q["ekin_l"] + q["epot"] + q["ebead"],
+              "r_f": np.array([centroid(o["r"], t) for t in range(T)]),
+              "v_f": np.array([centroid(o["v"], t) for t in range(T)]),
+              "step": float(sp.step), "max_steps": int(max_steps), **obs}
     return ScatterResult(ekin_i=q0["ekin_p"].copy(), ekin_f=q["ekin_p"].copy(), z_i=z_i, z_f=z_f,
                          steps=q["steps_done"].copy(), status=q["status"].copy(),
-                         shot_thru=SHOT_THRU_LIMIT.get(metal, -np.inf))
+                         shot_thru=SHOT_THRU_LIMIT.get(metal, -np.inf), record=record)
+
+
+# ---- the reference's mxt_fin record -------------------------------------------------------
+RAD2DEG = 180.0 / math.pi
+
+
+def fortran_f(x: float, w: int = 14, d: int = 7) -> str:
+    """Fortran Fw.d."""
+    return f"{x:{w}.{d}f}"
+
+
+def fortran_e(x: float, w: int = 21, d: int = 10) -> str:
+    """Fortran Ew.d (0.ddddE+xx, d significant digits)."""
+    if x == 0.0 or not math.isfinite(x):
+        body = ("0." + "0" * d + "E+00") if x == 0.0 else str(x)
+        return body.rjust(w)
+    mant, exp = f"{abs(x):.{d - 1}e}".split("e")
+    body = "0." + mant.replace(".", "") + f"E{int(exp) + 1:+03d}"
+    return (("-" if x < 0 else "") + body).rjust(w)
+
+
+def _polar_azi(v):
+    n = math.sqrt(float(np.dot(v, v)))
+    polar = math.acos(v[2] / n) * RAD2DEG if n > 0 else float("nan")
+    return polar, math.atan2(v[1], v[0]) * RAD2DEG
+
+
+def record_times(res: ScatterResult) -> tuple[np.ndarray, np.ndarray]:
+    """time and cl_appr_time as output_scatter writes them.  The loop of md_tian2.f90:78-98
+    leaves at the exit step S (time = (S-1) dt) or runs to completion (istep = nsteps + 1,
+    time = nsteps dt, one more collect of the last configuration).  check_for_closest_approach
+    (trajectory_info.f90:103-118) sets the time to k (the step of the minimum) and multiplies
+    it by dt on every call from then on: k dt^(calls - k + 1)."""
+    rec = res.record
+    dt = rec["step"]
+    exited = res.status != 0
+    S = res.steps.astype(np.int64)
+    time = np.where(exited, (S - 1) * dt, S * dt)
+    calls = np.where(exited, S, S + 1)
+    k = rec["cl_appr_step"].astype(np.int64)
+    with np.errstate(under="ignore", over="ignore"):
+        clt = np.where(k > 0, k * np.power(dt, (calls - k + 1).astype(float)), 0.0)
+    return time, clt
+
+
+def write_mxt_fin(directory, res: ScatterResult, first_id: int = 1) -> list:
+    """One traj/mxt_fin%08d.dat file per trajectory, in output_scatter's layout
+    (src/output_mod.f90:660-697): the 8-line initial block, a blank line, the 8-line final
+    block, a blank line and time, turn_pnts, cl_appr, cl_appr_time, r_min_p."""
+    from pathlib import Path
+    rec = res.record
+    if rec is None:
+        raise ValueError("the result holds no scatter record (run_to_exit collects it)")
+    d = Path(directory)
+    d.mkdir(parents=True, exist_ok=True)
+    time, clt = record_times(res)
+    paths = []
+    for t in range(len(res.z_f)):
+        pol_i, azi_i = _polar_azi(rec["v_i"][t])
+        pol_f, azi_f = _polar_azi(rec["v_f"][t])
+        f3 = lambda v: "".join(fortran_f(x) for x in v)  # noqa: E731
+        lines = [
+            "ekin_p_i = " + fortran_f(res.ekin_i[t]),
+            "ekin_l_i = " + fortran_f(rec["ekin_l_i"][t]),
+            "epot_i   = " + fortran_e(rec["epot_i"][t]),
+            "etotal_i = " + fortran_e(rec["etotal_i"][t]),
+            "r_i      = " + f3(rec["r_i"][t]),
+            "v_i      = " + f3(rec["v_i"][t]),
+            "polar_i  = " + fortran_f(180.0 - pol_i),
+            "azi_i    = " + fortran_f(azi_i),
+            "",
+            "ekin_p_f     = " + fortran_f(res.ekin_f[t]),
+            "ekin_l_f     = " + fortran_f(rec["ekin_l_f"][t]),
+            "epot_f       = " + fortran_e(rec["epot_f"][t]),
+            "etotal_f     = " + fortran_e(rec["etotal_f"][t]),
+            "r_f          = " + f3(rec["r_f"][t]),
+            "v_f          = " + f3(rec["v_f"][t]),
+            "polar_f      = " + fortran_f(pol_f),
+            "azi_f        = " + fortran_f(azi_f),
+            "",
+            "time         = " + fortran_f(time[t]),
+            "turn_pnts    = " + f"{int(rec['turn_pnts'][t]):12d}",
+            "cl_appr      = " + fortran_f(rec["cl_appr"][t]),
+            "cl_appr_time = " + fortran_f(clt[t]),
+            "r_min_p      = " + f3(rec["r_min_p"][t]),
+        ]
+        p = d / f"mxt_fin{first_id + t:08d}.dat"
+        p.write_text("\n".join(lines) + "\n")
+        paths.append(p)
+    return paths
+
+
+def read_mxt_fin(path) -> dict:
+    """The values of one mxt_fin file, taken as the reference's summary script takes them
+    (last whitespace-separated token(s) of each line, in line order)."""
+    lines = [l for l in open(path).read().splitlines()]
+    if len(lines) != 23:
+        raise ValueError(f"{path}: {len(lines)} lines, a finished trajectory has 23")
+    tok = [l.split() for l in lines]
+    vec = lambda i: np.array([float(x) for x in tok[i][-3:]])  # noqa: E731
+    num = lambda i: float(tok[i][-1])  # noqa: E731
+    return {"ekin_p_i": num(0), "ekin_l_i": num(1), "epot_i": num(2), "etotal_i": num(3), "r_i": vec(4),
+            "v_i": vec(5), "polar_i": num(6), "azi_i": num(7), "ekin_p_f": num(9), "ekin_l_f": num(10),
+            "epot_f": num(11), "etotal_f": num(12), "r_f": vec(13), "v_f": vec(14), "polar_f": num(15),
+            "azi_f": num(16), "time": num(18), "turn_pnts": int(tok[19][-1]), "cl_appr": num(20),
+            "cl_appr_time": num(21), "r_min_p": vec(22)}
 
 
 def compare(a: ScatterResult, b: ScatterResult) -> dict:
