@@ -6,7 +6,8 @@
 * ``mxt`` geometry files (src/md_init.f90:346-381): Fortran unformatted sequential,
   4-byte record markers, records (natoms, nbeads, ntypes) and
   (r, v, is_cart, is_fixed, idx, name, is_proj, simbox, isimbox); logicals are 4 bytes.
-* POSCAR (src/md_init.f90:195-342), the subset without repetitions.
+* POSCAR (src/md_init.f90:195-342) with the optional bead count, mobility flags and
+  velocity section, and ``create_repetitions`` (src/universe_mod.f90:120-217).
 """
 from __future__ import annotations
 
@@ -156,3 +157,122 @@ def write_mxt(path, u: Universe) -> None:
              np.where(np.asarray(u.is_proj), -1, 0).astype("<i4").tobytes(),
              np.asarray(u.simbox.T, "<f8").tobytes(), np.asarray(invert_matrix(u.simbox).T, "<f8").tobytes()]
     Path(path).write_bytes(rec(p1) + rec(b"".join(parts)))
+
+
+def create_repetitions(u: Universe, rep=(0, 0)) -> Universe:
+    """create_repetitions, src/universe_mod.f90:120-217: the non-projectile atoms are
+    repeated (1 + 2 rep[0]) x (1 + 2 rep[1]) times along the first two cell vectors (direct
+    offsets -rep..rep, the second index fastest), projectile atoms (those leading the atom
+    list) stay first and unmoved, and the first two cell vectors grow by the same factors."""
+    r1, r2 = int(rep[0]), int(rep[1])
+    if r1 < 0 or r2 < 0:
+        raise InputError("Error in create_repetitions: negative repetition")
+    if r1 == 0 and r2 == 0:
+        return u
+    proj_type = np.asarray(u.is_proj, bool)
+    nprojs = int(np.sum(proj_type[np.asarray(u.idx) - 1]))
+    if not np.all(proj_type[np.asarray(u.idx[:nprojs]) - 1]):
+        raise InputError("Error in create_repetitions: projectile atoms must lead the atom list")
+    box = np.asarray(u.simbox, float)
+    frac = np.einsum("ij,nbj->nbi", invert_matrix(box), u.r)  # direct coordinates
+    parts_r, parts = [frac[:nprojs]], {k: [getattr(u, k)[:nprojs]] for k in ("v", "m", "idx", "is_fixed")}
+    for i in range(-r1, r1 + 1):
+        for j in range(-r2, r2 + 1):
+            f = frac[nprojs:].copy()
+            f[..., 0] += i
+            f[..., 1] += j
+            parts_r.append(f)
+            for k in parts:
+                parts[k].append(getattr(u, k)[nprojs:])
+    r = np.einsum("ij,nbj->nbi", box, np.concatenate(parts_r))
+    big = box.copy()
+    big[:, 0] *= 1 + 2 * r1
+    big[:, 1] *= 1 + 2 * r2
+    return Universe(r=r, v=np.concatenate(parts["v"]).copy(), m=np.concatenate(parts["m"]).copy(),
+                    idx=np.concatenate(parts["idx"]).astype(np.int32), is_fixed=np.concatenate(parts["is_fixed"]).copy(),
+                    simbox=big, names=list(u.names), is_proj=np.array(u.is_proj, bool),
+                    algo=None if u.algo is None else np.array(u.algo))
+
+
+def read_poscar(path, nprojectiles: int = 1, masses_amu=None, rep=(0, 0)) -> Universe:
+    """read_poscar, src/md_init.f90:195-342: comment line; scaling constant; three cell
+    vectors; element names; atom counts, optionally preceded by ``:nbeads:``; coordinate
+    system (d/direct or c/cart/cartesian); coordinates, 3 per line or 3 plus mobility
+    flags T/F per line (atom-major, bead-minor); optionally a blank line and velocities in
+    the same order.  The first ``nprojectiles`` element types are projectiles.  Cartesian
+    coordinates are scaled by the constant, velocities are not; the result is Cartesian
+    after ``create_repetitions(rep)``.  Masses from ``masses_amu`` (element -> amu)."""
+    lines = Path(path).read_text().splitlines()
+    err = "Error in read_poscar: "
+    if len(lines) < 8:
+        raise InputError(err + "file too short")
+    try:
+        scale = float(lines[1].split()[0])
+    except (IndexError, ValueError):
+        raise InputError(err + "reading scaling constant") from None
+    try:
+        cell = np.array([[float(x) for x in lines[2 + k].split()[:3]] for k in range(3)])
+    except ValueError:
+        raise InputError(err + "reading simulation box") from None
+    if cell.shape != (3, 3):
+        raise InputError(err + "reading simulation box")
+    elements = lines[5].split()
+    counts_line = lines[6]
+    nbeads = 1
+    if ":" in counts_line:
+        a, b = counts_line.index(":"), counts_line.rindex(":")
+        try:
+            nbeads = int(counts_line[a + 1:b])
+        except ValueError:
+            raise InputError(err + "reading number of beads") from None
+        if nbeads < 1:
+            raise InputError(err + "reading number of beads")
+        counts_line = counts_line[b + 1:]
+    try:
+        natoms = [int(x) for x in counts_line.split()]
+    except ValueError:
+        raise InputError(err + "reading number of atoms") from None
+    if len(natoms) != len(elements) or any(n <= 0 for n in natoms):
+        raise InputError(err + "number of atoms could not be read")
+    csys = lines[7].strip().lower()
+    if csys not in ("d", "direct", "c", "cart", "cartesian"):
+        raise InputError(err + "reading coordinate system type (cartesian/direct)")
+    N = sum(natoms)
+    nrow = N * nbeads
+    body = lines[8:8 + nrow]
+    if len(body) < nrow:
+        raise InputError(err + "reading coordinates")
+    nwords = len(body[0].split())
+    if nwords not in (3, 6):
+        raise InputError(err + "cannot read coordinate section")
+    r = np.zeros((N, nbeads, 3))
+    fixed = np.zeros((N, nbeads, 3), bool)
+    for row, line in enumerate(body):
+        w = line.split()
+        if len(w) != nwords:
+            raise InputError(err + "reading atom coordinates and mobility flags")
+        i, b = divmod(row, nbeads)
+        r[i, b] = [float(x) for x in w[:3]]
+        if nwords == 6:
+            fixed[i, b] = [x == "F" for x in w[3:]]
+    v = np.zeros_like(r)
+    rest = lines[8 + nrow:]
+    if rest and rest[0].strip() == "":
+        vals = [float(x) for l in rest[1:] for x in l.split()]
+        if len(vals) < 3 * nrow:
+            raise InputError(err + "cannot read initial atom velocities")
+        v = np.array(vals[:3 * nrow]).reshape(N, nbeads, 3)
+    elif rest and rest[0].strip():
+        raise InputError(err + "cannot read initial atom velocities. Did you specify all species in the *.inp file?")
+    box = cell.T * scale  # simbox(:, k) = k-th vector
+    if csys.startswith("c"):
+        r = r * scale
+    else:
+        r = np.einsum("ij,nbj->nbi", box, r)
+    masses_amu = masses_amu or C.MASS_AMU
+    idx = np.concatenate([[k + 1] * n for k, n in enumerate(natoms)]).astype(np.int32)
+    m = np.array([masses_amu.get(elements[i - 1], np.nan) for i in idx]) * C.AMU2MASS
+    is_proj = np.arange(len(elements)) < nprojectiles
+    u = Universe(r=r, v=v, m=m, idx=idx, is_fixed=fixed, simbox=box, names=elements, is_proj=is_proj,
+                 algo=np.full(len(elements), C.PROP_ID_VERLET, np.int32))
+    return create_repetitions(u, rep)

@@ -4,6 +4,8 @@ Reads (only in the development container, where the reference tree is mounted):
   pes/EMT-HAu.pes, pes/EMT-HPt.pes          -> emt_params.json (parsed parameter blocks)
   conf/latt/mxt_00000001.dat                 -> mxt_latt.npz (decoded geometry)
   example/md/RuNNer_input/{input.nn,scaling.data,weights.006.data}
+  conf/example.POSCAR, conf/cart.POSCAR       -> poscar_ref.json (file text and its coordinate
+                                               block parsed by numpy, independently of io)
   example/md/conf/latt/mxt_00000001.dat      -> runner_cgraphene.npz (parsed network +
                                                geometry) and runner_cgraphene_ref.npz
                                                (oracle energy/forces/descriptors/neighbours)
@@ -33,6 +35,17 @@ def main(ref):
     u = io.read_mxt(ref / "conf" / "latt" / "mxt_00000001.dat")
     np.savez(HERE / "mxt_latt.npz", r=u.r, v=u.v, simbox=u.simbox, idx=u.idx, is_fixed=u.is_fixed,
              names=np.array(u.names), is_proj=u.is_proj)
+
+    pos = {}
+    for name in ("example.POSCAR", "cart.POSCAR"):
+        text = (ref / "conf" / name).read_text()
+        lines = text.splitlines()
+        scale = float(lines[1].split()[0])
+        cell = np.array([[float(x) for x in l.split()[:3]] for l in lines[2:5]])
+        coords = np.array([[float(x) for x in l.split()[:3]] for l in lines[8:] if l.strip()])
+        pos[name] = {"text": text, "scale": scale, "cell_rows": cell.tolist(), "coords": coords.tolist(),
+                     "elements": lines[5].split()}
+    (HERE / "poscar_ref.json").write_text(json.dumps(pos, indent=1))
 
     m = nene.read_runner(ref / "example" / "md" / "RuNNer_input")
     nene.save_npz(m, HERE / "runner_cgraphene.npz")
