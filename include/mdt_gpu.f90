@@ -21,6 +21,11 @@ module mdt_gpu
         integer(c_int32_t) :: use_exit, rng_mode
     end type mdt_prop_params
 
+    type, bind(C) :: mdt_refill_params
+        real(c_double)     :: z0, einc_min, einc_max, polar_min, polar_max, azimuth
+        integer(c_int64_t) :: seed
+    end type mdt_refill_params
+
     type, bind(C) :: mdt_traj_summary
         integer(c_int32_t) :: status, steps_done
         real(c_double)     :: epot, ekin_p, ekin_l, ebead
@@ -125,6 +130,19 @@ module mdt_gpu
             type(c_ptr), value :: ctx
             integer(c_int32_t), intent(out) :: turn_pnts(*), cl_appr_step(*)
             real(c_double), intent(out) :: cl_appr(*), r_min_p(*)
+        end function
+
+        integer(c_int32_t) function mdt_set_step_limit(ctx, max_steps) bind(C, name="mdt_set_step_limit")
+            import :: c_int32_t, c_ptr
+            type(c_ptr), value :: ctx
+            integer(c_int32_t), value :: max_steps
+        end function
+
+        integer(c_int32_t) function mdt_refill(ctx, p, generation, nrefilled) bind(C, name="mdt_refill")
+            import :: c_int32_t, c_ptr, mdt_refill_params
+            type(c_ptr), value :: ctx
+            type(mdt_refill_params), intent(in) :: p
+            integer(c_int32_t), intent(out) :: generation(*), nrefilled
         end function
 
         integer(c_int32_t) function mdt_set_pes(ctx, pes_kind, range_margin) bind(C, name="mdt_set_pes")

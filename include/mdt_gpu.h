@@ -51,6 +51,7 @@ extern "C" {
 #define MDT_TRAJ_RUNNING 0
 #define MDT_TRAJ_EXIT_UPPER 1   /* projectile above pul, md_tian2.f90:88-89 */
 #define MDT_TRAJ_EXIT_LOWER 2   /* projectile below pll, md_tian2.f90:91-92 */
+#define MDT_TRAJ_STEP_LIMIT 3   /* the step limit (nsteps) was reached, md_tian2.f90:78 */
 #define MDT_TRAJ_ERR_DENSITY -10 /* negative EMT density in ldfa, md_algo.f90:551-554 */
 
 typedef struct mdt_ctx mdt_ctx;
@@ -242,6 +243,31 @@ int32_t mdt_md_steps(mdt_ctx *ctx, int32_t nsteps, int32_t precision, const mdt_
    (3, nb, N) normal deviates, andersen_u (nb, N) uniforms.  NULL leaves one unset. */
 int32_t mdt_set_random_arrays(mdt_ctx *ctx, const double *randy, const double *zeta, const double *andersen_v,
                               const double *andersen_u);
+
+/* Per-trajectory step limit of the fused MD steps (the reference's nsteps): a trajectory
+   that has run max_steps steps stops with status MDT_TRAJ_STEP_LIMIT (0 = no limit). */
+int32_t mdt_set_step_limit(mdt_ctx *ctx, int32_t max_steps);
+
+/* Refill (prepare_next_traj, src/md_init.f90:880-944, on the device): every trajectory whose
+   status is not MDT_TRAJ_RUNNING gets the state of the last mdt_state_upload back, and its
+   projectile (atom 0, every bead) a new start: a uniform position in the plane of the first
+   two cell vectors at height z0 and the incidence velocity of set_proj_incidence
+   (md_init.f90:829-876) for an energy uniform in [einc_min, einc_max] eV, a polar angle
+   uniform in [polar_min, polar_max] degrees and the azimuth (degrees; < 0: uniform), drawn
+   from a counter-based generator keyed by (seed, trajectory, generation).  Status, step
+   count and trajectory observables restart; generation[t] (may be NULL) counts the refills
+   of each trajectory.  Forces are stale afterwards: call mdt_calc_force before the next
+   mdt_md_steps, as after an upload.  Lets a batch run a stream of trajectories on the GPU
+   without uploading new states (no replacement in the reference, which runs one trajectory
+   at a time). */
+typedef struct mdt_refill_params {
+    double z0;
+    double einc_min, einc_max;
+    double polar_min, polar_max;
+    double azimuth;
+    uint64_t seed;
+} mdt_refill_params;
+int32_t mdt_refill(mdt_ctx *ctx, const mdt_refill_params *p, int32_t *generation, int32_t *nrefilled);
 
 /* Trajectory observables of collect_trajectory_characteristics (src/trajectory_info.f90:
    47-75, 92-132, 243-250), tracked on the device by the fused MD steps (mdt_md_steps) after

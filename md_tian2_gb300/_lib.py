@@ -26,6 +26,13 @@ class PropParams(ct.Structure):
                 ("use_exit", ct.c_int32), ("rng_mode", ct.c_int32)]
 
 
+class RefillParams(ct.Structure):
+    """mdt_refill_params (include/mdt_gpu.h)."""
+    _fields_ = [("z0", ct.c_double), ("einc_min", ct.c_double), ("einc_max", ct.c_double),
+                ("polar_min", ct.c_double), ("polar_max", ct.c_double), ("azimuth", ct.c_double),
+                ("seed", ct.c_uint64)]
+
+
 class TrajSummary(ct.Structure):
     _fields_ = [("status", ct.c_int32), ("steps_done", ct.c_int32), ("epot", ct.c_double),
                 ("ekin_p", ct.c_double), ("ekin_l", ct.c_double), ("ebead", ct.c_double)]
@@ -77,6 +84,8 @@ SIGNATURES = {
     "mdt_nn_radial_kernel": (ct.c_int32, [ct.c_void_p, ct.c_int32]),
     "mdt_nn_radial_block": (ct.c_int32, [ct.c_void_p, ct.c_int32]),
     "mdt_traj_observables": (ct.c_int32, [ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p]),
+    "mdt_set_step_limit": (ct.c_int32, [ct.c_void_p, ct.c_int32]),
+    "mdt_refill": (ct.c_int32, [ct.c_void_p, ct.POINTER(RefillParams), ct.c_void_p, ct.POINTER(ct.c_int32)]),
     "mdt_nn_set_skin": (ct.c_int32, [ct.c_void_p, ct.c_double]),
     "mdt_nn_stats": (ct.c_int32, [ct.c_void_p, ct.c_void_p, ct.c_void_p]),
     "mdt_nn_neighbors": (ct.c_int32, [ct.c_void_p, ct.c_void_p, ct.c_void_p]),

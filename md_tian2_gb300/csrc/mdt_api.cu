@@ -34,6 +34,11 @@ struct mdt_ctx {
 
     // batch
     bool have_batch = false;
+    // refill: state of the last upload (6 SoA arrays), generation per trajectory, counter
+    double *tmpl = nullptr;
+    int *gen = nullptr, *refill_count = nullptr;
+    bool have_tmpl = false;
+    int step_limit = 0;
     int T = 0, ntypes = 0, max_atoms = 0, max_beads = 0;
     int64_t total_ba = 0, total_pairs = 0;
     int total_atoms = 0, total_beads = 0;
@@ -111,6 +116,9 @@ template <typename T> T *dalloc(mdt_ctx *c, size_t n, cudaError_t &e) {
 
 void free_batch(mdt_ctx *c) {
     c->X = NNScratch{};
+    c->tmpl = nullptr;
+    c->gen = c->refill_count = nullptr;
+    c->have_tmpl = false;
     c->skw = nullptr;
     c->skcnt = c->skok = nullptr;
     c->skref = nullptr;
@@ -178,6 +186,7 @@ PropParams to_dev(const mdt_ctx *c, const mdt_prop_params *p) {
     P.seed = p->seed;
     P.use_exit = p->use_exit;
     P.rng_mode = p->rng_mode;
+    P.max_steps = c->step_limit;
     P.randy = c->rnd[0];
     P.zeta = c->rnd[1];
     P.andersen_v = c->rnd[2];
@@ -1080,6 +1089,12 @@ int32_t mdt_batch_define(mdt_ctx *c, int32_t ntraj, const int32_t *natoms, const
     B.pair_scratch = nullptr;
     c->scratch_prec_bytes = 0;
     e = launch_obs_reset(c->stream, B);
+    if (e == cudaSuccess) {
+        c->tmpl = dalloc<double>(c, 6 * (size_t)ba, e);
+        if (e == cudaSuccess) c->gen = dalloc<int>(c, (size_t)ntraj + 1, e);
+        if (e == cudaSuccess) e = cudaMemsetAsync(c->gen, 0, sizeof(int) * ((size_t)ntraj + 1), c->stream);
+        c->refill_count = c->gen ? c->gen + ntraj : nullptr;
+    }
     if (e != cudaSuccess) {
         free_batch(c);
         return cuda_fail(c, e, "mdt_batch_define observables");
@@ -1107,6 +1122,12 @@ int32_t mdt_state_upload(mdt_ctx *c, const double *r, const double *v) {
     if (e == cudaSuccess) e = cudaMemsetAsync(B.status, 0, sizeof(int) * c->T, c->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(B.steps_done, 0, sizeof(int) * c->T, c->stream);
     if (e == cudaSuccess) e = launch_obs_reset(c->stream, B);
+    // the uploaded state is the template of mdt_refill
+    const double *cur[6] = {B.rx, B.ry, B.rz, B.vx, B.vy, B.vz};
+    for (int a = 0; a < 6 && e == cudaSuccess; ++a)
+        e = cudaMemcpyAsync(c->tmpl + a * (size_t)c->total_ba, cur[a], sizeof(double) * c->total_ba,
+                            cudaMemcpyDeviceToDevice, c->stream);
+    if (e == cudaSuccess && r && v) c->have_tmpl = true;
     return e == cudaSuccess ? MDT_OK : cuda_fail(c, e, "mdt_state_upload");
 }
 
@@ -1254,6 +1275,36 @@ int32_t mdt_md_steps(mdt_ctx *c, int32_t nsteps, int32_t precision, const mdt_pr
     cudaError_t e = launch_md_steps(cfg(c, precision), c->B, c->E, P, nsteps, precision);
     c->launches++;
     return e == cudaSuccess ? MDT_OK : cuda_fail(c, e, "mdt_md_steps");
+}
+
+int32_t mdt_set_step_limit(mdt_ctx *c, int32_t max_steps) {
+    if (!c) return MDT_ERR_ARG;
+    if (max_steps < 0) return fail(c, MDT_ERR_ARG, "max_steps < 0");
+    c->step_limit = max_steps;
+    return MDT_OK;
+}
+
+int32_t mdt_refill(mdt_ctx *c, const mdt_refill_params *p, int32_t *generation, int32_t *nrefilled) {
+    int rc = check_ready(c, false);
+    if (rc) return rc;
+    if (!p) return fail(c, MDT_ERR_ARG, "null mdt_refill_params");
+    if (!c->have_tmpl) return fail(c, MDT_ERR_STATE, "mdt_refill needs a state uploaded with r and v");
+    if (!(p->einc_min > 0.0) || !(p->einc_max >= p->einc_min) || !(p->polar_max >= p->polar_min) ||
+        !(p->polar_min >= 0.0) || !(p->polar_max < 90.0) || !std::isfinite(p->z0))
+        return fail(c, MDT_ERR_ARG, "mdt_refill: need 0 < einc_min <= einc_max, 0 <= polar_min <= polar_max < 90");
+    cudaError_t e = cudaMemsetAsync(c->refill_count, 0, sizeof(int), c->stream);
+    if (e == cudaSuccess)
+        e = launch_refill(c->stream, c->B, c->tmpl, c->total_ba, p->z0, p->einc_min, p->einc_max, p->polar_min,
+                          p->polar_max, p->azimuth, p->seed, c->gen, c->skok, c->refill_count);
+    c->launches++;
+    int n = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&n, c->refill_count, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess && generation)
+        e = cudaMemcpyAsync(generation, c->gen, sizeof(int) * c->T, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "mdt_refill");
+    if (nrefilled) *nrefilled = n;
+    return MDT_OK;
 }
 
 int32_t mdt_traj_observables(mdt_ctx *c, int32_t *turn_pnts, double *cl_appr, int32_t *cl_appr_step,

@@ -39,6 +39,7 @@ constexpr int kPropLangevinConst = 1007;
 constexpr int kStatusRunning = 0;
 constexpr int kStatusExitUpper = 1;   // projectile above pul (md_tian2.f90:88-89)
 constexpr int kStatusExitLower = 2;   // projectile below pll (md_tian2.f90:91-92)
+constexpr int kStatusStepLimit = 3;   // nsteps reached (the loop of md_tian2.f90:78 completed)
 constexpr int kStatusErrDensity = -10;  // ldfa: negative EMT density (md_algo.f90:551-554)
 constexpr int kStatusErrNonFinite = -11;
 
@@ -97,6 +98,7 @@ struct PropParams {
     uint64_t seed;
     int use_exit;             // stop trajectories at pul / pll
     int rng_mode;             // 0 = counter-based Philox, 1 = host-provided arrays
+    int max_steps;            // > 0: a trajectory stops after this many steps (nsteps)
     const double *randy;      // rng_mode 1: (ba, d) normal deviates for Langevin
     const double *zeta;       // rng_mode 1: PILE deviates
     const double *andersen_v; // rng_mode 1: Andersen unit deviates
@@ -147,6 +149,6 @@ __device__ __forceinline__ double uniform_deviate(uint64_t seed, uint32_t traj, 
 }
 
 enum RngStream : uint32_t { kStreamLangevin = 1, kStreamPile = 2, kStreamAndersenV = 3,
-                            kStreamAndersenU = 4 };
+                            kStreamAndersenU = 4, kStreamRefill = 5 };
 
 }  // namespace mdt

@@ -126,6 +126,8 @@ __global__ void __launch_bounds__(kBlock, 4) md_steps_kernel(Batch B, EmtConst E
                     if (up) B.status[t] = kStatusExitUpper;
                     else if (lo) B.status[t] = kStatusExitLower;
                 }
+                if (P.max_steps > 0 && step >= P.max_steps && B.status[t] == kStatusRunning)
+                    B.status[t] = kStatusStepLimit;
             }
             __syncthreads();
         }
@@ -147,6 +149,77 @@ __global__ void obs_reset_kernel(Batch B) {
 
 cudaError_t launch_obs_reset(cudaStream_t s, const Batch &B) {
     obs_reset_kernel<<<(B.ntraj + 255) / 256, 256, 0, s>>>(B);
+    return cudaGetLastError();
+}
+
+// Refill of stopped trajectories (the set-up of md_init.f90 for the next trajectory,
+// prepare_next_traj :880-944, on the device): every bead-atom of a trajectory whose status
+// is not running gets the state of the last upload back; the projectile (atom 0) is
+// placed at a uniform direct (u, v) in the first two cell vectors at height z0 with the
+// incidence velocity of set_proj_incidence (:829-876) for an energy, polar and azimuth
+// drawn uniformly (Philox keyed by seed, trajectory and generation), on every bead.
+struct RefillDev {
+    double z0, emin, emax, pmin, pmax, azimuth;  // azimuth < 0: uniform in [0, 360)
+    uint64_t seed;
+};
+
+__global__ void refill_kernel(Batch B, const double *tmpl, int64_t total_ba, RefillDev R, int *gen, int *skok,
+                              int *count) {
+    for (int t = blockIdx.x; t < B.ntraj; t += gridDim.x) {
+        if (B.status[t] == kStatusRunning) continue;  // uniform over the block
+        const TrajView T = traj_view(B, t);
+        const int64_t n = (int64_t)T.nb * T.N;
+        double *dst[6] = {B.rx, B.ry, B.rz, B.vx, B.vy, B.vz};
+        for (int64_t k = threadIdx.x; k < n; k += blockDim.x)
+            for (int a = 0; a < 6; ++a) dst[a][T.base + k] = tmpl[a * total_ba + T.base + k];
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const int g = gen[t] + 1;
+            gen[t] = g;
+            const uint32_t tt = (uint32_t)t, gg = (uint32_t)g;
+            const double u = uniform_deviate(R.seed, tt, gg, 0, kStreamRefill);
+            const double w = uniform_deviate(R.seed, tt, gg, 1, kStreamRefill);
+            const double e = R.emin + (R.emax - R.emin) * uniform_deviate(R.seed, tt, gg, 2, kStreamRefill);
+            const double pol =
+                (R.pmin + (R.pmax - R.pmin) * uniform_deviate(R.seed, tt, gg, 3, kStreamRefill)) * (kPi / 180.0);
+            const double azi = (R.azimuth < 0.0 ? 360.0 * uniform_deviate(R.seed, tt, gg, 4, kStreamRefill)
+                                                : R.azimuth) * (kPi / 180.0);
+            const double *h = B.box + 9 * (size_t)t;  // column major: h[3 k + d] = component d of vector k
+            const double x = h[0] * u + h[3] * w, y = h[1] * u + h[4] * w;
+            const double vinc = sqrt(2.0 * e / B.mass[T.aoff]);
+            const double vx = vinc * sin(pol) * cos(azi), vy = vinc * sin(pol) * sin(azi), vz = -vinc * cos(pol);
+            for (int b = 0; b < T.nb; ++b) {
+                const int64_t k = T.base + (int64_t)b * T.N;
+                B.rx[k] = x;
+                B.ry[k] = y;
+                B.rz[k] = R.z0;
+                B.vx[k] = vx;
+                B.vy[k] = vy;
+                B.vz[k] = vz;
+            }
+            if (skok)
+                for (int b = 0; b < T.nb; ++b) skok[B.bead_off[t] + b] = 0;
+            B.status[t] = kStatusRunning;
+            B.steps_done[t] = 0;
+            B.obs_turn[t] = 0;
+            B.obs_up[t] = 0;
+            B.obs_clstep[t] = 0;
+            B.obs_cl[t] = kDefaultReal;
+            B.obs_low[3 * t] = kDefaultReal;
+            B.obs_low[3 * t + 1] = kDefaultReal;
+            B.obs_low[3 * t + 2] = kDefaultReal;
+            atomicAdd(count, 1);
+        }
+        __syncthreads();
+    }
+}
+
+cudaError_t launch_refill(cudaStream_t s, const Batch &B, const double *tmpl, int64_t total_ba, double z0,
+                          double emin, double emax, double pmin, double pmax, double azimuth, uint64_t seed,
+                          int *gen, int *skok, int *count) {
+    const RefillDev R{z0, emin, emax, pmin, pmax, azimuth, seed};
+    const int grid = B.ntraj < 4096 ? (B.ntraj > 0 ? B.ntraj : 1) : 4096;
+    refill_kernel<<<grid, 128, 0, s>>>(B, tmpl, total_ba, R, gen, skok, count);
     return cudaGetLastError();
 }
 

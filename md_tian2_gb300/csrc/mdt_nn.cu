@@ -347,6 +347,8 @@ __global__ void __launch_bounds__(kNNBlock) nn_md_steps_kernel(Batch B, NNDev M,
                     if (up) B.status[t] = kStatusExitUpper;
                     else if (lo) B.status[t] = kStatusExitLower;
                 }
+                if (P.max_steps > 0 && step >= P.max_steps && B.status[t] == kStatusRunning)
+                    B.status[t] = kStatusStepLimit;
             }
             __syncthreads();
         }

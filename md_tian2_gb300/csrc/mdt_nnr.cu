@@ -832,6 +832,10 @@ __global__ void __launch_bounds__(kRBlockMax, 1)
                             run_next = 0;
                         }
                     }
+                    if (run_next && P.max_steps > 0 && step >= P.max_steps) {
+                        B.status[T.t] = kStatusStepLimit;
+                        run_next = 0;
+                    }
                 }
                 S.tr_stat[((step_i + 1) % 3) * kRMaxTraj + A.s] = run_next;
             }

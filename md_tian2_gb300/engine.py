@@ -261,5 +261,20 @@ class Engine:
                                                   low.ctypes.data), "mdt_traj_observables")
         return {"turn_pnts": turn, "cl_appr": cl, "cl_appr_step": clstep, "r_min_p": low}
 
+    def set_step_limit(self, max_steps: int) -> None:
+        """Stop each trajectory after max_steps steps (status 3); 0 = no limit."""
+        self._check(self.lib.mdt_set_step_limit(self.h, int(max_steps)), "mdt_set_step_limit")
+
+    def refill(self, z0: float = 6.0, einc=(0.5, 5.0), polar=(0.0, 60.0), azimuth: float = -1.0,
+               seed: int = 1):
+        """Restart every stopped trajectory from the uploaded state with a new projectile
+        start (mdt_refill); returns (generation per trajectory, number refilled)."""
+        from ._lib import RefillParams
+        p = RefillParams(z0, einc[0], einc[1], polar[0], polar[1], azimuth, seed & 0xFFFFFFFFFFFFFFFF)
+        gen = np.zeros(self.T, np.int32)
+        n = ct.c_int32(0)
+        self._check(self.lib.mdt_refill(self.h, ct.byref(p), gen.ctypes.data, ct.byref(n)), "mdt_refill")
+        return gen, int(n.value)
+
     def launch_count(self) -> int:
         return int(self.lib.mdt_launch_count(self.h))

@@ -263,3 +263,59 @@ def compare(a: ScatterResult, b: ScatterResult) -> dict:
         out["ks_d"] = d
         out["ks_p"] = float(min(1.0, max(0.0, p)))
     return out
+
+
+def run_campaign(eng, sp, total: int, refill: dict, precision: str = "fp64", max_steps: int = 10000,
+                 chunk: int = 1000, metal: str = "Au") -> ScatterResult:
+    """A stream of trajectories through a fixed batch: run ``chunk`` steps, take the
+    records of every trajectory that has stopped (exit test or the ``max_steps`` limit),
+    restart those slots on the device with new projectile starts (``Engine.refill(**refill)``)
+    and go on until ``total`` trajectories have finished.  Returns their scattering records
+    (the observables part: energies, projectile heights, steps, status)."""
+    if not sp.use_exit:
+        raise ValueError("run_campaign needs SimParams.use_exit (the pul/pll exit test)")
+    if max_steps <= 0:
+        raise ValueError("run_campaign needs a step limit (max_steps > 0)")
+    eng.set_step_limit(max_steps)
+    T = eng.T
+
+    def proj_z(o, t):
+        return eng.split(o["r"], t)[0, :, 2].mean()
+
+    eng.calc_force(sp, precision=precision)
+    q = eng.query(sp)
+    o = eng.download()
+    e_start = q["ekin_p"].copy()
+    z_start = np.array([proj_z(o, t) for t in range(T)])
+    cols = {k: [] for k in ("ekin_i", "ekin_f", "z_i", "z_f", "steps", "status")}
+    done = 0
+    try:
+        while done < total:
+            eng.md_steps(chunk, sp, precision=precision)
+            q = eng.query(sp)
+            fin = np.nonzero(q["status"] != 0)[0]
+            if len(fin) == 0:
+                continue
+            o = eng.download()
+            for t in fin[:total - done]:
+                cols["ekin_i"].append(e_start[t])
+                cols["ekin_f"].append(q["ekin_p"][t])
+                cols["z_i"].append(z_start[t])
+                cols["z_f"].append(proj_z(o, t))
+                cols["steps"].append(q["steps_done"][t])
+                cols["status"].append(q["status"][t])
+            done += min(len(fin), total - done)
+            if done >= total:
+                break
+            eng.refill(**refill)
+            eng.calc_force(sp, precision=precision)
+            q1 = eng.query(sp)
+            o1 = eng.download()
+            for t in fin:
+                e_start[t] = q1["ekin_p"][t]
+                z_start[t] = proj_z(o1, t)
+    finally:
+        eng.set_step_limit(0)
+    a = {k: np.array(v) for k, v in cols.items()}
+    return ScatterResult(ekin_i=a["ekin_i"], ekin_f=a["ekin_f"], z_i=a["z_i"], z_f=a["z_f"], steps=a["steps"],
+                         status=a["status"], shot_thru=SHOT_THRU_LIMIT.get(metal, -np.inf))

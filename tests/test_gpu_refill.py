@@ -1,0 +1,77 @@
+"""Device refill of stopped trajectories (mdt_refill) and the per-trajectory step limit:
+the restored slab equals the uploaded state exactly, the new projectile starts at z0 with
+an incidence energy and polar angle inside the requested ranges, status / steps /
+observables restart, running trajectories are untouched; then a stream of trajectories
+through a small batch (scatter.run_campaign)."""
+import numpy as np
+import pytest
+
+from md_tian2_gb300 import constants as C
+from md_tian2_gb300 import workloads as W
+from md_tian2_gb300.engine import Engine, SimParams
+from md_tian2_gb300.scatter import run_campaign
+
+pytestmark = pytest.mark.gpu
+
+
+def _engine(us):
+    eng = Engine(0)
+    eng.read_emt(W.emt_params())
+    eng.define(us)
+    eng.upload()
+    return eng
+
+
+def test_step_limit_and_refill(built_lib):
+    us = W.config2(6, seed=51)
+    eng = _engine(us)
+    sp = SimParams(step=0.1, gamma_const=1e-3, seed=4, pul=6.05, use_exit=True)
+    up = eng.download()
+    eng.set_step_limit(20)
+    eng.calc_force(sp)
+    eng.md_steps(10, sp)
+    gen, n = eng.refill(z0=6.0, einc=(1.0, 2.0), polar=(0.0, 30.0), seed=9)
+    assert n == 0 and not gen.any()  # nothing stopped yet
+    eng.md_steps(15, sp)
+    q = eng.query(sp)
+    assert (q["status"] == 3).all() and (q["steps_done"] == 20).all()
+    gen, n = eng.refill(z0=6.0, einc=(1.0, 2.0), polar=(0.0, 30.0), seed=9)
+    assert n == 6 and (gen == 1).all()
+    out = eng.download()
+    q = eng.query(sp)
+    assert (q["status"] == 0).all() and (q["steps_done"] == 0).all()
+    obs = eng.observables()
+    assert not obs["turn_pnts"].any() and (obs["cl_appr"] > 1e300).all()
+    m_h = C.MASS_AMU["H"] * C.AMU2MASS
+    for t, u in enumerate(us):
+        r, v = eng.split(out["r"], t), eng.split(out["v"], t)
+        r0, v0 = eng.split(up["r"], t), eng.split(up["v"], t)
+        assert np.array_equal(r[1:], r0[1:]) and np.array_equal(v[1:], v0[1:])  # slab restored
+        assert r[0, 0, 2] == 6.0
+        f = np.linalg.solve(u.simbox, r[0, 0])
+        assert 0.0 <= f[0] < 1.0 and 0.0 <= f[1] < 1.0
+        e = 0.5 * m_h * np.sum(v[0, 0] ** 2)
+        assert 1.0 - 1e-12 <= e <= 2.0 + 1e-12
+        polar = np.degrees(np.arccos(-v[0, 0, 2] / np.linalg.norm(v[0, 0])))
+        assert -1e-9 <= polar <= 30.0 + 1e-9
+    # a second refill of the same slots draws new starts
+    eng.md_steps(25, sp)
+    gen2, n2 = eng.refill(z0=6.0, einc=(1.0, 2.0), polar=(0.0, 30.0), seed=9)
+    out2 = eng.download()
+    assert n2 == 6 and (gen2 == 2).all()
+    assert not np.array_equal(eng.split(out2["r"], 0)[0], eng.split(out["r"], 0)[0])
+    eng.close()
+
+
+def test_campaign_streams_trajectories(built_lib):
+    us = W.config2(12, seed=52)
+    eng = _engine(us)
+    sp = SimParams(step=0.5, gamma_const=1e-3, seed=6, pul=6.05, use_exit=True)
+    res = run_campaign(eng, sp, total=40, refill={"z0": 6.0, "einc": (1.0, 3.0), "polar": (0.0, 45.0), "seed": 3},
+                       precision="fp64", max_steps=200, chunk=50)
+    eng.close()
+    assert len(res.z_f) == 40
+    assert set(np.unique(res.status)) <= {1, 3}
+    assert (res.steps <= 200).all() and (res.steps > 0).all()
+    assert (res.z_f[res.status == 1] > 6.05).all()
+    assert np.isfinite(res.ekin_i).all() and (res.ekin_i > 0).all()
