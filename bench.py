@@ -216,6 +216,32 @@ def cpu_baseline(seconds, cores=None):
                       f"{atom_steps} atom-steps; pool wall {wall:.1f} s incl. start-up"}
 
 
+def _ref_proc(conn, ntraj, seed, msteps):
+    """One host core of the reference arm: builds its config-2 trajectories once, then
+    advances them by ``msteps`` MD steps per request (steady-state stepping)."""
+    sys.path.insert(0, str(ROOT))
+    from md_tian2_gb300 import workloads as W
+    from oracle.oracle import OracleUniverse
+    us = W.config2(ntraj, seed=seed)
+    emt = W.emt_params()
+    sp = sim_params()
+    rng = np.random.default_rng(seed)
+    orcs = [OracleUniverse(u, emt) for u in us]
+    for o in orcs:
+        o.calc_force(sp)
+    conn.send("ready")
+    while conn.recv() is not None:
+        atom_steps = 0
+        for _ in range(msteps):
+            for o in orcs:
+                randy = rng.normal(size=o.r.shape)
+                o.propagate_1(sp, randy)
+                o.calc_force(sp)
+                o.propagate_2(sp, randy)
+                atom_steps += o.N * o.nb
+        conn.send(atom_steps)
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -225,27 +251,46 @@ def run_reference(args):
     oracle.build()
     cores = os.cpu_count() or 1
     ctx = mp.get_context("spawn")
-    per = 4
+    per, msteps = 4, 200
+    pipes, procs = [], []
+    for k in range(cores):
+        a, b = ctx.Pipe()
+        p = ctx.Process(target=_ref_proc, args=(b, per, 5000 + k, msteps), daemon=True)
+        p.start()
+        pipes.append(a)
+        procs.append(p)
+    for a in pipes:
+        a.recv()  # trajectories built, initial forces evaluated
     times, total = [], 0
-    with ctx.Pool(cores) as pool:
+    try:
         for s in range(args.warmup + args.steps):
             t0 = time.perf_counter()
-            res = pool.map(_cpu_worker, [(per, 5000 + k, 1, 0) for k in range(cores)])
+            for a in pipes:
+                a.send(1)
+            done = sum(a.recv() for a in pipes)
             dt = time.perf_counter() - t0
             if s >= args.warmup:
                 times.append(dt)
-                total += sum(r[0] for r in res)
+                total += done
+    finally:
+        for a in pipes:
+            a.send(None)
+        for p in procs:
+            p.join(timeout=10)
     el = sum(times)
     val = total / el
     line = {"impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "config-2 H/Au(111) EMT trajectories, bounded CPU sample",
-                       "sample_per_step": f"{cores} processes x {per} trajectories, build + 1 MD step each",
+            "config": {"workload": "config-2 H/Au(111) EMT trajectories (Verlet H, constant-friction Langevin Au, "
+                                   "dt 0.1 fs), bounded CPU sample",
+                       "sample_per_step": f"{cores} processes x {per} trajectories, {msteps} MD steps each "
+                                          "(trajectories built once before the warm-up)",
                        "l2": "n/a (CPU)"},
             "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores, "kind": "port",
                              "sample": "oracle/md_oracle.cpp restatement of the reference (no Fortran compiler "
-                                       "on this box), one MD step of a fresh trajectory sample per step"},
+                                       f"on this box): {cores} processes x {per} trajectories x {msteps} MD steps "
+                                       "per bench step, steady state"},
             "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -261,6 +306,22 @@ def run_reference(args):
 # 2*(24*32+32*32+32) + 64 softplus x 40, backward 2*(32+32*32+24*32) + 64 derivative x 20.
 FLOP_SURR_ENTRY = 70 + 156 + 252 + 14
 FLOP_SURR_ATOM = 2 * (24 * 32 + 32 * 32 + 32) + 64 * 40 + 2 * (32 + 32 * 32 + 24 * 32) + 64 * 20
+
+
+def replica_report(times, counts, dist=None, device="cpu"):
+    """Whole-job figures of N independent replicas: the slowest rank's times (max) and the
+    summed counts (atom-steps) over ranks; the only collective of the bench (the data
+    path has none).  Without a process group the local values."""
+    if dist is None:
+        return (*times, *counts)
+    import torch
+    t = torch.tensor(list(times) + list(counts), dtype=torch.float64, device=device)
+    mx = t.clone()
+    dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+    sm = t.clone()
+    dist.all_reduce(sm, op=dist.ReduceOp.SUM)
+    n = len(times)
+    return (*[mx[k].item() for k in range(n)], *[sm[n + k].item() for k in range(len(counts))])
 
 
 def steps_per_launch(steps, want):
@@ -461,16 +522,8 @@ def run_ours(args):
             traffic = None
 
     elapsed, elapsed_emt = ms * 1e-3, ms_emt * 1e-3
-    if dist:
-        t = torch.tensor([elapsed, float(done), e2e_s, float(e_atoms), elapsed_emt, float(done_emt)], device="cuda")
-        mx = t.clone()
-        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
-        sm = t.clone()
-        dist.all_reduce(sm, op=dist.ReduceOp.SUM)
-        elapsed, e2e_s, elapsed_emt = mx[0].item(), mx[2].item(), mx[4].item()
-        done_all, e_atoms_all, done_emt_all = sm[1].item(), sm[3].item(), sm[5].item()
-    else:
-        done_all, e_atoms_all, done_emt_all = done, e_atoms, done_emt
+    elapsed, e2e_s, elapsed_emt, done_all, e_atoms_all, done_emt_all = replica_report(
+        [elapsed, e2e_s, elapsed_emt], [float(done), float(e_atoms), float(done_emt)], dist, "cuda")
     if rank == 0:
         value = done_all / elapsed
         emt_value = done_emt_all / elapsed_emt
