@@ -147,7 +147,7 @@ int32_t mdt_nn_fast_path(mdt_ctx *ctx, int32_t enable);
 /* Within the fast path, radial-only models (every function a G2 under one cosine cutoff,
    at most two elements with the same (eta, r_s) list per neighbour element, one or two
    hidden layers of at most 32 nodes, one activation per layer) run on a thread-per-atom
-   kernel when the batch has single-bead trajectories of at most 640 atoms (and, for
+   kernel when the batch has single-bead trajectories of at most 512 atoms (and, for
    mdt_md_steps, Verlet or constant-friction Langevin propagators).  enable = 0 keeps
    them on the warp-per-atom fast kernel.  Returns 1 if the installed model qualifies,
    else 0 (no replacement in the reference: src/pes_nene_mod.f90:7145 has one path). */
