@@ -125,3 +125,12 @@ def test_hdnnp_oracle_two_elements_gradient(oracle_lib):
         rm[a, d] -= h
         fd = -(o.energy_force(elem, rp, u.simbox)[0] - o.energy_force(elem, rm, u.simbox)[0]) / (2 * h)
         assert abs(fd - F[a, d]) < 1e-6 * max(1.0, abs(F[a, d]))
+
+
+@pytest.mark.skipif(not REF.exists(), reason="reference tree not mounted")
+def test_poscar_fixtures_match_reference_files():
+    g = json.loads((GOLD / "poscar_ref.json").read_text())
+    for name in ("example.POSCAR", "cart.POSCAR"):
+        assert (REF / "conf" / name).read_text() == g[name]["text"]
+        u = io.read_poscar(REF / "conf" / name, nprojectiles=1)
+        assert np.allclose(u.r[:, 0, :], np.array(g[name]["coords"]) * g[name]["scale"], rtol=0, atol=0)
