@@ -597,7 +597,6 @@ bool radial_plan(mdt_ctx *c) {
     const int bmax = std::max(32, std::min(kRBlockMax, c->rmaxblock));
     if (c->max_atoms > bmax) return false;
     const int w0 = (int)std::max<int64_t>(1, (total + (int64_t)slots * bmax - 1) / ((int64_t)slots * bmax));
-    int64_t best = -1;
     std::vector<std::vector<int>> bestp;
     int bestb = 0;
     for (int w = w0; w <= w0 + 4; ++w) {
@@ -630,7 +629,6 @@ bool radial_plan(mdt_ctx *c) {
         const int block = (mx + 31) & ~31;
         if (block > bmax) continue;
         // fewest waves first: the largest CTAs keep the most warps per SM in flight
-        best = (int64_t)((np + slots - 1) / slots) * block;
         bestp = std::move(packs);
         bestb = block;
         break;

@@ -63,7 +63,7 @@ struct SmemR {
     int *tr_flag, *tr_d2, *tr_over, *tr_stat;
     float *tr_lat;                       // [s][24]: lattice rows (9), inverse rows (9), skin half-widths (3)
     double *red;
-    int *misc;                           // [0] pack, [1] trajectories, [2] running trajectories
+    int *misc;                           // [0] pack taken from the work queue
     unsigned char *emt;                  // EMT fallback area (aliases hb)
 };
 
@@ -126,7 +126,7 @@ __device__ __forceinline__ float small_to_float(unsigned b) {
 
 // One thread's view of its atom.
 struct AtomR {
-    int slot, s, i, st, N, ei, algo;
+    int s, i, st, N, ei, algo;    // pack trajectory, atom, first slot, atoms, element, propagator
     int64_t base;                 // bead-atom slot of atom 0 of the bead
     float xhi, yhi, zhi, xli, yli, zli;
     float L[9];                   // lattice rows (bohr)
@@ -745,11 +745,9 @@ __global__ void __launch_bounds__(kRBlockMax, 1)
                 S.tr_st[s] = st;
                 st += S.tr_n[s];
             }
-            S.misc[1] = pd.y;
         }
         __syncthreads();
         AtomR A;
-        A.slot = tid;
         A.s = -1;
         for (int s = 0; s < pd.y; ++s)
             if (tid >= S.tr_st[s] && tid < S.tr_st[s] + S.tr_n[s]) A.s = s;
