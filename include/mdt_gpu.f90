@@ -13,6 +13,8 @@ module mdt_gpu
     integer(c_int32_t), parameter :: MDT_PES_EMT = 2003, MDT_PES_NENE = 2008, MDT_PES_SURROGATE = 2100
     integer(c_int32_t), parameter :: MDT_ENERGY_AND_FORCE = 3001, MDT_ENERGY_ONLY = 3002
     integer(c_int32_t), parameter :: MDT_PREC_FP64 = 0, MDT_PREC_FP32 = 1
+    integer(c_int32_t), parameter :: MDT_TRAJ_RUNNING = 0, MDT_TRAJ_EXIT_UPPER = 1, MDT_TRAJ_EXIT_LOWER = 2, &
+                                     MDT_TRAJ_STEP_LIMIT = 3, MDT_TRAJ_ERR_DENSITY = -10
 
     type, bind(C) :: mdt_prop_params
         real(c_double)     :: step, Tsurf, Tproj, pile_tau, andersen_time, gamma_const
