@@ -71,3 +71,19 @@ def test_mxt_fin_layout_and_times(tmp_path):
         v = r.record["v_i"][t]
         assert abs(d["polar_i"] - (180 - np.degrees(np.arccos(v[2] / np.linalg.norm(v))))) < 1e-6
     assert "-0.3922094094E+03" in paths[0].read_text()
+
+
+def test_trajectory_info_restatement():
+    """The checker of the device observables on a hand-made projectile path: moving down
+    at the start, a turning point at each sign change of v_z, the first closest step, the
+    lowest centroid, and the minimum image across the cell boundary."""
+    from oracle.trajectory_info import TrajectoryInfo
+    ti = TrajectoryInfo(np.eye(3) * 10.0)
+    path = [(5.0, -1.0), (3.0, -1.0), (2.0, 1.0), (4.0, 1.0), (3.5, -1.0), (2.0, -1.0)]
+    for k, (z, vz) in enumerate(path, start=1):
+        r = np.array([[[9.5, 1.0, z]], [[0.5, 1.0, 0.0]]])  # 1 A apart in x through the boundary
+        v = np.array([[[0.0, 0.0, vz]], [[0.0, 0.0, 0.0]]])
+        ti(k, r, v)
+    assert ti.turn == 2
+    assert ti.clstep == 3 and abs(ti.cl - np.hypot(1.0, 2.0)) < 1e-12
+    assert np.allclose(ti.low, [9.5, 1.0, 2.0])

@@ -15,36 +15,10 @@ from md_tian2_gb300 import nene
 from md_tian2_gb300 import workloads as W
 from md_tian2_gb300.engine import PES_SURROGATE, Engine, SimParams
 from md_tian2_gb300.scatter import read_mxt_fin, run_to_exit, write_mxt_fin
+from oracle.trajectory_info import TrajectoryInfo as Collect
 
 pytestmark = pytest.mark.gpu
 MODEL = Path(__file__).resolve().parents[1] / "md_tian2_gb300" / "data" / "surrogate_radial.npz"
-HUGE = np.finfo(np.float64).max
-
-
-class Collect:
-    """collect_trajectory_characteristics (trajectory_info.f90:47-75, 92-132, 243-250)."""
-
-    def __init__(self, box):
-        self.box, self.ibox = box, np.linalg.inv(box)
-        self.turn, self.up, self.cl, self.clstep = 0, False, HUGE, 0
-        self.low = np.full(3, HUGE)
-        self.dist = {}
-
-    def __call__(self, k, r, v):
-        c = r.mean(axis=1)
-        if c[0, 2] < self.low[2]:
-            self.low = c[0].copy()
-        d = c[0] - c[1:]
-        f = d @ self.ibox.T
-        f -= np.round(f)
-        dist = np.sqrt(np.sum((f @ self.box.T) ** 2, axis=1)).min()
-        self.dist[k] = dist
-        if dist < self.cl:
-            self.cl, self.clstep = dist, k
-        down = v[0].mean(axis=0)[2] < 0
-        if down == self.up:
-            self.turn += 1
-            self.up = not down
 
 
 def _batch(seed=3):
