@@ -87,3 +87,22 @@ def test_force_beads_and_incidence_removes_bead_drift():
     w = md_init.set_proj_incidence(b, 1.0, 0.0, azimuth="0")
     assert np.allclose(w.v[0].mean(axis=0), [0.0, 0.0, -math.sqrt(2 / (C.MASS_AMU["H"] * C.AMU2MASS))])
     assert np.allclose(w.v[0, 1] - w.v[0, 0], [0.2, 0, 0])  # bead spread kept, drift removed
+
+
+def test_conf_merge_pipeline(tmp_path):
+    """The reference's `conf merge` start of a trajectory: a projectile read from a POSCAR,
+    the slab from an mxt file, merged with a fixed pip, incidence set, beads forced."""
+    from md_tian2_gb300 import io
+    p = tmp_path / "proj.POSCAR"
+    p.write_text("H\n1.0\n 10 0 0\n 0 10 0\n 0 0 10\n H\n 1\ncartesian\n0.0 0.0 0.0\n")
+    proj = io.read_poscar(p, nprojectiles=1)
+    slab = _slab()
+    u = md_init.merge_universes(slab, proj, pip=["2.0", "1.0", "6.0"], rng=np.random.default_rng(0),
+                                algo_p=C.PROP_ID_VERLET, algo_l=C.PROP_ID_LANGEVIN)
+    assert np.allclose(u.r[0, 0], [2.0, 1.0, 6.0] - slab.simbox @ np.trunc(np.linalg.solve(slab.simbox, [2.0, 1.0, 6.0])))
+    u = md_init.set_proj_incidence(u, 2.76, 45.0, azimuth="0")
+    u = md_init.force_beads(u, 2)
+    assert u.nbeads == 2 and u.natoms == slab.natoms + 1
+    assert u.names == ["H"] + slab.names and u.is_proj.tolist()[0]
+    ek = 0.5 * u.m[0] * np.sum(u.v[0, 0] ** 2)
+    assert ek == pytest.approx(2.76)
