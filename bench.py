@@ -171,129 +171,127 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------
-# CPU side: the oracle (restatement of the reference) on host cores
+# CPU side: the oracle (restatement of the reference) on host cores.  One harness for the
+# cpu_baseline block and the reference arm: every process builds its own trajectories
+# once, then steps them inside C (oracle.run_steps, no Python in the timed loop) for a
+# fixed slice of wall time; the aggregate rate is the sum of the per-process rates (each
+# process's atom-steps over its own busy time), so no process waits for another.
 # ---------------------------------------------------------------------------
-def _cpu_worker(args):
-    ntraj, seed, nsteps, budget = args
+CPU_PER_PROC = 4  # config-2 trajectories per process
+
+
+def _cpu_proc(conn, kind, ntraj, seed):
+    """One host core: builds its trajectories (config-2 sample, or config 1), evaluates the
+    initial forces, then answers each request (seconds) with (atom-steps, busy seconds)."""
     sys.path.insert(0, str(ROOT))
     from md_tian2_gb300 import workloads as W
-    from oracle.oracle import OracleUniverse
-    us = W.config2(ntraj, seed=seed)
-    emt = W.emt_params()
-    sp = sim_params()
-    rng = np.random.default_rng(seed)
-    orcs = [OracleUniverse(u, emt) for u in us]
-    for o in orcs:
-        o.calc_force(sp)
-    t0 = time.perf_counter()
-    atom_steps = 0
-    for s in range(nsteps):
-        for o in orcs:
-            randy = rng.normal(size=o.r.shape)
-            o.propagate_1(sp, randy)
-            o.calc_force(sp)
-            o.propagate_2(sp, randy)
-            atom_steps += o.N * o.nb
-        if budget and time.perf_counter() - t0 > budget:
-            break
-    return atom_steps, time.perf_counter() - t0
-
-
-def cpu_baseline(seconds, cores=None):
-    """Oracle on `cores` processes, each advancing its own sample of trajectories."""
-    import multiprocessing as mp
     from oracle import oracle
-    oracle.build()
-    cores = cores or os.cpu_count() or 1
-    ctx = mp.get_context("spawn")
-    per = 8
-    with ctx.Pool(cores) as pool:
-        t0 = time.perf_counter()
-        res = pool.map(_cpu_worker, [(per, 1000 + k, 10 ** 6, seconds) for k in range(cores)])
-        wall = time.perf_counter() - t0
-    atom_steps = sum(r[0] for r in res)
-    busy = max(r[1] for r in res)
-    return {"value": atom_steps / busy, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"{cores} processes x {per} config-2 trajectories (seeded), FP64 oracle "
-                      f"(C++ restatement of the reference's loops), {busy:.1f} s of stepping each, "
-                      f"{atom_steps} atom-steps; pool wall {wall:.1f} s incl. start-up"}
-
-
-def _ref_proc(conn, ntraj, seed, msteps):
-    """One host core of the reference arm: builds its config-2 trajectories once, then
-    advances them by ``msteps`` MD steps per request (steady-state stepping)."""
-    sys.path.insert(0, str(ROOT))
-    from md_tian2_gb300 import workloads as W
-    from oracle.oracle import OracleUniverse
-    us = W.config2(ntraj, seed=seed)
+    us = W.config2(ntraj, seed=seed) if kind == "config2" else W.config1(ntraj, seed=seed)
     emt = W.emt_params()
-    sp = sim_params()
-    rng = np.random.default_rng(seed)
-    orcs = [OracleUniverse(u, emt) for u in us]
+    sp = sim_params() if kind == "config2" else config1_params()
+    orcs = [oracle.OracleUniverse(u, emt) for u in us]
     for o in orcs:
         o.calc_force(sp)
     conn.send("ready")
-    while conn.recv() is not None:
-        atom_steps = 0
-        for _ in range(msteps):
-            for o in orcs:
-                randy = rng.normal(size=o.r.shape)
-                o.propagate_1(sp, randy)
-                o.calc_force(sp)
-                o.propagate_2(sp, randy)
-                atom_steps += o.N * o.nb
-        conn.send(atom_steps)
+    k = 0
+    while True:
+        sec = conn.recv()
+        if sec is None:
+            break
+        k += 1
+        conn.send(oracle.run_steps(orcs, sp, sec, seed=seed * 1000003 + k))
+
+
+class CpuPool:
+    """`cores` spawned processes, each with its own sample of the workload."""
+
+    def __init__(self, cores, kind="config2", per=CPU_PER_PROC, seed0=5000):
+        import multiprocessing as mp
+        from oracle import oracle
+        oracle.build()
+        ctx = mp.get_context("spawn")
+        self.pipes, self.procs = [], []
+        for k in range(cores):
+            a, b = ctx.Pipe()
+            pr = ctx.Process(target=_cpu_proc, args=(b, kind, per, seed0 + k), daemon=True)
+            pr.start()
+            self.pipes.append(a)
+            self.procs.append(pr)
+        for a in self.pipes:
+            a.recv()
+
+    def run(self, seconds):
+        """Every process steps for `seconds`; returns (aggregate rate, atom-steps, max busy s)."""
+        for a in self.pipes:
+            a.send(seconds)
+        res = [a.recv() for a in self.pipes]
+        return sum(n / el for n, el in res if el > 0), sum(n for n, _ in res), max(el for _, el in res)
+
+    def close(self):
+        for a in self.pipes:
+            a.send(None)
+        for pr in self.procs:
+            pr.join(timeout=10)
+
+
+def config1_params():
+    from md_tian2_gb300.engine import SimParams
+    return SimParams(step=0.1, pul=6.05, use_exit=True, seed=2024)
+
+
+def cpu_baseline(seconds, cores=None):
+    """The oracle on every host core (config-2 sample, the GPU arm's workload), plus one core
+    stepping config 1 (100 H/Au(111) 3x3 trajectories, Verlet)."""
+    cores = cores or os.cpu_count() or 1
+    pool = CpuPool(cores)
+    try:
+        rate, n, busy = pool.run(seconds)
+    finally:
+        pool.close()
+    one = CpuPool(1, kind="config1", per=100, seed0=1)
+    try:
+        rate1, n1, busy1 = one.run(max(2.0, seconds / 2))
+    finally:
+        one.close()
+    return {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{cores} processes x {CPU_PER_PROC} config-2 trajectories each (seeded), FP64 oracle "
+                      f"(C++ restatement of the reference's loops, g++ -O3), stepped in C for {busy:.1f} s per "
+                      f"process, {n} atom-steps; rate = sum of per-process atom-steps / busy seconds",
+            "single_core_config1": {"value": rate1, "unit": UNIT, "cores": 1,
+                                    "sample": f"100 config-1 trajectories (3x3 Au(111) + H, Verlet), {n1} "
+                                              f"atom-steps in {busy1:.1f} s"}}
 
 
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    import multiprocessing as mp
-    from oracle import oracle
-    oracle.build()
     cores = os.cpu_count() or 1
-    ctx = mp.get_context("spawn")
-    per, msteps = 4, 200
-    pipes, procs = [], []
-    for k in range(cores):
-        a, b = ctx.Pipe()
-        p = ctx.Process(target=_ref_proc, args=(b, per, 5000 + k, msteps), daemon=True)
-        p.start()
-        pipes.append(a)
-        procs.append(p)
-    for a in pipes:
-        a.recv()  # trajectories built, initial forces evaluated
-    times, total = [], 0
+    slice_s = 1.0
+    pool = CpuPool(cores)
+    rates, total = [], 0
     try:
         for s in range(args.warmup + args.steps):
-            t0 = time.perf_counter()
-            for a in pipes:
-                a.send(1)
-            done = sum(a.recv() for a in pipes)
-            dt = time.perf_counter() - t0
+            rate, n, _ = pool.run(slice_s)
             if s >= args.warmup:
-                times.append(dt)
-                total += done
+                rates.append(rate)
+                total += n
     finally:
-        for a in pipes:
-            a.send(None)
-        for p in procs:
-            p.join(timeout=10)
-    el = sum(times)
-    val = total / el
+        pool.close()
+    val = float(np.mean(rates))
     line = {"impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * slice_s,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": "config-2 H/Au(111) EMT trajectories (Verlet H, constant-friction Langevin Au, "
                                    "dt 0.1 fs), bounded CPU sample",
-                       "sample_per_step": f"{cores} processes x {per} trajectories, {msteps} MD steps each "
-                                          "(trajectories built once before the warm-up)",
+                       "sample_per_step": f"{cores} processes x {CPU_PER_PROC} trajectories, each stepping for "
+                                          f"{slice_s} s (trajectories built once before the warm-up)",
                        "l2": "n/a (CPU)"},
             "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores, "kind": "port",
                              "sample": "oracle/md_oracle.cpp restatement of the reference (no Fortran compiler "
-                                       f"on this box): {cores} processes x {per} trajectories x {msteps} MD steps "
-                                       "per bench step, steady state"},
+                                       f"on this box), g++ -O3: {cores} processes x {CPU_PER_PROC} trajectories "
+                                       f"stepped in C, {slice_s} s per bench step; rate = sum of per-process "
+                                       f"atom-steps / busy seconds; {total} atom-steps timed"},
             "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 

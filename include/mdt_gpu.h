@@ -46,6 +46,9 @@ extern "C" {
 /* force arithmetic */
 #define MDT_PREC_FP64 0
 #define MDT_PREC_FP32 1
+#define MDT_PREC_BF16 2 /* FP32 descriptors and forces, network GEMMs on the tensor cores with
+                           BF16 operands and FP32 accumulation (thread-per-atom kernel of
+                           radial-only networks); no counterpart in the reference */
 
 /* trajectory status (mdt_traj_summary.status) */
 #define MDT_TRAJ_RUNNING 0
@@ -53,6 +56,8 @@ extern "C" {
 #define MDT_TRAJ_EXIT_LOWER 2   /* projectile below pll, md_tian2.f90:91-92 */
 #define MDT_TRAJ_STEP_LIMIT 3   /* the step limit (nsteps) was reached, md_tian2.f90:78 */
 #define MDT_TRAJ_ERR_DENSITY -10 /* negative EMT density in ldfa, md_algo.f90:551-554 */
+#define MDT_TRAJ_ERR_NONFINITE -11 /* a position or velocity stopped being finite (fused MD
+                                      steps only; the reference has no such check) */
 
 typedef struct mdt_ctx mdt_ctx;
 
@@ -248,18 +253,24 @@ int32_t mdt_set_random_arrays(mdt_ctx *ctx, const double *randy, const double *z
    that has run max_steps steps stops with status MDT_TRAJ_STEP_LIMIT (0 = no limit). */
 int32_t mdt_set_step_limit(mdt_ctx *ctx, int32_t max_steps);
 
-/* Refill (prepare_next_traj, src/md_init.f90:880-944, on the device): every trajectory whose
-   status is not MDT_TRAJ_RUNNING gets the state of the last mdt_state_upload back, and its
-   projectile (atom 0, every bead) a new start: a uniform position in the plane of the first
-   two cell vectors at height z0 and the incidence velocity of set_proj_incidence
-   (md_init.f90:829-876) for an energy uniform in [einc_min, einc_max] eV, a polar angle
-   uniform in [polar_min, polar_max] degrees and the azimuth (degrees; < 0: uniform), drawn
-   from a counter-based generator keyed by (seed, trajectory, generation).  Status, step
-   count and trajectory observables restart; generation[t] (may be NULL) counts the refills
-   of each trajectory.  Forces are stale afterwards: call mdt_calc_force before the next
-   mdt_md_steps, as after an upload.  Lets a batch run a stream of trajectories on the GPU
-   without uploading new states (no replacement in the reference, which runs one trajectory
-   at a time). */
+/* Refill (prepare_next_traj, src/md_init.f90:880-944, on the device): every trajectory that
+   ended normally (status MDT_TRAJ_EXIT_UPPER, _EXIT_LOWER or _STEP_LIMIT) gets the state of the
+   last mdt_state_upload back, and its projectile (atom 0) a new start the way apply_pip
+   (md_init.f90:546-549) and set_proj_incidence (:829-876) place it: the bead centroid moves to
+   a uniform position in the plane of the first two cell vectors at height z0 (every bead moves
+   by target - centroid, so the ring polymer keeps its spread) and the bead velocities lose
+   their mean and gain the incidence velocity for an energy uniform in [einc_min, einc_max] eV,
+   a polar angle uniform in [polar_min, polar_max] degrees and the azimuth (degrees; < 0:
+   uniform), drawn from a counter-based generator keyed by (seed, trajectory, generation).
+   Trajectories with an error status (MDT_TRAJ_ERR_*) keep their state and status, so the
+   caller sees them.  Status, step count and trajectory observables restart; generation[t]
+   (may be NULL) counts the refills of each trajectory.  Forces are stale afterwards: call
+   mdt_calc_force before the next mdt_md_steps, as after an upload.
+   Differences from prepare_next_traj, which reads a new slab file and a new projectile file
+   for every trajectory and draws einc from N(einc, sigma_einc): a trajectory slot restarts
+   from its own uploaded slab every time (one slab microstate per slot; upload a new state to
+   change it), and einc is uniform.  Lets a batch run a stream of trajectories on the GPU
+   without uploading new states (the reference runs one trajectory at a time). */
 typedef struct mdt_refill_params {
     double z0;
     double einc_min, einc_max;
@@ -298,7 +309,7 @@ int32_t mdt_device_state(mdt_ctx *ctx, void **ptrs, int64_t *nslots);
  * (MDT_ERR_TOO_LARGE beyond).  All array arguments except simbox and the EMT
  * parameters are DEVICE pointers: idx (natoms, 1-based types), x/y/z positions (A),
  * outputs fx/fy/fz (eV/A, overwritten), energy (one double, eV, overwritten; NaN if a
- * type index is out of range), dens (embedded density per atom, may be NULL).
+ * type index is outside [1, ntypes]), dens (embedded density per atom, may be NULL).
  * simbox: host, 9 doubles column major.  EMT parameters and the pes table: host, as
  * for mdt_emt_set_params.  The call is asynchronous on `stream` (NULL = default
  * stream).  The first call on a device looks up the scratch array's address and must

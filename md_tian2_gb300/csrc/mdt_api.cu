@@ -84,6 +84,7 @@ struct mdt_ctx {
     int *rptraj = nullptr;     // trajectories of the packs
     int rnpack = 0, rblock = 0;
     int rmaxblock = kRBlockMax; // largest block the pack plan may use
+    int *tcerr = nullptr;       // device word: a tensor-core GEMM of the network timed out
 
     // training (buffers live with the batch)
     bool have_labels = false;
@@ -95,6 +96,10 @@ struct mdt_ctx {
 };
 
 namespace {
+
+const char *const kBf16Scope =
+    "MDT_PREC_BF16 runs the network GEMMs on the tensor cores in the thread-per-atom kernel only: a radial-only "
+    "network (mdt_nn_radial_kernel) on single-bead trajectories of at most 512 atoms";
 
 int fail(mdt_ctx *c, int code, const std::string &msg) {
     if (c) c->err = msg;
@@ -666,16 +671,32 @@ bool radial_plan(mdt_ctx *c) {
 // The thread-per-atom kernel runs FP32 forces of an admitted model; the fused MD step also
 // needs single-bead trajectories with Verlet or constant-friction Langevin propagators.
 bool use_radial(mdt_ctx *c, int precision, bool md) {
-    if (precision != MDT_PREC_FP32 || !c->R.ok || !c->radial_enabled || !c->fast_enabled) return false;
+    if ((precision != MDT_PREC_FP32 && precision != MDT_PREC_BF16) || !c->R.ok || !c->radial_enabled ||
+        !c->fast_enabled)
+        return false;
     if (md)
         for (int t = 0; t < c->ntypes; ++t)
             if (c->B.algo[t] != kPropVerlet && c->B.algo[t] != kPropLangevinConst) return false;
     return radial_plan(c);
 }
 
-int run_radial(mdt_ctx *c, const PropParams &P, int nsteps, int mode, bool surr) {
+int run_radial(mdt_ctx *c, const PropParams &P, int nsteps, int mode, bool surr, bool tc) {
     RadialNN &R = c->R;
     R.block = c->rblock;
+    R.tc = tc ? 1 : 0;
+    if (tc) {
+        int dev = 0, optin = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        if (nnr_smem(R) > (size_t)optin || nnr_emt_smem(c->max_atoms) > nnr_hb_bytes(R))
+            return fail(c, MDT_ERR_UNSUPPORTED, "BF16 network: trajectories too large for the kernel's shared memory");
+        if (!c->tcerr) {
+            cudaError_t e = cudaMalloc(&c->tcerr, sizeof(int));
+            if (e == cudaSuccess) e = cudaMemsetAsync(c->tcerr, 0, sizeof(int), c->stream);
+            if (e != cudaSuccess) return cuda_fail(c, e, "tensor-core status word");
+        }
+    }
+    c->X.tcerr = c->tcerr;
     const int per_sm = std::max(1, nnr_resident_ctas(R));
     const int grid = std::max(1, std::min(c->rnpack, c->num_sms * per_sm));
     int rc = ensure_mscr(c, grid, 1);
@@ -777,6 +798,7 @@ int32_t mdt_destroy(mdt_ctx *c) {
     free_batch(c);
     for (void *p : c->nnbufs) cudaFree(p);
     if (c->mscr) cudaFree(c->mscr);
+    if (c->tcerr) cudaFree(c->tcerr);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return MDT_OK;
@@ -789,7 +811,14 @@ int64_t mdt_launch_count(const mdt_ctx *c) { return c ? c->launches : -1; }
 int32_t mdt_synchronize(mdt_ctx *c) {
     if (!c) return MDT_ERR_ARG;
     cudaError_t e = cudaStreamSynchronize(c->stream);
-    return e == cudaSuccess ? MDT_OK : cuda_fail(c, e, "mdt_synchronize");
+    if (e != cudaSuccess) return cuda_fail(c, e, "mdt_synchronize");
+    if (c->tcerr) {
+        int h = 0;
+        e = cudaMemcpy(&h, c->tcerr, sizeof(int), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return cuda_fail(c, e, "mdt_synchronize");
+        if (h) return fail(c, MDT_ERR_CUDA, "a tensor-core GEMM of the network did not complete within its wait limit");
+    }
+    return MDT_OK;
 }
 
 int32_t mdt_set_stream(mdt_ctx *c, void *s) {
@@ -808,8 +837,8 @@ int32_t mdt_set_stream(mdt_ctx *c, void *s) {
     return MDT_OK;
 }
 
-// Derived constants of compute_emt_1species / compute_emt_2species
-// (src/pes_emt_mod.f90:258-307 and 521-592), computed in the same order.
+// read_emt's parameters and the derived constants of compute_emt_1species /
+// compute_emt_2species (src/pes_emt_mod.f90:258-307 and 521-592)
 int32_t mdt_emt_set_params(mdt_ctx *c, int32_t ntypes, const double *eta2, const double *n0, const double *e0,
                            const double *lambda, const double *v0, const double *kappa, const double *s0,
                            const int32_t *pes) {
@@ -817,64 +846,9 @@ int32_t mdt_emt_set_params(mdt_ctx *c, int32_t ntypes, const double *eta2, const
     if (ntypes < 1 || ntypes > kMaxTypes || !eta2 || !n0 || !e0 || !lambda || !v0 || !kappa || !s0 || !pes)
         return fail(c, MDT_ERR_ARG, "mdt_emt_set_params: bad arguments (1 <= ntypes <= 4)");
     EmtConst E{};
-    int slots[2] = {-1, -1}, ns = 0;
-    for (int t = 0; t < kMaxTypes; ++t) E.slot_of_type[t] = -1;
-    for (int t = 0; t < ntypes; ++t)
-        if (pes[t * ntypes + t] == MDT_PES_EMT) {
-            if (ns >= 2) return fail(c, MDT_ERR_UNSUPPORTED, "more than two EMT species (compute_emt_nspecies)");
-            slots[ns] = t;
-            E.slot_of_type[t] = ns++;
-        }
-    if (ns == 0) return fail(c, MDT_ERR_ARG, "no EMT species in the pes table");
-    E.nspecies = ns;
-    E.pair_mask = 0;
-    for (int a = 0; a < ntypes; ++a)
-        for (int b = 0; b < ntypes; ++b)
-            if (pes[b * ntypes + a] == MDT_PES_EMT && E.slot_of_type[a] >= 0 && E.slot_of_type[b] >= 0)
-                E.pair_mask |= 1u << (a * kMaxTypes + b);
-    const double beta = std::pow(16.0 * kPi / 3.0, 1.0 / 3.0) * (1.0 / kSqrt2);
-    const double nneighs[3] = {12.0, 6.0, 24.0};
-    double bs0[2] = {0, 0};
-    for (int s = 0; s < ns; ++s) {
-        const int t = slots[s];
-        E.eta2[s] = eta2[t];
-        E.n0[s] = n0[t];
-        E.e0[s] = e0[t];
-        E.lambda[s] = lambda[t];
-        E.kappa[s] = kappa[t];
-        E.v0[s] = v0[t];
-        bs0[s] = beta * s0[t];
-        E.betas0[s] = bs0[s];
-        E.betaeta2[s] = beta * eta2[t];
-        E.kappadbeta[s] = kappa[t] / beta;
-    }
-    const double rcut = (ns == 2 ? std::max(bs0[0], bs0[1]) : bs0[0]) * kSqrt3;
-    const double rr = 4.0 * rcut / (kSqrt3 + 2);
-    const double acut = 9.21034037197618 / (rr - rcut);
-    E.rcut = rcut;
-    E.acut = acut;
-    E.cut = 1.5 * rcut;
-    E.cut2 = E.cut * E.cut;
-    for (int s = 0; s < ns; ++s) {
-        const double rnn[3] = {bs0[s], bs0[s] * kSqrt2, bs0[s] * kSqrt3};
-        double x[3], g1 = 0, g2 = 0;
-        for (int k = 0; k < 3; ++k) x[k] = nneighs[k] * kTwelfth / (1 + std::exp(acut * (rnn[k] - rcut)));
-        for (int k = 0; k < 3; ++k) g1 += x[k] * std::exp(-E.eta2[s] * (rnn[k] - bs0[s]));
-        for (int k = 0; k < 3; ++k) g2 += x[k] * std::exp(-E.kappadbeta[s] * (rnn[k] - bs0[s]));
-        E.igamma1[s] = 1.0 / g1;
-        E.g2v0[s] = (1.0 / g2) * E.v0[s];
-        E.dens_exp[s] = 0.5 / kBohr2Ang - E.betaeta2[s];
-    }
-    E.chi[0][0] = E.chi[1][1] = 1.0;
-    E.chi[0][1] = E.chi[1][0] = 1.0;
-    if (ns == 2) {
-        const int t1 = slots[0], t2 = slots[1];
-        const double chi_21 = n0[t1] / n0[t2] * std::exp(0.5 / kBohr2Ang * (s0[t2] - s0[t1]));
-        const double chi_12 = 1.0 / chi_21;
-        E.chi[0][1] = chi_12;  // density at a type1 atom from a type2 neighbour
-        E.chi[1][0] = chi_21;
-        E.hh_quirk = 1;
-    }
+    const int rc = emt_derive_constants(ntypes, eta2, n0, e0, lambda, v0, kappa, s0, pes, E);
+    if (rc == MDT_ERR_UNSUPPORTED) return fail(c, rc, "more than two EMT species (compute_emt_nspecies)");
+    if (rc != MDT_OK) return fail(c, rc, "no EMT species in the pes table");
     c->E = E;
     c->have_emt = true;
     c->pes_ntypes = ntypes;
@@ -1196,14 +1170,18 @@ int32_t mdt_calc_force(mdt_ctx *c, int32_t flag, int32_t precision, const mdt_pr
     int rc = check_ready(c, c && c->pes_kind == MDT_PES_EMT);
     if (rc) return rc;
     if (flag != MDT_ENERGY_AND_FORCE && flag != MDT_ENERGY_ONLY) return fail(c, MDT_ERR_ARG, "bad flag");
-    if (precision != MDT_PREC_FP64 && precision != MDT_PREC_FP32) return fail(c, MDT_ERR_ARG, "bad precision");
+    if (precision != MDT_PREC_FP64 && precision != MDT_PREC_FP32 && precision != MDT_PREC_BF16)
+        return fail(c, MDT_ERR_ARG, "bad precision");
+    if (precision == MDT_PREC_BF16 && c->pes_kind == MDT_PES_EMT) return fail(c, MDT_ERR_UNSUPPORTED, kBf16Scope);
     if ((rc = check_params(c, p, false))) return rc;
     if (c->pes_kind != MDT_PES_EMT) {
         if ((rc = check_nn_ready(c))) return rc;
         if (c->pes_kind == MDT_PES_SURROGATE && (rc = ensure_scratch(c, MDT_PREC_FP64))) return rc;
         const PropParams P = to_dev(c, p);
         const bool surr = c->pes_kind == MDT_PES_SURROGATE;
-        if (use_radial(c, precision, false)) return run_radial(c, P, 0, flag == MDT_ENERGY_ONLY ? 1 : 0, surr);
+        if (use_radial(c, precision, false))
+            return run_radial(c, P, 0, flag == MDT_ENERGY_ONLY ? 1 : 0, surr, precision == MDT_PREC_BF16);
+        if (precision == MDT_PREC_BF16) return fail(c, MDT_ERR_UNSUPPORTED, kBf16Scope);
         const bool fast = use_fast(c, precision);
         const LaunchCfg fcfg = fast ? nnf_cfg(c) : LaunchCfg{};
         if (fast && (rc = ensure_mscr(c, fcfg.grid, 0))) return rc;
@@ -1247,7 +1225,9 @@ int32_t mdt_md_steps(mdt_ctx *c, int32_t nsteps, int32_t precision, const mdt_pr
     int rc = check_ready(c, c && c->pes_kind == MDT_PES_EMT);
     if (rc) return rc;
     if (nsteps < 0) return fail(c, MDT_ERR_ARG, "nsteps < 0");
-    if (precision != MDT_PREC_FP64 && precision != MDT_PREC_FP32) return fail(c, MDT_ERR_ARG, "bad precision");
+    if (precision != MDT_PREC_FP64 && precision != MDT_PREC_FP32 && precision != MDT_PREC_BF16)
+        return fail(c, MDT_ERR_ARG, "bad precision");
+    if (precision == MDT_PREC_BF16 && c->pes_kind == MDT_PES_EMT) return fail(c, MDT_ERR_UNSUPPORTED, kBf16Scope);
     if ((rc = check_params(c, p))) return rc;
     if (p->rng_mode == 1 && nsteps > 1) return fail(c, MDT_ERR_ARG, "rng_mode 1 supports one step per call");
     if (c->pes_kind != MDT_PES_EMT) {
@@ -1256,7 +1236,8 @@ int32_t mdt_md_steps(mdt_ctx *c, int32_t nsteps, int32_t precision, const mdt_pr
         if (nsteps == 0) return MDT_OK;
         const PropParams P = to_dev(c, p);
         const bool surr = c->pes_kind == MDT_PES_SURROGATE;
-        if (use_radial(c, precision, true)) return run_radial(c, P, nsteps, 2, surr);
+        if (use_radial(c, precision, true)) return run_radial(c, P, nsteps, 2, surr, precision == MDT_PREC_BF16);
+        if (precision == MDT_PREC_BF16) return fail(c, MDT_ERR_UNSUPPORTED, kBf16Scope);
         const bool fast = use_fast(c, precision);
         const LaunchCfg fcfg = fast ? nnf_cfg(c) : LaunchCfg{};
         if (fast && (rc = ensure_mscr(c, fcfg.grid, 0))) return rc;

@@ -39,6 +39,11 @@ int nnf_resident_ctas(const Batch &B, const NNDev &M, const FastNN &F);
 cudaError_t launch_nnf(const LaunchCfg &c, const Batch &B, const NNDev &M, const FastNN &F, const EmtConst &E,
                        const NNScratch &X, const PropParams &P, int nsteps, int mode, bool surrogate);
 
+// derived EMT constants (mdt_noalloc.cu), shared by both EMT entry points
+int emt_derive_constants(int32_t ntypes, const double *eta2, const double *n0, const double *e0,
+                         const double *lambda, const double *v0, const double *kappa, const double *s0,
+                         const int32_t *pes, EmtConst &E);
+
 cudaError_t launch_obs_reset(cudaStream_t s, const Batch &B);
 cudaError_t launch_refill(cudaStream_t s, const Batch &B, const double *tmpl, int64_t total_ba, double z0,
                           double emin, double emax, double pmin, double pmax, double azimuth, uint64_t seed,
@@ -49,6 +54,7 @@ cudaError_t launch_refill(cudaStream_t s, const Batch &B, const double *tmpl, in
 // admits, 0 = none): sets R.ka, R.kb, R.bla, R.blb
 bool nnr_shape(int cnt0, int cnt1, int nh, const int *maxbl, RadialNN &R);
 size_t nnr_smem(const RadialNN &R);
+size_t nnr_hb_bytes(const RadialNN &R);  // network buffer / tensor-core operand area (EMT fallback area)
 size_t nnr_emt_smem(int max_atoms);  // EMT fallback area (aliases the network buffers)
 int nnr_resident_ctas(const RadialNN &R);
 cudaError_t launch_nnr(const LaunchCfg &c, const Batch &B, const RadialNN &R, const EmtConst &E, const NNScratch &X,

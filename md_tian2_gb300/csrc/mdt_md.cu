@@ -103,7 +103,6 @@ __global__ void __launch_bounds__(kBlock, 4) md_steps_kernel(Batch B, EmtConst E
         const int t = order[w];
         const TrajView T = traj_view(B, t);
         load_cjk(B, t, S.cjk);
-        const int ty0 = B.type[T.aoff];
         for (int s = 0; s < nsteps; ++s) {
             if (B.status[t] != kStatusRunning) break;
             const int step = B.steps_done[t] + 1;
@@ -114,22 +113,7 @@ __global__ void __launch_bounds__(kBlock, 4) md_steps_kernel(Batch B, EmtConst E
                 const double dmin = closest_approach_step(B, T, S.cell, S.red);
                 if (threadIdx.x == 0) observe_step(B, T, step, dmin);
             }
-            if (threadIdx.x == 0) {
-                B.steps_done[t] = step;
-                if (P.use_exit && B.is_proj[ty0] && B.status[t] == kStatusRunning) {
-                    bool up = true, lo = true;
-                    for (int b = 0; b < T.nb; ++b) {
-                        const double z = B.rz[T.base + (int64_t)b * T.N];
-                        up = up && (z > P.pul);
-                        lo = lo && (z < P.pll);
-                    }
-                    if (up) B.status[t] = kStatusExitUpper;
-                    else if (lo) B.status[t] = kStatusExitLower;
-                }
-                if (P.max_steps > 0 && step >= P.max_steps && B.status[t] == kStatusRunning)
-                    B.status[t] = kStatusStepLimit;
-            }
-            __syncthreads();
+            end_of_step(B, P, T, step);
         }
     }
 }
@@ -153,20 +137,27 @@ cudaError_t launch_obs_reset(cudaStream_t s, const Batch &B) {
 }
 
 // Refill of stopped trajectories (the set-up of md_init.f90 for the next trajectory,
-// prepare_next_traj :880-944, on the device): every bead-atom of a trajectory whose status
-// is not running gets the state of the last upload back; the projectile (atom 0) is
-// placed at a uniform direct (u, v) in the first two cell vectors at height z0 with the
-// incidence velocity of set_proj_incidence (:829-876) for an energy, polar and azimuth
-// drawn uniformly (Philox keyed by seed, trajectory and generation), on every bead.
+// prepare_next_traj :880-944, on the device): every bead-atom of a trajectory that ended
+// normally (status 1-3; trajectories with an error status keep their state and status)
+// gets the state of the last upload back; then the projectile (atom 0) is moved the way
+// apply_pip (:546-549) and set_proj_incidence (:829-876) move it: its bead centroid goes to
+// a uniform direct (u, v) in the first two cell vectors at height z0 (r_b - centroid +
+// target, so the ring polymer keeps its spread), and its bead velocities lose their mean
+// (remove_atomic_com) and gain the incidence velocity for an energy, polar and azimuth
+// drawn uniformly (Philox keyed by seed, trajectory and generation).
 struct RefillDev {
     double z0, emin, emax, pmin, pmax, azimuth;  // azimuth < 0: uniform in [0, 360)
     uint64_t seed;
 };
 
+__device__ __forceinline__ bool refillable(int status) {
+    return status == kStatusExitUpper || status == kStatusExitLower || status == kStatusStepLimit;
+}
+
 __global__ void refill_kernel(Batch B, const double *tmpl, int64_t total_ba, RefillDev R, int *gen, int *skok,
                               int *count) {
     for (int t = blockIdx.x; t < B.ntraj; t += gridDim.x) {
-        if (B.status[t] == kStatusRunning) continue;  // uniform over the block
+        if (!refillable(B.status[t])) continue;  // uniform over the block
         const TrajView T = traj_view(B, t);
         const int64_t n = (int64_t)T.nb * T.N;
         double *dst[6] = {B.rx, B.ry, B.rz, B.vx, B.vy, B.vz};
@@ -185,17 +176,24 @@ __global__ void refill_kernel(Batch B, const double *tmpl, int64_t total_ba, Ref
             const double azi = (R.azimuth < 0.0 ? 360.0 * uniform_deviate(R.seed, tt, gg, 4, kStreamRefill)
                                                 : R.azimuth) * (kPi / 180.0);
             const double *h = B.box + 9 * (size_t)t;  // column major: h[3 k + d] = component d of vector k
-            const double x = h[0] * u + h[3] * w, y = h[1] * u + h[4] * w;
+            const double target[3] = {h[0] * u + h[3] * w, h[1] * u + h[4] * w, R.z0};
             const double vinc = sqrt(2.0 * e / B.mass[T.aoff]);
-            const double vx = vinc * sin(pol) * cos(azi), vy = vinc * sin(pol) * sin(azi), vz = -vinc * cos(pol);
-            for (int b = 0; b < T.nb; ++b) {
-                const int64_t k = T.base + (int64_t)b * T.N;
-                B.rx[k] = x;
-                B.ry[k] = y;
-                B.rz[k] = R.z0;
-                B.vx[k] = vx;
-                B.vy[k] = vy;
-                B.vz[k] = vz;
+            const double vi[3] = {vinc * sin(pol) * cos(azi), vinc * sin(pol) * sin(azi), -vinc * cos(pol)};
+            double *r[3] = {B.rx, B.ry, B.rz}, *v[3] = {B.vx, B.vy, B.vz};
+            for (int d = 0; d < 3; ++d) {
+                double cr = 0.0, cv = 0.0;
+                for (int b = 0; b < T.nb; ++b) {
+                    const int64_t k = T.base + (int64_t)b * T.N;
+                    cr += r[d][k];
+                    cv += v[d][k];
+                }
+                cr /= T.nb;
+                cv /= T.nb;
+                for (int b = 0; b < T.nb; ++b) {
+                    const int64_t k = T.base + (int64_t)b * T.N;
+                    r[d][k] = r[d][k] - cr + target[d];
+                    v[d][k] = v[d][k] - cv + vi[d];
+                }
             }
             if (skok)
                 for (int b = 0; b < T.nb; ++b) skok[B.bead_off[t] + b] = 0;

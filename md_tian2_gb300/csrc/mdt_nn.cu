@@ -324,7 +324,6 @@ __global__ void __launch_bounds__(kNNBlock) nn_md_steps_kernel(Batch B, NNDev M,
         const int t = order[w];
         const TrajView T = traj_view(B, t);
         load_cjk(B, t, SE.cjk);
-        const int ty0 = B.type[T.aoff];
         for (int s = 0; s < nsteps; ++s) {
             if (B.status[t] != kStatusRunning) break;
             const int step = B.steps_done[t] + 1;
@@ -335,22 +334,7 @@ __global__ void __launch_bounds__(kNNBlock) nn_md_steps_kernel(Batch B, NNDev M,
                 const double dmin = closest_approach_step(B, T, SE.cell, SE.red);
                 if (threadIdx.x == 0) observe_step(B, T, step, dmin);
             }
-            if (threadIdx.x == 0) {
-                B.steps_done[t] = step;
-                if (P.use_exit && B.is_proj[ty0] && B.status[t] == kStatusRunning) {
-                    bool up = true, lo = true;
-                    for (int b = 0; b < T.nb; ++b) {
-                        const double z = B.rz[T.base + (int64_t)b * T.N];
-                        up = up && (z > P.pul);
-                        lo = lo && (z < P.pll);
-                    }
-                    if (up) B.status[t] = kStatusExitUpper;
-                    else if (lo) B.status[t] = kStatusExitLower;
-                }
-                if (P.max_steps > 0 && step >= P.max_steps && B.status[t] == kStatusRunning)
-                    B.status[t] = kStatusStepLimit;
-            }
-            __syncthreads();
+            end_of_step(B, P, T, step);
         }
     }
 }

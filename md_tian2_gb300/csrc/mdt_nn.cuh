@@ -119,6 +119,26 @@ __host__ __device__ constexpr int nnr_hbw(int nin, int nh) {
     return nin > (nh == 2 ? 64 : 32) ? nin : (nh == 2 ? 64 : 32);
 }
 
+// Tensor-core (BF16 in, FP32 accumulate) network of the same kernel: the atoms of a CTA
+// are four 128-row tiles; per tile and layer one GEMM (M = 128) runs on tcgen05 with the
+// operand rows in shared memory and the accumulator in TMEM.  Inputs are padded to a
+// multiple of 16 (KP), hidden layers to 32; the operand buffer of a tile holds rows of
+// TW = max(KP, 32) bf16 values.  Per element the B operands are W1^T (32 x KP), W2^T and
+// W2 (32 x 32) and W1 (KP x 32), K-major; biases and the output weights stay FP32.
+__host__ __device__ constexpr int nnr_kp(int nin) { return (nin + 15) & ~15; }
+__host__ __device__ constexpr int nnr_tw(int nin) { return nnr_kp(nin) > 32 ? nnr_kp(nin) : 32; }
+__host__ __device__ constexpr int nnr_tc_bel(int nin) { return 2 * (32 * nnr_kp(nin) * 2) + 2 * 2048; }
+constexpr int kTcVec = 100;          // FP32 vector floats per element (b1, b2 / w2, w3, b3, pad)
+constexpr int kTcTiles = kRBlockMax / 128;
+constexpr int kTcCols = 512;         // TMEM columns of a CTA (D of both elements + a spill, per tile)
+constexpr size_t kTcEmtMin = 36864;  // the operand area doubles as the FP64 EMT fallback area
+__host__ __device__ constexpr size_t nnr_tc_hb(int nin) {
+    return (size_t)kTcTiles * 128 * nnr_tw(nin) * 2 > kTcEmtMin ? (size_t)kTcTiles * 128 * nnr_tw(nin) * 2
+                                                                  : kTcEmtMin;
+}
+__host__ __device__ constexpr int nnr_tc_cpt(int nin) { return 2 * nnr_tw(nin) + 32; }
+static_assert(kTcTiles * nnr_tc_cpt(48) <= kTcCols, "TMEM columns of the widest shape");
+
 struct RadialNN {
     int ok;
     int ka, kb, nh;                 // kernel shape: padded functions per group, hidden layers
@@ -145,6 +165,7 @@ struct RadialNN {
     const float4 *fscal;            // FastNN::scal / dscal (model order), permuted at kernel start
     const float *fdscal;
     int maxsf;
+    int tc;                         // 1: network GEMMs on the tensor cores (BF16 operands)
 };
 
 // ---------------------------------------------------------------------------
@@ -166,6 +187,7 @@ struct NNScratch {
     double *skref;
     int *skok;
     int skcap;
+    int *tcerr;        // set when a tensor-core GEMM did not complete within its wait limit
 };
 
 // ---------------------------------------------------------------------------

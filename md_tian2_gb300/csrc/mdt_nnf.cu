@@ -1242,7 +1242,6 @@ __global__ void __launch_bounds__(kFBlock, 3)
             nnf_calc_force<NG, ZM, G3ON>(B, M, F, E, X, P, S, SE, L, T, mode == 0);
             continue;
         }
-        const int ty0 = B.type[T.aoff];
         for (int s = 0; s < nsteps; ++s) {
             if (B.status[t] != kStatusRunning) break;
             const int step = B.steps_done[t] + 1;
@@ -1253,22 +1252,7 @@ __global__ void __launch_bounds__(kFBlock, 3)
                 const double dmin = closest_approach_step(B, T, SE.cell, SE.red);
                 if (threadIdx.x == 0) observe_step(B, T, step, dmin);
             }
-            if (threadIdx.x == 0) {
-                B.steps_done[t] = step;
-                if (P.use_exit && B.is_proj[ty0] && B.status[t] == kStatusRunning) {
-                    bool up = true, lo = true;
-                    for (int b = 0; b < T.nb; ++b) {
-                        const double z = B.rz[T.base + (int64_t)b * T.N];
-                        up = up && (z > P.pul);
-                        lo = lo && (z < P.pll);
-                    }
-                    if (up) B.status[t] = kStatusExitUpper;
-                    else if (lo) B.status[t] = kStatusExitLower;
-                }
-                if (P.max_steps > 0 && step >= P.max_steps && B.status[t] == kStatusRunning)
-                    B.status[t] = kStatusStepLimit;
-            }
-            __syncthreads();
+            end_of_step(B, P, T, step);
         }
     }
 }

@@ -38,6 +38,7 @@
 #include "mdt_nn.cuh"
 #include "mdt_acsf.cuh"
 #include "mdt_prop.cuh"
+#include "mdt_tc.cuh"
 
 namespace mdt {
 
@@ -59,8 +60,15 @@ struct SmemR {
     float *dscal;                        // [e][q]
     int *tr_t, *tr_st, *tr_n;
     // per-step flags, buffered by step (step & 1; tr_stat by step % 3): descriptors out of
-    // range, largest squared displacement, skin-list overflow, running during the step
-    int *tr_flag, *tr_d2, *tr_over, *tr_stat;
+    // range, largest squared displacement, skin-list overflow, state not finite, running
+    // during the step
+    int *tr_flag, *tr_d2, *tr_over, *tr_bad, *tr_stat;
+    // tensor-core network (TC kernels): A-operand tiles (alias hb), bf16 B operands and FP32
+    // vectors of both elements, one mbarrier per 128-row tile, the TMEM base address
+    unsigned char *at, *wb;
+    float *wv;
+    uint64_t *tcbar;
+    uint32_t *tslot;
     float *tr_lat;                       // [s][24]: lattice rows (9), inverse rows (9), skin half-widths (3)
     double *red;
     int *misc;                           // [0] pack taken from the work queue
@@ -73,14 +81,23 @@ __host__ __device__ constexpr size_t r16r(size_t b) { return (b + 15) & ~size_t(
 // compile-time constant of the shape, so no shared-memory address occupies a register)
 constexpr int kRS = kRBlockMax;
 
-__host__ __device__ constexpr size_t smem_r(int nin, int nh) {
-    return 6 * r16r(4 * (size_t)kRS) + r16r(12 * (size_t)kRS) + r16r(8 * (size_t)kRS) + r16r(64 * (size_t)kRS) +
-           r16r(8 * (size_t)kRS) + r16r(kRS) +
-           r16r(4 * (size_t)nnr_hbw(nin, nh) * kRS) + r16r(4 * (size_t)nnr_wtotal(nin, nh)) + r16r(16 * 2 * (size_t)nin) +
-           r16r(4 * 2 * (size_t)nin) + 3 * r16r(4 * kRMaxTraj) + 3 * r16r(8 * kRMaxTraj) + r16r(12 * kRMaxTraj) + r16r(4 * 24 * kRMaxTraj) + r16r(8 * 64) + r16r(16);
+// per-thread network buffer (FP32 network) or operand tiles (tensor-core network); either
+// doubles as the EMT fallback area
+__host__ __device__ constexpr size_t hb_bytes(int nin, int nh, bool tc) {
+    return tc ? nnr_tc_hb(nin) : 4 * (size_t)nnr_hbw(nin, nh) * kRS;
+}
+__host__ __device__ constexpr size_t w_bytes(int nin, int nh, bool tc) {
+    return tc ? 2 * (size_t)nnr_tc_bel(nin) + 2 * 4 * (size_t)kTcVec : 4 * (size_t)nnr_wtotal(nin, nh);
 }
 
-template <int NIN, int NH>
+__host__ __device__ constexpr size_t smem_r(int nin, int nh, bool tc) {
+    return 6 * r16r(4 * (size_t)kRS) + r16r(12 * (size_t)kRS) + r16r(8 * (size_t)kRS) + r16r(64 * (size_t)kRS) +
+           r16r(8 * (size_t)kRS) + r16r(kRS) + r16r(hb_bytes(nin, nh, tc)) + r16r(w_bytes(nin, nh, tc)) +
+           r16r(16 * 2 * (size_t)nin) + r16r(4 * 2 * (size_t)nin) + 3 * r16r(4 * kRMaxTraj) + 4 * r16r(8 * kRMaxTraj) +
+           r16r(12 * kRMaxTraj) + r16r(4 * 24 * kRMaxTraj) + r16r(8 * 64) + r16r(16) + r16r(8 * kTcTiles) + r16r(16);
+}
+
+template <int NIN, int NH, bool TC>
 __device__ __forceinline__ SmemR carve_r(unsigned char *base) {
     SmemR s;
     size_t off = 0;
@@ -100,9 +117,12 @@ __device__ __forceinline__ SmemR carve_r(unsigned char *base) {
     s.lc = (double *)take(64 * (size_t)kRS);
     s.im = (double *)take(8 * (size_t)kRS);
     s.elem = (int8_t *)take(kRS);
-    s.hb = (float *)take(4 * (size_t)nnr_hbw(NIN, NH) * kRS);
+    s.hb = (float *)take(hb_bytes(NIN, NH, TC));
     s.emt = (unsigned char *)s.hb;
-    s.w = (float *)take(4 * (size_t)nnr_wtotal(NIN, NH));
+    s.at = (unsigned char *)s.hb;
+    s.w = (float *)take(w_bytes(NIN, NH, TC));
+    s.wb = (unsigned char *)s.w;
+    s.wv = (float *)(s.wb + 2 * (size_t)nnr_tc_bel(NIN));
     s.scal = (float4 *)take(16 * 2 * (size_t)NIN);
     s.dscal = (float *)take(4 * 2 * (size_t)NIN);
     s.tr_t = (int *)take(4 * kRMaxTraj);
@@ -111,10 +131,13 @@ __device__ __forceinline__ SmemR carve_r(unsigned char *base) {
     s.tr_flag = (int *)take(8 * kRMaxTraj);
     s.tr_d2 = (int *)take(8 * kRMaxTraj);
     s.tr_over = (int *)take(8 * kRMaxTraj);
+    s.tr_bad = (int *)take(8 * kRMaxTraj);
     s.tr_stat = (int *)take(12 * kRMaxTraj);
     s.tr_lat = (float *)take(4 * 24 * kRMaxTraj);
     s.red = (double *)take(8 * 64);
     s.misc = (int *)take(16);
+    s.tcbar = (uint64_t *)take(8 * kTcTiles);
+    s.tslot = (uint32_t *)take(16);
     return s;
 }
 
@@ -449,16 +472,16 @@ __device__ __forceinline__ float nnr_network(const RadialNN &R, const SmemR &S, 
     return out;
 }
 
-// ---- one force evaluation of the atom: descriptors, network, forces ------------------
+// ---- one force evaluation of the atom: descriptors, (network,) forces --------------------
 // BLA / BLB: block length of the shifted-Gaussian recurrence of group 0 / 1 (0: one 2^x
-// per function)
-template <int KA, int KB, int NH, int BLA, int BLB>
-__device__ __forceinline__ double nnr_atom(const RadialNN &R, const NNScratch &X, const SmemR &S, const AtomR &A,
-                                           int tid, bool do_forces, int *flag, float &rmin2, float &fix, float &fiy,
-                                           float &fiz) {
-    constexpr int KT = KA + KB, bs = kRS;
-    const unsigned *sk = reinterpret_cast<const unsigned *>(X.skw) + A.base * X.skcap;
-    const int cnt = R.skin > 0.f ? X.skcnt[A.base + A.i] : -1;
+// per function).  Descriptors: the scaled symmetry functions in the padded grouped order,
+// the trajectory's out-of-range flag, the neighbour-list overflow and the nearest
+// neighbour entry (rmin2).
+template <int KA, int KB, int BLA, int BLB>
+__device__ __forceinline__ void nnr_descr(const RadialNN &R, const NNScratch &X, const SmemR &S, const AtomR &A,
+                                          const unsigned *sk, int cnt, int *flag, float &rmin2,
+                                          float (&xs)[KA + KB]) {
+    constexpr int KT = KA + KB;
     float G[KT];
 #pragma unroll
     for (int k = 0; k < KT; ++k) G[k] = 0.f;
@@ -505,16 +528,19 @@ __device__ __forceinline__ double nnr_atom(const RadialNN &R, const NNScratch &X
         for (int q = 0; q < KT; ++q) {
             const float4 c = sc[q];
             out |= G[q] < c.z || G[q] > c.w;
-            S.hb[q * bs + tid] = fmaf(c.x, G[q], c.y);
+            xs[q] = fmaf(c.x, G[q], c.y);
         }
         if (out) flag[A.s] = 1;
     }
-    const float e = nnr_network<KT, NH>(R, S, A.ei, tid, do_forces);
-    const double ea = (double)e + R.atom_energy[A.ei];
-    if (!do_forces) return ea;
-    float dG[KT];
-#pragma unroll
-    for (int q = 0; q < KT; ++q) dG[q] = S.hb[q * bs + tid];
+}
+
+// Forces of the atom from dE/dG (raw descriptors, padded grouped order) in reverse mode: the
+// centre's share returned in fix/fiy/fiz, the neighbours' by red.shared.
+template <int KA, int KB, int BLA, int BLB>
+__device__ __forceinline__ void nnr_forces(const RadialNN &R, const SmemR &S, const AtomR &A, const unsigned *sk,
+                                           int cnt, const float (&dG)[KA + KB], float &fix, float &fiy,
+                                           float &fiz) {
+    constexpr int bs = kRS;
     float fx = 0.f, fy = 0.f, fz = 0.f;
     for_neighbours(R, S, A, sk, cnt, [&](auto gc, int js, float dx, float dy, float dz, float r2) {
         constexpr int g = decltype(gc)::value;
@@ -574,8 +600,8 @@ __device__ __forceinline__ double nnr_atom(const RadialNN &R, const NNScratch &X
     fix = fx;
     fiy = fy;
     fiz = fz;
-    return ea;
 }
+
 
 // Weight blocks and scaling tables in shared memory from the model's current FP32 weights
 // (calconenn.f90 layout: layer l of element e is an n_(l-1) x n_l row-major matrix plus
@@ -629,6 +655,273 @@ __device__ void load_weights_r(const RadialNN &R, const SmemR &S) {
             S.dscal[e * nin + q] = s >= 0 ? R.fdscal[e * R.maxsf + s] : 0.f;
         }
     }
+}
+
+// ---- tensor-core network (BF16 operands, FP32 accumulation in TMEM) ----------------------
+// The same network as nnr_network, organised as GEMMs over 128-atom tiles: thread k of the
+// CTA is row k % 128 of tile k / 128 and the four warps of a tile reach TMEM lanes
+// 32 (w % 4) .. +31, i.e. exactly their own rows.  Per tile and layer: every thread writes its
+// operand row (bf16) to shared memory, the tile's threads meet at a named barrier, one thread
+// issues the MMAs for both elements' weights (D_e = A B_e^T, M = 128, K-steps of 16) and
+// commits them to the tile's mbarrier, every thread waits for it and reads its row of the
+// accumulator of its own element from TMEM.  Activations, biases, the output node and the
+// scaling stay FP32 in registers; the layer-1 values wait in TMEM (spill columns) for the
+// backward pass.  Four GEMMs per force evaluation: x W1, v1 W2, delta2 W2^T, delta1 W1^T.
+struct TcCtx {
+    uint32_t tmem;  // TMEM base of the CTA
+    uint64_t *bar;  // one mbarrier per tile
+    int *err;       // set when a GEMM did not complete within the wait limit
+};
+
+// A GEMM round takes microseconds; a wait that runs out of polls marks the error word, and
+// after that no thread waits again (the kernel finishes with wrong numbers instead of
+// stalling, and the host reports the error).
+constexpr uint32_t kTcMaxPolls = 1u << 18;
+
+// One GEMM round of the tile group: D_e (TMEM columns d0, d1) = A (K x 128 rows at a_s) x B_e^T
+// (N rows at b0_s / b1_s); all threads of the tile call it, returns with the result visible.
+template <int KK, int NN>
+__device__ __forceinline__ void tc_round(const TcCtx &C, int g, int nthr, uint32_t a_s, uint32_t b0_s, uint32_t b1_s,
+                                         bool two, uint32_t d0, uint32_t d1, uint32_t &phase) {
+    fence_async_smem();
+    tc_fence_before();
+    named_barrier(1 + g, nthr);
+    if ((threadIdx.x & 127) == 0) {
+        tc_fence_after();
+        constexpr uint32_t idesc = tc_idesc_bf16(128, NN);
+#pragma unroll
+        for (int ks = 0; ks < KK / 16; ++ks) {
+            const uint64_t ad = tc_desc(a_s + 256 * ks, 128, 16 * KK);
+            tc_mma_bf16(C.tmem + d0, ad, tc_desc(b0_s + 256 * ks, 128, 16 * KK), idesc, ks > 0);
+            if (two) tc_mma_bf16(C.tmem + d1, ad, tc_desc(b1_s + 256 * ks, 128, 16 * KK), idesc, ks > 0);
+        }
+        tc_commit(&C.bar[g]);
+    }
+    if (!*(volatile int *)C.err && !mbar_wait_bounded(&C.bar[g], phase, kTcMaxPolls)) atomicExch(C.err, 1);
+    phase ^= 1u;
+    tc_fence_after();
+}
+
+// 16 accumulator columns of the thread's row, from element 1's block when e1
+__device__ __forceinline__ void tc_ld_row(uint32_t t0, uint32_t t1, bool two, bool e1, float (&v)[16]) {
+    tmem_ld16(t0, v);
+    if (two) {
+        float w[16];
+        tmem_ld16(t1, w);
+        tmem_wait_ld();
+#pragma unroll
+        for (int j = 0; j < 16; ++j) v[j] = e1 ? w[j] : v[j];
+    } else {
+        tmem_wait_ld();
+    }
+}
+
+template <int N> __device__ __forceinline__ void act_vals(uint8_t a, float (&z)[N]) {
+    if (a == 'p') {
+#pragma unroll
+        for (int n = 0; n < N; ++n) z[n] = act_v<'p'>(z[n]);
+    } else if (a == 't') {
+#pragma unroll
+        for (int n = 0; n < N; ++n) z[n] = act_v<'t'>(z[n]);
+    } else if (a == 's') {
+#pragma unroll
+        for (int n = 0; n < N; ++n) z[n] = act_v<'s'>(z[n]);
+    }
+}
+template <int N> __device__ __forceinline__ void act_dvals(uint8_t a, const float (&v)[N], float (&d)[N]) {
+    if (a == 'p') {
+#pragma unroll
+        for (int n = 0; n < N; ++n) d[n] *= act_dv<'p'>(v[n]);
+    } else if (a == 't') {
+#pragma unroll
+        for (int n = 0; n < N; ++n) d[n] *= act_dv<'t'>(v[n]);
+    } else if (a == 's') {
+#pragma unroll
+        for (int n = 0; n < N; ++n) d[n] *= act_dv<'s'>(v[n]);
+    }
+}
+
+// B operands and FP32 vectors of both elements from the model's FP32 weights (calconenn.f90
+// layout, as load_weights_r reads it).  B1[n][q] = W1[q][n] (32 x KP), B2[n][p] = W2[p][n],
+// B3[p][n] = W2[p][n] (32 x 32), B4[q][p] = W1[q][p] (KP x 32); vectors: b1, then b2, w3, b3
+// (two hidden layers) or w2, b2 (one).
+template <int NIN, int NH>
+__device__ void load_weights_tc(const RadialNN &R, const SmemR &S) {
+    constexpr int KP = nnr_kp(NIN), BEL = nnr_tc_bel(NIN);
+    constexpr int oB2 = 32 * KP * 2, oB3 = oB2 + 2048, oB4 = oB3 + 2048;
+    const int tid = threadIdx.x, bs = blockDim.x;
+    for (int e = 0; e < R.nelem; ++e) {
+        const float *src = R.wf + (size_t)e * R.maxweights;
+        const int n1 = R.nodes[e][1], n2 = NH == 2 ? R.nodes[e][2] : 0;
+        const float *l1 = src + R.woff[e][1];
+        const float *l2 = src + R.woff[e][2];
+        auto w1 = [&](int q, int n) -> float {  // W1[q][n] in the padded grouped order
+            if (q >= NIN || n >= n1) return 0.f;
+            const int sidx = R.qsrc[e][q];
+            return sidx >= 0 ? l1[sidx * n1 + n] : 0.f;
+        };
+        auto w2 = [&](int p, int n) -> float { return (NH == 2 && p < n1 && n < n2) ? l2[p * n2 + n] : 0.f; };
+        unsigned char *wb = S.wb + (size_t)e * BEL;
+        // one 8-wide chunk per item: rows x (K / 8) chunks per matrix
+        for (int it = tid; it < 32 * (KP / 8); it += bs) {  // B1: row n, chunk k0 over q
+            const int n = it / (KP / 8), k0 = 8 * (it % (KP / 8));
+            float v[8];
+            for (int j = 0; j < 8; ++j) v[j] = w1(k0 + j, n);
+            st_bf16x8(wb + tc_offset(n, k0, KP), v);
+        }
+        for (int it = tid; it < 32 * 4; it += bs) {  // B2, B3
+            const int n = it / 4, k0 = 8 * (it % 4);
+            float v[8], u[8];
+            for (int j = 0; j < 8; ++j) {
+                v[j] = w2(k0 + j, n);  // B2[n][p] = W2[p][n]
+                u[j] = w2(n, k0 + j);  // B3[p][n] = W2[p][n], row p = n here
+            }
+            st_bf16x8(wb + oB2 + tc_offset(n, k0, 32), v);
+            st_bf16x8(wb + oB3 + tc_offset(n, k0, 32), u);
+        }
+        for (int it = tid; it < KP * 4; it += bs) {  // B4: row q, chunk over p
+            const int q = it / 4, k0 = 8 * (it % 4);
+            float v[8];
+            for (int j = 0; j < 8; ++j) v[j] = w1(q, k0 + j);
+            st_bf16x8(wb + oB4 + tc_offset(q, k0, 32), v);
+        }
+        float *vec = S.wv + e * kTcVec;
+        for (int n = tid; n < 32; n += bs) {
+            vec[n] = n < n1 ? l1[R.nodes[e][0] * n1 + n] : 0.f;                      // b1
+            if (NH == 2) {
+                const float *l3 = src + R.woff[e][3];
+                vec[32 + n] = n < n2 ? l2[n1 * n2 + n] : 0.f;                          // b2
+                vec[64 + n] = n < n2 ? l3[n] : 0.f;                                    // w3
+                if (n == 0) vec[96] = l3[n2];                                          // b3
+            } else {
+                vec[32 + n] = n < n1 ? l2[n] : 0.f;                                    // w2
+                if (n == 0) vec[64] = l2[n1];                                          // b2
+            }
+        }
+    }
+}
+
+// The network of this thread's atom on the tensor cores.  Every thread of the CTA calls it
+// (rows without an atom carry zeros).  Returns the atomic energy (output node, Ha); with
+// do_forces, dG receives dE/dG for the raw descriptors (padded grouped order).
+template <int NIN, int NH>
+__device__ __forceinline__ float nnr_network_tc(const RadialNN &R, const SmemR &S, const TcCtx &C, int ei,
+                                                const float (&xs)[NIN], bool do_forces, float (&dG)[NIN],
+                                                uint32_t &phase) {
+    constexpr int KP = nnr_kp(NIN), TW = nnr_tw(NIN), CPT = nnr_tc_cpt(NIN), BEL = nnr_tc_bel(NIN);
+    constexpr int oB2 = 32 * KP * 2, oB3 = oB2 + 2048, oB4 = oB3 + 2048;
+    const int tid = threadIdx.x, g = tid >> 7, row = tid & 127;
+    const int nthr = min(128, (int)blockDim.x - 128 * g);
+    unsigned char *at = S.at + (size_t)g * 128 * TW * 2;
+    const uint32_t a_s = smem_u32(at), b_s = smem_u32(S.wb);
+    const uint32_t lane = ((uint32_t)((tid >> 5) & 3) * 32u) << 16;
+    const uint32_t c0 = (uint32_t)(g * CPT), c1 = c0 + TW, cs = c0 + 2 * TW;
+    const bool two = R.nelem > 1, e1 = ei == 1;
+    const float *vec = S.wv + ei * kTcVec;
+    const float rn1 = R.rn[0];
+    const uint8_t a1 = R.act[0];
+    // ---- layer 1: x W1 -------------------------------------------------------------------
+#pragma unroll
+    for (int k0 = 0; k0 < KP; k0 += 8) {
+        float v[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) v[j] = (k0 + j < NIN) ? xs[k0 + j] : 0.f;
+        st_bf16x8(at + tc_offset(row, k0, KP), v);
+    }
+    tc_round<KP, 32>(C, g, nthr, a_s, b_s, b_s + BEL, two, c0, c1, phase);
+    float o = 0.f;  // output-node sum (one hidden layer)
+#pragma unroll
+    for (int h = 0; h < 32; h += 16) {
+        float z[16];
+        tc_ld_row(C.tmem + lane + c0 + h, C.tmem + lane + c1 + h, two, e1, z);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) z[j] = (z[j] + vec[h + j]) * rn1;
+        act_vals<16>(a1, z);
+        tmem_st16(C.tmem + lane + cs + h, z);  // layer-1 values for the backward pass
+        if (NH == 2) {
+            st_bf16x8(at + tc_offset(row, h, 32), z);
+            st_bf16x8(at + tc_offset(row, h + 8, 32), z + 8);
+        } else {
+#pragma unroll
+            for (int j = 0; j < 16; ++j) o = fmaf(vec[32 + h + j], z[j], o);
+        }
+    }
+    tmem_wait_st();
+    float out, g1;
+    if (NH == 2) {
+        // ---- layer 2: v1 W2; output node -------------------------------------------------
+        tc_round<32, 32>(C, g, nthr, a_s, b_s + oB2, b_s + BEL + oB2, two, c0, c1, phase);
+        const float rn2 = R.rn[1];
+        const uint8_t a2 = R.act[1];
+#pragma unroll
+        for (int h = 0; h < 32; h += 16) {
+            float z[16];
+            tc_ld_row(C.tmem + lane + c0 + h, C.tmem + lane + c1 + h, two, e1, z);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                float v, dv;
+                act_d(a2, (z[j] + vec[32 + h + j]) * rn2, v, dv);
+                o = fmaf(vec[64 + h + j], v, o);
+            }
+        }
+        float vo, dvo;
+        act_d(R.act[2], (o + vec[96]) * R.rn[2], vo, dvo);
+        out = vo;
+        if (!do_forces) return out;
+        // delta2 = w3 f'(layer-2 sum) g2, from the accumulator still in TMEM
+        const float g2 = R.rn[2] * dvo * rn2;
+#pragma unroll
+        for (int h = 0; h < 32; h += 16) {
+            float z[16];
+            tc_ld_row(C.tmem + lane + c0 + h, C.tmem + lane + c1 + h, two, e1, z);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                float v, dv;
+                act_d(a2, (z[j] + vec[32 + h + j]) * rn2, v, dv);
+                z[j] = vec[64 + h + j] * dv * g2;
+            }
+            st_bf16x8(at + tc_offset(row, h, 32), z);
+            st_bf16x8(at + tc_offset(row, h + 8, 32), z + 8);
+        }
+        // ---- delta1 = (delta2 W2^T) rn1 f'(v1) -------------------------------------------
+        tc_round<32, 32>(C, g, nthr, a_s, b_s + oB3, b_s + BEL + oB3, two, c0, c1, phase);
+        g1 = rn1;
+    } else {
+        float vo, dvo;
+        act_d(R.act[1], (o + vec[64]) * R.rn[1], vo, dvo);
+        out = vo;
+        if (!do_forces) return out;
+        g1 = R.rn[1] * dvo * rn1;
+    }
+#pragma unroll
+    for (int h = 0; h < 32; h += 16) {
+        float d[16], v1[16];
+        if (NH == 2) {
+            tc_ld_row(C.tmem + lane + c0 + h, C.tmem + lane + c1 + h, two, e1, d);
+        } else {
+#pragma unroll
+            for (int j = 0; j < 16; ++j) d[j] = vec[32 + h + j];
+        }
+        tmem_ld16(C.tmem + lane + cs + h, v1);
+        tmem_wait_ld();
+#pragma unroll
+        for (int j = 0; j < 16; ++j) d[j] *= g1;
+        act_dvals<16>(a1, v1, d);
+        st_bf16x8(at + tc_offset(row, h, 32), d);
+        st_bf16x8(at + tc_offset(row, h + 8, 32), d + 8);
+    }
+    // ---- dE/dG_q = dscal_q (delta1 W1^T)_q ---------------------------------------------
+    tc_round<32, KP>(C, g, nthr, a_s, b_s + oB4, b_s + BEL + oB4, two, c0, c1, phase);
+    const float *ds = S.dscal + ei * NIN;
+#pragma unroll
+    for (int q0 = 0; q0 < KP; q0 += 16) {
+        float z[16];
+        tc_ld_row(C.tmem + lane + c0 + q0, C.tmem + lane + c1 + q0, two, e1, z);
+#pragma unroll
+        for (int j = 0; j < 16; ++j)
+            if (q0 + j < NIN) dG[q0 + j] = z[j] * ds[q0 + j];
+    }
+    return out;
 }
 
 // Propagators of the fused step for single-bead atoms.  The constant-friction Langevin
@@ -695,18 +988,37 @@ __device__ __forceinline__ void lc_half2(const Batch &B, const PropParams &P, co
 
 // mode 0: forces, 1: energies only, 2: nsteps fused MD steps (propagate_1, forces,
 // propagate_2, exit test), as the other network kernels.
-template <int KA, int KB, int NH, int BLA, int BLB>
+template <int KA, int KB, int NH, int BLA, int BLB, bool TC>
 __global__ void __launch_bounds__(kRBlockMax, 1)
     nnr_kernel(Batch B, RadialNN R, EmtConst E, NNScratch X, PropParams P, const int2 *packs, const int *ptraj, int npack,
                int *counter, int nsteps, int mode) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     constexpr int KT = KA + KB, bs = kRS;
     const int tid = threadIdx.x;
-    const SmemR S = carve_r<KT, NH>(smem_raw);
+    const SmemR S = carve_r<KT, NH, TC>(smem_raw);
     SmemEmt<double> SE = carve_smem<double>(S.emt, B.max_atoms, B.max_beads);
     SE.red = S.red;
     SE.cjk = S.red;  // single-bead trajectories only: the ring-polymer table is never read
-    load_weights_r<KT, NH>(R, S);
+    TcCtx C{0u, S.tcbar, X.tcerr};
+    uint32_t phase = 0;  // parity of this thread's tile mbarrier
+    if constexpr (TC) {
+        load_weights_tc<KT, NH>(R, S);
+        if (tid < 32) {
+            tmem_alloc(S.tslot, kTcCols);
+            tmem_relinquish();
+        }
+        if (tid == 0) {
+            for (int g = 0; g < kTcTiles; ++g) mbar_init(&S.tcbar[g], 1);
+            fence_mbar_init();
+        }
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        C.tmem = *S.tslot;
+    } else {
+        load_weights_r<KT, NH>(R, S);
+    }
     __syncthreads();
     const bool do_forces = mode != 1;
     for (;;) {
@@ -725,6 +1037,7 @@ __global__ void __launch_bounds__(kRBlockMax, 1)
                 S.tr_over[b * kRMaxTraj + tid] = 0;
                 S.tr_flag[b * kRMaxTraj + tid] = 0;
                 S.tr_d2[b * kRMaxTraj + tid] = 0;
+                S.tr_bad[b * kRMaxTraj + tid] = 0;
             }
             for (int b = 0; b < 3; ++b) S.tr_stat[b * kRMaxTraj + tid] = run;
             double lat[18];
@@ -776,12 +1089,14 @@ __global__ void __launch_bounds__(kRBlockMax, 1)
         // needs only the positions after the first half-step, so the projectile's thread
         // decides whether its trajectory runs the next step before (A).
         const int steps = mode == 2 ? nsteps : 1;
+        int last = -1;  // last step run by the pack
         for (int step_i = 0; step_i < steps; ++step_i) {
             const int cur = step_i & 1, nxt = cur ^ 1;
             const int *stat = S.tr_stat + (step_i % 3) * kRMaxTraj;
             bool any = false;
             for (int s = 0; s < pd.y; ++s) any |= stat[s] != 0;
             if (!any) break;  // every trajectory of the pack has stopped (uniform: flags are stable)
+            last = step_i;
             const bool active = A.s >= 0 && stat[A.s] != 0;
             const int step = steps0 + step_i + 1;
             int *flag = S.tr_flag + cur * kRMaxTraj;
@@ -808,6 +1123,8 @@ __global__ void __launch_bounds__(kRBlockMax, 1)
                 S.xl[tid] = A.xli;
                 S.yl[tid] = A.yli;
                 S.zl[tid] = A.zli;
+                if (mode == 2 && !isfinite((rx + ry) + (rz + B.vx[k]) + (B.vy[k] + B.vz[k])))
+                    S.tr_bad[cur * kRMaxTraj + A.s] = 1;
                 if (R.skin > 0.f) {
                     const double *r0 = X.skref + 3 * k;
                     const float ddx = (float)(rx - r0[0]), ddy = (float)(ry - r0[1]), ddz = (float)(rz - r0[2]);
@@ -820,7 +1137,12 @@ __global__ void __launch_bounds__(kRBlockMax, 1)
                 int run_next = active ? 1 : 0;
                 if (active && mode == 2) {
                     B.steps_done[T.t] = step;
-                    if (P.use_exit && B.is_proj[B.type[T.aoff]]) {
+                    // a bead-atom of the trajectory was not finite after the previous step's
+                    // first half-step: this step is its last
+                    if (S.tr_bad[nxt * kRMaxTraj + A.s]) {
+                        B.status[T.t] = kStatusErrNonFinite;
+                        run_next = 0;
+                    } else if (P.use_exit && B.is_proj[B.type[T.aoff]]) {
                         const double z = B.rz[T.base];
                         if (z > P.pul) {
                             B.status[T.t] = kStatusExitUpper;
@@ -845,12 +1167,18 @@ __global__ void __launch_bounds__(kRBlockMax, 1)
                 S.tr_flag[nxt * kRMaxTraj + tid] = 0;
                 S.tr_d2[nxt * kRMaxTraj + tid] = 0;
                 S.tr_over[nxt * kRMaxTraj + tid] = 0;
+                S.tr_bad[nxt * kRMaxTraj + tid] = 0;
             }
             // ---- forces; skin lists rebuilt when invalid or when some atom of the
             // trajectory moved more than half the skin (displacements in A, skin in bohr) ----
             const float half = 0.5f * R.skin * (float)kBohr2Ang;
             float fix = 0.f, fiy = 0.f, fiz = 0.f;
             float rmin2 = INFINITY;  // nearest neighbour entry (bohr^2): the closest approach of atom 0
+            const unsigned *sk = reinterpret_cast<const unsigned *>(X.skw) + A.base * X.skcap;
+            int cnt = -1;
+            float xs[KT], dG[KT];
+#pragma unroll
+            for (int q = 0; q < KT; ++q) xs[q] = 0.f;
             if (active) {
                 const int64_t k = A.base + A.i;
                 const int bead = B.bead_off[T.t];
@@ -863,7 +1191,23 @@ __global__ void __launch_bounds__(kRBlockMax, 1)
                     r0[1] = B.ry[k];
                     r0[2] = B.rz[k];
                 }
-                S.ea[tid] = nnr_atom<KA, KB, NH, BLA, BLB>(R, X, S, A, tid, do_forces, flag, rmin2, fix, fiy, fiz);
+                cnt = R.skin > 0.f ? X.skcnt[k] : -1;
+                nnr_descr<KA, KB, BLA, BLB>(R, X, S, A, sk, cnt, flag, rmin2, xs);
+            }
+            float e_at = 0.f;
+            if constexpr (TC) {
+                // every thread of the CTA: the GEMMs are per 128-row tile
+                e_at = nnr_network_tc<KT, NH>(R, S, C, active ? A.ei : 0, xs, do_forces, dG, phase);
+            } else if (active) {
+#pragma unroll
+                for (int q = 0; q < KT; ++q) S.hb[q * bs + tid] = xs[q];
+                e_at = nnr_network<KT, NH>(R, S, A.ei, tid, do_forces);
+#pragma unroll
+                for (int q = 0; q < KT; ++q) dG[q] = S.hb[q * bs + tid];
+            }
+            if (active) {
+                S.ea[tid] = (double)e_at + R.atom_energy[A.ei];
+                if (do_forces) nnr_forces<KA, KB, BLA, BLB>(R, S, A, sk, cnt, dG, fix, fiy, fiz);
             }
             __syncthreads();  // (B)
             // per-trajectory energy and skin-list state: one warp per trajectory, strided FP64
@@ -937,28 +1281,39 @@ __global__ void __launch_bounds__(kRBlockMax, 1)
                 if (A.i == 0) observe_step(B, T, step, rmin2 < INFINITY ? (double)sqrtf(rmin2) * kBohr2Ang : kDefaultReal);
             }
         }
+        // a state that stopped being finite in the launch's last step retires the trajectory too
+        if (mode == 2 && last >= 0 && A.s >= 0 && A.i == 0 && S.tr_bad[(last & 1) * kRMaxTraj + A.s] &&
+            B.status[T.t] == kStatusRunning)
+            B.status[T.t] = kStatusErrNonFinite;
+    }
+    if constexpr (TC) {
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        if (tid < 32) tmem_dealloc(C.tmem, kTcCols);
     }
 }
 
-template <int KA, int KB, int NH, int BLA, int BLB>
+template <int KA, int KB, int NH, int BLA, int BLB, bool TC>
 cudaError_t nnr_launch_t(const LaunchCfg &c, const Batch &B, const RadialNN &R, const EmtConst &E,
                          const NNScratch &X, const PropParams &P, const int2 *packs, const int *ptraj, int npack,
                          size_t sm, int nsteps, int mode) {
     cudaError_t e = cudaMemsetAsync(c.counter, 0, sizeof(int), c.stream);
     if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(nnr_kernel<KA, KB, NH, BLA, BLB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    e = cudaFuncSetAttribute(nnr_kernel<KA, KB, NH, BLA, BLB, TC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
-    nnr_kernel<KA, KB, NH, BLA, BLB><<<c.grid, R.block, sm, c.stream>>>(B, R, E, X, P, packs, ptraj, npack,
-                                                                        c.counter, nsteps, mode);
+    nnr_kernel<KA, KB, NH, BLA, BLB, TC><<<c.grid, R.block, sm, c.stream>>>(B, R, E, X, P, packs, ptraj, npack,
+                                                                            c.counter, nsteps, mode);
     return cudaGetLastError();
 }
 
-template <int KA, int KB, int NH, int BLA, int BLB>
+template <int KA, int KB, int NH, int BLA, int BLB, bool TC>
 int nnr_occupancy_t(int block, size_t sm) {
     int n = 0;
-    cudaFuncSetAttribute(nnr_kernel<KA, KB, NH, BLA, BLB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, nnr_kernel<KA, KB, NH, BLA, BLB>, block, sm);
-    return n;
+    cudaFuncSetAttribute(nnr_kernel<KA, KB, NH, BLA, BLB, TC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, nnr_kernel<KA, KB, NH, BLA, BLB, TC>, block, sm);
+    // a CTA of the tensor-core kernels holds all 512 TMEM columns of its SM
+    return TC ? (n > 0 ? 1 : 0) : n;
 }
 
 }  // namespace
@@ -985,7 +1340,9 @@ bool nnr_shape(int cnt0, int cnt1, int nh, const int *maxbl, RadialNN &R) {
     return found;
 }
 
-size_t nnr_smem(const RadialNN &R) { return smem_r(R.nin, R.nh); }
+size_t nnr_smem(const RadialNN &R) { return smem_r(R.nin, R.nh, R.tc != 0); }
+
+size_t nnr_hb_bytes(const RadialNN &R) { return hb_bytes(R.nin, R.nh, R.tc != 0); }
 
 size_t nnr_emt_smem(int max_atoms) { return smem_bytes(max_atoms, 1, 8); }
 
@@ -993,7 +1350,8 @@ int nnr_resident_ctas(const RadialNN &R) {
     const size_t sm = nnr_smem(R);
 #define MDT_OCC(A_, B_, H_, LA_, LB_)                                                   \
     if (R.ka == A_ && R.kb == B_ && R.nh == H_ && R.bla == LA_ && R.blb == LB_) \
-        return nnr_occupancy_t<A_, B_, H_, LA_, LB_>(R.block, sm);
+        return R.tc ? nnr_occupancy_t<A_, B_, H_, LA_, LB_, true>(R.block, sm)   \
+                    : nnr_occupancy_t<A_, B_, H_, LA_, LB_, false>(R.block, sm);
     MDT_NNR_SHAPES(MDT_OCC)
 #undef MDT_OCC
     return 0;
@@ -1004,7 +1362,8 @@ cudaError_t launch_nnr(const LaunchCfg &c, const Batch &B, const RadialNN &R, co
     const size_t sm = nnr_smem(R);
 #define MDT_LAUNCH(A_, B_, H_, LA_, LB_)                                                                      \
     if (R.ka == A_ && R.kb == B_ && R.nh == H_ && R.bla == LA_ && R.blb == LB_)                       \
-        return nnr_launch_t<A_, B_, H_, LA_, LB_>(c, B, R, E, X, P, packs, ptraj, npack, sm, nsteps, mode);
+        return R.tc ? nnr_launch_t<A_, B_, H_, LA_, LB_, true>(c, B, R, E, X, P, packs, ptraj, npack, sm, nsteps, mode) \
+                    : nnr_launch_t<A_, B_, H_, LA_, LB_, false>(c, B, R, E, X, P, packs, ptraj, npack, sm, nsteps, mode);
     MDT_NNR_SHAPES(MDT_LAUNCH)
 #undef MDT_LAUNCH
     return cudaErrorInvalidValue;

@@ -29,23 +29,15 @@
 #include "../../include/mdt_gpu.h"
 #include "mdt_common.cuh"
 #include "mdt_emt.cuh"
+#include "mdt_internal.h"
 
 namespace mdt {
-namespace {
 
-constexpr int kNoAllocMaxAtoms = 256;
-constexpr size_t kNoAllocScratch = 6 * (size_t)kNoAllocMaxAtoms * (kNoAllocMaxAtoms / 2);
-
-static __device__ __align__(256) double g_noalloc_pair_scratch[kNoAllocScratch];
-
-constexpr int kMaxDevices = 64;
-std::mutex g_setup_mutex;
-double *g_scratch_addr[kMaxDevices] = {nullptr};
-
-// EMT constants of compute_emt_1species / compute_emt_2species
-// (src/pes_emt_mod.f90:258-307 and 521-592), same expressions and order as the
-// context path's mdt_emt_set_params.
-int emt_constants(int32_t ntypes, const double *eta2, const double *n0, const double *e0, const double *lambda,
+// Derived EMT constants of compute_emt_1species / compute_emt_2species
+// (src/pes_emt_mod.f90:258-307 and 521-592), in the reference's order of operations; shared
+// by mdt_emt_set_params and the allocation-free entry point.  Returns MDT_OK,
+// MDT_ERR_UNSUPPORTED (more than two EMT species) or MDT_ERR_ARG (no EMT species).
+int emt_derive_constants(int32_t ntypes, const double *eta2, const double *n0, const double *e0, const double *lambda,
                   const double *v0, const double *kappa, const double *s0, const int32_t *pes, EmtConst &E) {
     E = EmtConst{};
     int slots[2] = {-1, -1}, ns = 0;
@@ -107,6 +99,17 @@ int emt_constants(int32_t ntypes, const double *eta2, const double *n0, const do
     return MDT_OK;
 }
 
+namespace {
+
+constexpr int kNoAllocMaxAtoms = 256;
+constexpr size_t kNoAllocScratch = 6 * (size_t)kNoAllocMaxAtoms * (kNoAllocMaxAtoms / 2);
+
+static __device__ __align__(256) double g_noalloc_pair_scratch[kNoAllocScratch];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_setup_mutex;
+double *g_scratch_addr[kMaxDevices] = {nullptr};
+
 // invert_matrix, src/useful_things.f90:296-321 (column major), as mdt_batch_define does
 bool invert_cell(const double *A, double *B) {
     auto a = [&](int i, int j) { return A[(j - 1) * 3 + (i - 1)]; };
@@ -135,7 +138,8 @@ constexpr int kNoAllocBlock = 128;
 
 // One CTA evaluates the configuration with the same device function as the context
 // path (emt_bead), pointed at caller buffers and the file-scope scratch.
-__global__ void __launch_bounds__(kNoAllocBlock) emt_noalloc_kernel(int N, CellArg cell, EmtConst E, const double *x,
+__global__ void __launch_bounds__(kNoAllocBlock) emt_noalloc_kernel(int N, int ntypes, CellArg cell, EmtConst E,
+                                                                     const double *x,
                                                                      const double *y, const double *z,
                                                                      const int32_t *idx, double *fx, double *fy,
                                                                      double *fz, double *energy, double *dens,
@@ -163,7 +167,7 @@ __global__ void __launch_bounds__(kNoAllocBlock) emt_noalloc_kernel(int N, CellA
     __syncthreads();
     for (int i = threadIdx.x; i < N; i += blockDim.x) {
         int ty = idx[i] - 1;
-        if (ty < 0 || ty >= kMaxTypes) {
+        if (ty < 0 || ty >= ntypes) {  // a type outside the parameter table
             s_bad = 1;
             ty = 0;
         }
@@ -216,7 +220,7 @@ extern "C" int32_t mdt_emt_force_noalloc(int32_t natoms, const int32_t *idx, con
         ntypes > kMaxTypes || !eta2 || !n0 || !e0 || !lambda || !v0 || !kappa || !s0 || !pes)
         return MDT_ERR_ARG;
     EmtConst E;
-    int rc = emt_constants(ntypes, eta2, n0, e0, lambda, v0, kappa, s0, pes, E);
+    int rc = emt_derive_constants(ntypes, eta2, n0, e0, lambda, v0, kappa, s0, pes, E);
     if (rc != MDT_OK) return rc;
     CellArg cell;
     for (int k = 0; k < 9; ++k) cell.h[k] = simbox[k];
@@ -234,7 +238,7 @@ extern "C" int32_t mdt_emt_force_noalloc(int32_t natoms, const int32_t *idx, con
         scratch = g_scratch_addr[dev];
     }
     const size_t sm = ((natoms + 15) & ~15) + ((8 * (size_t)natoms + 15) & ~size_t(15)) + smem_bytes(natoms, 1, 8);
-    emt_noalloc_kernel<<<1, kNoAllocBlock, sm, (cudaStream_t)stream>>>(natoms, cell, E, x, y, z, idx, fx, fy, fz,
+    emt_noalloc_kernel<<<1, kNoAllocBlock, sm, (cudaStream_t)stream>>>(natoms, ntypes, cell, E, x, y, z, idx, fx, fy, fz,
                                                                        energy, dens, scratch);
     return cudaGetLastError() == cudaSuccess ? MDT_OK : MDT_ERR_CUDA;
 }

@@ -434,6 +434,41 @@ static __device__ void ring_polymer_step(const Batch &B, const PropParams &P, co
     __syncthreads();
 }
 
+// End of one fused MD step of the CTA that owns trajectory T (md_tian2.f90:78-92): the step
+// count, the exit test on the projectile's beads, the step limit, and retirement of a
+// trajectory whose state stopped being finite.  The reference has no such check (a NaN
+// propagates until the run ends); here every bead-atom's position and velocity is
+// tested after the step, and a broken trajectory stops with kStatusErrNonFinite while the
+// others of the batch go on untouched.  An error status already set (ldfa's negative
+// density) is kept.
+static __device__ void end_of_step(const Batch &B, const PropParams &P, const TrajView &T, int step) {
+    int bad = 0;
+    const int tot = T.N * T.nb;
+    for (int s = threadIdx.x; s < tot; s += blockDim.x) {
+        const int64_t k = T.base + s;
+        const double a = (B.rx[k] + B.ry[k]) + (B.rz[k] + B.vx[k]) + (B.vy[k] + B.vz[k]);
+        bad |= isfinite(a) ? 0 : 1;
+    }
+    bad = __syncthreads_or(bad);
+    if (threadIdx.x == 0) {
+        const int t = T.t;
+        B.steps_done[t] = step;
+        if (bad && B.status[t] == kStatusRunning) B.status[t] = kStatusErrNonFinite;
+        if (P.use_exit && B.is_proj[B.type[T.aoff]] && B.status[t] == kStatusRunning) {
+            bool up = true, lo = true;
+            for (int b = 0; b < T.nb; ++b) {
+                const double z = B.rz[T.base + (int64_t)b * T.N];
+                up = up && (z > P.pul);
+                lo = lo && (z < P.pll);
+            }
+            if (up) B.status[t] = kStatusExitUpper;
+            else if (lo) B.status[t] = kStatusExitLower;
+        }
+        if (P.max_steps > 0 && step >= P.max_steps && B.status[t] == kStatusRunning) B.status[t] = kStatusStepLimit;
+    }
+    __syncthreads();
+}
+
 static __device__ void load_cjk(const Batch &B, int t, double *cjk_s) {
     const int nb = B.nbeads[t];
     if (nb <= 1) return;

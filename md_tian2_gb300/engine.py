@@ -18,7 +18,7 @@ from ._lib import EngineError, NNModelC, PropParams, TrajSummary, load
 from .io import EmtParams
 from .universe import Universe
 
-PREC = {"fp64": 0, "fp32": 1}
+PREC = {"fp64": 0, "fp32": 1, "bf16": 2}
 PES_EMT, PES_NENE, PES_SURROGATE = C.PES_ID_EMT, C.PES_ID_NENE, 2100
 
 

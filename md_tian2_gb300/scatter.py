@@ -271,7 +271,9 @@ def run_campaign(eng, sp, total: int, refill: dict, precision: str = "fp64", max
     records of every trajectory that has stopped (exit test or the ``max_steps`` limit),
     restart those slots on the device with new projectile starts (``Engine.refill(**refill)``)
     and go on until ``total`` trajectories have finished.  Returns their scattering records
-    (the observables part: energies, projectile heights, steps, status)."""
+    (the observables part: energies, projectile heights, steps, status).  A trajectory that
+    stops with an error status (negative) is recorded once with that status; refill leaves
+    its slot stopped, so the batch goes on with one slot fewer."""
     if not sp.use_exit:
         raise ValueError("run_campaign needs SimParams.use_exit (the pul/pll exit test)")
     if max_steps <= 0:
@@ -289,11 +291,14 @@ def run_campaign(eng, sp, total: int, refill: dict, precision: str = "fp64", max
     z_start = np.array([proj_z(o, t) for t in range(T)])
     cols = {k: [] for k in ("ekin_i", "ekin_f", "z_i", "z_f", "steps", "status")}
     done = 0
+    dead = np.zeros(T, bool)  # slots stopped by an error status, already recorded
     try:
         while done < total:
+            if dead.all():
+                raise RuntimeError("run_campaign: every trajectory slot stopped with an error status")
             eng.md_steps(chunk, sp, precision=precision)
             q = eng.query(sp)
-            fin = np.nonzero(q["status"] != 0)[0]
+            fin = np.nonzero((q["status"] != 0) & ~dead)[0]
             if len(fin) == 0:
                 continue
             o = eng.download()
@@ -305,6 +310,7 @@ def run_campaign(eng, sp, total: int, refill: dict, precision: str = "fp64", max
                 cols["steps"].append(q["steps_done"][t])
                 cols["status"].append(q["status"][t])
             done += min(len(fin), total - done)
+            dead[fin[q["status"][fin] < 0]] = True
             if done >= total:
                 break
             eng.refill(**refill)

@@ -18,6 +18,8 @@ import ctypes as ct
 import time
 from dataclasses import dataclass
 
+from pathlib import Path
+
 import numpy as np
 
 from . import constants as C
@@ -59,6 +61,15 @@ def generate_dataset(ntraj: int = 4096, nsamples: int = 8, every: int = 50, seed
             out_f.append(f.copy())
     eng.close()
     return Dataset(out_u, np.array(out_e), out_f)
+
+
+SHIPPED = Path(__file__).resolve().parent / "data" / "surrogate_radial.npz"
+
+
+def shipped_surrogate() -> nene.NNModel:
+    """The trained H/Au surrogate shipped with the package (24 radial G2 -> 32 -> 32 -> 1
+    softplus; provenance in data/surrogate_radial.json)."""
+    return nene.load_npz(SHIPPED)
 
 
 def surrogate_model(seed: int = 11, descriptor: str = "acsf") -> nene.NNModel:

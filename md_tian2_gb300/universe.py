@@ -63,6 +63,11 @@ class Universe:
     def isimbox(self) -> np.ndarray:
         return invert_matrix(self.simbox)
 
+    def copy(self) -> "Universe":
+        return Universe(self.r.copy(), self.v.copy(), self.m.copy(), self.idx.copy(), self.is_fixed.copy(),
+                        self.simbox.copy(), list(self.names), None if self.is_proj is None else self.is_proj.copy(),
+                        None if self.algo is None else self.algo.copy())
+
     def force_beads(self, nb: int) -> "Universe":
         """post_process's bead replication, src/md_init.f90:630-671."""
         rep = lambda a: np.repeat(a[:, :1, :], nb, axis=1).copy()  # noqa: E731

@@ -11,6 +11,9 @@
  */
 #include "md_oracle.h"
 
+#include <algorithm>
+#include <chrono>
+
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -1003,6 +1006,49 @@ int orc_run_verlet(orc_universe *u, const orc_params *p, int nsteps, double pul)
         if (all_above && u->is_proj[u->idx[0] - 1]) break;
     }
     return istep > nsteps ? nsteps : istep;
+}
+
+namespace {
+// splitmix64 (Steele, Lea, Flood, OOPSLA 2014): 64-bit counter generator
+struct SplitMix {
+    uint64_t x;
+    uint64_t next() {
+        uint64_t z = (x += 0x9E3779B97F4A7C15ull);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        return z ^ (z >> 31);
+    }
+    double u01() { return ((double)(next() >> 11) + 0.5) * (1.0 / 9007199254740992.0); }  // (0, 1)
+    double normal() { return std::sqrt(-2.0 * std::log(u01())) * std::cos(2.0 * kPi * u01()); }
+};
+}  // namespace
+
+int64_t orc_run_steps(orc_universe **u, int n, const orc_params *p, double seconds, int64_t max_sweeps,
+                      uint64_t seed, double *elapsed) {
+    size_t mx = 0;
+    for (int k = 0; k < n; ++k) mx = std::max(mx, (size_t)3 * u[k]->nbeads * u[k]->natoms);
+    std::vector<double> randy(mx), zeta(mx), av(mx), au(mx);
+    SplitMix g{seed};
+    const auto t0 = std::chrono::steady_clock::now();
+    int64_t atom_steps = 0;
+    double el = 0.0;
+    for (int64_t sweep = 0; sweep < max_sweeps; ++sweep) {
+        for (int k = 0; k < n; ++k) {
+            const size_t m = (size_t)3 * u[k]->nbeads * u[k]->natoms;
+            for (size_t i = 0; i < m; ++i) {
+                randy[i] = g.normal();
+                zeta[i] = g.normal();
+                av[i] = g.normal();
+                au[i] = g.u01();
+            }
+            if (orc_md_step(u[k], p, randy.data(), zeta.data(), av.data(), au.data())) return -1;
+            atom_steps += (int64_t)u[k]->natoms * u[k]->nbeads;
+        }
+        el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        if (el >= seconds) break;
+    }
+    if (elapsed) *elapsed = el;
+    return atom_steps;
 }
 
 }  // extern "C"

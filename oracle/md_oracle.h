@@ -7,11 +7,12 @@
  *
  * Parity status: unpinned by the reference itself.  The reference is Fortran and no
  * Fortran compiler exists in the build environment, so no reference run produced
- * golden vectors.  The restatement is pinned instead to (a) the reference's own
+ * golden vectors.  The restatement is checked instead against (a) the reference's own
  * parameter fixtures (pes/EMT-*.pes), (b) its binary geometry fixtures
- * (conf/latt/mxt_00000001.dat and siblings), (c) analytic properties (finite-difference gradients,
- * Newton's third law, NVE conservation) and (d) a second, independent numpy
- * transcription of the same Fortran loops (tests/golden/make_golden.py).
+ * (conf/latt/mxt_00000001.dat and siblings) and (c) analytic properties (finite-difference
+ * gradients, Newton's third law, NVE conservation, the force-sum rule of check_forces).
+ * tests/golden/runner_cgraphene_ref.npz holds this oracle's own output on the reference's
+ * example network: a regression fixture, not an independent golden vector.
  *
  * Layout: every per-trajectory array is in the reference's Fortran order,
  * r(3, nbeads, natoms) -> r[(i*nb + b)*3 + d], exactly like `type universe`
@@ -92,6 +93,15 @@ int orc_md_step(orc_universe *u, const orc_params *p, const double *randy,
 /* Velocity-Verlet trajectory for the CPU baseline: runs up to nsteps steps, stopping
    when every bead of atom 1 is above pul (md_tian2.f90:78-92).  Returns steps done. */
 int orc_run_verlet(orc_universe *u, const orc_params *p, int nsteps, double pul);
+
+/* Steady-state stepping for the timed CPU baseline: MD steps (orc_md_step) over the n
+   universes round robin, every universe one step per sweep, until `seconds` of wall time
+   have passed (checked after each sweep) or max_sweeps sweeps are done.  The Langevin and
+   thermostat deviates come from a counter generator (splitmix64, Box-Muller) keyed by
+   seed, so no Python runs inside the timed loop.  Returns the atom-steps done (natoms x
+   nbeads per universe-step); *elapsed receives the seconds spent.  Negative on error. */
+int64_t orc_run_steps(orc_universe **u, int n, const orc_params *p, double seconds, int64_t max_sweeps,
+                      uint64_t seed, double *elapsed);
 
 #ifdef __cplusplus
 }

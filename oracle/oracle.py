@@ -28,7 +28,10 @@ def build(force: bool = False) -> Path:
         return LIB
     BUILD.mkdir(exist_ok=True)
     tmp = LIB.with_suffix(".tmp.so")
-    cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-o", str(tmp)] + [str(HERE / s) for s in SOURCES]
+    # -O3 without -ffast-math keeps IEEE semantics in source order (the checker's values do
+    # not depend on it); no -march=native: the same flags build the same results on the x86
+    # build machine and the Arm GPU hosts
+    cmd = ["g++", "-O3", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-o", str(tmp)] + [str(HERE / s) for s in SOURCES]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"oracle build failed:\n{r.stderr}")
@@ -69,8 +72,25 @@ def lib():
         _lib.orc_bead_epot.argtypes = [P(CUniverse), P(Params)]
         _lib.orc_bead_epot.restype = ct.c_double
         _lib.orc_atom_ekin.argtypes = [P(CUniverse), P(ct.c_double), P(ct.c_double)]
+        _lib.orc_bead_ekin.argtypes = [P(CUniverse), P(ct.c_double), P(ct.c_double)]
         _lib.orc_remove_com_velocity.argtypes = [P(CUniverse)]
+        _lib.orc_run_steps.argtypes = [ct.c_void_p, ct.c_int, P(Params), ct.c_double, ct.c_int64, ct.c_uint64,
+                                       P(ct.c_double)]
+        _lib.orc_run_steps.restype = ct.c_int64
     return _lib
+
+
+def run_steps(orcs, sp, seconds: float, max_sweeps: int = 1 << 40, seed: int = 1):
+    """Steady-state MD stepping of OracleUniverse objects inside C (orc_run_steps) for
+    ``seconds`` of wall time; returns (atom-steps, elapsed seconds)."""
+    arr = (ct.POINTER(CUniverse) * len(orcs))(*[ct.pointer(o.c) for o in orcs])
+    p = OracleUniverse.params(sp)
+    el = ct.c_double()
+    n = lib().orc_run_steps(ct.cast(arr, ct.c_void_p), len(orcs), ct.byref(p), seconds, max_sweeps,
+                            seed & 0xFFFFFFFFFFFFFFFF, ct.byref(el))
+    if n < 0:
+        raise RuntimeError("orc_run_steps failed")
+    return int(n), el.value
 
 
 class OracleUniverse:
@@ -143,6 +163,11 @@ class OracleUniverse:
     def atom_ekin(self):
         ep, el = ct.c_double(), ct.c_double()
         lib().orc_atom_ekin(ct.byref(self.c), ct.byref(ep), ct.byref(el))
+        return ep.value, el.value
+
+    def bead_ekin(self):
+        ep, el = ct.c_double(), ct.c_double()
+        lib().orc_bead_ekin(ct.byref(self.c), ct.byref(ep), ct.byref(el))
         return ep.value, el.value
 
     def bead_epot(self, sp):

@@ -8,8 +8,12 @@ Reads (only in the development container, where the reference tree is mounted):
                                                block parsed by numpy, independently of io)
   example/md/conf/latt/mxt_00000001.dat      -> runner_cgraphene.npz (parsed network +
                                                geometry) and runner_cgraphene_ref.npz
-                                               (oracle energy/forces/descriptors/neighbours)
-Usage:  python tests/golden/make_golden.py /root/reference
+                                               (the oracle's own energy/forces/descriptors/
+                                               neighbours: a regression fixture that keeps
+                                               the oracle and the GPU path from drifting,
+                                               not an independent golden vector)
+Usage:  python tests/golden/make_golden.py <reference checkout>
+        (default: MDT_REFERENCE_ROOT, else a directory named reference beside the repository)
 """
 import json
 import sys
@@ -64,4 +68,12 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) > 1:
+        main(sys.argv[1])
+    else:
+        sys.path.insert(0, str(HERE.parent.parent))
+        from tests.refroot import reference_root
+        root = reference_root()
+        if root is None:
+            sys.exit("no reference checkout: pass its path or set MDT_REFERENCE_ROOT")
+        main(str(root))

@@ -63,6 +63,60 @@ def test_step_limit_and_refill(built_lib):
     eng.close()
 
 
+def test_refill_keeps_ring_polymer_spread(built_lib):
+    """nb > 1: the projectile's beads move by (target - centroid) as in apply_pip, and their
+    velocities lose their mean and gain the incidence velocity as in set_proj_incidence, so
+    the bead spread and the internal bead velocities of the uploaded state are kept."""
+    rng = np.random.default_rng(53)
+    us = []
+    for nb in (4, 8):
+        u = W.h_on_metal(rng, "Pt", 3, 0.5, 0.0, 0.0, 300.0, C.PROP_ID_PILE, C.PROP_ID_PILE, z0=4.0, nbeads=nb)
+        u.r[0] += rng.normal(scale=0.05, size=u.r[0].shape)  # zero-point spread of the projectile
+        u.v[0] += rng.normal(scale=0.01, size=u.v[0].shape)  # internal bead velocities
+        us.append(u)
+    eng = Engine(0)
+    eng.read_emt(W.emt_params("H", "Pt"))
+    eng.define(us)
+    eng.upload()
+    up = eng.download()
+    sp = SimParams(step=0.1, seed=4)
+    eng.set_step_limit(3)
+    eng.calc_force(sp)
+    eng.md_steps(3, sp)
+    gen, n = eng.refill(z0=6.0, einc=(0.2, 0.4), polar=(0.0, 0.0), azimuth=0.0, seed=2)
+    assert n == 2
+    out = eng.download()
+    m_h = C.MASS_AMU["H"] * C.AMU2MASS
+    for t, u in enumerate(us):
+        r, v = eng.split(out["r"], t)[0], eng.split(out["v"], t)[0]   # (nb, 3) of the projectile
+        r0, v0 = eng.split(up["r"], t)[0], eng.split(up["v"], t)[0]
+        assert np.allclose(r - r.mean(0), r0 - r0.mean(0), rtol=0, atol=1e-12)
+        assert np.allclose(v - v.mean(0), v0 - v0.mean(0), rtol=0, atol=1e-14)
+        assert abs(r.mean(0)[2] - 6.0) < 1e-12
+        vc = v.mean(0)
+        assert abs(vc[0]) < 1e-14 and abs(vc[1]) < 1e-14 and vc[2] < 0.0  # normal incidence
+        assert 0.2 - 1e-12 <= 0.5 * m_h * np.sum(vc ** 2) <= 0.4 + 1e-12
+        assert np.array_equal(eng.split(out["r"], t)[1:], eng.split(up["r"], t)[1:])
+    eng.close()
+
+
+def test_error_status_is_not_refilled(built_lib):
+    us = W.config2(4, seed=54)
+    bad = [u.copy() for u in us]
+    bad[2].r[3, 0, 1] = np.nan
+    eng = _engine(bad)
+    sp = SimParams(step=0.1, gamma_const=1e-3, seed=4)
+    eng.set_step_limit(5)
+    eng.calc_force(sp)
+    eng.md_steps(5, sp)
+    q = eng.query(sp)
+    assert q["status"][2] == -11 and (q["status"][[0, 1, 3]] == 3).all()
+    gen, n = eng.refill(seed=1)
+    q = eng.query(sp)
+    assert n == 3 and gen[2] == 0 and q["status"][2] == -11 and (q["status"][[0, 1, 3]] == 0).all()
+    eng.close()
+
+
 def test_campaign_streams_trajectories(built_lib):
     us = W.config2(12, seed=52)
     eng = _engine(us)

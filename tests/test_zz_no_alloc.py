@@ -1,5 +1,5 @@
 """The allocation-free EMT entry point (mdt_emt_force_noalloc) against the regular
-context path, called through the C ABI on device buffers the test owns.
+context path and the FP64 oracle, called through the C ABI on device buffers the test owns.
 
 This entry point is for callers that may not allocate device memory themselves; it
 keeps its pair scratch in a file-scope device array shared by all calls.  The test
@@ -38,12 +38,19 @@ def _context_path(u, emt):
     return out["f"].reshape(-1, 3), out["epot"][0], out["dens"]
 
 
-def _noalloc(lib, u, emt, torch):
+def _oracle(u, emt):
+    from oracle.oracle import OracleUniverse
+    o = OracleUniverse(u, emt)
+    o.calc_force(SimParams())
+    return o.f[:, 0, :], float(o.epot[0]), o.dens[:, 0]
+
+
+def _noalloc(lib, u, emt, torch, idx_override=None):
     dev = torch.device("cuda", 0)
     n = u.natoms
     r = torch.tensor(u.r[:, 0, :], dtype=torch.float64, device=dev)
     x, y, z = (r[:, d].contiguous() for d in range(3))
-    idx = torch.tensor(u.idx, dtype=torch.int32, device=dev)
+    idx = torch.tensor(u.idx if idx_override is None else idx_override, dtype=torch.int32, device=dev)
     f = torch.zeros((3, n), dtype=torch.float64, device=dev)
     e = torch.zeros(1, dtype=torch.float64, device=dev)
     dens = torch.zeros(n, dtype=torch.float64, device=dev)
@@ -59,17 +66,36 @@ def _noalloc(lib, u, emt, torch):
     return f.T.cpu().numpy(), float(e.cpu()[0]), dens.cpu().numpy()
 
 
-def test_noalloc_matches_context_path_twice(built_lib):
+def test_noalloc_matches_context_path_twice(built_lib, oracle_lib):
     torch = pytest.importorskip("torch")
     lib = load()
     emt = W.emt_params()
     for seed, k in ((1, 4), (2, 3)):  # two calls in a row, different sizes
         u = _config(seed, k)
         f_ref, e_ref, d_ref = _context_path(u, emt)
+        f_o, e_o, d_o = _oracle(u, emt)
         f, e, d = _noalloc(lib, u, emt, torch)
         assert np.abs(f - f_ref).max() < FORCE_TOL
         assert abs(e - e_ref) < EPOT_TOL
         np.testing.assert_allclose(d, d_ref, rtol=1e-12)
+        assert np.abs(f - f_o).max() < FORCE_TOL
+        assert abs(e - e_o) < EPOT_TOL
+        np.testing.assert_allclose(d, d_o, rtol=1e-12)
+
+
+def test_noalloc_type_outside_table_gives_nan_energy(built_lib):
+    """A 1-based type index beyond the parameter table's ntypes (here 3 with two types)
+    makes the energy NaN instead of silently dropping the atom."""
+    torch = pytest.importorskip("torch")
+    lib = load()
+    emt = W.emt_params()
+    u = _config(3, 3)
+    idx = np.array(u.idx, np.int32)
+    idx[4] = 3
+    _, e, _ = _noalloc(lib, u, emt, torch, idx_override=idx)
+    assert np.isnan(e)
+    _, e_ok, _ = _noalloc(lib, u, emt, torch)  # the next call is clean again
+    assert np.isfinite(e_ok)
 
 
 def test_noalloc_rejects_oversized_configuration(built_lib):
