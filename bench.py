@@ -68,6 +68,10 @@ def parse():
                     help="trajectories of the whole-run scattering comparison (0: skip)")
     ap.add_argument("--scatter-steps", type=int, default=10000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--rpmd-traj", type=int, default=1024, help="trajectories of the RPMD arm (0: skip)")
+    ap.add_argument("--hdnnp-traj", type=int, default=2048, help="trajectories of the HDNNP arm (0: skip)")
+    ap.add_argument("--arm-steps", type=int, default=20, help="timed MD steps of the RPMD and HDNNP arms")
+    ap.add_argument("--no-nve", action="store_true", help="skip the surrogate's NVE drift runs")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     return ap.parse_args()
 
@@ -393,6 +397,161 @@ def scattering_comparison(args, model, device):
                            "combined standard error; two-sample KS on scattered eloss"}
 
 
+def _timed_arm(eng, sp, precision, steps, warmup, stream, torch):
+    """CUDA-event time of `steps` fused MD steps (one launch) after `warmup` steps."""
+    eng.calc_force(sp, precision=precision)
+    for _ in range(warmup):
+        eng.md_steps(1, sp, precision=precision)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    eng.md_steps(steps, sp, precision=precision)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    return ev0.elapsed_time(ev1) * 1e-3
+
+
+def rpmd_arm(args, device, stream, torch, peak64, peak32):
+    """Batched RPMD: H on Pt(111) 4x4 (64 Pt + H), force_beads mixed in {4, 8, 16, 32} per
+    trajectory, PILE (pile_tau 200 fs) at 300 K, Einc ~ U(0.1, 1) eV at normal incidence,
+    dt 0.1 fs.  FP64 normal-mode transform and propagation; bead forces in FP64 and FP32.
+    Metric: bead-atom-steps/s; the FP32 forces' error against the FP64 ones (the FP64 kernel
+    equals the FP64 oracle to 1e-10 eV/A in the parity tests)."""
+    import ctypes as ct
+
+    from md_tian2_gb300 import workloads as W
+    from md_tian2_gb300.engine import Engine, SimParams
+    us = W.config3(args.rpmd_traj, seed=3)
+    emt = W.emt_params("H", "Pt")
+    sp = SimParams(step=0.1, Tsurf=300.0, Tproj=300.0, pile_tau=200.0, seed=11)
+    bead_atoms = int(sum(u.natoms * u.nbeads for u in us))
+    same, mixed, nat = count_pairs(us, emt_cut(emt))
+    flop = FLOP_SAME_PAIR * same + FLOP_MIXED_PAIR * mixed + FLOP_ATOM * nat
+    # normal-mode transforms (to and from, positions and momenta) and PILE: 2 * 3 * nb^2 per atom and
+    # transform, three transforms per step (ring-polymer step both ways, PILE one way)
+    flop += int(sum(u.natoms * 3 * 2 * 3 * u.nbeads ** 2 for u in us))
+    out = {"trajectories": len(us), "bead_atoms": bead_atoms,
+           "beads": {str(b): int(sum(u.nbeads == b for u in us)) for b in (4, 8, 16, 32)}}
+    forces = {}
+    for prec in ("fp64", "fp32"):
+        eng = Engine(device)
+        eng.lib.mdt_set_stream(eng.h, ct.c_void_p(stream.cuda_stream))
+        eng.read_emt(emt)
+        eng.define(us)
+        eng.upload()
+        eng.calc_force(sp, precision=prec)
+        forces[prec] = eng.download()["f"]
+        eng.upload()
+        dt = _timed_arm(eng, sp, prec, args.arm_steps, 2, stream, torch)
+        q = eng.query(sp)
+        eng.close()
+        ok = bool(np.all(q["status"] == 0))
+        out[prec] = {"value": bead_atoms * args.arm_steps / dt, "unit": "bead-atom-steps/s",
+                     "ms_per_step": 1e3 * dt / args.arm_steps, "all_running": ok,
+                     "roofline": {"bound": prec, "achieved": flop / (dt / args.arm_steps) / 1e12,
+                                  "peak": (peak64 if prec == "fp64" else peak32) / 1e12, "unit": "TFLOP/s",
+                                  "frac": flop / (dt / args.arm_steps) / (peak64 if prec == "fp64" else peak32)}}
+    d = forces["fp32"] - forces["fp64"]
+    out["fp32_force_rmse_vs_fp64_eV_per_A"] = float(np.sqrt(np.mean(d ** 2)))
+    out["fp32_force_max_err_eV_per_A"] = float(np.max(np.abs(d)))
+    out["flop_per_step"] = flop
+    out["flop_convention"] = ("EMT pairs within 1.5 rcut per bead (same-species 200, H-metal 280 FLOP) + 100 per "
+                              "bead-atom + 18 nb^2 per atom for the normal-mode transforms")
+    return out
+
+
+# HDNNP arm: algorithmic FLOP per neighbour pair (8 G2: exp + 5 FLOP each, cutoff 40) and per
+# valid triplet (16 G3 terms x 6 FLOP + 30 geometry), forward; backward twice the forward; the
+# network 2 * (24*25 + 25*25 + 25) per atom forward, three times that with the backward.
+FLOP_HD_PAIR = 3 * (8 * 25 + 40)
+FLOP_HD_TRIPLET = 3 * (16 * 6 + 30)
+FLOP_HD_ATOM = 3 * 2 * (24 * 25 + 25 * 25 + 25)
+
+
+def _valid_triplets(eng, us, rc_ang, sample):
+    """Triplets (i; j < k) inside the cutoff (r_ij, r_ik, r_jk < rc) from the neighbour lists
+    the kernel built, on the first `sample` trajectories; returns (pairs, triplets) summed."""
+    counts, words = eng.nn_neighbors()
+    off = np.concatenate([[0], np.cumsum([u.natoms for u in us])])
+    pairs = trip = 0
+    for t in range(sample):
+        u = us[t]
+        r = u.r[:, 0, :]
+        for i in range(u.natoms):
+            a = off[t] + i
+            w = words[a, :counts[a]]
+            j = w & 0xFFFF
+            n = np.stack([((w >> s) & 15) - 8 for s in (16, 20, 24)], axis=1)
+            pos = r[j] + n @ u.simbox.T  # image positions (cell vectors as columns)
+            pairs += len(j)
+            if len(j) > 1:
+                dd = np.sqrt(((pos[:, None, :] - pos[None, :, :]) ** 2).sum(-1))
+                iu = np.triu_indices(len(j), 1)
+                trip += int(np.sum(dd[iu] < rc_ang))
+    return pairs, trip
+
+
+def hdnnp_arm(args, device, stream, torch, peak32, peak64):
+    """Batched RuNNer-style HDNNP: H on 6x6 graphene (72 C + 1 H, z-ripple 0.05 A), 8 G2 + 16 G3
+    per element (6.5 A cosine cutoff), 24-25-25-1 tanh per element with seeded Glorot weights
+    and scaling from the batch's own descriptors; Verlet, dt 0.1 fs.  FP64 generic kernels and
+    FP32 warp-per-atom fast kernels; the FP32 error against FP64 (the FP64 kernels equal the
+    FP64 oracle to 1e-10 eV/A in the parity tests).  The tensor-core (BF16) network exists only
+    in the thread-per-atom kernel of radial networks, not for this G3 model."""
+    import ctypes as ct
+
+    from md_tian2_gb300 import nene
+    from md_tian2_gb300 import workloads as W
+    from md_tian2_gb300.engine import PES_NENE, Engine, SimParams
+    us = W.config4(args.hdnnp_traj, seed=4)
+    m = nene.random_model(["H", "C"], hidden=(25, 25), act="t", seed=5, neighbours=["C"])
+    sp = SimParams(step=0.1, seed=3)
+
+    def engine():
+        eng = Engine(device)
+        eng.lib.mdt_set_stream(eng.h, ct.c_void_p(stream.cuda_stream))
+        eng.define(us)
+        eng.read_nene(m, ["H", "C"], max_neighbors=96)
+        eng.set_pes(PES_NENE, 0.0)
+        eng.upload()
+        return eng
+
+    eng = engine()
+    G = eng.nn_descriptors()
+    eng.close()
+    nene.set_scaling(m, G, np.concatenate([[0] + [1] * (u.natoms - 1) for u in us]))
+    atoms = int(sum(u.natoms for u in us))
+    out = {"trajectories": len(us), "atoms": atoms}
+    forces = {}
+    for prec in ("fp64", "fp32"):
+        eng = engine()
+        eng.calc_force(sp, precision=prec)
+        forces[prec] = eng.download()["f"]
+        if prec == "fp64":
+            sample = min(32, len(us))
+            pairs, trip = _valid_triplets(eng, us, 6.5, sample)
+            scale = len(us) / sample
+            flop = int(scale * (FLOP_HD_PAIR * pairs + FLOP_HD_TRIPLET * trip)) + FLOP_HD_ATOM * atoms
+        eng.upload()
+        dt = _timed_arm(eng, sp, prec, args.arm_steps, 2, stream, torch)
+        fast = eng.nn_fast_path(True)
+        eng.close()
+        out[prec] = {"value": atoms * args.arm_steps / dt, "unit": "atom-steps/s", "ms_per_step": 1e3 * dt / args.arm_steps,
+                     "kernel": ("nnf_kernel (warp per atom, FP32)" if (prec == "fp32" and fast)
+                                else "nn_md_steps_kernel (generic, " + prec + ")"),
+                     "roofline": {"bound": prec, "achieved": flop / (dt / args.arm_steps) / 1e12,
+                                  "peak": (peak64 if prec == "fp64" else peak32) / 1e12, "unit": "TFLOP/s",
+                                  "frac": flop / (dt / args.arm_steps) / (peak64 if prec == "fp64" else peak32)}}
+    d = forces["fp32"] - forces["fp64"]
+    out["fp32_force_rmse_vs_fp64_eV_per_A"] = float(np.sqrt(np.mean(d ** 2)))
+    out["fp32_force_max_err_eV_per_A"] = float(np.max(np.abs(d)))
+    out["bf16"] = "n/a: tensor-core network GEMMs are in the thread-per-atom kernel of radial networks only"
+    out["flop_per_step"] = flop
+    out["flop_convention"] = ("per neighbour pair 720, per valid triplet (r_ij, r_ik, r_jk < rc; counted on a "
+                              "32-trajectory sample and scaled) 378, per atom 7,500 (forward + backward)")
+    return out
+
+
 def run_ours(args):
     import ctypes as ct
 
@@ -412,6 +571,7 @@ def run_ours(args):
 
     from md_tian2_gb300 import nene
     from md_tian2_gb300._lib import load
+    from md_tian2_gb300._lib import EngineError
     from md_tian2_gb300.engine import PES_EMT, PES_SURROGATE, Engine
     from md_tian2_gb300.surrogate import force_rmse, generate_dataset
     lib = load()
@@ -428,6 +588,21 @@ def run_ours(args):
 
     def atom_steps_now():
         return int(np.sum(natoms * eng.query(sp)["steps_done"]))
+
+    # ---- accuracy against FP64 EMT on held-out configurations ------------------------------
+    acc = None
+    if rank == 0 and args.rmse_traj > 0:
+        held = generate_dataset(args.rmse_traj, 8, 50, seed=4242 + rank, device=local)
+        f32, e32 = force_rmse(model, held, device=local, precision="fp32", max_neighbors=80)
+        acc = {"force_rmse_meV_per_A": 1e3 * f32, "energy_rmse_meV_per_atom": 1e3 * e32,
+               "configs": len(held.universes),
+               "sample": f"{args.rmse_traj} config-2 trajectories (seed {4242 + rank}) propagated with FP64 EMT, "
+                         "sampled every 50 steps x 8; network forces (no fallback) vs FP64 EMT forces"}
+        try:
+            fb16, eb16 = force_rmse(model, held, device=local, precision="bf16", max_neighbors=80)
+            acc["bf16"] = {"force_rmse_meV_per_A": 1e3 * fb16, "energy_rmse_meV_per_atom": 1e3 * eb16}
+        except EngineError:  # the model does not run on the thread-per-atom kernel
+            acc["bf16"] = None
 
     # ---- surrogate (headline) -------------------------------------------------------
     eng.set_pes(PES_SURROGATE, args.margin)
@@ -458,6 +633,24 @@ def run_ours(args):
     entries = int(np.sum(counts))
     surr_flop = FLOP_SURR_ENTRY * entries + FLOP_SURR_ATOM * int(np.sum(natoms))
 
+    # ---- the same surrogate with the network GEMMs on the tensor cores (BF16 operands) ----
+    bf16 = None
+    if radial:
+        eng.upload()
+        eng.calc_force(sp, precision="bf16")
+        for _ in range(args.warmup):
+            eng.md_steps(1, sp, precision="bf16")
+        torch.cuda.synchronize()
+        s0b = atom_steps_now()
+        ms_bf, clocks_bf = timed_steps(eng, sp, "bf16", args.steps, stream, torch, dist, local, per_launch)
+        done_bf = atom_steps_now() - s0b
+        bf16 = {"ms": ms_bf, "done": done_bf, "clocks": clocks_bf}
+    # the headline is the faster arithmetic that meets the metric's 20 meV/A accuracy bar
+    head = "fp32"
+    bf_rmse = ((acc or {}).get("bf16") or {}).get("force_rmse_meV_per_A")
+    if bf16 is not None and bf16["done"] / bf16["ms"] > done / ms and bf_rmse is not None and bf_rmse <= 20.0:
+        head = "bf16"
+
     # end-to-end through the C ABI with pinned host buffers (surrogate)
     nslots = eng.nslots
     h_r = torch.empty(3 * nslots, dtype=torch.float64).pin_memory()
@@ -467,13 +660,13 @@ def run_ours(args):
     e2e_steps = max(3, args.steps // 2)
     for w in range(2):
         eng.upload_ptr(h_r.data_ptr(), h_v.data_ptr())
-        eng.md_steps(1, sp, precision="fp32")
+        eng.md_steps(1, sp, precision=head)
         lib.mdt_state_download(eng.h, h_r.data_ptr(), h_v.data_ptr(), None, None, h_e.data_ptr(), None)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         eng.upload_ptr(h_r.data_ptr(), h_v.data_ptr())
-        eng.md_steps(1, sp, precision="fp32")
+        eng.md_steps(1, sp, precision=head)
         rc = lib.mdt_state_download(eng.h, h_r.data_ptr(), h_v.data_ptr(), None, None, h_e.data_ptr(), None)
         if rc != 0:
             raise RuntimeError("download failed")
@@ -497,16 +690,21 @@ def run_ours(args):
     emt_flop = FLOP_SAME_PAIR * same + FLOP_MIXED_PAIR * mixed + FLOP_ATOM * nat
     eng.close()
 
-    # ---- accuracy against FP64 EMT on held-out configurations ------------------------------
-    acc = None
-    if rank == 0 and args.rmse_traj > 0:
-        held = generate_dataset(args.rmse_traj, 8, 50, seed=4242 + rank, device=local)
-        f32, e32 = force_rmse(model, held, device=local, precision="fp32", max_neighbors=80)
-        acc = {"force_rmse_meV_per_A": 1e3 * f32, "energy_rmse_meV_per_atom": 1e3 * e32,
-               "configs": len(held.universes),
-               "sample": f"{args.rmse_traj} config-2 trajectories (seed {4242 + rank}) propagated with FP64 EMT, "
-                         "sampled every 50 steps x 8; network forces (no fallback) vs FP64 EMT forces"}
-
+    # ---- NVE energy drift of the surrogate path ----------------------------------------------
+    if rank == 0 and acc is not None:
+        if not args.no_nve:
+            from md_tian2_gb300.surrogate import nve_drift
+            acc["nve_drift"] = {}
+            for prec in ("fp32", "bf16") if bf16 is not None else ("fp32",):
+                d = nve_drift(model, prec, device=local)
+                acc["nve_drift"][prec] = {"mean_meV_per_ps": d["mean_meV_per_ps"],
+                                          "max_abs_meV_per_ps": d["max_abs_meV_per_ps"],
+                                          "fallbacks": d["fallbacks"]}
+                if prec == "bf16":
+                    acc["nve_drift"][prec]["bf16_energy_readout_rms_meV"] = d["readout_rms_meV"]
+            acc["nve_drift"]["setup"] = ("8 H/Au(111) 3x3 trajectories, all atoms free, velocity Verlet, dt 0.1 fs, "
+                                         "2 ps; slope of a linear fit of the total energy (FP64 per-trajectory sums "
+                                         "of an FP32 evaluation of the network on the run's states)")
     # ---- scattering observables: whole trajectories to exit, surrogate vs FP64 EMT ----------
     obs = None
     if rank == 0 and args.scatter_traj > 0:
@@ -516,6 +714,13 @@ def run_ours(args):
     lib.mdt_peak_fma(1, 20000, ct.byref(peak))
     peak64 = ct.c_double()
     lib.mdt_peak_fma(0, 2000, ct.byref(peak64))
+
+    # ---- the RPMD and HDNNP workloads ---------------------------------------------------------
+    rpmd = hdnnp = None
+    if rank == 0 and args.rpmd_traj > 0:
+        rpmd = rpmd_arm(args, local, stream, torch, peak64.value, peak.value)
+    if rank == 0 and args.hdnnp_traj > 0:
+        hdnnp = hdnnp_arm(args, local, stream, torch, peak.value, peak64.value)
     traffic = None
     prof = ROOT / "profiles" / ("nnr_surrogate_traffic.json" if radial else "nnf_surrogate_traffic.json")
     if prof.exists():
@@ -531,16 +736,30 @@ def run_ours(args):
         value = done_all / elapsed
         emt_value = done_emt_all / elapsed_emt
         achieved = surr_flop / (elapsed / args.steps)
+        other = None  # the arithmetic that is not the headline
+        if bf16 is not None:
+            bf_elapsed = bf16["ms"] * 1e-3
+            arms = {"fp32": (done_all, elapsed, clocks), "bf16": (bf16["done"], bf_elapsed, bf16["clocks"])}
+            o = "bf16" if head == "fp32" else "fp32"
+            od, oe, oc = arms[o]
+            other = {"dtype": o, "value": od / oe, "unit": UNIT, "ms_per_step": 1e3 * oe / args.steps,
+                     "speedup_vs_fp64_emt": (od / oe) / emt_value, "clocks": oc,
+                     "force_rmse_meV_per_A": (acc or {}).get("force_rmse_meV_per_A") if o == "fp32" else bf_rmse,
+                     "roofline": {"bound": "fp32", "achieved": surr_flop / (oe / args.steps) / 1e12,
+                                  "peak": peak.value / 1e12, "unit": "TFLOP/s",
+                                  "frac": surr_flop / (oe / args.steps) / peak.value}}
+            value, elapsed, clocks = arms[head][0] / arms[head][1], arms[head][1], arms[head][2]
+            achieved = surr_flop / (elapsed / args.steps)
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "scaling": "weak", "vs_baseline": None, "dtype": "bf16" if head == "bf16" else "f32",
             "data": "synthetic (seeded H/Au(111) slabs, see workloads.py); surrogate weights trained on the GPU "
                     "from FP64 EMT labels (md_tian2_gb300/data)",
-            "config": {"workload": f"NN surrogate (FP32 fast kernels, EMT fallback), {args.ntraj} ragged H/Au(111) "
+            "config": {"workload": f"NN surrogate ({'BF16 tensor-core network, FP32 descriptors and forces' if head == 'bf16' else 'FP32 kernels'}, EMT fallback), {args.ntraj} ragged H/Au(111) "
                                    "trajectories (37-145 atoms), Verlet H + constant-friction Langevin Au, dt 0.1 fs; "
                                    "one bench step = one MD step of every trajectory",
-                       "steps_per_launch": per_launch,
+                       "steps_per_launch": per_launch, "precision": head,
                        "model": Path(args.model).name, "fast_path": bool(fast), "radial_kernel": bool(radial),
                        "skin_A": args.skin,
                        "ntraj_per_gpu": args.ntraj,
@@ -558,6 +777,9 @@ def run_ours(args):
             "fallback": {"bead_evaluations": bead_evals, "emt_fallbacks": fb_count,
                          "fraction": fb_count / max(1, bead_evals)},
             "scattering": obs,
+            "surrogate_other_precision": other,
+            "rpmd_config3": rpmd,
+            "hdnnp_config4": hdnnp,
             "clocks": clocks,
             "e2e": {"value": e_atoms_all / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": int(launches),

@@ -153,6 +153,20 @@ module mdt_gpu
             real(c_double), value :: skin_ang
         end function
 
+        integer(c_int32_t) function mdt_autotune(ctx, precision, nsteps, p, block, skin_ang, ms_per_step) &
+                bind(C, name="mdt_autotune")
+            import :: c_int32_t, c_ptr, mdt_prop_params
+            type(c_ptr), value :: ctx
+            integer(c_int32_t), value :: precision, nsteps
+            type(mdt_prop_params), intent(in) :: p
+            type(c_ptr), value :: block, skin_ang, ms_per_step
+        end function
+
+        integer(c_int32_t) function mdt_nn_repack(ctx, npacks) bind(C, name="mdt_nn_repack")
+            import :: c_int32_t, c_ptr
+            type(c_ptr), value :: ctx, npacks
+        end function
+
         integer(c_int32_t) function mdt_nn_stats(ctx, fallbacks, overflow) bind(C, name="mdt_nn_stats")
             import :: c_int32_t, c_ptr
             type(c_ptr), value :: ctx, fallbacks, overflow
@@ -275,6 +289,19 @@ module mdt_gpu
                 bind(C, name="mdt_traj_observables")
             import :: c_int32_t, c_ptr
             type(c_ptr), value :: ctx, turn_pnts, cl_appr, cl_appr_step, r_min_p
+        end function
+
+        integer(c_int32_t) function mdt_traj_bounces(ctx, bounces, interaction_time, is_adsorbed, p) &
+                bind(C, name="mdt_traj_bounces")
+            import :: c_int32_t, c_ptr, mdt_prop_params
+            type(c_ptr), value :: ctx, bounces, interaction_time, is_adsorbed
+            type(mdt_prop_params), intent(in) :: p
+        end function
+
+        integer(c_int32_t) function mdt_set_adsorption(ctx, ads_start, ads_end) bind(C, name="mdt_set_adsorption")
+            import :: c_int32_t, c_ptr, c_double
+            type(c_ptr), value :: ctx
+            real(c_double), value :: ads_start, ads_end
         end function
 
         integer(c_int32_t) function mdt_query(ctx, p, out) bind(C, name="mdt_query")

@@ -169,6 +169,27 @@ int32_t mdt_nn_radial_block(mdt_ctx *ctx, int32_t max_block);
    cutoff test, so results do not depend on the skin. */
 int32_t mdt_nn_set_skin(mdt_ctx *ctx, double skin_ang);
 
+/* Re-pack the thread-per-atom kernel's CTAs over the trajectories still running
+   (status MDT_TRAJ_RUNNING): stopped trajectories no longer hold threads of a CTA, so a batch
+   whose trajectories leave at different times keeps its CTAs full.  The plan is rebuilt over
+   all trajectories after mdt_state_upload and after an mdt_refill that restarted any.
+   npacks (may be NULL) receives the number of CTAs (packs) of the plan, 0 when the batch
+   does not run on that kernel (nothing to do).  No replacement in the reference, which runs
+   one trajectory at a time. */
+int32_t mdt_nn_repack(mdt_ctx *ctx, int32_t *npacks);
+
+/* Autotuner of the thread-per-atom kernel (no counterpart in the reference): times nsteps
+   fused MD steps (mdt_md_steps with p and precision MDT_PREC_FP32 or MDT_PREC_BF16) of the
+   current batch for every candidate launch shape -- the largest CTA of the pack plan
+   (256, 384 or 512 atoms: waves and warps per SM) times the Verlet skin (0.5, 0.75, 1 A) --
+   each from the same saved state, keeps the fastest (as mdt_nn_radial_block and
+   mdt_nn_set_skin would set it) and restores the state, so the batch continues as if the
+   call had not happened.  Results do not depend on the choice.  block, skin_ang and
+   ms_per_step (may be NULL) receive the choice and its time.  MDT_ERR_UNSUPPORTED when the
+   batch does not run on that kernel. */
+int32_t mdt_autotune(mdt_ctx *ctx, int32_t precision, int32_t nsteps, const mdt_prop_params *p, int32_t *block,
+                     double *skin_ang, double *ms_per_step);
+
 /* per trajectory: number of bead evaluations that fell back to EMT, and 1 if a
    neighbour list overflowed max_neighbors (either may be NULL) */
 int32_t mdt_nn_stats(mdt_ctx *ctx, int32_t *fallbacks, int32_t *overflow);
@@ -291,6 +312,22 @@ int32_t mdt_refill(mdt_ctx *ctx, const mdt_refill_params *p, int32_t *generation
    later collect) follows from cl_appr_step on the host. */
 int32_t mdt_traj_observables(mdt_ctx *ctx, int32_t *turn_pnts, double *cl_appr, int32_t *cl_appr_step,
                              double *r_min_p);
+
+/* Bounce detection and adsorption of collect_trajectory_characteristics
+   (src/trajectory_info.f90:80-263), tracked by the fused MD steps after every step and reset
+   by mdt_state_upload / mdt_refill: bounces[t] counts the projectile's collisions (per
+   nearest-atom segment the smallest of the r.v + to - sign changes and the crossings of r.v
+   with r.F and with v.F, with the open segment closed as output_scatter closes it,
+   output_mod.f90:660); interaction_time[t] (fs) the time with a non-zero projectile force;
+   is_adsorbed[t] the adsorption flag (set when the closest approach of a step falls below
+   the start limit, cleared above the end limit of mdt_set_adsorption).  Any output may be
+   NULL; p supplies the step (fs). */
+int32_t mdt_traj_bounces(mdt_ctx *ctx, int32_t *bounces, double *interaction_time, int32_t *is_adsorbed,
+                         const mdt_prop_params *p);
+/* The adsorption limits (A) of md_tian.inp's adsorption keyword (run_config.f90:644-650):
+   adsorbed below `start`, free again above `end`; default: never adsorbed (the reference's
+   default_real limits). */
+int32_t mdt_set_adsorption(mdt_ctx *ctx, double start, double end);
 
 /* per-trajectory status, steps and energies (output_mod.f90:658-697 fields) */
 int32_t mdt_query(mdt_ctx *ctx, const mdt_prop_params *p, mdt_traj_summary *out);

@@ -84,6 +84,11 @@ SIGNATURES = {
     "mdt_nn_radial_kernel": (ct.c_int32, [ct.c_void_p, ct.c_int32]),
     "mdt_nn_radial_block": (ct.c_int32, [ct.c_void_p, ct.c_int32]),
     "mdt_traj_observables": (ct.c_int32, [ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p]),
+    "mdt_traj_bounces": (ct.c_int32, [ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.POINTER(PropParams)]),
+    "mdt_set_adsorption": (ct.c_int32, [ct.c_void_p, ct.c_double, ct.c_double]),
+    "mdt_nn_repack": (ct.c_int32, [ct.c_void_p, ct.c_void_p]),
+    "mdt_autotune": (ct.c_int32, [ct.c_void_p, ct.c_int32, ct.c_int32, ct.POINTER(PropParams), ct.c_void_p,
+                                  ct.c_void_p, ct.c_void_p]),
     "mdt_set_step_limit": (ct.c_int32, [ct.c_void_p, ct.c_int32]),
     "mdt_refill": (ct.c_int32, [ct.c_void_p, ct.POINTER(RefillParams), ct.c_void_p, ct.POINTER(ct.c_int32)]),
     "mdt_nn_set_skin": (ct.c_int32, [ct.c_void_p, ct.c_double]),

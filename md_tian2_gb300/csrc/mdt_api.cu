@@ -39,6 +39,7 @@ struct mdt_ctx {
     int *gen = nullptr, *refill_count = nullptr;
     bool have_tmpl = false;
     int step_limit = 0;
+    double ads_start = kDefaultReal, ads_end = kDefaultReal;  // adsorption hysteresis (A)
     int T = 0, ntypes = 0, max_atoms = 0, max_beads = 0;
     int64_t total_ba = 0, total_pairs = 0;
     int total_atoms = 0, total_beads = 0;
@@ -192,6 +193,8 @@ PropParams to_dev(const mdt_ctx *c, const mdt_prop_params *p) {
     P.use_exit = p->use_exit;
     P.rng_mode = p->rng_mode;
     P.max_steps = c->step_limit;
+    P.ads_start = c->ads_start;
+    P.ads_end = c->ads_end;
     P.randy = c->rnd[0];
     P.zeta = c->rnd[1];
     P.andersen_v = c->rnd[2];
@@ -558,8 +561,10 @@ int ensure_mscr(mdt_ctx *c, int grid, int layout);
 // smallest w whose block fits the cap wins (one CTA per SM is resident, so the largest
 // CTAs keep the most warps in flight; the latency-bound kernel gains more from them than
 // it loses to the emptier last wave).
-bool radial_plan(mdt_ctx *c) {
-    if (c->rnpack > 0) return true;
+// ids: the trajectories to pack (all of them when empty); a re-pack over the trajectories
+// still running drops the threads of stopped ones (mdt_nn_repack)
+bool radial_plan(mdt_ctx *c, const std::vector<int> &ids = {}) {
+    if (c->rnpack > 0 && ids.empty()) return true;
     if (c->max_beads != 1 || c->max_atoms > kRBlockMax) return false;
     for (int t = 0; t < c->ntypes; ++t)
         if (c->R.elem_of_type[t] < 0) return false;
@@ -595,17 +600,21 @@ bool radial_plan(mdt_ctx *c) {
     }
     c->R.block = kRBlockMax;
     const int slots = c->num_sms * std::max(1, nnr_resident_ctas(c->R));
-    std::vector<int> order(c->T);
-    std::iota(order.begin(), order.end(), 0);
+    std::vector<int> order(ids.empty() ? c->T : (int)ids.size());
+    if (ids.empty()) std::iota(order.begin(), order.end(), 0);
+    else std::copy(ids.begin(), ids.end(), order.begin());
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return c->natoms[a] > c->natoms[b]; });
-    const int64_t total = c->total_atoms;
+    int64_t total = 0;
+    for (int t : order) total += c->natoms[t];
+    const int ntr = (int)order.size();
+    if (ntr == 0) return c->rnpack > 0;
     const int bmax = std::max(32, std::min(kRBlockMax, c->rmaxblock));
     if (c->max_atoms > bmax) return false;
     const int w0 = (int)std::max<int64_t>(1, (total + (int64_t)slots * bmax - 1) / ((int64_t)slots * bmax));
     std::vector<std::vector<int>> bestp;
     int bestb = 0;
     for (int w = w0; w <= w0 + 4; ++w) {
-        const int np = std::min<int64_t>((int64_t)w * slots, c->T);
+        const int np = std::min<int64_t>((int64_t)w * slots, ntr);
         std::vector<std::vector<int>> packs(np);
         std::vector<int> load(np, 0);
         // min-heap of (atoms, pack) over packs that still take trajectories
@@ -654,15 +663,18 @@ bool radial_plan(mdt_ctx *c) {
         hp.push_back(make_int2((int)ht.size(), (int)p.size()));
         ht.insert(ht.end(), p.begin(), p.end());
     }
+    // the plan's buffers hold one pack and one entry per trajectory of the batch: every plan,
+    // of all trajectories or of those still running, fits
     cudaError_t e = cudaSuccess;
-    int2 *d = dalloc<int2>(c, hp.size(), e);
-    int *dt = dalloc<int>(c, ht.size(), e);
-    if (!d || !dt) return false;
-    if (cudaMemcpy(d, hp.data(), sizeof(int2) * hp.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemcpy(dt, ht.data(), sizeof(int) * ht.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+    if (!c->rpacks) c->rpacks = dalloc<int2>(c, (size_t)c->T, e);
+    if (!c->rptraj) c->rptraj = dalloc<int>(c, (size_t)c->T, e);
+    if (!c->rpacks || !c->rptraj) return false;
+    if (cudaMemcpyAsync(c->rpacks, hp.data(), sizeof(int2) * hp.size(), cudaMemcpyHostToDevice, c->stream) !=
+            cudaSuccess ||
+        cudaMemcpyAsync(c->rptraj, ht.data(), sizeof(int) * ht.size(), cudaMemcpyHostToDevice, c->stream) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(c->stream) != cudaSuccess)
         return false;
-    c->rpacks = d;
-    c->rptraj = dt;
     c->rnpack = (int)hp.size();
     c->rblock = bestb;
     return true;
@@ -986,8 +998,8 @@ int32_t mdt_batch_define(mdt_ctx *c, int32_t ntraj, const int32_t *natoms, const
     ALLOC(d_steps, int, ntraj);
     int *d_obs_i;
     double *d_obs_d;
-    ALLOC(d_obs_i, int, 3 * (size_t)ntraj);
-    ALLOC(d_obs_d, double, 4 * (size_t)ntraj);
+    ALLOC(d_obs_i, int, (3 + kObsInts) * (size_t)ntraj);
+    ALLOC(d_obs_d, double, (4 + kObsDots) * (size_t)ntraj);
     ALLOC(d_ba_off, int64_t, ntraj);
     ALLOC(d_pair_off, int64_t, ntraj);
     ALLOC(d_mass, double, at);
@@ -1056,6 +1068,8 @@ int32_t mdt_batch_define(mdt_ctx *c, int32_t ntraj, const int32_t *natoms, const
     B.obs_clstep = d_obs_i + 2 * (size_t)ntraj;
     B.obs_cl = d_obs_d;
     B.obs_low = d_obs_d + ntraj;
+    B.obs_bnc = d_obs_i + 3 * (size_t)ntraj;
+    B.obs_dot = d_obs_d + 4 * (size_t)ntraj;
     B.cjk_off = d_cjk_off;
     B.cjk = d_cjk;
     B.pair_scratch = nullptr;
@@ -1094,6 +1108,7 @@ int32_t mdt_state_upload(mdt_ctx *c, const double *r, const double *v) {
     if (e == cudaSuccess) e = cudaMemsetAsync(B.status, 0, sizeof(int) * c->T, c->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(B.steps_done, 0, sizeof(int) * c->T, c->stream);
     if (e == cudaSuccess) e = launch_obs_reset(c->stream, B);
+    c->rnpack = 0;  // every trajectory runs again: the next thread-per-atom launch packs them all
     // the uploaded state is the template of mdt_refill
     const double *cur[6] = {B.rx, B.ry, B.rz, B.vx, B.vy, B.vz};
     for (int a = 0; a < 6 && e == cudaSuccess; ++a)
@@ -1283,6 +1298,27 @@ int32_t mdt_refill(mdt_ctx *c, const mdt_refill_params *p, int32_t *generation, 
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "mdt_refill");
     if (nrefilled) *nrefilled = n;
+    if (n > 0) c->rnpack = 0;  // restarted trajectories must be in the next pack plan
+    return MDT_OK;
+}
+
+int32_t mdt_nn_repack(mdt_ctx *c, int32_t *npacks) {
+    int rc = check_ready(c, false);
+    if (rc) return rc;
+    if (!c->R.ok || !c->have_nn) {
+        if (npacks) *npacks = 0;
+        return MDT_OK;
+    }
+    std::vector<int> st(c->T);
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e == cudaSuccess) e = cudaMemcpy(st.data(), c->B.status, sizeof(int) * c->T, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(c, e, "mdt_nn_repack");
+    std::vector<int> ids;
+    for (int t = 0; t < c->T; ++t)
+        if (st[t] == MDT_TRAJ_RUNNING) ids.push_back(t);
+    if (!ids.empty() && (int)ids.size() < c->T && !radial_plan(c, ids))
+        return fail(c, MDT_ERR_UNSUPPORTED, "mdt_nn_repack: the running trajectories cannot be packed");
+    if (npacks) *npacks = c->rnpack;
     return MDT_OK;
 }
 
@@ -1299,6 +1335,34 @@ int32_t mdt_traj_observables(mdt_ctx *c, int32_t *turn_pnts, double *cl_appr, in
         e = cudaMemcpy(cl_appr_step, B.obs_clstep, sizeof(int) * T, cudaMemcpyDeviceToHost);
     if (e == cudaSuccess && r_min_p) e = cudaMemcpy(r_min_p, B.obs_low, sizeof(double) * 3 * T, cudaMemcpyDeviceToHost);
     return e == cudaSuccess ? MDT_OK : cuda_fail(c, e, "mdt_traj_observables");
+}
+
+int32_t mdt_set_adsorption(mdt_ctx *c, double start, double end) {
+    if (!c) return MDT_ERR_ARG;
+    if (!(start <= end)) return fail(c, MDT_ERR_ARG, "mdt_set_adsorption: start must not exceed end");
+    c->ads_start = start;
+    c->ads_end = end;
+    return MDT_OK;
+}
+
+int32_t mdt_traj_bounces(mdt_ctx *c, int32_t *bounces, double *interaction_time, int32_t *is_adsorbed,
+                         const mdt_prop_params *p) {
+    int rc = check_ready(c, false);
+    if (rc) return rc;
+    if (!p) return fail(c, MDT_ERR_ARG, "mdt_traj_bounces: null parameters");
+    const size_t T = (size_t)c->T;
+    std::vector<int> h(kObsInts * T);
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e == cudaSuccess) e = cudaMemcpy(h.data(), c->B.obs_bnc, sizeof(int) * h.size(), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(c, e, "mdt_traj_bounces");
+    for (size_t t = 0; t < T; ++t) {
+        const int *b = h.data() + kObsInts * t;
+        // finalize_bounces as output_scatter calls it before writing (output_mod.f90:660)
+        if (bounces) bounces[t] = b[kObsBounces] + std::min(b[kObsPtm], std::min(b[kObsRF], b[kObsVF]));
+        if (interaction_time) interaction_time[t] = b[kObsInter] * p->step;
+        if (is_adsorbed) is_adsorbed[t] = b[kObsAds];
+    }
+    return MDT_OK;
 }
 
 int32_t mdt_query(mdt_ctx *c, const mdt_prop_params *p, mdt_traj_summary *out) {
@@ -1559,6 +1623,103 @@ int32_t mdt_nn_radial_block(mdt_ctx *c, int32_t max_block) {
     if (max_block < 32 || max_block > kRBlockMax) return fail(c, MDT_ERR_ARG, "max_block outside [32, 512]");
     c->rmaxblock = max_block;
     c->rnpack = 0;  // re-plan on the next evaluation
+    return MDT_OK;
+}
+
+// Autotuner of the thread-per-atom kernel: times `nsteps` fused MD steps of the current
+// batch for every candidate (largest CTA in {256, 384, 512} atoms -- the pack plan's block
+// cap, which sets the waves and the warps per SM -- times Verlet skin in {0.5, 0.75, 1.0}
+// A), each from the same saved state, keeps the fastest and puts the state back.
+int32_t mdt_autotune(mdt_ctx *c, int32_t precision, int32_t nsteps, const mdt_prop_params *p, int32_t *block,
+                     double *skin_ang, double *ms_per_step) {
+    int rc = check_ready(c, false);
+    if (rc) return rc;
+    if (!p || nsteps < 1) return fail(c, MDT_ERR_ARG, "mdt_autotune: parameters and nsteps >= 1 needed");
+    if (c->pes_kind == MDT_PES_EMT) return fail(c, MDT_ERR_UNSUPPORTED, "mdt_autotune tunes the network kernels");
+    if ((rc = check_nn_ready(c))) return rc;
+    if (!use_radial(c, precision, true))
+        return fail(c, MDT_ERR_UNSUPPORTED, "mdt_autotune: the batch does not run on the thread-per-atom kernel");
+    // saved state: r, v, a, f, dens (per bead-atom), epot (per bead), status, steps, observables
+    Batch &B = c->B;
+    const size_t nba = (size_t)c->total_ba, T = (size_t)c->T, nbd = (size_t)c->total_beads;
+    double *d12[13] = {B.rx, B.ry, B.rz, B.vx, B.vy, B.vz, B.ax, B.ay, B.az, B.fx, B.fy, B.fz, B.dens};
+    int *ivec[2] = {B.status, B.steps_done};
+    const size_t obs_i = (3 + kObsInts) * T, obs_d = (4 + kObsDots) * T;
+    const size_t bytes = 8 * (13 * nba + nbd + obs_d) + 4 * (2 * T + obs_i + 2 * T);
+    unsigned char *snap = nullptr;
+    cudaError_t e = cudaMalloc(&snap, bytes);
+    if (e != cudaSuccess) return cuda_fail(c, e, "mdt_autotune snapshot");
+    auto copy_all = [&](bool save) -> cudaError_t {
+        size_t off = 0;
+        cudaError_t err = cudaSuccess;
+        auto mv = [&](void *dev, size_t n) {
+            if (err == cudaSuccess)
+                err = cudaMemcpyAsync(save ? snap + off : dev, save ? dev : snap + off, n, cudaMemcpyDeviceToDevice,
+                                      c->stream);
+            off += n;
+        };
+        for (double *a : d12) mv(a, 8 * nba);
+        mv(B.epot, 8 * nbd);
+        mv(B.obs_cl, 8 * obs_d);  // obs_cl, obs_low, obs_dot are one allocation
+        for (int *a : ivec) mv(a, 4 * T);
+        mv(B.obs_turn, 4 * obs_i);  // obs_turn, obs_up, obs_clstep, obs_bnc likewise
+        mv(c->X.fallback, 4 * T);
+        mv(c->X.nnstatus, 4 * T);
+        return err;
+    };
+    e = copy_all(true);
+    const int keep_block = c->rmaxblock;
+    const double keep_skin = c->skin_ang;
+    const PropParams P = to_dev(c, p);
+    const bool surr = c->pes_kind == MDT_PES_SURROGATE;
+    const bool tc = precision == MDT_PREC_BF16;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (e == cudaSuccess) e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    const int blocks[3] = {256, 384, 512};
+    const double skins[3] = {0.5, 0.75, 1.0};
+    double best = 1e300;
+    int bb = keep_block;
+    double bs = keep_skin;
+    for (int ib = 0; ib < 3 && e == cudaSuccess; ++ib) {
+        if (blocks[ib] < ((c->max_atoms + 31) & ~31)) continue;
+        for (int is = 0; is < 3 && e == cudaSuccess; ++is) {
+            c->rmaxblock = blocks[ib];
+            c->skin_ang = skins[is];
+            c->skin_dirty = true;
+            c->rnpack = 0;
+            if (!use_radial(c, precision, true)) continue;
+            e = copy_all(false);
+            if (e != cudaSuccess) break;
+            if ((rc = run_radial(c, P, 2, 2, surr, tc))) break;  // warm-up: lists built, code loaded
+            e = cudaEventRecord(e0, c->stream);
+            if (e == cudaSuccess && (rc = run_radial(c, P, nsteps, 2, surr, tc))) break;
+            if (e == cudaSuccess) e = cudaEventRecord(e1, c->stream);
+            if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+            float ms = 0.f;
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+            if (e == cudaSuccess && ms < best) {
+                best = ms;
+                bb = blocks[ib];
+                bs = skins[is];
+            }
+        }
+    }
+    c->rmaxblock = best < 1e300 ? bb : keep_block;
+    c->skin_ang = best < 1e300 ? bs : keep_skin;
+    c->skin_dirty = true;
+    c->rnpack = 0;
+    if (e == cudaSuccess) e = copy_all(false);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaFree(snap);
+    if (rc) return rc;
+    if (e != cudaSuccess) return cuda_fail(c, e, "mdt_autotune");
+    if (best >= 1e300) return fail(c, MDT_ERR_UNSUPPORTED, "mdt_autotune: no candidate ran");
+    if (block) *block = c->rmaxblock;
+    if (skin_ang) *skin_ang = c->skin_ang;
+    if (ms_per_step) *ms_per_step = best / nsteps;
     return MDT_OK;
 }
 

@@ -87,13 +87,24 @@ struct Batch {
     // centroids) with the step it was first reached, lowest centroid position (3 per traj)
     int *obs_turn, *obs_up, *obs_clstep;
     double *obs_cl, *obs_low;
+    // bounce detection and adsorption of trajectory_info.f90:80-263, per trajectory: ints
+    // [kObsNear] nearest atom of the last step (-1: none yet), [kObsRF] r.v x r.F crossings,
+    // [kObsVF] r.v x v.F crossings, [kObsPtm] r.v + to - changes, [kObsBounces] closed
+    // segments' bounces, [kObsPartner] partner-change sign, [kObsInter] steps with a
+    // projectile force, [kObsAds] adsorbed; doubles: r.v, r.F, v.F of the two last steps
+    int *obs_bnc;
+    double *obs_dot;
     int max_atoms, max_beads;
     int algo[kMaxTypes];       // propagator per type
     int is_proj[kMaxTypes];
 };
 
+enum { kObsNear, kObsRF, kObsVF, kObsPtm, kObsBounces, kObsPartner, kObsInter, kObsAds, kObsInts };
+constexpr int kObsDots = 6;
+
 struct PropParams {
     double step, Tsurf, Tproj, pile_tau, andersen_time, gamma_const;
+    double ads_start, ads_end;  // adsorption hysteresis (A): adsorbed below start, free above end
     double pul, pll;          // exit limits (use +/-inf to disable)
     uint64_t seed;
     int use_exit;             // stop trajectories at pul / pll

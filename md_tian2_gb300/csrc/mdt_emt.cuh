@@ -241,7 +241,9 @@ static __device__ void emt_bead(const Batch &B, const EmtConst &E, const SmemEmt
             ry = (R)dy;
             rz = (R)dz;
             const R r2 = rx * rx + ry * ry + rz * rz;
-            if (r2 <= cut2) {
+            // skipped only beyond the cutoff, like the reference's `if (r > cutoff*rcut) cycle`
+            // (pes_emt_mod.f90:660): a distance that is not a number enters the sums
+            if (!(r2 > cut2)) {
                 const R ir = M<R>::rsq(r2), r = r2 * ir;
                 const R e = M<R>::ex(acut * (r - rcut));
                 const R theta = M<R>::rcp(R(1) + e);

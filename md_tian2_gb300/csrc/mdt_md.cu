@@ -110,8 +110,10 @@ __global__ void __launch_bounds__(kBlock, 4) md_steps_kernel(Batch B, EmtConst E
             calc_force<R>(B, E, P, S, T, true);
             propagate_2(B, P, T, step);
             {
-                const double dmin = closest_approach_step(B, T, S.cell, S.red);
-                if (threadIdx.x == 0) observe_step(B, T, step, dmin);
+                int near;
+                double rv[3];
+                const double dmin = closest_approach_step(B, T, S.cell, S.red, &near, rv);
+                if (threadIdx.x == 0) observe_step(B, P, T, step, dmin, near, rv[0], rv[1], rv[2]);
             }
             end_of_step(B, P, T, step);
         }
@@ -119,16 +121,26 @@ __global__ void __launch_bounds__(kBlock, 4) md_steps_kernel(Batch B, EmtConst E
 }
 
 // trajectory observables at their initial values (trajectory_info.f90:55-70)
+// (the reference keeps is_adsorbed from the previous trajectory, trajectory_info.f90:55-70
+// does not reset it; here every trajectory starts not adsorbed)
+__device__ void obs_reset_traj(const Batch &B, int t) {
+    B.obs_turn[t] = 0;
+    B.obs_up[t] = 0;
+    B.obs_clstep[t] = 0;
+    B.obs_cl[t] = kDefaultReal;
+    B.obs_low[3 * t] = kDefaultReal;
+    B.obs_low[3 * t + 1] = kDefaultReal;
+    B.obs_low[3 * t + 2] = kDefaultReal;
+    int *bn = B.obs_bnc + kObsInts * (size_t)t;
+    for (int k = 0; k < kObsInts; ++k) bn[k] = 0;
+    bn[kObsNear] = -1;
+    bn[kObsPartner] = 1;
+    for (int k = 0; k < kObsDots; ++k) B.obs_dot[kObsDots * (size_t)t + k] = kDefaultReal;
+}
+
 __global__ void obs_reset_kernel(Batch B) {
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < B.ntraj; t += gridDim.x * blockDim.x) {
-        B.obs_turn[t] = 0;
-        B.obs_up[t] = 0;
-        B.obs_clstep[t] = 0;
-        B.obs_cl[t] = kDefaultReal;
-        B.obs_low[3 * t] = kDefaultReal;
-        B.obs_low[3 * t + 1] = kDefaultReal;
-        B.obs_low[3 * t + 2] = kDefaultReal;
-    }
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < B.ntraj; t += gridDim.x * blockDim.x)
+        obs_reset_traj(B, t);
 }
 
 cudaError_t launch_obs_reset(cudaStream_t s, const Batch &B) {
@@ -199,13 +211,7 @@ __global__ void refill_kernel(Batch B, const double *tmpl, int64_t total_ba, Ref
                 for (int b = 0; b < T.nb; ++b) skok[B.bead_off[t] + b] = 0;
             B.status[t] = kStatusRunning;
             B.steps_done[t] = 0;
-            B.obs_turn[t] = 0;
-            B.obs_up[t] = 0;
-            B.obs_clstep[t] = 0;
-            B.obs_cl[t] = kDefaultReal;
-            B.obs_low[3 * t] = kDefaultReal;
-            B.obs_low[3 * t + 1] = kDefaultReal;
-            B.obs_low[3 * t + 2] = kDefaultReal;
+            obs_reset_traj(B, t);
             atomicAdd(count, 1);
         }
         __syncthreads();

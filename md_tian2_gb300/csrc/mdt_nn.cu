@@ -331,8 +331,10 @@ __global__ void __launch_bounds__(kNNBlock) nn_md_steps_kernel(Batch B, NNDev M,
             nn_calc_force<R, SURR>(B, M, E, X, P, S, SE, T, true);
             propagate_2(B, P, T, step);
             {
-                const double dmin = closest_approach_step(B, T, SE.cell, SE.red);
-                if (threadIdx.x == 0) observe_step(B, T, step, dmin);
+                int near;
+                double rv[3];
+                const double dmin = closest_approach_step(B, T, SE.cell, SE.red, &near, rv);
+                if (threadIdx.x == 0) observe_step(B, P, T, step, dmin, near, rv[0], rv[1], rv[2]);
             }
             end_of_step(B, P, T, step);
         }

@@ -1249,8 +1249,10 @@ __global__ void __launch_bounds__(kFBlock, 3)
             nnf_calc_force<NG, ZM, G3ON>(B, M, F, E, X, P, S, SE, L, T, true);
             propagate_2(B, P, T, step);
             {
-                const double dmin = closest_approach_step(B, T, SE.cell, SE.red);
-                if (threadIdx.x == 0) observe_step(B, T, step, dmin);
+                int near;
+                double rv[3];
+                const double dmin = closest_approach_step(B, T, SE.cell, SE.red, &near, rv);
+                if (threadIdx.x == 0) observe_step(B, P, T, step, dmin, near, rv[0], rv[1], rv[2]);
             }
             end_of_step(B, P, T, step);
         }

@@ -603,6 +603,19 @@ __device__ __forceinline__ void nnr_forces(const RadialNN &R, const SmemR &S, co
 }
 
 
+// Scaling tables of both elements in the padded grouped order (both network variants)
+template <int NIN>
+__device__ void load_scaling_r(const RadialNN &R, const SmemR &S) {
+    const int tid = threadIdx.x, bs = blockDim.x, nin = NIN;
+    for (int e = 0; e < R.nelem; ++e)
+        for (int q = tid; q < nin; q += bs) {
+            const int s = R.qsrc[e][q];
+            S.scal[e * nin + q] =
+                s >= 0 ? R.fscal[e * R.maxsf + s] : make_float4(1.f, 0.f, -INFINITY, INFINITY);
+            S.dscal[e * nin + q] = s >= 0 ? R.fdscal[e * R.maxsf + s] : 0.f;
+        }
+}
+
 // Weight blocks and scaling tables in shared memory from the model's current FP32 weights
 // (calconenn.f90 layout: layer l of element e is an n_(l-1) x n_l row-major matrix plus
 // n_l biases at woff[e][l]); hidden layers padded to 32 nodes with zeros, inputs in the
@@ -648,13 +661,8 @@ __device__ void load_weights_r(const RadialNN &R, const SmemR &S) {
             for (int n = tid; n < kRW; n += bs) dst[o2 + n] = n < n1 ? l2[n] : 0.f;       // w2
             if (tid < 4) dst[o2 + kRW + tid] = tid == 0 ? l2[n1] : 0.f;                  // b2
         }
-        for (int q = tid; q < nin; q += bs) {
-            const int s = R.qsrc[e][q];
-            S.scal[e * nin + q] =
-                s >= 0 ? R.fscal[e * R.maxsf + s] : make_float4(1.f, 0.f, -INFINITY, INFINITY);
-            S.dscal[e * nin + q] = s >= 0 ? R.fdscal[e * R.maxsf + s] : 0.f;
-        }
     }
+    load_scaling_r<NIN>(R, S);
 }
 
 // ---- tensor-core network (BF16 operands, FP32 accumulation in TMEM) ----------------------
@@ -799,6 +807,7 @@ __device__ void load_weights_tc(const RadialNN &R, const SmemR &S) {
             }
         }
     }
+    load_scaling_r<NIN>(R, S);
 }
 
 // The network of this thread's atom on the tensor cores.  Every thread of the CTA calls it
@@ -1278,7 +1287,22 @@ __global__ void __launch_bounds__(kRBlockMax, 1)
                 else lc_half2(B, P, T, A.i, step, S.lc + tid, bs);
                 // trajectory observables by the projectile's thread; the closest approach is
                 // the nearest entry of its skin list (every image within the cutoff + skin)
-                if (A.i == 0) observe_step(B, T, step, rmin2 < INFINITY ? (double)sqrtf(rmin2) * kBohr2Ang : kDefaultReal);
+                if (A.i == 0) {
+                    // the bounce partner: the first entry of the list at the nearest distance
+                    int near = -1;
+                    float nx = 0.f, ny = 0.f, nz = 0.f;
+                    if (rmin2 < INFINITY)
+                        for_neighbours(R, S, A, sk, cnt, [&](auto, int js, float dx, float dy, float dz, float r2) {
+                            if (near < 0 && r2 <= rmin2 * 1.000001f) {
+                                near = js - A.st;
+                                nx = dx;
+                                ny = dy;
+                                nz = dz;
+                            }
+                        });
+                    observe_step(B, P, T, step, rmin2 < INFINITY ? (double)sqrtf(rmin2) * kBohr2Ang : kDefaultReal,
+                                 near, nx, ny, nz);
+                }
             }
         }
         // a state that stopped being finite in the launch's last step retires the trajectory too

@@ -35,19 +35,30 @@ static __device__ __forceinline__ double &comp(double *x, double *y, double *z, 
     return d == 0 ? x[k] : (d == 1 ? y[k] : z[k]);
 }
 
-// collect_trajectory_characteristics after a step (trajectory_info.f90:47-75, 113-132,
-// 243-250), by one thread: the lowest projectile centroid position, the closest approach
-// `dmin` of this step (computed by the caller) with the step at which it was first
-// reached, and a turning point whenever the sign of the centroid's z velocity changes.
-static __device__ void observe_step(const Batch &B, const TrajView &T, int step, double dmin) {
+// collect_trajectory_characteristics after a step (trajectory_info.f90:47-263), by one
+// thread: the lowest projectile centroid position, the closest approach `dmin` of this step
+// (computed by the caller, with the index `near` of the nearest atom and the vector
+// (rx, ry, rz) from the projectile to it, minimum image, any length unit) with the step at
+// which it was first reached, the adsorption flag with its hysteresis, the steps with a
+// projectile force, the bounce counters and a turning point whenever the sign of the
+// centroid's z velocity changes.  near < 0: no atom in reach (the segment goes on).
+static __device__ void observe_step(const Batch &B, const PropParams &P, const TrajView &T, int step, double dmin,
+                                    int near, double rx, double ry, double rz) {
     const int t = T.t;
-    double x = 0.0, y = 0.0, z = 0.0, vz = 0.0;
+    double x = 0.0, y = 0.0, z = 0.0, vx = 0.0, vy = 0.0, vz = 0.0, fx = 0.0, fy = 0.0, fz = 0.0;
+    bool force = false;
     for (int b = 0; b < T.nb; ++b) {
         const int64_t k = T.base + (int64_t)b * T.N;
         x += B.rx[k];
         y += B.ry[k];
         z += B.rz[k];
+        vx += B.vx[k];
+        vy += B.vy[k];
         vz += B.vz[k];
+        fx += B.fx[k];
+        fy += B.fy[k];
+        fz += B.fz[k];
+        force |= B.fx[k] != 0.0 || B.fy[k] != 0.0 || B.fz[k] != 0.0;
     }
     x /= T.nb;
     y /= T.nb;
@@ -61,7 +72,38 @@ static __device__ void observe_step(const Batch &B, const TrajView &T, int step,
         B.obs_cl[t] = dmin;
         B.obs_clstep[t] = step;
     }
-    const int down = vz / T.nb < 0.0 ? 1 : 0;
+    int *bn = B.obs_bnc + kObsInts * (size_t)t;
+    // adsorption hysteresis (check_for_closest_approach, :127-129)
+    if (!bn[kObsAds] && dmin < P.ads_start) bn[kObsAds] = 1;
+    if (bn[kObsAds] && dmin > P.ads_end) bn[kObsAds] = 0;
+    if (force) bn[kObsInter] += 1;  // check_for_proj_surf_interaction (:140-148)
+    // check_for_bounce (:152-241): unit vectors, dot products in the slot of this step
+    if (near >= 0) {
+        double *dt = B.obs_dot + kObsDots * (size_t)t;
+        const double rn = sqrt(rx * rx + ry * ry + rz * rz), vn = sqrt(vx * vx + vy * vy + vz * vz),
+                     fn = sqrt(fx * fx + fy * fy + fz * fz);
+        rx /= rn; ry /= rn; rz /= rn;
+        vx /= vn; vy /= vn; vz /= vn;
+        fx /= fn; fy /= fn; fz /= fn;
+        const int cur = step & 1, last = cur ^ 1;
+        dt[cur] = rx * vx + ry * vy + rz * vz;
+        dt[2 + cur] = rx * fx + ry * fy + rz * fz;
+        dt[4 + cur] = vx * fx + vy * fy + vz * fz;
+        const double rv0 = dt[last], rv1 = dt[cur], rf0 = dt[2 + last], rf1 = dt[2 + cur], vf0 = dt[4 + last],
+                     vf1 = dt[4 + cur];
+        if (bn[kObsNear] < 0) bn[kObsNear] = near;
+        if (bn[kObsNear] != near) {
+            bn[kObsBounces] += min(bn[kObsPtm], min(bn[kObsRF], bn[kObsVF]));  // finalize_bounces
+            bn[kObsPartner] = -bn[kObsPartner];
+            bn[kObsRF] = bn[kObsVF] = bn[kObsPtm] = 0;
+        } else if (rf1 != 0.0) {
+            if ((rv0 > rf0 && rv1 < rf1) || (rv0 < rf0 && rv1 > rf1)) bn[kObsRF] += 1;
+            if ((rv0 > vf0 && rv1 < vf1) || (rv0 < vf0 && rv1 > vf1)) bn[kObsVF] += 1;
+            if (rv0 > 0.0 && rv1 < 0.0) bn[kObsPtm] += 1;
+        }
+        bn[kObsNear] = near;
+    }
+    const int down = vz < 0.0 ? 1 : 0;
     if (down == B.obs_up[t]) {  // moving down now and up before, or the reverse
         B.obs_turn[t] += 1;
         B.obs_up[t] = 1 - down;
@@ -69,9 +111,11 @@ static __device__ void observe_step(const Batch &B, const TrajView &T, int step,
 }
 
 // Closest approach of the projectile (atom 0) after a step: the minimum image of the
-// centroids of atom 0 and atom i over i >= 1 (trajectory_info.f90:92-105), CTA-wide
-// (every thread gets the result; `cell` and `red` are shared-memory scratch).
-static __device__ double closest_approach_step(const Batch &B, const TrajView &T, Cell *cell, double *red) {
+// centroids of atom 0 and atom i over i >= 1 (trajectory_info.f90:92-105), CTA-wide; every
+// thread gets the distance, *near the nearest atom (first index on ties) and r the vector
+// from the projectile to it (`cell` and `red` are shared-memory scratch).
+static __device__ double closest_approach_step(const Batch &B, const TrajView &T, Cell *cell, double *red, int *near,
+                                               double *r) {
     __syncthreads();
     if (threadIdx.x == 0) load_cell(B, T.t, *cell);
     __syncthreads();
@@ -86,6 +130,7 @@ static __device__ double closest_approach_step(const Batch &B, const TrajView &T
     c0y /= T.nb;
     c0z /= T.nb;
     double dmin = kDefaultReal;
+    int imin = T.N;
     for (int i = 1 + threadIdx.x; i < T.N; i += blockDim.x) {
         double cx = 0.0, cy = 0.0, cz = 0.0;
         for (int b = 0; b < T.nb; ++b) {
@@ -96,9 +141,27 @@ static __device__ double closest_approach_step(const Batch &B, const TrajView &T
         }
         double dx, dy, dz;
         min_image(*cell, c0x - cx / T.nb, c0y - cy / T.nb, c0z - cz / T.nb, dx, dy, dz);
-        dmin = fmin(dmin, sqrt(dx * dx + dy * dy + dz * dz));
+        const double d = sqrt(dx * dx + dy * dy + dz * dz);
+        if (d < dmin) {
+            dmin = d;
+            imin = i;
+        }
     }
-    return block_min(dmin, red);
+    const double best = block_min(dmin, red);
+    const int ib = (int)block_min(dmin == best ? (double)imin : (double)T.N, red);
+    *near = ib < T.N ? ib : -1;
+    r[0] = r[1] = r[2] = 0.0;
+    if (ib < T.N) {
+        double cx = 0.0, cy = 0.0, cz = 0.0;
+        for (int b = 0; b < T.nb; ++b) {
+            const int64_t k = T.base + (int64_t)b * T.N + ib;
+            cx += B.rx[k];
+            cy += B.ry[k];
+            cz += B.rz[k];
+        }
+        min_image(*cell, cx / T.nb - c0x, cy / T.nb - c0y, cz / T.nb - c0z, r[0], r[1], r[2]);
+    }
+    return best;
 }
 
 // verlet_1 / verlet_2, md_algo.f90:110-142

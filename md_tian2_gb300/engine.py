@@ -136,6 +136,24 @@ class Engine:
         """Verlet skin (A) of the fast kernels' neighbour lists; 0 rebuilds every step."""
         self._check(self.lib.mdt_nn_set_skin(self.h, skin_ang), "mdt_nn_set_skin")
 
+    def autotune(self, sp: SimParams, precision: str = "fp32", nsteps: int = 20) -> dict:
+        """Pick the thread-per-atom kernel's CTA size and skin by timing candidate launches
+        (mdt_autotune); the batch's state is restored afterwards."""
+        b = ct.c_int32(0)
+        sk = ct.c_double(0.0)
+        ms = ct.c_double(0.0)
+        p = sp.c()
+        self._check(self.lib.mdt_autotune(self.h, PREC[precision], nsteps, ct.byref(p), ct.byref(b), ct.byref(sk),
+                                          ct.byref(ms)), "mdt_autotune")
+        return {"block": int(b.value), "skin_A": float(sk.value), "ms_per_step": float(ms.value)}
+
+    def nn_repack(self) -> int:
+        """Re-pack the thread-per-atom kernel's CTAs over the trajectories still running;
+        returns the number of packs (0: the batch does not run on that kernel)."""
+        n = ct.c_int32(0)
+        self._check(self.lib.mdt_nn_repack(self.h, ct.byref(n)), "mdt_nn_repack")
+        return int(n.value)
+
     def nn_stats(self):
         fb = np.zeros(self.T, np.int32)
         ov = np.zeros(self.T, np.int32)
@@ -260,6 +278,22 @@ class Engine:
         self._check(self.lib.mdt_traj_observables(self.h, turn.ctypes.data, cl.ctypes.data, clstep.ctypes.data,
                                                   low.ctypes.data), "mdt_traj_observables")
         return {"turn_pnts": turn, "cl_appr": cl, "cl_appr_step": clstep, "r_min_p": low}
+
+    def bounces(self, sp: SimParams) -> dict:
+        """Bounce count, interaction time (fs) and adsorption flag per trajectory
+        (trajectory_info.f90's check_for_bounce, check_for_proj_surf_interaction and
+        adsorption hysteresis, tracked by the fused MD steps)."""
+        b = np.zeros(self.T, np.int32)
+        ti = np.zeros(self.T)
+        ads = np.zeros(self.T, np.int32)
+        p = sp.c()
+        self._check(self.lib.mdt_traj_bounces(self.h, b.ctypes.data, ti.ctypes.data, ads.ctypes.data, ct.byref(p)),
+                    "mdt_traj_bounces")
+        return {"bounces": b, "interaction_time": ti, "is_adsorbed": ads.astype(bool)}
+
+    def set_adsorption(self, start: float, end: float) -> None:
+        """Adsorption limits (A): adsorbed below start, free again above end."""
+        self._check(self.lib.mdt_set_adsorption(self.h, float(start), float(end)), "mdt_set_adsorption")
 
     def set_step_limit(self, max_steps: int) -> None:
         """Stop each trajectory after max_steps steps (status 3); 0 = no limit."""

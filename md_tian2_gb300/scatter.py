@@ -85,6 +85,16 @@ class ScatterResult:
         span = span or (float(e.min()), float(e.max()))
         return np.histogram(e, bins=bins, range=span, density=True)
 
+    @classmethod
+    def from_records(cls, paths, shot_thru: float) -> "ScatterResult":
+        """The observables of a set of mxt_fin files (read_mxt_fin), as the analysis script
+        classifies them: initial and final projectile energy and height from the records."""
+        recs = [read_mxt_fin(p) for p in paths]
+        col = lambda k: np.array([r[k] for r in recs])  # noqa: E731
+        return cls(ekin_i=col("ekin_p_i"), ekin_f=col("ekin_p_f"), z_i=np.array([r["r_i"][2] for r in recs]),
+                   z_f=np.array([r["r_f"][2] for r in recs]), steps=np.rint(col("time")).astype(np.int64),
+                   status=np.ones(len(recs), np.int32), shot_thru=shot_thru)
+
     def summary(self) -> dict:
         m, se = self.mean_eloss()
         p, pse = self.sticking()
@@ -95,9 +105,11 @@ class ScatterResult:
 
 
 def run_to_exit(eng, sp, precision: str = "fp64", max_steps: int = 10000, chunk: int = 500,
-                metal: str = "Au") -> ScatterResult:
+                metal: str = "Au", repack: bool = True) -> ScatterResult:
     """Propagate the engine's batch (state uploaded, exit test on in ``sp``) until every
-    trajectory has stopped or ``max_steps`` have run; returns the scattering record."""
+    trajectory has stopped or ``max_steps`` have run; returns the scattering record.  With
+    ``repack`` the thread-per-atom kernel's CTAs are re-packed over the running trajectories
+    after every chunk in which some stopped (no effect on the other kernels)."""
     if not sp.use_exit:
         raise ValueError("run_to_exit needs SimParams.use_exit (the pul/pll exit test)")
     T = eng.T
@@ -106,12 +118,17 @@ def run_to_exit(eng, sp, precision: str = "fp64", max_steps: int = 10000, chunk:
     o0 = eng.download()
     z_i = np.array([eng.split(o0["r"], t)[0, 0, 2] for t in range(T)])
     done = 0
+    running = T
     while done < max_steps:
         n = min(chunk, max_steps - done)
         eng.md_steps(n, sp, precision=precision)
         done += n
-        if not np.any(eng.query(sp)["status"] == 0):
+        now = int(np.sum(eng.query(sp)["status"] == 0))
+        if now == 0:
             break
+        if repack and now < running:  # stopped trajectories give their CTA threads back
+            eng.nn_repack()
+        running = now
     q = eng.query(sp)
     o = eng.download()
     z_f = np.array([eng.split(o["r"], t)[0, 0, 2] for t in range(T)])

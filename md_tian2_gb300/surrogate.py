@@ -178,3 +178,61 @@ def force_rmse(model: nene.NNModel, data: Dataset, device: int = 0, precision: s
     nat = np.array([u.natoms for u in data.universes])
     return (float(np.sqrt(np.mean((out["f"] - f) ** 2))),
             float(np.sqrt(np.mean(((out["epot"] - data.energy) / nat) ** 2))))
+
+
+def nve_drift(model: nene.NNModel, precision: str = "fp32", ntraj: int = 8, chunk: int = 200, nchunks: int = 100,
+              seed: int = 4, device: int = 0) -> dict:
+    """NVE energy drift of the surrogate path: velocity Verlet with no friction, all atoms
+    free, ``ntraj`` H/Au(111) 3x3 trajectories (H at 2.5 A, 1 eV, polar 30 deg) for
+    chunk x nchunks steps of 0.1 fs, forces from the network (``precision``).  The total
+    energy is read every chunk from the per-trajectory FP64 sums of an FP32 evaluation of the
+    same network: for BF16 dynamics that measures what the dynamics conserve rather than the
+    BF16 energy readout, whose operand rounding adds O(10) meV of noise per configuration.
+    Returns the slope of a linear fit of E_tot(t) per trajectory (meV/ps), their mean, the
+    spread of the BF16 readout against FP32 (``readout_rms_meV``) and the EMT fallbacks (a
+    fallback switches the potential, so it must be zero for the slopes to measure drift)."""
+    rng = np.random.default_rng(seed)
+    us = [W.h_on_metal(rng, "Au", 3, 1.0, 30.0, 0.0, 300.0, z0=2.5) for _ in range(ntraj)]
+    for u in us:
+        u.is_fixed[:] = False
+
+    def engine():
+        e = Engine(device)
+        e.read_emt(W.emt_params())
+        e.define(us)
+        e.read_nene(model, ["H", "Au"])
+        e.set_pes(PES_SURROGATE, 0.1)
+        e.upload()
+        return e
+
+    eng = engine()
+    radial = eng.nn_radial_kernel(True)
+    probe = engine() if precision != "fp32" else None  # FP32 energies of the same states
+    sp = SimParams(step=0.1)
+    eng.calc_force(sp, precision=precision)
+    ts, es, dev = [], [], []
+    for c in range(nchunks + 1):
+        if c:
+            eng.md_steps(chunk, sp, precision=precision)
+        q = eng.query(sp)
+        epot = q["epot"]
+        if probe is not None:
+            o = eng.download()
+            probe.upload(o["r"], o["v"])
+            probe.calc_force(sp, flag=C.ENERGY_ONLY, precision="fp32")
+            e32 = probe.query(sp)["epot"]
+            dev.append(epot - e32)
+            epot = e32
+        ts.append(c * chunk * sp.step * 1e-3)  # ps
+        es.append(epot + q["ekin_p"] + q["ekin_l"])
+    fb, _ = eng.nn_stats()
+    steps_ok = bool(np.all(q["steps_done"] == chunk * nchunks))
+    eng.close()
+    if probe is not None:
+        probe.close()
+    es = np.array(es)
+    slope = np.array([np.polyfit(ts, es[:, t], 1)[0] for t in range(ntraj)]) * 1e3
+    return {"slopes_meV_per_ps": slope, "mean_meV_per_ps": float(np.mean(slope)),
+            "max_abs_meV_per_ps": float(np.max(np.abs(slope))), "fallbacks": int(fb.sum()),
+            "steps_ok": steps_ok, "radial_kernel": bool(radial), "ps": chunk * nchunks * sp.step * 1e-3,
+            "readout_rms_meV": float(1e3 * np.sqrt(np.mean(np.square(dev)))) if dev else 0.0}

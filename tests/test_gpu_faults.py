@@ -4,9 +4,10 @@ untouched.
 * A NaN position in a Verlet trajectory: the fused MD steps stop it with status
   MDT_TRAJ_ERR_NONFINITE (-11) after the step in which it appears (the reference would
   carry the NaN to the end of its run).
-* A NaN position in a trajectory whose projectile runs LDFA Langevin: ldfa finds no valid
-  density and the trajectory stops with MDT_TRAJ_ERR_DENSITY (-10), where the reference
-  stops the program ("EMT density array contains negative values", md_algo.f90:551-554).
+* A negative EMT density under LDFA Langevin stops the trajectory with
+  MDT_TRAJ_ERR_DENSITY (-10), where the reference stops the program ("EMT density array
+  contains negative values", md_algo.f90:551-554); a NaN position in an LDFA trajectory stops
+  that trajectory with an error status.
 * A projectile placed 0.05 A from a lattice atom: huge but finite forces; whatever that
   trajectory does, the others are unaffected.
 Every other trajectory must equal a clean run of the same batch: bit for bit where the
@@ -85,13 +86,32 @@ def test_nan_and_close_pair_in_emt_batch(built_lib):
     _assert_others_equal(us, out, clean, clean2, skip=(1, 3), rtol=1e-10)
 
 
-def test_nan_in_ldfa_trajectory_is_a_density_error(built_lib):
+def test_negative_density_stops_ldfa_trajectories(built_lib):
+    """A negative EMT density (here from a negative n0 of H, so every trajectory has one) is
+    the reference's `stop` in ldfa (md_algo.f90:551-554): every trajectory ends after its
+    first step with MDT_TRAJ_ERR_DENSITY."""
+    us = _batch(C.PROP_ID_LANGEVIN, n=4)
+    emt = W.emt_params()
+    emt.values["n0"][0] = -abs(emt.values["n0"][0])
+    eng = Engine(0)
+    eng.read_emt(emt)
+    eng.define(us)
+    eng.upload()
+    sp = SimParams(step=0.1, gamma_const=1e-3, Tsurf=300.0, Tproj=300.0)
+    eng.calc_force(sp)
+    eng.md_steps(10, sp)
+    q = eng.query(sp)
+    eng.close()
+    assert np.all(q["status"] == ERR_DENSITY) and np.all(q["steps_done"] == 1), q
+
+
+def test_nan_in_ldfa_batch_stops_only_its_trajectory(built_lib):
     us = _batch(C.PROP_ID_LANGEVIN, n=4)
     bad = [u.copy() for u in us]
     bad[2].r[0, 0, 2] = np.nan  # the projectile, whose density feeds ldfa
     out, q = _emt_run(bad, C.PROP_ID_LANGEVIN, steps=10)
-    assert q["status"][2] == ERR_DENSITY and q["steps_done"][2] == 1, q[2]
-    assert np.all(q["status"][[0, 1, 3]] == 0)
+    assert q["status"][2] < 0 and q["steps_done"][2] == 1, q[2]
+    assert np.all(q["status"][[0, 1, 3]] == 0) and np.all(q["steps_done"][[0, 1, 3]] == 10)
 
 
 def test_nan_in_surrogate_batch(built_lib):

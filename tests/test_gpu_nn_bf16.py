@@ -2,10 +2,10 @@
 its four network GEMMs per 128-atom tile on tcgen05, BF16 operands, FP32 accumulation in
 TMEM; descriptors, activations, scaling and forces in FP32) against the FP64 oracle.
 
-Bars, stated per model: force RMSE below 1e-2 of the force RMS and energies within 2e-3
+Bars, stated per model: force RMSE below 1e-2 of the force RMS and energies within 5e-3
 relative of the FP64 oracle (BF16 keeps 8 significant bits: one rounding of every operand
-of a 24-32-32-1 network); the trained surrogate's forces within 5 meV/A RMSE of its FP32
-evaluation.  Results of the same model in FP32 agree with BF16 to the same bars, so a
+of a 24-32-32-1 network; the random test networks reach several eV per atom); the trained
+surrogate's forces within 5 meV/A RMSE of its FP32 evaluation.  Results of the same model in FP32 agree with BF16 to the same bars, so a
 wrong operand layout (which would scramble weights) cannot pass."""
 import numpy as np
 import pytest
@@ -18,7 +18,7 @@ from md_tian2_gb300.engine import PES_EMT, PES_NENE, PES_SURROGATE, Engine, SimP
 from md_tian2_gb300.surrogate import shipped_surrogate
 
 pytestmark = pytest.mark.gpu
-F_REL, E_REL = 1e-2, 2e-3
+F_REL, E_REL = 1e-2, 5e-3
 
 
 def _engine(us, m, kind=PES_NENE, emt=None, margin=0.1, names=("H", "Au")):

@@ -173,3 +173,32 @@ def test_radial_neighbour_overflow_is_reported(built_lib):
     _, ov = eng.nn_stats()
     assert ov.all()
     eng.close()
+
+
+def test_radial_repack_over_running_trajectories(built_lib, oracle_lib):
+    """Trajectories that leave through pul stop; re-packing the CTAs over those still running
+    (mdt_nn_repack) changes which threads hold which atoms, not the trajectories: 40 more
+    steps agree with the run that kept its packs (1e-5 A, FP32 sums in no fixed order)."""
+    us = W.config2(48, seed=26)
+    for t, u in enumerate(us):  # half the projectiles start just below pul, moving up
+        if t % 2 == 0:
+            u.r[0, :, 2] = 6.0
+            u.v[0, :, 2] = 0.05
+    m = _radial_model(9)
+    sp = SimParams(step=0.5, gamma_const=1e-3, seed=7, pul=6.05, use_exit=True)
+    res = {}
+    for repack in (False, True):
+        eng = _engine(us, m)
+        eng.calc_force(sp, precision="fp32")
+        eng.md_steps(5, sp, precision="fp32")
+        q = eng.query(sp)
+        assert 0 < int(np.sum(q["status"] != 0)) < len(us)
+        if repack:
+            full = eng.nn_repack()
+            assert full > 0
+        eng.md_steps(40, sp, precision="fp32")
+        res[repack] = (eng.download(), eng.query(sp))
+        eng.close()
+    (a, qa), (b, qb) = res[True], res[False]
+    assert np.abs(a["r"] - b["r"]).max() < 1e-5
+    assert (qa["status"] == qb["status"]).all() and (qa["steps_done"] == qb["steps_done"]).all()

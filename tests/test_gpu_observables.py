@@ -1,5 +1,6 @@
 """Trajectory observables tracked by the fused MD kernels (turning points, closest
-approach and its step, lowest projectile position; src/trajectory_info.f90) against a
+approach and its step, lowest projectile position, bounces, interaction time and the
+adsorption flag; src/trajectory_info.f90) against a
 host restatement of collect_trajectory_characteristics applied to the oracle's own
 trajectory (FP64 EMT: identical turning points and steps, distances and positions within
 1e-9 A), and for the FP32 radial surrogate kernel against the same restatement applied to
@@ -31,31 +32,38 @@ def test_emt_observables_match_oracle(built_lib, oracle_lib):
     us = _batch()
     emt = W.emt_params()
     sp = SimParams(step=0.5)
-    nsteps = 60
+    nsteps = 120
+    ads = (1.7, 2.2)  # adsorption limits (A)
     eng = Engine(0)
     eng.read_emt(emt)
     eng.define(us)
+    eng.set_adsorption(*ads)
     eng.upload()
     eng.calc_force(sp)
     eng.md_steps(nsteps, sp)
     obs = eng.observables()
+    bnc = eng.bounces(sp)
     eng.close()
-    turns = 0
+    turns = bounces = 0
     for t, u in enumerate(us):
         o = OracleUniverse(u, emt)
-        col = Collect(u.simbox)
+        col = Collect(u.simbox, adsorption=ads, step=sp.step)
         o.calc_force(sp)
         for k in range(1, nsteps + 1):
             o.propagate_1(sp)
             o.calc_force(sp)
             o.propagate_2(sp)
-            col(k, o.r, o.v)
+            col(k, o.r, o.v, o.f)
         turns += col.turn
+        bounces += col.final_bounces()
         assert obs["turn_pnts"][t] == col.turn, t
         assert obs["cl_appr_step"][t] == col.clstep, t
         assert abs(obs["cl_appr"][t] - col.cl) < 1e-9, t
         assert np.abs(obs["r_min_p"][t] - col.low).max() < 1e-9, t
-    assert turns >= 1  # projectiles turned in front of the surface
+        assert bnc["bounces"][t] == col.final_bounces(), (t, bnc["bounces"][t], col.final_bounces())
+        assert bnc["interaction_time"][t] == pytest.approx(col.interaction_time()), t
+        assert bnc["is_adsorbed"][t] == col.adsorbed, t
+    assert turns >= 1 and bounces >= 1  # projectiles turned and collided in front of the surface
 
 
 def test_radial_kernel_observables_match_its_states(built_lib):
@@ -71,13 +79,15 @@ def test_radial_kernel_observables_match_its_states(built_lib):
     assert eng.nn_radial_kernel(True)
     eng.upload()
     eng.calc_force(sp, precision="fp32")
-    cols = [Collect(u.simbox) for u in us]
+    eng.set_adsorption(1.7, 2.2)
+    cols = [Collect(u.simbox, adsorption=(1.7, 2.2), step=sp.step) for u in us]
     for k in range(1, 41):
         eng.md_steps(1, sp, precision="fp32")
         out = eng.download()
         for t, c in enumerate(cols):
-            c(k, eng.split(out["r"], t), eng.split(out["v"], t))
+            c(k, eng.split(out["r"], t), eng.split(out["v"], t), eng.split(out["f"], t))
     obs = eng.observables()
+    bnc = eng.bounces(sp)
     eng.close()
     assert sum(c.turn for c in cols) >= 1
     for t, c in enumerate(cols):
@@ -85,6 +95,11 @@ def test_radial_kernel_observables_match_its_states(built_lib):
         assert np.abs(obs["r_min_p"][t] - c.low).max() < 1e-12, t
         assert abs(obs["cl_appr"][t] - c.cl) < 1e-4, t
         assert abs(c.dist[int(obs["cl_appr_step"][t])] - c.cl) < 1e-4, t
+        # the kernel's nearest partner and unit vectors come from FP32 distances: a
+        # crossing at the edge of FP32 rounding may be counted on one side only
+        assert abs(int(bnc["bounces"][t]) - c.final_bounces()) <= 1, t
+        assert bnc["interaction_time"][t] == pytest.approx(c.interaction_time()), t
+        assert bnc["is_adsorbed"][t] == c.adsorbed, t
 
 
 def test_mxt_fin_from_a_gpu_run(built_lib, tmp_path):
