@@ -72,6 +72,9 @@ def parse():
     ap.add_argument("--hdnnp-traj", type=int, default=2048, help="trajectories of the HDNNP arm (0: skip)")
     ap.add_argument("--arm-steps", type=int, default=20, help="timed MD steps of the RPMD and HDNNP arms")
     ap.add_argument("--no-nve", action="store_true", help="skip the surrogate's NVE drift runs")
+    ap.add_argument("--profile-arm", choices=["fp32", "bf16", "emt"], default=None,
+                    help="run only this arm's warm-up and timed MD steps (no report): the workload of the "
+                         "ncu captures under profiles/")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     return ap.parse_args()
 
@@ -357,7 +360,7 @@ def timed_steps(eng, sp, precision, steps, stream, torch, dist=None, clock_index
     return ev0.elapsed_time(ev1), (clk.summary() if clk else None)
 
 
-def scattering_comparison(args, model, device):
+def scattering_comparison(args, model, device, prec_surr="fp32"):
     """Config-2 trajectories from identical initial states run to their exit (pul) or the
     step limit with the surrogate (FP32 kernels, EMT fallback) and with plain FP64 EMT:
     the analysis script's observables, their two-sample comparison and the wall time of
@@ -370,7 +373,7 @@ def scattering_comparison(args, model, device):
     us = W.config2(args.scatter_traj, seed=7)
     sp = SimParams(step=0.1, gamma_const=1e-3, Tsurf=300.0, Tproj=300.0, seed=2024, pul=6.05, use_exit=True)
     res, wall, fb = {}, {}, 0
-    for kind, prec in ((PES_SURROGATE, "fp32"), (PES_EMT, "fp64")):
+    for kind, prec in ((PES_SURROGATE, prec_surr), (PES_EMT, "fp64")):
         eng = Engine(device)
         eng.read_emt(W.emt_params())
         eng.define(us)
@@ -388,6 +391,7 @@ def scattering_comparison(args, model, device):
         eng.close()
     s, e = res[PES_SURROGATE], res[PES_EMT]
     return {"trajectories": args.scatter_traj, "max_steps": args.scatter_steps,
+            "surrogate_precision": prec_surr,
             "surrogate": s.summary(), "emt_fp64": e.summary(), "compare": compare(s, e),
             "wall_s": {"surrogate": wall[PES_SURROGATE], "emt_fp64": wall[PES_EMT]},
             "time_to_solution_speedup": wall[PES_EMT] / wall[PES_SURROGATE],
@@ -589,41 +593,70 @@ def run_ours(args):
     def atom_steps_now():
         return int(np.sum(natoms * eng.query(sp)["steps_done"]))
 
-    # ---- accuracy against FP64 EMT on held-out configurations ------------------------------
+    # ---- accuracy of every network arithmetic: held-out force RMSE against FP64 EMT and NVE drift
+    PRECS = ("fp32", "bf16", "bf16x3")  # network on CUDA cores, tensor cores with BF16 / split BF16 operands
     acc = None
     if rank == 0 and args.rmse_traj > 0:
+        from md_tian2_gb300.surrogate import nve_drift
         held = generate_dataset(args.rmse_traj, 8, 50, seed=4242 + rank, device=local)
-        f32, e32 = force_rmse(model, held, device=local, precision="fp32", max_neighbors=80)
-        acc = {"force_rmse_meV_per_A": 1e3 * f32, "energy_rmse_meV_per_atom": 1e3 * e32,
-               "configs": len(held.universes),
+        acc = {"configs": len(held.universes),
                "sample": f"{args.rmse_traj} config-2 trajectories (seed {4242 + rank}) propagated with FP64 EMT, "
                          "sampled every 50 steps x 8; network forces (no fallback) vs FP64 EMT forces"}
-        try:
-            fb16, eb16 = force_rmse(model, held, device=local, precision="bf16", max_neighbors=80)
-            acc["bf16"] = {"force_rmse_meV_per_A": 1e3 * fb16, "energy_rmse_meV_per_atom": 1e3 * eb16}
-        except EngineError:  # the model does not run on the thread-per-atom kernel
-            acc["bf16"] = None
+        for prec in PRECS:
+            try:
+                f_, e_ = force_rmse(model, held, device=local, precision=prec, max_neighbors=80)
+            except EngineError:  # tensor-core arithmetic: the model does not run on the thread-per-atom kernel
+                acc[prec] = None
+                continue
+            acc[prec] = {"force_rmse_meV_per_A": 1e3 * f_, "energy_rmse_meV_per_atom": 1e3 * e_}
+            if not args.no_nve:
+                d = nve_drift(model, prec, device=local)
+                acc[prec]["nve_drift_meV_per_ps"] = {"mean": d["mean_meV_per_ps"], "max_abs": d["max_abs_meV_per_ps"],
+                                                     "fallbacks": d["fallbacks"]}
+                if prec != "fp32":
+                    acc[prec]["nve_drift_meV_per_ps"]["energy_readout_rms_meV"] = d["readout_rms_meV"]
+        acc["force_rmse_meV_per_A"] = acc["fp32"]["force_rmse_meV_per_A"]
+        acc["energy_rmse_meV_per_atom"] = acc["fp32"]["energy_rmse_meV_per_atom"]
+        if not args.no_nve:
+            acc["nve_setup"] = ("8 H/Au(111) 3x3 trajectories, all atoms free, velocity Verlet, dt 0.1 fs, 2 ps; slope "
+                                "of a linear fit of the total energy (FP64 per-trajectory sums of an FP32 evaluation "
+                                "of the network on the run's states)")
 
-    # ---- surrogate (headline) -------------------------------------------------------
+    if args.profile_arm:
+        prec = "fp64" if args.profile_arm == "emt" else args.profile_arm
+        eng.set_pes(PES_EMT if args.profile_arm == "emt" else PES_SURROGATE, args.margin)
+        eng.nn_set_skin(args.skin)
+        eng.upload()
+        eng.calc_force(sp, precision=prec)
+        for _ in range(args.warmup):
+            eng.md_steps(1, sp, precision=prec)
+        eng.md_steps(args.steps, sp, precision=prec)
+        eng.synchronize()
+        eng.close()
+        print(json.dumps({"profile_arm": args.profile_arm, "ntraj": args.ntraj, "steps": args.steps}), flush=True)
+        return
+
+    # ---- surrogate (headline): the same trajectories in every network arithmetic ----------------
     eng.set_pes(PES_SURROGATE, args.margin)
     eng.nn_set_skin(args.skin)
     fast = eng.nn_fast_path(True)
     radial = eng.nn_radial_kernel(True)
     kname = ("nnr_kernel (thread per atom, fused MD step, surrogate)" if radial
              else "nnf_kernel (warp per atom, fused MD step, surrogate)")
-    eng.upload()
-    eng.calc_force(sp, precision="fp32")
-    for _ in range(args.warmup):
-        eng.md_steps(1, sp, precision="fp32")
-    torch.cuda.synchronize()
-    s0 = atom_steps_now()
-    launches0 = eng.launch_count()
-    fb0 = int(eng.nn_stats()[0].sum())
     per_launch = steps_per_launch(args.steps, args.steps_per_launch)
-    ms, clocks = timed_steps(eng, sp, "fp32", args.steps, stream, torch, dist, local, per_launch)
-    launches = eng.launch_count() - launches0
-    done = atom_steps_now() - s0
-    fb_count = int(eng.nn_stats()[0].sum()) - fb0
+    arms = {}
+    for prec in PRECS if radial else ("fp32",):
+        eng.upload()
+        eng.calc_force(sp, precision=prec)
+        for _ in range(args.warmup):
+            eng.md_steps(1, sp, precision=prec)
+        torch.cuda.synchronize()
+        s0 = atom_steps_now()
+        launches0 = eng.launch_count()
+        fb0 = int(eng.nn_stats()[0].sum())
+        ms_, clocks_ = timed_steps(eng, sp, prec, args.steps, stream, torch, dist, local, per_launch)
+        arms[prec] = {"ms": ms_, "clocks": clocks_, "done": atom_steps_now() - s0,
+                      "launches": eng.launch_count() - launches0, "fallbacks": int(eng.nn_stats()[0].sum()) - fb0}
     bead_evals = int(np.sum([u.nbeads for u in universes])) * args.steps
     # neighbour entries of the step (the warp-per-atom kernel writes the per-atom lists)
     eng.nn_radial_kernel(False)
@@ -633,23 +666,20 @@ def run_ours(args):
     entries = int(np.sum(counts))
     surr_flop = FLOP_SURR_ENTRY * entries + FLOP_SURR_ATOM * int(np.sum(natoms))
 
-    # ---- the same surrogate with the network GEMMs on the tensor cores (BF16 operands) ----
-    bf16 = None
-    if radial:
-        eng.upload()
-        eng.calc_force(sp, precision="bf16")
-        for _ in range(args.warmup):
-            eng.md_steps(1, sp, precision="bf16")
-        torch.cuda.synchronize()
-        s0b = atom_steps_now()
-        ms_bf, clocks_bf = timed_steps(eng, sp, "bf16", args.steps, stream, torch, dist, local, per_launch)
-        done_bf = atom_steps_now() - s0b
-        bf16 = {"ms": ms_bf, "done": done_bf, "clocks": clocks_bf}
-    # the headline is the faster arithmetic that meets the metric's 20 meV/A accuracy bar
-    head = "fp32"
-    bf_rmse = ((acc or {}).get("bf16") or {}).get("force_rmse_meV_per_A")
-    if bf16 is not None and bf16["done"] / bf16["ms"] > done / ms and bf_rmse is not None and bf_rmse <= 20.0:
-        head = "bf16"
+    # the headline is the fastest arithmetic that meets the metric's 20 meV/A force bar and the
+    # 1 meV/ps NVE drift target (where measured)
+    def meets(prec):
+        a = (acc or {}).get(prec)
+        if acc is None:
+            return prec == "fp32"
+        if not a or a["force_rmse_meV_per_A"] > 20.0:
+            return False
+        drift = a.get("nve_drift_meV_per_ps")
+        return drift is None or abs(drift["mean"]) <= 1.0
+    ok = [q for q in arms if meets(q)] or ["fp32"]
+    head = max(ok, key=lambda q: arms[q]["done"] / arms[q]["ms"])
+    ms, clocks, done = arms[head]["ms"], arms[head]["clocks"], arms[head]["done"]
+    launches, fb_count = arms[head]["launches"], arms[head]["fallbacks"]
 
     # end-to-end through the C ABI with pinned host buffers (surrogate)
     nslots = eng.nslots
@@ -690,25 +720,10 @@ def run_ours(args):
     emt_flop = FLOP_SAME_PAIR * same + FLOP_MIXED_PAIR * mixed + FLOP_ATOM * nat
     eng.close()
 
-    # ---- NVE energy drift of the surrogate path ----------------------------------------------
-    if rank == 0 and acc is not None:
-        if not args.no_nve:
-            from md_tian2_gb300.surrogate import nve_drift
-            acc["nve_drift"] = {}
-            for prec in ("fp32", "bf16") if bf16 is not None else ("fp32",):
-                d = nve_drift(model, prec, device=local)
-                acc["nve_drift"][prec] = {"mean_meV_per_ps": d["mean_meV_per_ps"],
-                                          "max_abs_meV_per_ps": d["max_abs_meV_per_ps"],
-                                          "fallbacks": d["fallbacks"]}
-                if prec == "bf16":
-                    acc["nve_drift"][prec]["bf16_energy_readout_rms_meV"] = d["readout_rms_meV"]
-            acc["nve_drift"]["setup"] = ("8 H/Au(111) 3x3 trajectories, all atoms free, velocity Verlet, dt 0.1 fs, "
-                                         "2 ps; slope of a linear fit of the total energy (FP64 per-trajectory sums "
-                                         "of an FP32 evaluation of the network on the run's states)")
     # ---- scattering observables: whole trajectories to exit, surrogate vs FP64 EMT ----------
     obs = None
     if rank == 0 and args.scatter_traj > 0:
-        obs = scattering_comparison(args, model, local)
+        obs = scattering_comparison(args, model, local, head)
 
     peak = ct.c_double()
     lib.mdt_peak_fma(1, 20000, ct.byref(peak))
@@ -736,27 +751,22 @@ def run_ours(args):
         value = done_all / elapsed
         emt_value = done_emt_all / elapsed_emt
         achieved = surr_flop / (elapsed / args.steps)
-        other = None  # the arithmetic that is not the headline
-        if bf16 is not None:
-            bf_elapsed = bf16["ms"] * 1e-3
-            arms = {"fp32": (done_all, elapsed, clocks), "bf16": (bf16["done"], bf_elapsed, bf16["clocks"])}
-            o = "bf16" if head == "fp32" else "fp32"
-            od, oe, oc = arms[o]
-            other = {"dtype": o, "value": od / oe, "unit": UNIT, "ms_per_step": 1e3 * oe / args.steps,
-                     "speedup_vs_fp64_emt": (od / oe) / emt_value, "clocks": oc,
-                     "force_rmse_meV_per_A": (acc or {}).get("force_rmse_meV_per_A") if o == "fp32" else bf_rmse,
-                     "roofline": {"bound": "fp32", "achieved": surr_flop / (oe / args.steps) / 1e12,
-                                  "peak": peak.value / 1e12, "unit": "TFLOP/s",
-                                  "frac": surr_flop / (oe / args.steps) / peak.value}}
-            value, elapsed, clocks = arms[head][0] / arms[head][1], arms[head][1], arms[head][2]
-            achieved = surr_flop / (elapsed / args.steps)
+        network_arms = {}
+        for q, a in arms.items():
+            el_q = a["ms"] * 1e-3
+            network_arms[q] = {"value": a["done"] / el_q, "unit": UNIT, "ms_per_step": 1e3 * el_q / args.steps,
+                               "speedup_vs_fp64_emt": (a["done"] / el_q) / emt_value, "clocks": a["clocks"],
+                               "accuracy": (acc or {}).get(q), "meets_accuracy_gates": meets(q),
+                               "roofline": {"bound": "fp32", "achieved": surr_flop / (el_q / args.steps) / 1e12,
+                                            "peak": peak.value / 1e12, "unit": "TFLOP/s",
+                                            "frac": surr_flop / (el_q / args.steps) / peak.value}}
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "bf16" if head == "bf16" else "f32",
+            "scaling": "weak", "vs_baseline": None, "dtype": {"fp32": "f32", "bf16": "bf16", "bf16x3": "bf16x3"}[head],
             "data": "synthetic (seeded H/Au(111) slabs, see workloads.py); surrogate weights trained on the GPU "
                     "from FP64 EMT labels (md_tian2_gb300/data)",
-            "config": {"workload": f"NN surrogate ({'BF16 tensor-core network, FP32 descriptors and forces' if head == 'bf16' else 'FP32 kernels'}, EMT fallback), {args.ntraj} ragged H/Au(111) "
+            "config": {"workload": f"NN surrogate ({ {'fp32': 'FP32 kernels', 'bf16': 'BF16 tensor-core network, FP32 descriptors and forces', 'bf16x3': 'tensor-core network with split BF16 operands, FP32 descriptors and forces'}[head] }, EMT fallback), {args.ntraj} ragged H/Au(111) "
                                    "trajectories (37-145 atoms), Verlet H + constant-friction Langevin Au, dt 0.1 fs; "
                                    "one bench step = one MD step of every trajectory",
                        "steps_per_launch": per_launch, "precision": head,
@@ -777,7 +787,7 @@ def run_ours(args):
             "fallback": {"bead_evaluations": bead_evals, "emt_fallbacks": fb_count,
                          "fraction": fb_count / max(1, bead_evals)},
             "scattering": obs,
-            "surrogate_other_precision": other,
+            "network_arithmetic": network_arms,
             "rpmd_config3": rpmd,
             "hdnnp_config4": hdnnp,
             "clocks": clocks,

@@ -21,7 +21,8 @@ module mdt_gpu
     integer(c_int32_t), parameter :: MDT_PROP_VERLET = 1001, MDT_PROP_LANGEVIN = 1003, MDT_PROP_ANDERSEN = 1005, &
                                      MDT_PROP_PILE = 1006, MDT_PROP_LANGEVIN_CONST = 1007
     integer(c_int32_t), parameter :: MDT_ENERGY_AND_FORCE = 3001, MDT_ENERGY_ONLY = 3002
-    integer(c_int32_t), parameter :: MDT_PREC_FP64 = 0, MDT_PREC_FP32 = 1, MDT_PREC_BF16 = 2
+    integer(c_int32_t), parameter :: MDT_PREC_FP64 = 0, MDT_PREC_FP32 = 1, MDT_PREC_BF16 = 2, &
+                                     MDT_PREC_BF16X3 = 3
     integer(c_int32_t), parameter :: MDT_TRAJ_RUNNING = 0, MDT_TRAJ_EXIT_UPPER = 1, MDT_TRAJ_EXIT_LOWER = 2, &
                                      MDT_TRAJ_STEP_LIMIT = 3, MDT_TRAJ_ERR_DENSITY = -10, &
                                      MDT_TRAJ_ERR_NONFINITE = -11
@@ -283,6 +284,12 @@ module mdt_gpu
             type(mdt_refill_params), intent(in) :: p
             type(c_ptr), value :: generation
             integer(c_int32_t), intent(out) :: nrefilled
+        end function
+
+        integer(c_int32_t) function mdt_refill_draws(ctx, draws) bind(C, name="mdt_refill_draws")
+            import :: c_int32_t, c_ptr, c_double
+            type(c_ptr), value :: ctx
+            real(c_double), intent(out) :: draws(*)
         end function
 
         integer(c_int32_t) function mdt_traj_observables(ctx, turn_pnts, cl_appr, cl_appr_step, r_min_p) &

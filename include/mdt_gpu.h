@@ -49,6 +49,8 @@ extern "C" {
 #define MDT_PREC_BF16 2 /* FP32 descriptors and forces, network GEMMs on the tensor cores with
                            BF16 operands and FP32 accumulation (thread-per-atom kernel of
                            radial-only networks); no counterpart in the reference */
+#define MDT_PREC_BF16X3 3 /* as MDT_PREC_BF16 with every operand split in a BF16 high and low
+                             part, three MMAs per K step (about 16 significant bits) */
 
 /* trajectory status (mdt_traj_summary.status) */
 #define MDT_TRAJ_RUNNING 0
@@ -300,6 +302,11 @@ typedef struct mdt_refill_params {
     uint64_t seed;
 } mdt_refill_params;
 int32_t mdt_refill(mdt_ctx *ctx, const mdt_refill_params *p, int32_t *generation, int32_t *nrefilled);
+/* What the last mdt_refill drew for each trajectory: draws[5 t .. 5 t + 4] = the direct
+   in-plane coordinates u, v of the new centroid, the incidence energy (eV), the polar and
+   the azimuth angle (degrees); NaN for trajectories it did not restart.  Lets a host replay
+   the start with md_init's apply_pip / set_proj_incidence (no reference counterpart). */
+int32_t mdt_refill_draws(mdt_ctx *ctx, double *draws);
 
 /* Trajectory observables of collect_trajectory_characteristics (src/trajectory_info.f90:
    47-75, 92-132, 243-250), tracked on the device by the fused MD steps (mdt_md_steps) after

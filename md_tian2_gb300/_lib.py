@@ -87,6 +87,7 @@ SIGNATURES = {
     "mdt_traj_bounces": (ct.c_int32, [ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.POINTER(PropParams)]),
     "mdt_set_adsorption": (ct.c_int32, [ct.c_void_p, ct.c_double, ct.c_double]),
     "mdt_nn_repack": (ct.c_int32, [ct.c_void_p, ct.c_void_p]),
+    "mdt_refill_draws": (ct.c_int32, [ct.c_void_p, ct.c_void_p]),
     "mdt_autotune": (ct.c_int32, [ct.c_void_p, ct.c_int32, ct.c_int32, ct.POINTER(PropParams), ct.c_void_p,
                                   ct.c_void_p, ct.c_void_p]),
     "mdt_set_step_limit": (ct.c_int32, [ct.c_void_p, ct.c_int32]),

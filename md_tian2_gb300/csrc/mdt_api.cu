@@ -37,6 +37,7 @@ struct mdt_ctx {
     // refill: state of the last upload (6 SoA arrays), generation per trajectory, counter
     double *tmpl = nullptr;
     int *gen = nullptr, *refill_count = nullptr;
+    double *draws = nullptr;  // per trajectory the last refill's draws (u, w, einc, polar, azimuth)
     bool have_tmpl = false;
     int step_limit = 0;
     double ads_start = kDefaultReal, ads_end = kDefaultReal;  // adsorption hysteresis (A)
@@ -99,7 +100,8 @@ struct mdt_ctx {
 namespace {
 
 const char *const kBf16Scope =
-    "MDT_PREC_BF16 runs the network GEMMs on the tensor cores in the thread-per-atom kernel only: a radial-only "
+    "MDT_PREC_BF16 / MDT_PREC_BF16X3 run the network GEMMs on the tensor cores in the thread-per-atom kernel only: "
+    "a radial-only "
     "network (mdt_nn_radial_kernel) on single-bead trajectories of at most 512 atoms";
 
 int fail(mdt_ctx *c, int code, const std::string &msg) {
@@ -124,6 +126,7 @@ void free_batch(mdt_ctx *c) {
     c->X = NNScratch{};
     c->tmpl = nullptr;
     c->gen = c->refill_count = nullptr;
+    c->draws = nullptr;
     c->have_tmpl = false;
     c->skw = nullptr;
     c->skcnt = c->skok = nullptr;
@@ -683,7 +686,8 @@ bool radial_plan(mdt_ctx *c, const std::vector<int> &ids = {}) {
 // The thread-per-atom kernel runs FP32 forces of an admitted model; the fused MD step also
 // needs single-bead trajectories with Verlet or constant-friction Langevin propagators.
 bool use_radial(mdt_ctx *c, int precision, bool md) {
-    if ((precision != MDT_PREC_FP32 && precision != MDT_PREC_BF16) || !c->R.ok || !c->radial_enabled ||
+    if ((precision != MDT_PREC_FP32 && precision != MDT_PREC_BF16 && precision != MDT_PREC_BF16X3) || !c->R.ok ||
+        !c->radial_enabled ||
         !c->fast_enabled)
         return false;
     if (md)
@@ -692,10 +696,14 @@ bool use_radial(mdt_ctx *c, int precision, bool md) {
     return radial_plan(c);
 }
 
-int run_radial(mdt_ctx *c, const PropParams &P, int nsteps, int mode, bool surr, bool tc) {
+// tcm: network on CUDA cores (0), tensor cores with BF16 operands (1), split BF16 operands (2)
+int tc_mode(int precision) { return precision == MDT_PREC_BF16 ? 1 : precision == MDT_PREC_BF16X3 ? 2 : 0; }
+
+int run_radial(mdt_ctx *c, const PropParams &P, int nsteps, int mode, bool surr, int tcm) {
     RadialNN &R = c->R;
     R.block = c->rblock;
-    R.tc = tc ? 1 : 0;
+    R.tc = tcm;
+    const bool tc = tcm != 0;
     if (tc) {
         int dev = 0, optin = 0;
         cudaGetDevice(&dev);
@@ -1080,6 +1088,7 @@ int32_t mdt_batch_define(mdt_ctx *c, int32_t ntraj, const int32_t *natoms, const
         if (e == cudaSuccess) c->gen = dalloc<int>(c, (size_t)ntraj + 1, e);
         if (e == cudaSuccess) e = cudaMemsetAsync(c->gen, 0, sizeof(int) * ((size_t)ntraj + 1), c->stream);
         c->refill_count = c->gen ? c->gen + ntraj : nullptr;
+        if (e == cudaSuccess) c->draws = dalloc<double>(c, 5 * (size_t)ntraj, e);
     }
     if (e != cudaSuccess) {
         free_batch(c);
@@ -1185,9 +1194,8 @@ int32_t mdt_calc_force(mdt_ctx *c, int32_t flag, int32_t precision, const mdt_pr
     int rc = check_ready(c, c && c->pes_kind == MDT_PES_EMT);
     if (rc) return rc;
     if (flag != MDT_ENERGY_AND_FORCE && flag != MDT_ENERGY_ONLY) return fail(c, MDT_ERR_ARG, "bad flag");
-    if (precision != MDT_PREC_FP64 && precision != MDT_PREC_FP32 && precision != MDT_PREC_BF16)
-        return fail(c, MDT_ERR_ARG, "bad precision");
-    if (precision == MDT_PREC_BF16 && c->pes_kind == MDT_PES_EMT) return fail(c, MDT_ERR_UNSUPPORTED, kBf16Scope);
+    if (precision < MDT_PREC_FP64 || precision > MDT_PREC_BF16X3) return fail(c, MDT_ERR_ARG, "bad precision");
+    if (tc_mode(precision) && c->pes_kind == MDT_PES_EMT) return fail(c, MDT_ERR_UNSUPPORTED, kBf16Scope);
     if ((rc = check_params(c, p, false))) return rc;
     if (c->pes_kind != MDT_PES_EMT) {
         if ((rc = check_nn_ready(c))) return rc;
@@ -1195,8 +1203,8 @@ int32_t mdt_calc_force(mdt_ctx *c, int32_t flag, int32_t precision, const mdt_pr
         const PropParams P = to_dev(c, p);
         const bool surr = c->pes_kind == MDT_PES_SURROGATE;
         if (use_radial(c, precision, false))
-            return run_radial(c, P, 0, flag == MDT_ENERGY_ONLY ? 1 : 0, surr, precision == MDT_PREC_BF16);
-        if (precision == MDT_PREC_BF16) return fail(c, MDT_ERR_UNSUPPORTED, kBf16Scope);
+            return run_radial(c, P, 0, flag == MDT_ENERGY_ONLY ? 1 : 0, surr, tc_mode(precision));
+        if (tc_mode(precision)) return fail(c, MDT_ERR_UNSUPPORTED, kBf16Scope);
         const bool fast = use_fast(c, precision);
         const LaunchCfg fcfg = fast ? nnf_cfg(c) : LaunchCfg{};
         if (fast && (rc = ensure_mscr(c, fcfg.grid, 0))) return rc;
@@ -1240,9 +1248,8 @@ int32_t mdt_md_steps(mdt_ctx *c, int32_t nsteps, int32_t precision, const mdt_pr
     int rc = check_ready(c, c && c->pes_kind == MDT_PES_EMT);
     if (rc) return rc;
     if (nsteps < 0) return fail(c, MDT_ERR_ARG, "nsteps < 0");
-    if (precision != MDT_PREC_FP64 && precision != MDT_PREC_FP32 && precision != MDT_PREC_BF16)
-        return fail(c, MDT_ERR_ARG, "bad precision");
-    if (precision == MDT_PREC_BF16 && c->pes_kind == MDT_PES_EMT) return fail(c, MDT_ERR_UNSUPPORTED, kBf16Scope);
+    if (precision < MDT_PREC_FP64 || precision > MDT_PREC_BF16X3) return fail(c, MDT_ERR_ARG, "bad precision");
+    if (tc_mode(precision) && c->pes_kind == MDT_PES_EMT) return fail(c, MDT_ERR_UNSUPPORTED, kBf16Scope);
     if ((rc = check_params(c, p))) return rc;
     if (p->rng_mode == 1 && nsteps > 1) return fail(c, MDT_ERR_ARG, "rng_mode 1 supports one step per call");
     if (c->pes_kind != MDT_PES_EMT) {
@@ -1251,8 +1258,8 @@ int32_t mdt_md_steps(mdt_ctx *c, int32_t nsteps, int32_t precision, const mdt_pr
         if (nsteps == 0) return MDT_OK;
         const PropParams P = to_dev(c, p);
         const bool surr = c->pes_kind == MDT_PES_SURROGATE;
-        if (use_radial(c, precision, true)) return run_radial(c, P, nsteps, 2, surr, precision == MDT_PREC_BF16);
-        if (precision == MDT_PREC_BF16) return fail(c, MDT_ERR_UNSUPPORTED, kBf16Scope);
+        if (use_radial(c, precision, true)) return run_radial(c, P, nsteps, 2, surr, tc_mode(precision));
+        if (tc_mode(precision)) return fail(c, MDT_ERR_UNSUPPORTED, kBf16Scope);
         const bool fast = use_fast(c, precision);
         const LaunchCfg fcfg = fast ? nnf_cfg(c) : LaunchCfg{};
         if (fast && (rc = ensure_mscr(c, fcfg.grid, 0))) return rc;
@@ -1287,9 +1294,10 @@ int32_t mdt_refill(mdt_ctx *c, const mdt_refill_params *p, int32_t *generation, 
         !(p->polar_min >= 0.0) || !(p->polar_max < 90.0) || !std::isfinite(p->z0))
         return fail(c, MDT_ERR_ARG, "mdt_refill: need 0 < einc_min <= einc_max, 0 <= polar_min <= polar_max < 90");
     cudaError_t e = cudaMemsetAsync(c->refill_count, 0, sizeof(int), c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->draws, 0xFF, sizeof(double) * 5 * (size_t)c->T, c->stream);  // NaN
     if (e == cudaSuccess)
         e = launch_refill(c->stream, c->B, c->tmpl, c->total_ba, p->z0, p->einc_min, p->einc_max, p->polar_min,
-                          p->polar_max, p->azimuth, p->seed, c->gen, c->skok, c->refill_count);
+                          p->polar_max, p->azimuth, p->seed, c->gen, c->skok, c->refill_count, c->draws);
     c->launches++;
     int n = 0;
     if (e == cudaSuccess) e = cudaMemcpyAsync(&n, c->refill_count, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
@@ -1300,6 +1308,17 @@ int32_t mdt_refill(mdt_ctx *c, const mdt_refill_params *p, int32_t *generation, 
     if (nrefilled) *nrefilled = n;
     if (n > 0) c->rnpack = 0;  // restarted trajectories must be in the next pack plan
     return MDT_OK;
+}
+
+int32_t mdt_refill_draws(mdt_ctx *c, double *draws) {
+    int rc = check_ready(c, false);
+    if (rc) return rc;
+    if (!draws) return fail(c, MDT_ERR_ARG, "mdt_refill_draws: null output");
+    if (!c->draws) return fail(c, MDT_ERR_STATE, "mdt_refill_draws: no refill yet");
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(draws, c->draws, sizeof(double) * 5 * (size_t)c->T, cudaMemcpyDeviceToHost);
+    return e == cudaSuccess ? MDT_OK : cuda_fail(c, e, "mdt_refill_draws");
 }
 
 int32_t mdt_nn_repack(mdt_ctx *c, int32_t *npacks) {
@@ -1672,7 +1691,7 @@ int32_t mdt_autotune(mdt_ctx *c, int32_t precision, int32_t nsteps, const mdt_pr
     const double keep_skin = c->skin_ang;
     const PropParams P = to_dev(c, p);
     const bool surr = c->pes_kind == MDT_PES_SURROGATE;
-    const bool tc = precision == MDT_PREC_BF16;
+    const int tc = tc_mode(precision);
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (e == cudaSuccess) e = cudaEventCreate(&e0);
     if (e == cudaSuccess) e = cudaEventCreate(&e1);

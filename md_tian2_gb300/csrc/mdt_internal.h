@@ -47,7 +47,7 @@ int emt_derive_constants(int32_t ntypes, const double *eta2, const double *n0, c
 cudaError_t launch_obs_reset(cudaStream_t s, const Batch &B);
 cudaError_t launch_refill(cudaStream_t s, const Batch &B, const double *tmpl, int64_t total_ba, double z0,
                           double emin, double emax, double pmin, double pmax, double azimuth, uint64_t seed,
-                          int *gen, int *skok, int *count);
+                          int *gen, int *skok, int *count, double *draws);
 
 // FP32 thread-per-atom kernel of radial-only models (mdt_nnr.cu)
 // shape of a model (group counts, hidden layers; maxbl[g] = longest recurrence block group g

@@ -167,7 +167,7 @@ __device__ __forceinline__ bool refillable(int status) {
 }
 
 __global__ void refill_kernel(Batch B, const double *tmpl, int64_t total_ba, RefillDev R, int *gen, int *skok,
-                              int *count) {
+                              int *count, double *draws) {
     for (int t = blockIdx.x; t < B.ntraj; t += gridDim.x) {
         if (!refillable(B.status[t])) continue;  // uniform over the block
         const TrajView T = traj_view(B, t);
@@ -183,10 +183,17 @@ __global__ void refill_kernel(Batch B, const double *tmpl, int64_t total_ba, Ref
             const double u = uniform_deviate(R.seed, tt, gg, 0, kStreamRefill);
             const double w = uniform_deviate(R.seed, tt, gg, 1, kStreamRefill);
             const double e = R.emin + (R.emax - R.emin) * uniform_deviate(R.seed, tt, gg, 2, kStreamRefill);
-            const double pol =
-                (R.pmin + (R.pmax - R.pmin) * uniform_deviate(R.seed, tt, gg, 3, kStreamRefill)) * (kPi / 180.0);
-            const double azi = (R.azimuth < 0.0 ? 360.0 * uniform_deviate(R.seed, tt, gg, 4, kStreamRefill)
-                                                : R.azimuth) * (kPi / 180.0);
+            const double pol_deg = R.pmin + (R.pmax - R.pmin) * uniform_deviate(R.seed, tt, gg, 3, kStreamRefill);
+            const double pol = pol_deg * (kPi / 180.0);
+            const double azi_deg = R.azimuth < 0.0 ? 360.0 * uniform_deviate(R.seed, tt, gg, 4, kStreamRefill)
+                                                   : R.azimuth;
+            const double azi = azi_deg * (kPi / 180.0);
+            double *dr = draws + 5 * (size_t)t;
+            dr[0] = u;
+            dr[1] = w;
+            dr[2] = e;
+            dr[3] = pol_deg;
+            dr[4] = azi_deg;
             const double *h = B.box + 9 * (size_t)t;  // column major: h[3 k + d] = component d of vector k
             const double target[3] = {h[0] * u + h[3] * w, h[1] * u + h[4] * w, R.z0};
             const double vinc = sqrt(2.0 * e / B.mass[T.aoff]);
@@ -220,10 +227,10 @@ __global__ void refill_kernel(Batch B, const double *tmpl, int64_t total_ba, Ref
 
 cudaError_t launch_refill(cudaStream_t s, const Batch &B, const double *tmpl, int64_t total_ba, double z0,
                           double emin, double emax, double pmin, double pmax, double azimuth, uint64_t seed,
-                          int *gen, int *skok, int *count) {
+                          int *gen, int *skok, int *count, double *draws) {
     const RefillDev R{z0, emin, emax, pmin, pmax, azimuth, seed};
     const int grid = B.ntraj < 4096 ? (B.ntraj > 0 ? B.ntraj : 1) : 4096;
-    refill_kernel<<<grid, 128, 0, s>>>(B, tmpl, total_ba, R, gen, skok, count);
+    refill_kernel<<<grid, 128, 0, s>>>(B, tmpl, total_ba, R, gen, skok, count, draws);
     return cudaGetLastError();
 }
 

@@ -83,21 +83,27 @@ constexpr int kRS = kRBlockMax;
 
 // per-thread network buffer (FP32 network) or operand tiles (tensor-core network); either
 // doubles as the EMT fallback area
-__host__ __device__ constexpr size_t hb_bytes(int nin, int nh, bool tc) {
-    return tc ? nnr_tc_hb(nin) : 4 * (size_t)nnr_hbw(nin, nh) * kRS;
+// tcm: 0 FP32 network, 1 BF16 operands, 2 BF16 operands split in a high and a low part
+// (the A tiles and the B operands exist twice)
+__host__ __device__ constexpr size_t hb_bytes(int nin, int nh, int tcm) {
+    return tcm == 0 ? 4 * (size_t)nnr_hbw(nin, nh) * kRS
+                    : (tcm == 2 && 2 * (size_t)kTcTiles * 128 * nnr_tw(nin) * 2 > nnr_tc_hb(nin)
+                           ? 2 * (size_t)kTcTiles * 128 * nnr_tw(nin) * 2
+                           : nnr_tc_hb(nin));
 }
-__host__ __device__ constexpr size_t w_bytes(int nin, int nh, bool tc) {
-    return tc ? 2 * (size_t)nnr_tc_bel(nin) + 2 * 4 * (size_t)kTcVec : 4 * (size_t)nnr_wtotal(nin, nh);
+__host__ __device__ constexpr size_t w_bytes(int nin, int nh, int tcm) {
+    return tcm == 0 ? 4 * (size_t)nnr_wtotal(nin, nh)
+                    : (size_t)(tcm == 2 ? 2 : 1) * 2 * nnr_tc_bel(nin) + 2 * 4 * (size_t)kTcVec;
 }
 
-__host__ __device__ constexpr size_t smem_r(int nin, int nh, bool tc) {
+__host__ __device__ constexpr size_t smem_r(int nin, int nh, int tc) {
     return 6 * r16r(4 * (size_t)kRS) + r16r(12 * (size_t)kRS) + r16r(8 * (size_t)kRS) + r16r(64 * (size_t)kRS) +
            r16r(8 * (size_t)kRS) + r16r(kRS) + r16r(hb_bytes(nin, nh, tc)) + r16r(w_bytes(nin, nh, tc)) +
            r16r(16 * 2 * (size_t)nin) + r16r(4 * 2 * (size_t)nin) + 3 * r16r(4 * kRMaxTraj) + 4 * r16r(8 * kRMaxTraj) +
            r16r(12 * kRMaxTraj) + r16r(4 * 24 * kRMaxTraj) + r16r(8 * 64) + r16r(16) + r16r(8 * kTcTiles) + r16r(16);
 }
 
-template <int NIN, int NH, bool TC>
+template <int NIN, int NH, int TC>
 __device__ __forceinline__ SmemR carve_r(unsigned char *base) {
     SmemR s;
     size_t off = 0;
@@ -122,7 +128,7 @@ __device__ __forceinline__ SmemR carve_r(unsigned char *base) {
     s.at = (unsigned char *)s.hb;
     s.w = (float *)take(w_bytes(NIN, NH, TC));
     s.wb = (unsigned char *)s.w;
-    s.wv = (float *)(s.wb + 2 * (size_t)nnr_tc_bel(NIN));
+    s.wv = (float *)(s.wb + (size_t)(TC == 2 ? 2 : 1) * 2 * nnr_tc_bel(NIN));
     s.scal = (float4 *)take(16 * 2 * (size_t)NIN);
     s.dscal = (float *)take(4 * 2 * (size_t)NIN);
     s.tr_t = (int *)take(4 * kRMaxTraj);
@@ -688,9 +694,13 @@ constexpr uint32_t kTcMaxPolls = 1u << 18;
 
 // One GEMM round of the tile group: D_e (TMEM columns d0, d1) = A (K x 128 rows at a_s) x B_e^T
 // (N rows at b0_s / b1_s); all threads of the tile call it, returns with the result visible.
-template <int KK, int NN>
+// SPLIT: A = A_hi + A_lo and B = B_hi + B_lo (each a BF16 operand; the low parts at a_lo
+// bytes after the high A tile and b_lo bytes after the high B operands) and
+// D = A_hi B_hi + A_lo B_hi + A_hi B_lo: three MMAs per K step, about 16 significant bits.
+template <int KK, int NN, bool SPLIT>
 __device__ __forceinline__ void tc_round(const TcCtx &C, int g, int nthr, uint32_t a_s, uint32_t b0_s, uint32_t b1_s,
-                                         bool two, uint32_t d0, uint32_t d1, uint32_t &phase) {
+                                         bool two, uint32_t d0, uint32_t d1, uint32_t &phase, uint32_t a_lo = 0,
+                                         uint32_t b_lo = 0) {
     fence_async_smem();
     tc_fence_before();
     named_barrier(1 + g, nthr);
@@ -699,15 +709,39 @@ __device__ __forceinline__ void tc_round(const TcCtx &C, int g, int nthr, uint32
         constexpr uint32_t idesc = tc_idesc_bf16(128, NN);
 #pragma unroll
         for (int ks = 0; ks < KK / 16; ++ks) {
-            const uint64_t ad = tc_desc(a_s + 256 * ks, 128, 16 * KK);
-            tc_mma_bf16(C.tmem + d0, ad, tc_desc(b0_s + 256 * ks, 128, 16 * KK), idesc, ks > 0);
-            if (two) tc_mma_bf16(C.tmem + d1, ad, tc_desc(b1_s + 256 * ks, 128, 16 * KK), idesc, ks > 0);
+            const uint32_t ao = a_s + 256 * ks, bo0 = b0_s + 256 * ks, bo1 = b1_s + 256 * ks;
+            const uint64_t ad = tc_desc(ao, 128, 16 * KK);
+            tc_mma_bf16(C.tmem + d0, ad, tc_desc(bo0, 128, 16 * KK), idesc, ks > 0);
+            if (two) tc_mma_bf16(C.tmem + d1, ad, tc_desc(bo1, 128, 16 * KK), idesc, ks > 0);
+            if constexpr (SPLIT) {
+                const uint64_t al = tc_desc(ao + a_lo, 128, 16 * KK);
+                tc_mma_bf16(C.tmem + d0, al, tc_desc(bo0, 128, 16 * KK), idesc, true);
+                tc_mma_bf16(C.tmem + d0, ad, tc_desc(bo0 + b_lo, 128, 16 * KK), idesc, true);
+                if (two) {
+                    tc_mma_bf16(C.tmem + d1, al, tc_desc(bo1, 128, 16 * KK), idesc, true);
+                    tc_mma_bf16(C.tmem + d1, ad, tc_desc(bo1 + b_lo, 128, 16 * KK), idesc, true);
+                }
+            }
         }
         tc_commit(&C.bar[g]);
     }
     if (!*(volatile int *)C.err && !mbar_wait_bounded(&C.bar[g], phase, kTcMaxPolls)) atomicExch(C.err, 1);
     phase ^= 1u;
     tc_fence_after();
+}
+
+// eight FP32 values as one 16-byte chunk of BF16 operand row; with SPLIT also the rounding
+// residuals (x - bf16(x)) as the chunk of the low part, `lo` bytes further on
+__device__ __forceinline__ float bf16_value(float x) { return __uint_as_float(pack_bf16x2(x, 0.f) << 16); }
+template <bool SPLIT>
+__device__ __forceinline__ void st_row8(unsigned char *chunk, size_t lo, const float *v) {
+    st_bf16x8(chunk, v);
+    if constexpr (SPLIT) {
+        float r[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) r[j] = v[j] - bf16_value(v[j]);
+        st_bf16x8(chunk + lo, r);
+    }
 }
 
 // 16 accumulator columns of the thread's row, from element 1's block when e1
@@ -753,7 +787,7 @@ template <int N> __device__ __forceinline__ void act_dvals(uint8_t a, const floa
 // layout, as load_weights_r reads it).  B1[n][q] = W1[q][n] (32 x KP), B2[n][p] = W2[p][n],
 // B3[p][n] = W2[p][n] (32 x 32), B4[q][p] = W1[q][p] (KP x 32); vectors: b1, then b2, w3, b3
 // (two hidden layers) or w2, b2 (one).
-template <int NIN, int NH>
+template <int NIN, int NH, bool SPLIT>
 __device__ void load_weights_tc(const RadialNN &R, const SmemR &S) {
     constexpr int KP = nnr_kp(NIN), BEL = nnr_tc_bel(NIN);
     constexpr int oB2 = 32 * KP * 2, oB3 = oB2 + 2048, oB4 = oB3 + 2048;
@@ -770,12 +804,13 @@ __device__ void load_weights_tc(const RadialNN &R, const SmemR &S) {
         };
         auto w2 = [&](int p, int n) -> float { return (NH == 2 && p < n1 && n < n2) ? l2[p * n2 + n] : 0.f; };
         unsigned char *wb = S.wb + (size_t)e * BEL;
+        const size_t lo = 2 * (size_t)BEL;  // low parts of the split operands
         // one 8-wide chunk per item: rows x (K / 8) chunks per matrix
         for (int it = tid; it < 32 * (KP / 8); it += bs) {  // B1: row n, chunk k0 over q
             const int n = it / (KP / 8), k0 = 8 * (it % (KP / 8));
             float v[8];
             for (int j = 0; j < 8; ++j) v[j] = w1(k0 + j, n);
-            st_bf16x8(wb + tc_offset(n, k0, KP), v);
+            st_row8<SPLIT>(wb + tc_offset(n, k0, KP), lo, v);
         }
         for (int it = tid; it < 32 * 4; it += bs) {  // B2, B3
             const int n = it / 4, k0 = 8 * (it % 4);
@@ -784,14 +819,14 @@ __device__ void load_weights_tc(const RadialNN &R, const SmemR &S) {
                 v[j] = w2(k0 + j, n);  // B2[n][p] = W2[p][n]
                 u[j] = w2(n, k0 + j);  // B3[p][n] = W2[p][n], row p = n here
             }
-            st_bf16x8(wb + oB2 + tc_offset(n, k0, 32), v);
-            st_bf16x8(wb + oB3 + tc_offset(n, k0, 32), u);
+            st_row8<SPLIT>(wb + oB2 + tc_offset(n, k0, 32), lo, v);
+            st_row8<SPLIT>(wb + oB3 + tc_offset(n, k0, 32), lo, u);
         }
         for (int it = tid; it < KP * 4; it += bs) {  // B4: row q, chunk over p
             const int q = it / 4, k0 = 8 * (it % 4);
             float v[8];
             for (int j = 0; j < 8; ++j) v[j] = w1(q, k0 + j);
-            st_bf16x8(wb + oB4 + tc_offset(q, k0, 32), v);
+            st_row8<SPLIT>(wb + oB4 + tc_offset(q, k0, 32), lo, v);
         }
         float *vec = S.wv + e * kTcVec;
         for (int n = tid; n < 32; n += bs) {
@@ -813,7 +848,7 @@ __device__ void load_weights_tc(const RadialNN &R, const SmemR &S) {
 // The network of this thread's atom on the tensor cores.  Every thread of the CTA calls it
 // (rows without an atom carry zeros).  Returns the atomic energy (output node, Ha); with
 // do_forces, dG receives dE/dG for the raw descriptors (padded grouped order).
-template <int NIN, int NH>
+template <int NIN, int NH, bool SPLIT>
 __device__ __forceinline__ float nnr_network_tc(const RadialNN &R, const SmemR &S, const TcCtx &C, int ei,
                                                 const float (&xs)[NIN], bool do_forces, float (&dG)[NIN],
                                                 uint32_t &phase) {
@@ -823,6 +858,8 @@ __device__ __forceinline__ float nnr_network_tc(const RadialNN &R, const SmemR &
     const int nthr = min(128, (int)blockDim.x - 128 * g);
     unsigned char *at = S.at + (size_t)g * 128 * TW * 2;
     const uint32_t a_s = smem_u32(at), b_s = smem_u32(S.wb);
+    constexpr size_t ALO = (size_t)kTcTiles * 128 * TW * 2;  // low A parts after all high tiles
+    constexpr uint32_t BLO = 2 * BEL;                          // low B parts after both elements
     const uint32_t lane = ((uint32_t)((tid >> 5) & 3) * 32u) << 16;
     const uint32_t c0 = (uint32_t)(g * CPT), c1 = c0 + TW, cs = c0 + 2 * TW;
     const bool two = R.nelem > 1, e1 = ei == 1;
@@ -835,9 +872,9 @@ __device__ __forceinline__ float nnr_network_tc(const RadialNN &R, const SmemR &
         float v[8];
 #pragma unroll
         for (int j = 0; j < 8; ++j) v[j] = (k0 + j < NIN) ? xs[k0 + j] : 0.f;
-        st_bf16x8(at + tc_offset(row, k0, KP), v);
+        st_row8<SPLIT>(at + tc_offset(row, k0, KP), ALO, v);
     }
-    tc_round<KP, 32>(C, g, nthr, a_s, b_s, b_s + BEL, two, c0, c1, phase);
+    tc_round<KP, 32, SPLIT>(C, g, nthr, a_s, b_s, b_s + BEL, two, c0, c1, phase, ALO, BLO);
     float o = 0.f;  // output-node sum (one hidden layer)
 #pragma unroll
     for (int h = 0; h < 32; h += 16) {
@@ -848,8 +885,8 @@ __device__ __forceinline__ float nnr_network_tc(const RadialNN &R, const SmemR &
         act_vals<16>(a1, z);
         tmem_st16(C.tmem + lane + cs + h, z);  // layer-1 values for the backward pass
         if (NH == 2) {
-            st_bf16x8(at + tc_offset(row, h, 32), z);
-            st_bf16x8(at + tc_offset(row, h + 8, 32), z + 8);
+            st_row8<SPLIT>(at + tc_offset(row, h, 32), ALO, z);
+            st_row8<SPLIT>(at + tc_offset(row, h + 8, 32), ALO, z + 8);
         } else {
 #pragma unroll
             for (int j = 0; j < 16; ++j) o = fmaf(vec[32 + h + j], z[j], o);
@@ -859,7 +896,7 @@ __device__ __forceinline__ float nnr_network_tc(const RadialNN &R, const SmemR &
     float out, g1;
     if (NH == 2) {
         // ---- layer 2: v1 W2; output node -------------------------------------------------
-        tc_round<32, 32>(C, g, nthr, a_s, b_s + oB2, b_s + BEL + oB2, two, c0, c1, phase);
+        tc_round<32, 32, SPLIT>(C, g, nthr, a_s, b_s + oB2, b_s + BEL + oB2, two, c0, c1, phase, ALO, BLO);
         const float rn2 = R.rn[1];
         const uint8_t a2 = R.act[1];
 #pragma unroll
@@ -889,11 +926,11 @@ __device__ __forceinline__ float nnr_network_tc(const RadialNN &R, const SmemR &
                 act_d(a2, (z[j] + vec[32 + h + j]) * rn2, v, dv);
                 z[j] = vec[64 + h + j] * dv * g2;
             }
-            st_bf16x8(at + tc_offset(row, h, 32), z);
-            st_bf16x8(at + tc_offset(row, h + 8, 32), z + 8);
+            st_row8<SPLIT>(at + tc_offset(row, h, 32), ALO, z);
+            st_row8<SPLIT>(at + tc_offset(row, h + 8, 32), ALO, z + 8);
         }
         // ---- delta1 = (delta2 W2^T) rn1 f'(v1) -------------------------------------------
-        tc_round<32, 32>(C, g, nthr, a_s, b_s + oB3, b_s + BEL + oB3, two, c0, c1, phase);
+        tc_round<32, 32, SPLIT>(C, g, nthr, a_s, b_s + oB3, b_s + BEL + oB3, two, c0, c1, phase, ALO, BLO);
         g1 = rn1;
     } else {
         float vo, dvo;
@@ -916,11 +953,11 @@ __device__ __forceinline__ float nnr_network_tc(const RadialNN &R, const SmemR &
 #pragma unroll
         for (int j = 0; j < 16; ++j) d[j] *= g1;
         act_dvals<16>(a1, v1, d);
-        st_bf16x8(at + tc_offset(row, h, 32), d);
-        st_bf16x8(at + tc_offset(row, h + 8, 32), d + 8);
+        st_row8<SPLIT>(at + tc_offset(row, h, 32), ALO, d);
+        st_row8<SPLIT>(at + tc_offset(row, h + 8, 32), ALO, d + 8);
     }
     // ---- dE/dG_q = dscal_q (delta1 W1^T)_q ---------------------------------------------
-    tc_round<32, KP>(C, g, nthr, a_s, b_s + oB4, b_s + BEL + oB4, two, c0, c1, phase);
+    tc_round<32, KP, SPLIT>(C, g, nthr, a_s, b_s + oB4, b_s + BEL + oB4, two, c0, c1, phase, ALO, BLO);
     const float *ds = S.dscal + ei * NIN;
 #pragma unroll
     for (int q0 = 0; q0 < KP; q0 += 16) {
@@ -997,7 +1034,7 @@ __device__ __forceinline__ void lc_half2(const Batch &B, const PropParams &P, co
 
 // mode 0: forces, 1: energies only, 2: nsteps fused MD steps (propagate_1, forces,
 // propagate_2, exit test), as the other network kernels.
-template <int KA, int KB, int NH, int BLA, int BLB, bool TC>
+template <int KA, int KB, int NH, int BLA, int BLB, int TC>
 __global__ void __launch_bounds__(kRBlockMax, 1)
     nnr_kernel(Batch B, RadialNN R, EmtConst E, NNScratch X, PropParams P, const int2 *packs, const int *ptraj, int npack,
                int *counter, int nsteps, int mode) {
@@ -1011,7 +1048,7 @@ __global__ void __launch_bounds__(kRBlockMax, 1)
     TcCtx C{0u, S.tcbar, X.tcerr};
     uint32_t phase = 0;  // parity of this thread's tile mbarrier
     if constexpr (TC) {
-        load_weights_tc<KT, NH>(R, S);
+        load_weights_tc<KT, NH, TC == 2>(R, S);
         if (tid < 32) {
             tmem_alloc(S.tslot, kTcCols);
             tmem_relinquish();
@@ -1206,7 +1243,7 @@ __global__ void __launch_bounds__(kRBlockMax, 1)
             float e_at = 0.f;
             if constexpr (TC) {
                 // every thread of the CTA: the GEMMs are per 128-row tile
-                e_at = nnr_network_tc<KT, NH>(R, S, C, active ? A.ei : 0, xs, do_forces, dG, phase);
+                e_at = nnr_network_tc<KT, NH, TC == 2>(R, S, C, active ? A.ei : 0, xs, do_forces, dG, phase);
             } else if (active) {
 #pragma unroll
                 for (int q = 0; q < KT; ++q) S.hb[q * bs + tid] = xs[q];
@@ -1318,7 +1355,7 @@ __global__ void __launch_bounds__(kRBlockMax, 1)
     }
 }
 
-template <int KA, int KB, int NH, int BLA, int BLB, bool TC>
+template <int KA, int KB, int NH, int BLA, int BLB, int TC>
 cudaError_t nnr_launch_t(const LaunchCfg &c, const Batch &B, const RadialNN &R, const EmtConst &E,
                          const NNScratch &X, const PropParams &P, const int2 *packs, const int *ptraj, int npack,
                          size_t sm, int nsteps, int mode) {
@@ -1331,13 +1368,13 @@ cudaError_t nnr_launch_t(const LaunchCfg &c, const Batch &B, const RadialNN &R, 
     return cudaGetLastError();
 }
 
-template <int KA, int KB, int NH, int BLA, int BLB, bool TC>
+template <int KA, int KB, int NH, int BLA, int BLB, int TC>
 int nnr_occupancy_t(int block, size_t sm) {
     int n = 0;
     cudaFuncSetAttribute(nnr_kernel<KA, KB, NH, BLA, BLB, TC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, nnr_kernel<KA, KB, NH, BLA, BLB, TC>, block, sm);
     // a CTA of the tensor-core kernels holds all 512 TMEM columns of its SM
-    return TC ? (n > 0 ? 1 : 0) : n;
+    return TC ? (n > 0 ? 1 : 0) : n;  // (tensor-core variants: one CTA per SM)
 }
 
 }  // namespace
@@ -1364,9 +1401,9 @@ bool nnr_shape(int cnt0, int cnt1, int nh, const int *maxbl, RadialNN &R) {
     return found;
 }
 
-size_t nnr_smem(const RadialNN &R) { return smem_r(R.nin, R.nh, R.tc != 0); }
+size_t nnr_smem(const RadialNN &R) { return smem_r(R.nin, R.nh, R.tc); }
 
-size_t nnr_hb_bytes(const RadialNN &R) { return hb_bytes(R.nin, R.nh, R.tc != 0); }
+size_t nnr_hb_bytes(const RadialNN &R) { return hb_bytes(R.nin, R.nh, R.tc); }
 
 size_t nnr_emt_smem(int max_atoms) { return smem_bytes(max_atoms, 1, 8); }
 
@@ -1374,8 +1411,9 @@ int nnr_resident_ctas(const RadialNN &R) {
     const size_t sm = nnr_smem(R);
 #define MDT_OCC(A_, B_, H_, LA_, LB_)                                                   \
     if (R.ka == A_ && R.kb == B_ && R.nh == H_ && R.bla == LA_ && R.blb == LB_) \
-        return R.tc ? nnr_occupancy_t<A_, B_, H_, LA_, LB_, true>(R.block, sm)   \
-                    : nnr_occupancy_t<A_, B_, H_, LA_, LB_, false>(R.block, sm);
+        return R.tc == 2 ? nnr_occupancy_t<A_, B_, H_, LA_, LB_, 2>(R.block, sm)       \
+               : R.tc == 1 ? nnr_occupancy_t<A_, B_, H_, LA_, LB_, 1>(R.block, sm)     \
+                           : nnr_occupancy_t<A_, B_, H_, LA_, LB_, 0>(R.block, sm);
     MDT_NNR_SHAPES(MDT_OCC)
 #undef MDT_OCC
     return 0;
@@ -1386,8 +1424,9 @@ cudaError_t launch_nnr(const LaunchCfg &c, const Batch &B, const RadialNN &R, co
     const size_t sm = nnr_smem(R);
 #define MDT_LAUNCH(A_, B_, H_, LA_, LB_)                                                                      \
     if (R.ka == A_ && R.kb == B_ && R.nh == H_ && R.bla == LA_ && R.blb == LB_)                       \
-        return R.tc ? nnr_launch_t<A_, B_, H_, LA_, LB_, true>(c, B, R, E, X, P, packs, ptraj, npack, sm, nsteps, mode) \
-                    : nnr_launch_t<A_, B_, H_, LA_, LB_, false>(c, B, R, E, X, P, packs, ptraj, npack, sm, nsteps, mode);
+        return R.tc == 2 ? nnr_launch_t<A_, B_, H_, LA_, LB_, 2>(c, B, R, E, X, P, packs, ptraj, npack, sm, nsteps, mode) \
+               : R.tc == 1 ? nnr_launch_t<A_, B_, H_, LA_, LB_, 1>(c, B, R, E, X, P, packs, ptraj, npack, sm, nsteps, mode) \
+                           : nnr_launch_t<A_, B_, H_, LA_, LB_, 0>(c, B, R, E, X, P, packs, ptraj, npack, sm, nsteps, mode);
     MDT_NNR_SHAPES(MDT_LAUNCH)
 #undef MDT_LAUNCH
     return cudaErrorInvalidValue;

@@ -18,7 +18,7 @@ from ._lib import EngineError, NNModelC, PropParams, TrajSummary, load
 from .io import EmtParams
 from .universe import Universe
 
-PREC = {"fp64": 0, "fp32": 1, "bf16": 2}
+PREC = {"fp64": 0, "fp32": 1, "bf16": 2, "bf16x3": 3}
 PES_EMT, PES_NENE, PES_SURROGATE = C.PES_ID_EMT, C.PES_ID_NENE, 2100
 
 
@@ -309,6 +309,13 @@ class Engine:
         n = ct.c_int32(0)
         self._check(self.lib.mdt_refill(self.h, ct.byref(p), gen.ctypes.data, ct.byref(n)), "mdt_refill")
         return gen, int(n.value)
+
+    def refill_draws(self) -> np.ndarray:
+        """(T, 5): u, v, einc (eV), polar, azimuth (deg) the last refill drew; NaN rows for
+        trajectories it did not restart."""
+        d = np.zeros((self.T, 5))
+        self._check(self.lib.mdt_refill_draws(self.h, d.ctypes.data), "mdt_refill_draws")
+        return d
 
     def launch_count(self) -> int:
         return int(self.lib.mdt_launch_count(self.h))

@@ -9,8 +9,12 @@
  * Fortran compiler exists in the build environment, so no reference run produced
  * golden vectors.  The restatement is checked instead against (a) the reference's own
  * parameter fixtures (pes/EMT-*.pes), (b) its binary geometry fixtures
- * (conf/latt/mxt_00000001.dat and siblings) and (c) analytic properties (finite-difference
- * gradients, Newton's third law, NVE conservation, the force-sum rule of check_forces).
+ * (conf/latt/mxt_00000001.dat and siblings), (c) analytic properties (finite-difference
+ * gradients, Newton's third law, NVE conservation, the force-sum rule of check_forces) and
+ * (d) a second, independent restatement of the EMT and RuNNer energies in torch FP64
+ * (tests/test_cpu_oracle_autodiff.py, with its own neighbour search), whose energies equal
+ * this oracle's and whose autograd forces equal this oracle's hand-derived forces; the one
+ * place they must differ, the reference's H-H density-derivative quirk, they do.
  * tests/golden/runner_cgraphene_ref.npz holds this oracle's own output on the reference's
  * example network: a regression fixture, not an independent golden vector.
  *

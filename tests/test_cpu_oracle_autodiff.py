@@ -1,4 +1,5 @@
-"""A second, independent restatement of the reference's EMT energy, written in torch FP64
+"""A second, independent restatement of the reference's EMT and RuNNer HDNNP energies,
+written in torch FP64.  EMT:
 from compute_emt_1species / compute_emt_2species (src/pes_emt_mod.f90:230-477, 483-1027):
 energies must equal the oracle's (oracle/md_oracle.cpp) to round-off, and forces taken by
 automatic differentiation of that energy must equal the oracle's hand-derived forces (the
@@ -8,7 +9,10 @@ torch's.
 
 Configurations have one projectile: the reference's type1-type1 derivative quirk
 (pes_emt_mod.f90:705, eta2 of type2 in the H-H density derivative) only acts between two
-projectile atoms, where autograd and the reference deliberately differ."""
+projectile atoms, where autograd and the reference deliberately differ (checked too).
+HDNNP: the shipped RuNNer C network and a random H/C model with G2 and G3 over two
+neighbour elements; energies to 1e-9 relative, autograd forces against the oracle's
+forward-mode dG/dx contraction (getshortatomic.f90:263-322) to 1e-8 relative."""
 import math
 
 import numpy as np
@@ -167,3 +171,129 @@ def test_oracle_keeps_the_reference_h_h_derivative_quirk(oracle_lib):
             assert d < 1e-9, d
         else:
             assert d > 1e-4, d
+
+
+# ---------------------------------------------------------------------------------------
+# RuNNer HDNNP (compute_nene): a torch restatement of the energy from the symmetry-function
+# definitions (atomsymfunction2.f90, atomsymfunction3Andi.f90, getcutoff.f90), the scaling of
+# getshortatomic.f90:174-236 and the network of calconenn.f90:83-153, with its own periodic
+# neighbour search; forces by autograd against the oracle's forward-mode dG/dx contraction.
+# ---------------------------------------------------------------------------------------
+ANG2BOHR = 1.0 / BOHR2ANG
+HA2EV = 27.21138602
+
+
+def _cutoff(kind, r, rc):
+    x = r / rc
+    if kind == 1:
+        return 0.5 * (torch.cos(math.pi * x) + 1.0)
+    if kind == 6:
+        return ((15.0 - 6.0 * x) * x - 10.0) * x ** 3 + 1.0
+    raise ValueError(kind)
+
+
+def _act(a, x):
+    return {"t": torch.tanh, "l": lambda v: v, "p": lambda v: torch.log(torch.exp(v) + 1.0),
+            "s": torch.sigmoid}[a](x)
+
+
+def hdnnp_energy(model, elem, r_ang, simbox):
+    """Total energy (eV) of one configuration; r_ang a leaf tensor (N, 3) in A."""
+    box = np.asarray(simbox, float)
+    x = r_ang * ANG2BOHR
+    lat = torch.tensor(box.T * ANG2BOHR)  # rows: lattice vectors (bohr)
+    n = x.shape[0]
+    rc_max = max(sf.rc for sfs in model.sfs for sf in sfs)
+    # image range from the plane spacings
+    inv = np.linalg.inv(box.T * ANG2BOHR)
+    reach = [int(math.ceil(rc_max * np.linalg.norm(inv[:, d]))) for d in range(3)]
+    shifts = np.array([(a, b, c) for a in range(-reach[0], reach[0] + 1) for b in range(-reach[1], reach[1] + 1)
+                       for c in range(-reach[2], reach[2] + 1)], float)
+    sh = torch.tensor(shifts) @ lat  # (S, 3)
+    zs = np.array([model.z[e] for e in elem])
+    etot = torch.zeros((), dtype=torch.float64)
+    for i in range(n):
+        e = elem[i]
+        pos = (x[None, :, :] + sh[:, None, :]).reshape(-1, 3)  # every image of every atom
+        zn = np.tile(zs, len(shifts))
+        d = pos - x[i]
+        r2 = (d * d).sum(1)
+        self_mask = np.zeros(len(zn), bool)
+        self_mask[np.where(np.all(shifts == 0, axis=1))[0][0] * n + i] = True
+        keep = ((r2.detach().numpy() <= rc_max ** 2) & ~self_mask)
+        d, zn = d[keep], zn[keep]
+        r = torch.sqrt(r2[keep])  # (the atom itself, at distance 0, is out before the square root)
+        G = []
+        for sf in model.sfs[e]:
+            inside = r <= sf.rc
+            if sf.type == 2:
+                m = torch.tensor((zn == sf.e1)) & inside
+                rr = r[m]
+                G.append(torch.sum(torch.exp(-sf.eta * (rr - sf.rshift) ** 2) * _cutoff(model.cutoff_type, rr, sf.rc)))
+            else:
+                q3, q4 = np.triu_indices(len(r), 1)
+                ok = (((zn[q3] == sf.e1) & (zn[q4] == sf.e2)) | ((zn[q3] == sf.e2) & (zn[q4] == sf.e1)))
+                q3, q4 = q3[ok], q4[ok]
+                rij, rik = r[q3], r[q4]
+                djk = d[q3] - d[q4]
+                rjk = torch.sqrt((djk * djk).sum(1))
+                m = (rij <= sf.rc) & (rik <= sf.rc) & (rjk <= sf.rc)
+                rij, rik, rjk = rij[m], rik[m], rjk[m]
+                cos = (d[q3][m] * d[q4][m]).sum(1) / (rij * rik)
+                plam = 1.0 + sf.lam * cos
+                ang = torch.where(plam > 0, plam, torch.zeros_like(plam)) ** sf.zeta
+                fc = (_cutoff(model.cutoff_type, rij, sf.rc) * _cutoff(model.cutoff_type, rik, sf.rc) *
+                      _cutoff(model.cutoff_type, rjk, sf.rc))
+                G.append(2.0 ** (1.0 - sf.zeta) * torch.sum(ang * torch.exp(-sf.eta * (rij ** 2 + rik ** 2 + rjk ** 2))
+                                                         * fc))
+        G = torch.stack(G)
+        if model.scalesym:
+            smin = torch.tensor(np.asarray(model.smin[e], float))
+            smax = torch.tensor(np.asarray(model.smax[e], float))
+            G = (G - smin) / (smax - smin) * (model.scmax - model.scmin) + model.scmin
+        nodes, w = model.nodes[e], np.asarray(model.weights[e], float)
+        val, ic = G, 0
+        for layer in range(1, len(nodes)):
+            W_ = torch.tensor(w[ic:ic + nodes[layer - 1] * nodes[layer]].reshape(nodes[layer - 1], nodes[layer]))
+            ic += nodes[layer - 1] * nodes[layer]
+            b = torch.tensor(w[ic:ic + nodes[layer]])
+            ic += nodes[layer]
+            s = val @ W_ + b
+            acts = model.acts[e][layer - 1]
+            val = torch.stack([_act(acts[k], s[k]) for k in range(nodes[layer])])
+        etot = etot + val[0]
+    return etot * HA2EV
+
+
+def _wrapped(r, box):
+    f = r @ np.linalg.inv(box).T
+    f -= np.floor(f)
+    return f @ box.T
+
+
+@pytest.mark.parametrize("case", ["shipped C network", "random H/C G2+G3"])
+def test_hdnnp_oracle_forces_equal_autodiff(oracle_lib, case):
+    from pathlib import Path
+
+    from md_tian2_gb300 import nene
+    from oracle.oracle import NNOracle
+    gold = Path(__file__).resolve().parent / "golden"
+    if case.startswith("shipped"):
+        m = nene.load_npz(gold / "runner_cgraphene.npz")
+        g = np.load(gold / "cgraphene_geometry.npz")
+        r0, box = _wrapped(g["r"], g["simbox"]), g["simbox"]
+        elem = np.zeros(len(r0), int)
+    else:
+        rng = np.random.default_rng(3)
+        u = W.h_on_graphene(rng, 1.0, z0=1.6, k=3)
+        m = nene.random_model(["H", "C"], hidden=(12, 10), act="t", seed=2, neighbours=["H", "C"])
+        m.cutoff_type = 6
+        r0, box = _wrapped(u.r[:, 0, :], u.simbox), u.simbox
+        elem = np.array([0] + [1] * (u.natoms - 1))
+    E0, F0 = NNOracle(m).energy_force(elem, r0, box)
+    r = torch.tensor(r0, dtype=torch.float64, requires_grad=True)
+    e = hdnnp_energy(m, elem, r, box)
+    e.backward()
+    f = -r.grad.numpy()
+    assert abs(e.item() - E0) < 1e-9 * max(1.0, abs(E0)), (e.item(), E0)
+    assert np.abs(f - F0).max() < 1e-8 * max(1.0, np.abs(F0).max()), np.abs(f - F0).max()

@@ -1,11 +1,15 @@
-"""GPU parity of the BF16 tensor-core network (MDT_PREC_BF16: the thread-per-atom kernel with
-its four network GEMMs per 128-atom tile on tcgen05, BF16 operands, FP32 accumulation in
-TMEM; descriptors, activations, scaling and forces in FP32) against the FP64 oracle.
+"""GPU parity of the tensor-core network (the thread-per-atom kernel with its four network
+GEMMs per 128-atom tile on tcgen05, FP32 accumulation in TMEM; descriptors, activations,
+scaling and forces in FP32) against the FP64 oracle, in its two operand formats:
+MDT_PREC_BF16 (BF16 operands) and MDT_PREC_BF16X3 (every operand split in a BF16 high and
+low part, three MMAs per K step).
 
-Bars, stated per model: force RMSE below 1e-2 of the force RMS and energies within 5e-3
-relative of the FP64 oracle (BF16 keeps 8 significant bits: one rounding of every operand
-of a 24-32-32-1 network; the random test networks reach several eV per atom); the trained
-surrogate's forces within 5 meV/A RMSE of its FP32 evaluation.  Results of the same model in FP32 agree with BF16 to the same bars, so a
+Bars, stated per format: BF16 force RMSE below 1e-2 of the force RMS and energies within
+5e-3 relative of the FP64 oracle (BF16 keeps 8 significant bits: one rounding of every
+operand of a 24-32-32-1 network; the random test networks reach several eV per atom);
+BF16X3 force RMSE below 2e-4 of the force RMS and energies within 1e-4 relative (about 16
+significant bits, near the FP32 kernel's 1e-4 and 5e-5); the trained surrogate's forces
+within 5 meV/A (BF16) and 0.5 meV/A (BF16X3) RMSE of its FP32 evaluation.  Results of the same model in FP32 agree with BF16 to the same bars, so a
 wrong operand layout (which would scramble weights) cannot pass."""
 import numpy as np
 import pytest
@@ -18,7 +22,7 @@ from md_tian2_gb300.engine import PES_EMT, PES_NENE, PES_SURROGATE, Engine, SimP
 from md_tian2_gb300.surrogate import shipped_surrogate
 
 pytestmark = pytest.mark.gpu
-F_REL, E_REL = 1e-2, 5e-3
+BARS = {"bf16": (1e-2, 5e-3), "bf16x3": (2e-4, 1e-4)}  # force RMSE / force RMS, energy relative
 
 
 def _engine(us, m, kind=PES_NENE, emt=None, margin=0.1, names=("H", "Au")):
@@ -49,14 +53,16 @@ def _scaled(us, m):
     return m
 
 
+@pytest.mark.parametrize("prec", ["bf16", "bf16x3"])
 @pytest.mark.parametrize("hidden,act", [((32, 32), "p"), ((32,), "t"), ((20, 25), "s")])
-def test_bf16_network_matches_oracle(built_lib, oracle_lib, hidden, act):
+def test_bf16_network_matches_oracle(built_lib, oracle_lib, hidden, act, prec):
     from oracle.oracle import NNOracle
+    F_REL, E_REL = BARS[prec]
     us = W.config2(9, seed=61)
     m = _scaled(us[:4], _model(3, hidden, act))
     eng = _engine(us, m)
     assert eng.nn_radial_kernel(True)
-    eng.calc_force(SimParams(), precision="bf16")
+    eng.calc_force(SimParams(), precision=prec)
     out = eng.download()
     eng.close()
     o = NNOracle(m)
@@ -74,13 +80,16 @@ def test_bf16_network_matches_oracle(built_lib, oracle_lib, hidden, act):
     assert err > 0.0  # the tensor-core path really rounds its operands
 
 
-def test_bf16_energy_only_and_packs(built_lib, oracle_lib):
-    """A ragged batch of several packs: BF16 against FP32 on the same kernel, forces and
-    energies, and the energy-only evaluation equals the energies of the full one."""
+@pytest.mark.parametrize("tprec", ["bf16", "bf16x3"])
+def test_bf16_energy_only_and_packs(built_lib, oracle_lib, tprec):
+    """A ragged batch of several packs: the tensor-core network against FP32 on the same
+    kernel, forces and energies, and the energy-only evaluation equals the energies of the
+    full one."""
+    F_REL, E_REL = BARS[tprec]
     us = W.config2(60, seed=62)
     m = _scaled(us[:8], _model(5))
     res = {}
-    for prec in ("fp32", "bf16"):
+    for prec in ("fp32", tprec):
         eng = _engine(us, m)
         eng.calc_force(SimParams(), precision=prec)
         o = eng.download()
@@ -88,32 +97,34 @@ def test_bf16_energy_only_and_packs(built_lib, oracle_lib):
         o["epot_only"] = eng.download()["epot"]
         res[prec] = o
         eng.close()
-    a, b = res["bf16"], res["fp32"]
+    a, b = res[tprec], res["fp32"]
     rms = np.sqrt(np.mean(b["f"] ** 2))
     assert np.sqrt(np.mean((a["f"] - b["f"]) ** 2)) < F_REL * rms
     assert np.all(np.abs(a["epot"] - b["epot"]) < E_REL * np.maximum(1.0, np.abs(b["epot"])))
     assert np.allclose(a["epot_only"], a["epot"], rtol=0, atol=1e-9)
 
 
-def test_bf16_shipped_surrogate_md_steps(built_lib, oracle_lib):
-    """The trained surrogate: forces within 5 meV/A RMSE of its FP32 evaluation, and 20 fused
-    MD steps in BF16 track the FP32 steps (positions within 1e-3 A)."""
+@pytest.mark.parametrize("tprec,fbar,rbar", [("bf16", 5e-3, 1e-3), ("bf16x3", 5e-4, 1e-4)])
+def test_bf16_shipped_surrogate_md_steps(built_lib, oracle_lib, tprec, fbar, rbar):
+    """The trained surrogate: forces within 5 meV/A (BF16) / 0.5 meV/A (BF16X3) RMSE of its
+    FP32 evaluation, and 20 fused MD steps track the FP32 steps (positions within 1e-3 /
+    1e-4 A)."""
     us = W.config2(16, seed=63)
     emt = W.emt_params()
     m = shipped_surrogate()
     sp = SimParams(step=0.1, gamma_const=1e-3, seed=5)
     res = {}
-    for prec in ("fp32", "bf16"):
+    for prec in ("fp32", tprec):
         eng = _engine(us, m, kind=PES_SURROGATE, emt=emt)
         eng.calc_force(sp, precision=prec)
         f0 = eng.download()["f"]
         eng.md_steps(20, sp, precision=prec)
         res[prec] = (f0, eng.download(), eng.query(sp))
         eng.close()
-    fa, a, qa = res["bf16"]
+    fa, a, qa = res[tprec]
     fb, b, qb = res["fp32"]
-    assert np.sqrt(np.mean((fa - fb) ** 2)) < 5e-3
-    assert np.abs(a["r"] - b["r"]).max() < 1e-3
+    assert np.sqrt(np.mean((fa - fb) ** 2)) < fbar
+    assert np.abs(a["r"] - b["r"]).max() < rbar
     assert (qa["status"] == qb["status"]).all() and (qa["steps_done"] == 20).all()
 
 

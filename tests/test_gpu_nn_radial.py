@@ -202,3 +202,27 @@ def test_radial_repack_over_running_trajectories(built_lib, oracle_lib):
     (a, qa), (b, qb) = res[True], res[False]
     assert np.abs(a["r"] - b["r"]).max() < 1e-5
     assert (qa["status"] == qb["status"]).all() and (qa["steps_done"] == qb["steps_done"]).all()
+
+
+def test_autotune_picks_a_shape_and_restores_the_state(built_lib, oracle_lib):
+    """mdt_autotune times every candidate (CTA cap x skin) from the same saved state, keeps
+    the fastest and puts the state back: positions, velocities, step counts and observables
+    are bit-identical to before the call, and the batch runs on with the chosen shape."""
+    from md_tian2_gb300.surrogate import shipped_surrogate
+    us = W.config2(256, seed=27)
+    emt = W.emt_params()
+    sp = SimParams(step=0.1, gamma_const=1e-3, seed=3, pul=6.05, use_exit=True)
+    eng = _engine(us, shipped_surrogate(), kind=PES_SURROGATE, emt=emt)
+    eng.calc_force(sp, precision="fp32")
+    eng.md_steps(7, sp, precision="fp32")
+    before, qb, ob = eng.download(), eng.query(sp), eng.observables()
+    res = eng.autotune(sp, "fp32", nsteps=10)
+    after, qa, oa = eng.download(), eng.query(sp), eng.observables()
+    assert res["block"] in (256, 384, 512) and res["skin_A"] in (0.5, 0.75, 1.0) and res["ms_per_step"] > 0
+    for k in ("r", "v", "f"):
+        assert np.array_equal(before[k], after[k]), k
+    assert (qa["steps_done"] == qb["steps_done"]).all() and (qa["status"] == qb["status"]).all()
+    assert np.array_equal(ob["cl_appr"], oa["cl_appr"])
+    eng.md_steps(5, sp, precision="fp32")
+    assert (eng.query(sp)["steps_done"] >= qb["steps_done"]).all()
+    eng.close()

@@ -129,3 +129,49 @@ def test_campaign_streams_trajectories(built_lib):
     assert (res.steps <= 200).all() and (res.steps > 0).all()
     assert (res.z_f[res.status == 1] > 6.05).all()
     assert np.isfinite(res.ekin_i).all() and (res.ekin_i > 0).all()
+
+
+def test_refill_matches_host_md_init(built_lib):
+    """The device refill against the host restatement of md_init (md_tian2_gb300.md_init):
+    each restarted trajectory's draws (mdt_refill_draws: u, v, einc, polar, azimuth) fed to
+    apply_pip with a numeric pip (the centroid moved to u a1 + v a2 + z0 e_z, md_init.f90:
+    498-553) and to set_proj_incidence (:829-876) give the device's projectile beads to
+    1e-12 (A, A/fs); trajectories not restarted report NaN draws."""
+    from md_tian2_gb300.md_init import apply_pip, set_proj_incidence
+    from md_tian2_gb300.universe import Universe
+    rng = np.random.default_rng(55)
+    us = []
+    for nb in (4, 8, 4):
+        u = W.h_on_metal(rng, "Pt", 3, 0.5, 10.0, 20.0, 300.0, C.PROP_ID_PILE, C.PROP_ID_PILE, z0=4.0, nbeads=nb)
+        u.r[0] += rng.normal(scale=0.05, size=u.r[0].shape)
+        u.v[0] += rng.normal(scale=0.01, size=u.v[0].shape)
+        us.append(u)
+    eng = Engine(0)
+    eng.read_emt(W.emt_params("H", "Pt"))
+    eng.define(us)
+    eng.upload()
+    up = eng.download()
+    sp = SimParams(step=0.1, seed=4)
+    eng.set_step_limit(3)
+    eng.calc_force(sp)
+    eng.md_steps(3, sp)
+    eng.set_step_limit(0)
+    gen, n = eng.refill(z0=6.5, einc=(0.2, 0.9), polar=(0.0, 40.0), azimuth=-1.0, seed=8)
+    assert n == 3
+    draws = eng.refill_draws()
+    out = eng.download()
+    for t, u in enumerate(us):
+        du, dv, e, pol, azi = draws[t]
+        box = u.simbox
+        pip = [du * box[0, 0] + dv * box[0, 1], du * box[1, 0] + dv * box[1, 1], 6.5]
+        r0, v0 = eng.split(up["r"], t)[0], eng.split(up["v"], t)[0]  # (nb, 3) uploaded projectile
+        proj = Universe(r=r0[None].copy(), v=v0[None].copy(), m=u.m[:1].copy(), idx=np.array([1], np.int32),
+                        is_fixed=np.zeros((1, u.nbeads, 3), bool), simbox=box.copy(), names=["H"],
+                        is_proj=np.array([True]), algo=np.array([C.PROP_ID_PILE], np.int32))
+        host = set_proj_incidence(apply_pip(proj, pip, rng), einc=e, polar_deg=pol, azimuth=str(azi))
+        assert np.abs(eng.split(out["r"], t)[0] - host.r[0]).max() < 1e-12, t
+        assert np.abs(eng.split(out["v"], t)[0] - host.v[0]).max() < 1e-12, t
+        assert 0.2 <= e <= 0.9 and 0.0 <= pol <= 40.0 and 0.0 <= azi < 360.0
+    gen2, n2 = eng.refill(seed=9)  # nothing stopped: nothing restarted, every row NaN
+    assert n2 == 0 and np.isnan(eng.refill_draws()).all()
+    eng.close()
