@@ -72,7 +72,7 @@ def parse():
     ap.add_argument("--hdnnp-traj", type=int, default=2048, help="trajectories of the HDNNP arm (0: skip)")
     ap.add_argument("--arm-steps", type=int, default=20, help="timed MD steps of the RPMD and HDNNP arms")
     ap.add_argument("--no-nve", action="store_true", help="skip the surrogate's NVE drift runs")
-    ap.add_argument("--profile-arm", choices=["fp32", "bf16", "emt"], default=None,
+    ap.add_argument("--profile-arm", choices=["fp32", "bf16", "bf16x3", "emt"], default=None,
                     help="run only this arm's warm-up and timed MD steps (no report): the workload of the "
                          "ncu captures under profiles/")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
@@ -596,7 +596,7 @@ def run_ours(args):
     # ---- accuracy of every network arithmetic: held-out force RMSE against FP64 EMT and NVE drift
     PRECS = ("fp32", "bf16", "bf16x3")  # network on CUDA cores, tensor cores with BF16 / split BF16 operands
     acc = None
-    if rank == 0 and args.rmse_traj > 0:
+    if rank == 0 and args.rmse_traj > 0 and not args.profile_arm:
         from md_tian2_gb300.surrogate import nve_drift
         held = generate_dataset(args.rmse_traj, 8, 50, seed=4242 + rank, device=local)
         acc = {"configs": len(held.universes),
@@ -736,13 +736,8 @@ def run_ours(args):
         rpmd = rpmd_arm(args, local, stream, torch, peak64.value, peak.value)
     if rank == 0 and args.hdnnp_traj > 0:
         hdnnp = hdnnp_arm(args, local, stream, torch, peak.value, peak64.value)
-    traffic = None
-    prof = ROOT / "profiles" / ("nnr_surrogate_traffic.json" if radial else "nnf_surrogate_traffic.json")
-    if prof.exists():
-        try:
-            traffic = json.loads(prof.read_text()).get("bytes_per_launch")
-        except Exception:
-            traffic = None
+    traffic = profile_bytes("nnr_surrogate_traffic.json" if radial else "nnf_surrogate_traffic.json")
+    traffic_emt = profile_bytes("emt_md_steps_traffic.json")
 
     elapsed, elapsed_emt = ms * 1e-3, ms_emt * 1e-3
     elapsed, e2e_s, elapsed_emt, done_all, e_atoms_all, done_emt_all = replica_report(
@@ -781,7 +776,10 @@ def run_ours(args):
                          "dtype": args.precision, "clocks": clocks_emt,
                          "roofline": {"bound": args.precision, "achieved": emt_flop / (elapsed_emt / args.steps) / 1e12,
                                       "peak": (peak64.value if args.precision == "fp64" else peak.value) / 1e12,
-                                      "unit": "TFLOP/s"}},
+                                      "unit": "TFLOP/s",
+                                      "frac": emt_flop / (elapsed_emt / args.steps)
+                                      / (peak64.value if args.precision == "fp64" else peak.value),
+                                      "traffic": traffic_emt if args.precision == "fp64" else None}},
             "speedup_vs_fp64_emt": value / emt_value,
             "accuracy": acc,
             "fallback": {"bead_evaluations": bead_evals, "emt_fallbacks": fb_count,
@@ -804,6 +802,19 @@ def run_ours(args):
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+def profile_bytes(name):
+    """DRAM bytes per MD step of a kernel, from the summary of its ncu capture under profiles/
+    (dram__bytes_read.sum + dram__bytes_write.sum, scaled to the bench's workload); None when
+    no capture is committed."""
+    prof = ROOT / "profiles" / name
+    if not prof.exists():
+        return None
+    try:
+        return json.loads(prof.read_text()).get("bytes_per_step")
+    except (OSError, ValueError):
+        return None
 
 
 def main():

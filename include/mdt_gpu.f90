@@ -343,6 +343,14 @@ module mdt_gpu
             real(c_double), intent(out) :: flops_per_s
         end function
 
+        integer(c_int32_t) function mdt_rng_deviates(kind, seed, traj, step, stream, n, out) &
+                bind(C, name="mdt_rng_deviates")
+            import :: c_int32_t, c_int64_t, c_double
+            integer(c_int32_t), value :: kind, traj, step, stream
+            integer(c_int64_t), value :: seed, n
+            real(c_double), intent(out) :: out(*)
+        end function
+
         integer(c_int64_t) function mdt_launch_count(ctx) bind(C, name="mdt_launch_count")
             import :: c_int64_t, c_ptr
             type(c_ptr), value :: ctx

@@ -371,6 +371,16 @@ int32_t mdt_emt_force_noalloc(int32_t natoms, const int32_t *idx, const double *
  * counterpart (the reference has no GPU code). */
 int32_t mdt_peak_fma(int32_t precision, int32_t iters, double *flops_per_s);
 
+/* The deviates the propagators draw, for statistical checks of the generator (the
+ * reference's counterpart is its normal deviate, src/useful_things.f90:121-173, Box-Muller
+ * in FP64 on the compiler's random_number).  out[i] = the deviate of (seed, traj, step,
+ * slot i, stream) for i < n: kind 0 the N(0,1) deviate of the Langevin/PILE/Andersen noise
+ * (Box-Muller in FP32 on 24-bit uniforms of a Philox4x32-10 block), kind 1 the uniform in
+ * [0, 1) with 53 random bits; stream 1 Langevin, 2 PILE, 3 Andersen velocities, 4 Andersen
+ * uniforms, 5 refill.  n <= 2^32; allocates and frees its own device buffer. */
+int32_t mdt_rng_deviates(int32_t kind, uint64_t seed, int32_t traj, int32_t step, int32_t stream, int64_t n,
+                         double *out);
+
 /* ---- work counters ---------------------------------------------------------- */
 /* number of kernel launches this context issued since creation */
 int64_t mdt_launch_count(const mdt_ctx *ctx);

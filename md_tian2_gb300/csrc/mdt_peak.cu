@@ -1,4 +1,5 @@
-// mdt_peak.cu -- FP64 / FP32 fused-multiply-add throughput microbenchmark.
+// mdt_peak.cu -- FP64 / FP32 fused-multiply-add throughput microbenchmark, and a read-out of
+// the thermostats' deviate streams for statistical checks.
 //
 // The EMT force kernels are bound by CUDA-core arithmetic, not by HBM or tensor cores,
 // so their roofline denominator is the GPU's measured FMA rate: every thread keeps 8
@@ -7,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/mdt_gpu.h"
+#include "mdt_common.cuh"
 
 namespace {
 
@@ -51,7 +53,35 @@ template <typename T> double run(int iters) {
     return flops / (ms * 1e-3);
 }
 
+// out[i] = the deviate the propagators draw at (seed, traj, step, slot i, stream)
+__global__ void deviates_kernel(double *out, int64_t n, int32_t kind, uint64_t seed, uint32_t traj,
+                                uint32_t step, uint32_t stream) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = kind == 0 ? mdt::normal_deviate(seed, traj, step, (uint32_t)i, stream)
+                           : mdt::uniform_deviate(seed, traj, step, (uint32_t)i, stream);
+}
+
 }  // namespace
+
+extern "C" int32_t mdt_rng_deviates(int32_t kind, uint64_t seed, int32_t traj, int32_t step, int32_t stream,
+                                    int64_t n, double *out) {
+    if (!out || n < 0 || n > ((int64_t)1 << 32) || (kind != 0 && kind != 1) || traj < 0 || step < 0 ||
+        stream < 1 || stream > 5)
+        return MDT_ERR_ARG;
+    if (n == 0) return MDT_OK;
+    double *d = nullptr;
+    if (cudaMalloc(&d, sizeof(double) * n) != cudaSuccess) return MDT_ERR_NOMEM;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t want = (n + 255) / 256;
+    const int grid = (int)(want < (int64_t)sms * 16 ? want : (int64_t)sms * 16);
+    deviates_kernel<<<grid, 256>>>(d, n, kind, seed, (uint32_t)traj, (uint32_t)step, (uint32_t)stream);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpy(out, d, sizeof(double) * n, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    return e == cudaSuccess ? MDT_OK : MDT_ERR_CUDA;
+}
 
 extern "C" int32_t mdt_peak_fma(int32_t precision, int32_t iters, double *flops_per_s) {
     if (!flops_per_s || iters < 1) return MDT_ERR_ARG;
