@@ -314,6 +314,17 @@ def run_reference(args):
 # 2*(24*32+32*32+32) + 64 softplus x 40, backward 2*(32+32*32+24*32) + 64 derivative x 20.
 FLOP_SURR_ENTRY = 70 + 156 + 252 + 14
 FLOP_SURR_ATOM = 2 * (24 * 32 + 32 * 32 + 32) + 64 * 40 + 2 * (32 + 32 * 32 + 24 * 32) + 64 * 20
+# the part of it the tensor-core arithmetics run as GEMMs: layers 1 and 2 forward and the two
+# backward products to dE/dG (the 32 -> 1 output layer stays on the CUDA cores)
+FLOP_SURR_GEMM = 2 * (24 * 32 + 32 * 32) + 2 * (32 * 32 + 24 * 32)
+
+
+def bf16_peak():
+    """Dense BF16 tensor peak of this machine's GB300 (TFLOP/s, burst) from MEASURED_PEAKS.json."""
+    try:
+        return float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["bf16_tflops"])
+    except (OSError, ValueError, KeyError):
+        return 1900.0  # fallback: an earlier GB300 measurement
 
 
 def replica_report(times, counts, dist=None, device="cpu"):
@@ -755,6 +766,15 @@ def run_ours(args):
                                "roofline": {"bound": "fp32", "achieved": surr_flop / (el_q / args.steps) / 1e12,
                                             "peak": peak.value / 1e12, "unit": "TFLOP/s",
                                             "frac": surr_flop / (el_q / args.steps) / peak.value}}
+            if q != "fp32":
+                # the network GEMMs against the tensor peak (algorithmic FLOP: BF16X3 issues three
+                # MMAs per K step for the same products)
+                gemm = FLOP_SURR_GEMM * int(np.sum(natoms)) / (el_q / args.steps) / 1e12
+                network_arms[q]["tensor_roofline"] = {
+                    "bound": "tensor", "achieved": gemm, "peak": bf16_peak(), "unit": "TFLOP/s",
+                    "frac": gemm / bf16_peak(), "mma_per_k_step": 3 if q == "bf16x3" else 1,
+                    "flop_per_step": FLOP_SURR_GEMM * int(np.sum(natoms)),
+                    "peak_source": "MEASURED_PEAKS.json bf16_tflops (cuBLAS BF16 GEMM, burst)"}
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,

@@ -351,6 +351,13 @@ module mdt_gpu
             real(c_double), intent(out) :: out(*)
         end function
 
+        integer(c_int32_t) function mdt_wait_check(max_polls, arrive, timed_out, ms) bind(C, name="mdt_wait_check")
+            import :: c_int32_t, c_double
+            integer(c_int32_t), value :: max_polls, arrive
+            integer(c_int32_t), intent(out) :: timed_out
+            real(c_double), intent(out) :: ms
+        end function
+
         integer(c_int64_t) function mdt_launch_count(ctx) bind(C, name="mdt_launch_count")
             import :: c_int64_t, c_ptr
             type(c_ptr), value :: ctx

@@ -381,6 +381,15 @@ int32_t mdt_peak_fma(int32_t precision, int32_t iters, double *flops_per_s);
 int32_t mdt_rng_deviates(int32_t kind, uint64_t seed, int32_t traj, int32_t step, int32_t stream, int64_t n,
                          double *out);
 
+/* The bounded wait of the tensor-core network (every mbarrier wait of a GEMM round gives up
+ * after max_polls tries, 0 = the kernels' own limit, sets an error word that mdt_synchronize
+ * reports, and the kernel returns instead of stalling), run alone on one CTA: with arrive = 0
+ * nothing completes the barrier and timed_out must come back 1, with arrive = 1 a thread
+ * arrives first and it must come back 0; ms (may be NULL) receives the kernel's time.
+ * Lets a caller check on its own GPU that a lost MMA completion ends in an error status,
+ * not a hang.  No reference counterpart (the reference has no GPU code). */
+int32_t mdt_wait_check(int32_t max_polls, int32_t arrive, int32_t *timed_out, double *ms);
+
 /* ---- work counters ---------------------------------------------------------- */
 /* number of kernel launches this context issued since creation */
 int64_t mdt_launch_count(const mdt_ctx *ctx);

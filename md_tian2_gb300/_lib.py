@@ -78,6 +78,7 @@ SIGNATURES = {
     "mdt_device_state": (ct.c_int32, [ct.c_void_p, ct.POINTER(ct.c_void_p), ct.POINTER(ct.c_int64)]),
     "mdt_launch_count": (ct.c_int64, [ct.c_void_p]),
     "mdt_peak_fma": (ct.c_int32, [ct.c_int32, ct.c_int32, c_double_p]),
+    "mdt_wait_check": (ct.c_int32, [ct.c_int32, ct.c_int32, ct.POINTER(ct.c_int32), c_double_p]),
     "mdt_rng_deviates": (ct.c_int32, [ct.c_int32, ct.c_uint64, ct.c_int32, ct.c_int32, ct.c_int32, ct.c_int64,
                                       c_double_p]),
     "mdt_nn_set_model": (ct.c_int32, [ct.c_void_p, ct.POINTER(NNModelC), ct.c_int32, c_int32_p, ct.c_int32]),

@@ -39,6 +39,7 @@
 #include "mdt_acsf.cuh"
 #include "mdt_prop.cuh"
 #include "mdt_tc.cuh"
+#include "../../include/mdt_gpu.h"
 
 namespace mdt {
 
@@ -1432,4 +1433,46 @@ cudaError_t launch_nnr(const LaunchCfg &c, const Batch &B, const RadialNN &R, co
     return cudaErrorInvalidValue;
 }
 
+// The tensor-core network's wait, exercised alone: every thread waits (max_polls tries, as a
+// GEMM round does) on an mbarrier of one arrival; with arrive the CTA's thread 0 arrives
+// first, without it nothing ever completes the phase and every wait must give up and set
+// the error word.
+__global__ void wait_check_kernel(uint32_t max_polls, int arrive, int *err) {
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    if (arrive && threadIdx.x == 0) mbar_arrive(&bar);
+    if (!mbar_wait_bounded(&bar, 0u, max_polls)) atomicExch(err, 1);
+}
+
 }  // namespace mdt
+
+extern "C" int32_t mdt_wait_check(int32_t max_polls, int32_t arrive, int32_t *timed_out, double *ms) {
+    if (!timed_out || max_polls < 0) return MDT_ERR_ARG;
+    const uint32_t polls = max_polls == 0 ? mdt::kTcMaxPolls : (uint32_t)max_polls;
+    int *err = nullptr;
+    if (cudaMalloc(&err, sizeof(int)) != cudaSuccess) return MDT_ERR_NOMEM;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaError_t e = cudaMemset(err, 0, sizeof(int));
+    cudaEventRecord(e0);
+    if (e == cudaSuccess) mdt::wait_check_kernel<<<1, 128>>>(polls, arrive ? 1 : 0, err);
+    cudaEventRecord(e1);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    int h = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(&h, err, sizeof(int), cudaMemcpyDeviceToHost);
+    float t = 0.f;
+    if (e == cudaSuccess) cudaEventElapsedTime(&t, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(err);
+    if (e != cudaSuccess) return MDT_ERR_CUDA;
+    *timed_out = h;
+    if (ms) *ms = t;
+    return MDT_OK;
+}

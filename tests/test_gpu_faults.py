@@ -12,7 +12,10 @@ untouched.
   trajectory does, the others are unaffected.
 Every other trajectory must equal a clean run of the same batch: bit for bit where the
 kernel is deterministic (checked by running the clean batch twice), else within the
-run-to-run spread of the kernel's unordered FP32 shared-memory sums."""
+run-to-run spread of the kernel's unordered FP32 shared-memory sums.
+
+* The tensor-core network's bounded wait, on a barrier that nothing completes: it gives up
+  within its poll limit, reports the time-out, and the GPU goes on computing correctly."""
 import numpy as np
 import pytest
 
@@ -145,3 +148,32 @@ def test_nan_in_surrogate_batch(built_lib):
     assert np.all(q["steps_done"][others] == qc["steps_done"][others])
     # unordered red.shared sums: runs of the same batch differ by FP32 rounding
     _assert_others_equal(us, out, clean, clean2, skip=(4,), rtol=1e-6)
+
+
+def test_tensor_core_wait_gives_up_and_the_gpu_stays_usable(built_lib):
+    import ctypes as ct
+    from md_tian2_gb300._lib import load
+    lib = load()
+    to, ms = ct.c_int32(-1), ct.c_double(-1.0)
+    assert lib.mdt_wait_check(0, 1, ct.byref(to), ct.byref(ms)) == 0
+    assert to.value == 0  # a completed phase is seen
+    assert lib.mdt_wait_check(0, 0, ct.byref(to), ct.byref(ms)) == 0
+    assert to.value == 1  # the lost completion ends in the error word
+    assert 0.0 < ms.value < 5000.0, ms.value  # within the limit, not a hang
+    # the context-free check left the device usable: a split-BF16 evaluation right after
+    # agrees with FP32 on the same batch, and its own error word stays clear
+    us = W.config2(8, seed=65)
+    res = {}
+    for prec in ("fp32", "bf16x3"):
+        eng = Engine(0)
+        eng.read_emt(W.emt_params())
+        eng.define(us)
+        eng.read_nene(shipped_surrogate(), ["H", "Au"], max_neighbors=80)
+        eng.set_pes(PES_SURROGATE, 0.1)
+        eng.upload()
+        eng.calc_force(SimParams(), precision=prec)
+        eng.synchronize()
+        res[prec] = eng.download()["f"]
+        eng.close()
+    rms = np.sqrt(np.mean(res["fp32"] ** 2))
+    assert np.sqrt(np.mean((res["bf16x3"] - res["fp32"]) ** 2)) < 2e-4 * rms

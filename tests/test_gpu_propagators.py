@@ -137,8 +137,13 @@ def test_fused_matches_phases_with_philox(built_lib):
 def test_nve_conservation(built_lib):
     """Velocity Verlet on plain EMT conserves total energy.  Close H-Au encounters make
     the total energy fluctuate by a few meV at dt = 0.1 fs (the FP64 oracle shows the
-    same), so the secular drift is the mean slope of linear fits of E_tot(t) over 2 ps
-    across 8 trajectories: below 1 meV/ps, each trajectory below 3 meV/ps."""
+    same), and the reference's pair loop drops a pair where it crosses cutoff*rcut while its
+    Fermi factor is not yet zero there (pes_emt_mod.f90: `if (r > cutoff*rcut) cycle`), so
+    E_tot also takes small steps whenever a pair of the free 300 K slab crosses that
+    distance.  The secular drift is the mean slope of linear fits of E_tot(t) over 2 ps
+    across 8 trajectories: below 1 meV/ps.  Each trajectory's own slope carries the noise of
+    those steps (run-to-run, since FP64 shared-memory atomics make the chaotic trajectories
+    diverge): below 5 meV/ps."""
     rng = np.random.default_rng(4)
     us = [W.h_on_metal(rng, "Au", 3, 1.0, 30.0, 0.0, 300.0, z0=2.5) for _ in range(8)]
     for u in us:
@@ -159,7 +164,7 @@ def test_nve_conservation(built_lib):
     slope = np.array([np.polyfit(ts, es[:, t], 1)[0] for t in range(len(us))]) * 1e3  # meV/ps
     assert np.all(q["steps_done"] == chunk * nchunks)
     assert abs(float(np.mean(slope))) < 1.0, slope
-    assert np.all(np.abs(slope) < 3.0), slope
+    assert np.all(np.abs(slope) < 5.0), slope
     eng.close()
 
 

@@ -6,7 +6,8 @@
   ragged batch (the bench measures ~4x; the bar leaves room for a shared GPU);
 - physics: from identical initial states, the scattering observables of the reference's
   analysis (mean energy loss of scattered projectiles, sticking probability, energy-loss
-  distribution) agree with FP64 EMT within statistical error (|z| < 4, KS p > 1e-3)."""
+  distribution) agree with FP64 EMT within statistical error (|z| < 3.5, two-sample KS
+  p > 0.01)."""
 import time
 from pathlib import Path
 
@@ -70,6 +71,6 @@ def test_scattering_observables_match_fp64_emt(built_lib):
     a, b = res[PES_EMT], res[PES_SURROGATE]
     assert a.scattered.sum() > 100 and b.scattered.sum() > 100
     c = compare(b, a)
-    assert abs(c["mean_eloss_z"]) < 4.0, c
-    assert abs(c["sticking_z"]) < 4.0, c
-    assert c["ks_p"] > 1e-3, c
+    assert abs(c["mean_eloss_z"]) < 3.5, c
+    assert abs(c["sticking_z"]) < 3.5, c
+    assert c["ks_p"] > 0.01, c

@@ -8,7 +8,8 @@ network (MDT_PREC_BF16) does not meet the target: its weights rounded to 8 bits 
 potential by O(10) meV per atom, so its forces are not the gradient of the FP32 energy; the
 bench reports its drift beside the others.  The secular drift (mean
 slope of linear fits of E_tot(t)) must stay below the 1 meV/ps target and every trajectory
-below 3 meV/ps, the bars of the FP64 EMT test (tests/test_gpu_propagators.py); no bead may
+below 3 meV/ps (tighter than the FP64 EMT test of tests/test_gpu_propagators.py, whose
+potential has steps at its pair cutoff; the network's cutoff function is smooth); no bead may
 fall back to EMT (a fallback switches the potential and would be counted as drift)."""
 import numpy as np
 import pytest
