@@ -85,6 +85,7 @@ struct mdt_ctx {
     int2 *rpacks = nullptr;    // (offset into rptraj, count) per pack
     int *rptraj = nullptr;     // trajectories of the packs
     int rnpack = 0, rblock = 0;
+    bool rfull = false;         // the plan packs every trajectory of the batch (not a re-pack)
     int rmaxblock = kRBlockMax; // largest block the pack plan may use
     int *tcerr = nullptr;       // device word: a tensor-core GEMM of the network timed out
 
@@ -680,6 +681,7 @@ bool radial_plan(mdt_ctx *c, const std::vector<int> &ids = {}) {
         return false;
     c->rnpack = (int)hp.size();
     c->rblock = bestb;
+    c->rfull = ntr == c->T;
     return true;
 }
 
@@ -1117,7 +1119,10 @@ int32_t mdt_state_upload(mdt_ctx *c, const double *r, const double *v) {
     if (e == cudaSuccess) e = cudaMemsetAsync(B.status, 0, sizeof(int) * c->T, c->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(B.steps_done, 0, sizeof(int) * c->T, c->stream);
     if (e == cudaSuccess) e = launch_obs_reset(c->stream, B);
-    c->rnpack = 0;  // every trajectory runs again: the next thread-per-atom launch packs them all
+    // every trajectory runs again: a re-pack over the running ones gives way to a plan of all of
+    // them (a plan of all trajectories stays: the cells did not change, and the skin lists
+    // check every atom's displacement since their build, whatever moved it)
+    if (!c->rfull) c->rnpack = 0;
     // the uploaded state is the template of mdt_refill
     const double *cur[6] = {B.rx, B.ry, B.rz, B.vx, B.vy, B.vz};
     for (int a = 0; a < 6 && e == cudaSuccess; ++a)
@@ -1306,7 +1311,7 @@ int32_t mdt_refill(mdt_ctx *c, const mdt_refill_params *p, int32_t *generation, 
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "mdt_refill");
     if (nrefilled) *nrefilled = n;
-    if (n > 0) c->rnpack = 0;  // restarted trajectories must be in the next pack plan
+    if (n > 0 && !c->rfull) c->rnpack = 0;  // restarted trajectories must be in the next pack plan
     return MDT_OK;
 }
 

@@ -49,7 +49,7 @@ constexpr int kRW = 32;          // padded hidden width
 constexpr double kHa2eVR = 27.21138602;
 
 struct SmemR {
-    float *xh, *yh, *zh, *xl, *yl, *zl;  // [slot] unwrapped positions (bohr), FP32 hi/lo split
+    float4 *ph, *pl;                     // [slot] unwrapped positions (bohr), FP32 hi/lo split (x, y, z, 0)
     float *f3;                           // [3][bs] neighbour force accumulators (Ha/bohr)
     double *ea;                          // [slot] atomic energies (Ha)
     double *lc;                          // [8][slot] Langevin coefficients of the atom (see LcR)
@@ -98,7 +98,7 @@ __host__ __device__ constexpr size_t w_bytes(int nin, int nh, int tcm) {
 }
 
 __host__ __device__ constexpr size_t smem_r(int nin, int nh, int tc) {
-    return 6 * r16r(4 * (size_t)kRS) + r16r(12 * (size_t)kRS) + r16r(8 * (size_t)kRS) + r16r(64 * (size_t)kRS) +
+    return 2 * r16r(16 * (size_t)kRS) + r16r(12 * (size_t)kRS) + r16r(8 * (size_t)kRS) + r16r(64 * (size_t)kRS) +
            r16r(8 * (size_t)kRS) + r16r(kRS) + r16r(hb_bytes(nin, nh, tc)) + r16r(w_bytes(nin, nh, tc)) +
            r16r(16 * 2 * (size_t)nin) + r16r(4 * 2 * (size_t)nin) + 3 * r16r(4 * kRMaxTraj) + 4 * r16r(8 * kRMaxTraj) +
            r16r(12 * kRMaxTraj) + r16r(4 * 24 * kRMaxTraj) + r16r(8 * 64) + r16r(16) + r16r(8 * kTcTiles) + r16r(16);
@@ -113,12 +113,8 @@ __device__ __forceinline__ SmemR carve_r(unsigned char *base) {
         off += r16r(bytes);
         return p;
     };
-    s.xh = (float *)take(4 * (size_t)kRS);
-    s.yh = (float *)take(4 * (size_t)kRS);
-    s.zh = (float *)take(4 * (size_t)kRS);
-    s.xl = (float *)take(4 * (size_t)kRS);
-    s.yl = (float *)take(4 * (size_t)kRS);
-    s.zl = (float *)take(4 * (size_t)kRS);
+    s.ph = (float4 *)take(16 * (size_t)kRS);
+    s.pl = (float4 *)take(16 * (size_t)kRS);
     s.f3 = (float *)take(12 * (size_t)kRS);
     s.ea = (double *)take(8 * (size_t)kRS);
     s.lc = (double *)take(64 * (size_t)kRS);
@@ -163,9 +159,10 @@ struct AtomR {
 };
 
 __device__ __forceinline__ void rel_pos(const SmemR &S, const AtomR &A, int js, float &dx, float &dy, float &dz) {
-    dx = (S.xh[js] - A.xhi) + (S.xl[js] - A.xli);
-    dy = (S.yh[js] - A.yhi) + (S.yl[js] - A.yli);
-    dz = (S.zh[js] - A.zhi) + (S.zl[js] - A.zli);
+    const float4 h = S.ph[js], l = S.pl[js];  // one 16-byte load per part
+    dx = (h.x - A.xhi) + (l.x - A.xli);
+    dy = (h.y - A.yhi) + (l.y - A.yli);
+    dz = (h.z - A.zhi) + (l.z - A.zli);
 }
 
 // Skin-list entry: j (bits 0-9) and the image (n1, n2, n3) in the unwrapped frame, each
@@ -483,10 +480,11 @@ __device__ __forceinline__ float nnr_network(const RadialNN &R, const SmemR &S, 
 // BLA / BLB: block length of the shifted-Gaussian recurrence of group 0 / 1 (0: one 2^x
 // per function).  Descriptors: the scaled symmetry functions in the padded grouped order,
 // the trajectory's out-of-range flag, the neighbour-list overflow and the nearest
-// neighbour entry (rmin2).
+// neighbour entry (rmin2) with its atom (near: the first entry of the walk at that
+// distance).
 template <int KA, int KB, int BLA, int BLB>
 __device__ __forceinline__ void nnr_descr(const RadialNN &R, const NNScratch &X, const SmemR &S, const AtomR &A,
-                                          const unsigned *sk, int cnt, int *flag, float &rmin2,
+                                          const unsigned *sk, int cnt, int *flag, float &rmin2, int &near,
                                           float (&xs)[KA + KB]) {
     constexpr int KT = KA + KB;
     float G[KT];
@@ -498,6 +496,7 @@ __device__ __forceinline__ void nnr_descr(const RadialNN &R, const NNScratch &X,
         constexpr int K = g == 0 ? KA : KB, off = g == 0 ? 0 : KA, BL = g == 0 ? BLA : BLB;
         const bool inside = r2 < R.rc2;
         nn += inside ? 1 : 0;
+        near = r2 < rmin2 ? js : near;
         rmin2 = fminf(rmin2, r2);
         const float r = r2 * rsqrtf(r2);
         const float fc = inside ? fc_of_s(r2 * R.inv_rc2) : 0.f;
@@ -1164,12 +1163,8 @@ __global__ void __launch_bounds__(kRBlockMax, 1)
                 A.xli = (float)(x - (double)A.xhi);
                 A.yli = (float)(y - (double)A.yhi);
                 A.zli = (float)(z - (double)A.zhi);
-                S.xh[tid] = A.xhi;
-                S.yh[tid] = A.yhi;
-                S.zh[tid] = A.zhi;
-                S.xl[tid] = A.xli;
-                S.yl[tid] = A.yli;
-                S.zl[tid] = A.zli;
+                S.ph[tid] = make_float4(A.xhi, A.yhi, A.zhi, 0.f);
+                S.pl[tid] = make_float4(A.xli, A.yli, A.zli, 0.f);
                 if (mode == 2 && !isfinite((rx + ry) + (rz + B.vx[k]) + (B.vy[k] + B.vz[k])))
                     S.tr_bad[cur * kRMaxTraj + A.s] = 1;
                 if (R.skin > 0.f) {
@@ -1221,6 +1216,7 @@ __global__ void __launch_bounds__(kRBlockMax, 1)
             const float half = 0.5f * R.skin * (float)kBohr2Ang;
             float fix = 0.f, fiy = 0.f, fiz = 0.f;
             float rmin2 = INFINITY;  // nearest neighbour entry (bohr^2): the closest approach of atom 0
+            int near_js = -1;        // its atom (slot of the pack)
             const unsigned *sk = reinterpret_cast<const unsigned *>(X.skw) + A.base * X.skcap;
             int cnt = -1;
             float xs[KT], dG[KT];
@@ -1239,7 +1235,7 @@ __global__ void __launch_bounds__(kRBlockMax, 1)
                     r0[2] = B.rz[k];
                 }
                 cnt = R.skin > 0.f ? X.skcnt[k] : -1;
-                nnr_descr<KA, KB, BLA, BLB>(R, X, S, A, sk, cnt, flag, rmin2, xs);
+                nnr_descr<KA, KB, BLA, BLB>(R, X, S, A, sk, cnt, flag, rmin2, near_js, xs);
             }
             float e_at = 0.f;
             if constexpr (TC) {
@@ -1326,20 +1322,38 @@ __global__ void __launch_bounds__(kRBlockMax, 1)
                 // trajectory observables by the projectile's thread; the closest approach is
                 // the nearest entry of its skin list (every image within the cutoff + skin)
                 if (A.i == 0) {
-                    // the bounce partner: the first entry of the list at the nearest distance
+                    // the bounce partner: the atom of the nearest entry, found by the descriptor
+                    // walk; its displacement is the minimum image of the unwrapped difference
+                    // (the nearest atom lies far inside half a cell).  Should that image not
+                    // reproduce the entry's distance (a cell too skewed for rounding fractional
+                    // coordinates), the step has no partner and the bounce segment goes on.
                     int near = -1;
                     float nx = 0.f, ny = 0.f, nz = 0.f;
-                    if (rmin2 < INFINITY)
-                        for_neighbours(R, S, A, sk, cnt, [&](auto, int js, float dx, float dy, float dz, float r2) {
-                            if (near < 0 && r2 <= rmin2 * 1.000001f) {
-                                near = js - A.st;
-                                nx = dx;
-                                ny = dy;
-                                nz = dz;
-                            }
-                        });
-                    observe_step(B, P, T, step, rmin2 < INFINITY ? (double)sqrtf(rmin2) * kBohr2Ang : kDefaultReal,
-                                 near, nx, ny, nz);
+                    if (rmin2 < INFINITY && near_js >= 0) {
+                        float dx, dy, dz;
+                        rel_pos(S, A, near_js, dx, dy, dz);
+                        const float *TL = S.tr_lat + 24 * A.s;
+                        float f[3];
+#pragma unroll
+                        for (int d = 0; d < 3; ++d)
+                            f[d] = rintf(TL[9 + 3 * d] * dx + TL[9 + 3 * d + 1] * dy + TL[9 + 3 * d + 2] * dz);
+                        dx -= fmaf(f[0], A.L[0], fmaf(f[1], A.L[3], f[2] * A.L[6]));
+                        dy -= fmaf(f[0], A.L[1], fmaf(f[1], A.L[4], f[2] * A.L[7]));
+                        dz -= fmaf(f[0], A.L[2], fmaf(f[1], A.L[5], f[2] * A.L[8]));
+                        if (fabsf(dx * dx + dy * dy + dz * dz - rmin2) <= 1e-4f * rmin2) {
+                            near = near_js - A.st;
+                            nx = dx;
+                            ny = dy;
+                            nz = dz;
+                        }
+                    }
+                    // single bead: the centroid is atom 0 itself, its state in this thread's slot
+                    const int64_t k = A.base;
+                    const double fx0 = B.fx[k], fy0 = B.fy[k], fz0 = B.fz[k];
+                    observe_core(B, P, T.t, step,
+                                 rmin2 < INFINITY ? (double)sqrtf(rmin2) * kBohr2Ang : kDefaultReal, near, nx, ny,
+                                 nz, B.rx[k], B.ry[k], B.rz[k], B.vx[k], B.vy[k], B.vz[k], fx0, fy0, fz0,
+                                 fx0 != 0.0 || fy0 != 0.0 || fz0 != 0.0);
                 }
             }
         }

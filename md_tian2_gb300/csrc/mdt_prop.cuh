@@ -42,9 +42,67 @@ static __device__ __forceinline__ double &comp(double *x, double *y, double *z, 
 // which it was first reached, the adsorption flag with its hysteresis, the steps with a
 // projectile force, the bounce counters and a turning point whenever the sign of the
 // centroid's z velocity changes.  near < 0: no atom in reach (the segment goes on).
+// The observables' state of trajectory t is read once, up front (independent loads, one
+// memory round trip), updated in registers and written back: the projectile's thread runs
+// this between two CTA barriers, so its latency is the whole CTA's.
+static __device__ void observe_core(const Batch &B, const PropParams &P, int t, int step, double dmin, int near,
+                                    double rx, double ry, double rz, double x, double y, double z, double vx,
+                                    double vy, double vz, double fx, double fy, double fz, bool force) {
+    int *bn = B.obs_bnc + kObsInts * (size_t)t;
+    double *dt = B.obs_dot + kObsDots * (size_t)t;
+    const int cur = step & 1, last = cur ^ 1;
+    const double low_z = B.obs_low[3 * t + 2], cl = B.obs_cl[t];
+    const int up = B.obs_up[t], turn = B.obs_turn[t];
+    int s[kObsInts];
+#pragma unroll
+    for (int k = 0; k < kObsInts; ++k) s[k] = bn[k];
+    const double rv0 = dt[last], rf0 = dt[2 + last], vf0 = dt[4 + last];
+    if (z < low_z) {
+        B.obs_low[3 * t] = x;
+        B.obs_low[3 * t + 1] = y;
+        B.obs_low[3 * t + 2] = z;
+    }
+    if (dmin < cl) {
+        B.obs_cl[t] = dmin;
+        B.obs_clstep[t] = step;
+    }
+    // adsorption hysteresis (check_for_closest_approach, :127-129)
+    if (!s[kObsAds] && dmin < P.ads_start) s[kObsAds] = 1;
+    if (s[kObsAds] && dmin > P.ads_end) s[kObsAds] = 0;
+    if (force) s[kObsInter] += 1;  // check_for_proj_surf_interaction (:140-148)
+    // check_for_bounce (:152-241): unit vectors, dot products in the slot of this step
+    if (near >= 0) {
+        const double ir = 1.0 / sqrt(rx * rx + ry * ry + rz * rz), iv = 1.0 / sqrt(vx * vx + vy * vy + vz * vz),
+                     iff = 1.0 / sqrt(fx * fx + fy * fy + fz * fz);
+        const double rv1 = (rx * vx + ry * vy + rz * vz) * (ir * iv);
+        const double rf1 = (rx * fx + ry * fy + rz * fz) * (ir * iff);
+        const double vf1 = (vx * fx + vy * fy + vz * fz) * (iv * iff);
+        dt[cur] = rv1;
+        dt[2 + cur] = rf1;
+        dt[4 + cur] = vf1;
+        const int prev = s[kObsNear] < 0 ? near : s[kObsNear];
+        if (prev != near) {
+            s[kObsBounces] += min(s[kObsPtm], min(s[kObsRF], s[kObsVF]));  // finalize_bounces
+            s[kObsPartner] = -s[kObsPartner];
+            s[kObsRF] = s[kObsVF] = s[kObsPtm] = 0;
+        } else if (rf1 != 0.0) {
+            if ((rv0 > rf0 && rv1 < rf1) || (rv0 < rf0 && rv1 > rf1)) s[kObsRF] += 1;
+            if ((rv0 > vf0 && rv1 < vf1) || (rv0 < vf0 && rv1 > vf1)) s[kObsVF] += 1;
+            if (rv0 > 0.0 && rv1 < 0.0) s[kObsPtm] += 1;
+        }
+        s[kObsNear] = near;
+    }
+#pragma unroll
+    for (int k = 0; k < kObsInts; ++k) bn[k] = s[k];
+    const int down = vz < 0.0 ? 1 : 0;
+    if (down == up) {  // moving down now and up before, or the reverse
+        B.obs_turn[t] = turn + 1;
+        B.obs_up[t] = 1 - down;
+    }
+}
+
 static __device__ void observe_step(const Batch &B, const PropParams &P, const TrajView &T, int step, double dmin,
                                     int near, double rx, double ry, double rz) {
-    const int t = T.t;
     double x = 0.0, y = 0.0, z = 0.0, vx = 0.0, vy = 0.0, vz = 0.0, fx = 0.0, fy = 0.0, fz = 0.0;
     bool force = false;
     for (int b = 0; b < T.nb; ++b) {
@@ -60,54 +118,8 @@ static __device__ void observe_step(const Batch &B, const PropParams &P, const T
         fz += B.fz[k];
         force |= B.fx[k] != 0.0 || B.fy[k] != 0.0 || B.fz[k] != 0.0;
     }
-    x /= T.nb;
-    y /= T.nb;
-    z /= T.nb;
-    if (z < B.obs_low[3 * t + 2]) {
-        B.obs_low[3 * t] = x;
-        B.obs_low[3 * t + 1] = y;
-        B.obs_low[3 * t + 2] = z;
-    }
-    if (dmin < B.obs_cl[t]) {
-        B.obs_cl[t] = dmin;
-        B.obs_clstep[t] = step;
-    }
-    int *bn = B.obs_bnc + kObsInts * (size_t)t;
-    // adsorption hysteresis (check_for_closest_approach, :127-129)
-    if (!bn[kObsAds] && dmin < P.ads_start) bn[kObsAds] = 1;
-    if (bn[kObsAds] && dmin > P.ads_end) bn[kObsAds] = 0;
-    if (force) bn[kObsInter] += 1;  // check_for_proj_surf_interaction (:140-148)
-    // check_for_bounce (:152-241): unit vectors, dot products in the slot of this step
-    if (near >= 0) {
-        double *dt = B.obs_dot + kObsDots * (size_t)t;
-        const double rn = sqrt(rx * rx + ry * ry + rz * rz), vn = sqrt(vx * vx + vy * vy + vz * vz),
-                     fn = sqrt(fx * fx + fy * fy + fz * fz);
-        rx /= rn; ry /= rn; rz /= rn;
-        vx /= vn; vy /= vn; vz /= vn;
-        fx /= fn; fy /= fn; fz /= fn;
-        const int cur = step & 1, last = cur ^ 1;
-        dt[cur] = rx * vx + ry * vy + rz * vz;
-        dt[2 + cur] = rx * fx + ry * fy + rz * fz;
-        dt[4 + cur] = vx * fx + vy * fy + vz * fz;
-        const double rv0 = dt[last], rv1 = dt[cur], rf0 = dt[2 + last], rf1 = dt[2 + cur], vf0 = dt[4 + last],
-                     vf1 = dt[4 + cur];
-        if (bn[kObsNear] < 0) bn[kObsNear] = near;
-        if (bn[kObsNear] != near) {
-            bn[kObsBounces] += min(bn[kObsPtm], min(bn[kObsRF], bn[kObsVF]));  // finalize_bounces
-            bn[kObsPartner] = -bn[kObsPartner];
-            bn[kObsRF] = bn[kObsVF] = bn[kObsPtm] = 0;
-        } else if (rf1 != 0.0) {
-            if ((rv0 > rf0 && rv1 < rf1) || (rv0 < rf0 && rv1 > rf1)) bn[kObsRF] += 1;
-            if ((rv0 > vf0 && rv1 < vf1) || (rv0 < vf0 && rv1 > vf1)) bn[kObsVF] += 1;
-            if (rv0 > 0.0 && rv1 < 0.0) bn[kObsPtm] += 1;
-        }
-        bn[kObsNear] = near;
-    }
-    const int down = vz < 0.0 ? 1 : 0;
-    if (down == B.obs_up[t]) {  // moving down now and up before, or the reverse
-        B.obs_turn[t] += 1;
-        B.obs_up[t] = 1 - down;
-    }
+    observe_core(B, P, T.t, step, dmin, near, rx, ry, rz, x / T.nb, y / T.nb, z / T.nb, vx, vy, vz, fx, fy, fz,
+                 force);
 }
 
 // Closest approach of the projectile (atom 0) after a step: the minimum image of the
