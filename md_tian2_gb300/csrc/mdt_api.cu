@@ -86,6 +86,9 @@ struct mdt_ctx {
     int *rptraj = nullptr;     // trajectories of the packs
     int rnpack = 0, rblock = 0;
     bool rfull = false;         // the plan packs every trajectory of the batch (not a re-pack)
+    double *lcoef = nullptr;    // constant-friction Langevin coefficients of the thread-per-atom kernel
+    double lc_key[4] = {0, 0, 0, 0};  // (gamma, step, Tsurf, Tproj) they were formed for
+    bool lc_valid = false;
     int rmaxblock = kRBlockMax; // largest block the pack plan may use
     int *tcerr = nullptr;       // device word: a tensor-core GEMM of the network timed out
 
@@ -138,6 +141,8 @@ void free_batch(mdt_ctx *c) {
     c->rpacks = nullptr;
     c->rptraj = nullptr;
     c->rnpack = c->rblock = 0;
+    c->lcoef = nullptr;
+    c->lc_valid = false;
     c->have_labels = false;
     c->nn_maxnb_alloc = 0;
     for (auto &b : c->bufs) cudaFree(b.p);
@@ -729,6 +734,22 @@ int run_radial(mdt_ctx *c, const PropParams &P, int nsteps, int mode, bool surr,
     R.surrogate = surr ? 1 : 0;
     R.fscal = c->F.scal;
     R.fdscal = c->F.dscal;
+    if (mode == 2) {
+        // constant-friction coefficients depend on (gamma, dt, T) and the batch's masses and
+        // propagators (fixed by mdt_batch_define): formed once per parameter set
+        const double key[4] = {P.gamma_const, P.step, P.Tsurf, P.Tproj};
+        if (!c->lcoef || !c->lc_valid || std::memcmp(key, c->lc_key, sizeof(key)) != 0) {
+            cudaError_t e = cudaSuccess;
+            if (!c->lcoef) c->lcoef = dalloc<double>(c, 8 * (size_t)c->total_ba, e);
+            if (!c->lcoef) return fail(c, MDT_ERR_NOMEM, "Langevin coefficient buffer");
+            e = launch_nnr_lcoef(c->stream, c->B, P, c->ba_traj, c->total_ba, c->lcoef);
+            c->launches++;
+            if (e != cudaSuccess) return cuda_fail(c, e, "Langevin coefficients");
+            std::memcpy(c->lc_key, key, sizeof(key));
+            c->lc_valid = true;
+        }
+    }
+    c->X.lcoef = c->lcoef;
     const cudaError_t e = launch_nnr(LaunchCfg{c->stream, grid, c->order, c->counter}, c->B, R, c->E, c->X, P,
                                      c->rpacks, c->rptraj, c->rnpack, nsteps, mode);
     c->launches++;

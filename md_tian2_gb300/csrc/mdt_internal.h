@@ -57,6 +57,11 @@ size_t nnr_smem(const RadialNN &R);
 size_t nnr_hb_bytes(const RadialNN &R);  // network buffer / tensor-core operand area (EMT fallback area)
 size_t nnr_emt_smem(int max_atoms);  // EMT fallback area (aliases the network buffers)
 int nnr_resident_ctas(const RadialNN &R);
+// the constant-friction Langevin coefficients of every single-bead slot (8 per slot) for
+// the propagation parameters P: the thread-per-atom kernel reads them instead of forming
+// them (FP64 exp, sqrt and divisions) for every pack of every launch
+cudaError_t launch_nnr_lcoef(cudaStream_t s, const Batch &B, const PropParams &P, const int *ba_traj,
+                             int64_t total_ba, double *lcoef);
 cudaError_t launch_nnr(const LaunchCfg &c, const Batch &B, const RadialNN &R, const EmtConst &E, const NNScratch &X,
                        const PropParams &P, const int2 *packs, const int *ptraj, int npack, int nsteps, int mode);
 

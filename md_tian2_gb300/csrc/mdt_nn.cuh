@@ -188,6 +188,7 @@ struct NNScratch {
     int *skok;
     int skcap;
     int *tcerr;        // set when a tensor-core GEMM did not complete within its wait limit
+    const double *lcoef;  // thread-per-atom kernel: constant-friction Langevin coefficients, 8 per slot
 };
 
 // ---------------------------------------------------------------------------

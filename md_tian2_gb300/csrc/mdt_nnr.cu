@@ -1126,7 +1126,11 @@ __global__ void __launch_bounds__(kRBlockMax, 1)
             const int ty = B.type[T.aoff + A.i];
             A.algo = B.algo[ty];
             S.im[tid] = 1.0 / B.mass[T.aoff + A.i];
-            if (mode == 2 && A.algo == kPropLangevinConst) lc_setup(B, P, T, A.i, S.lc + tid, bs);
+            if (mode == 2 && A.algo == kPropLangevinConst) {
+                const double *src = X.lcoef + kLcN * (A.base + A.i);
+#pragma unroll
+                for (int q = 0; q < kLcN; ++q) S.lc[q * bs + tid] = src[q];
+            }
         }
         const int steps0 = A.s >= 0 ? B.steps_done[T.t] : 0;
         __syncthreads();  // pack set-up read before any thread of the pack writes state
@@ -1445,6 +1449,22 @@ cudaError_t launch_nnr(const LaunchCfg &c, const Batch &B, const RadialNN &R, co
     MDT_NNR_SHAPES(MDT_LAUNCH)
 #undef MDT_LAUNCH
     return cudaErrorInvalidValue;
+}
+
+__global__ void lcoef_kernel(Batch B, PropParams P, const int *ba_traj, int64_t total_ba, double *lcoef) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < total_ba; k += (int64_t)gridDim.x * blockDim.x) {
+        const int t = ba_traj[k];
+        const TrajView T = traj_view(B, t);
+        const int i = (int)(k - T.base);
+        if (T.nb == 1 && B.algo[B.type[T.aoff + i]] == kPropLangevinConst) lc_setup(B, P, T, i, lcoef + kLcN * k, 1);
+    }
+}
+
+cudaError_t launch_nnr_lcoef(cudaStream_t s, const Batch &B, const PropParams &P, const int *ba_traj,
+                             int64_t total_ba, double *lcoef) {
+    const int grid = (int)std::min<int64_t>((total_ba + 255) / 256, 4096);
+    lcoef_kernel<<<std::max(grid, 1), 256, 0, s>>>(B, P, ba_traj, total_ba, lcoef);
+    return cudaGetLastError();
 }
 
 // The tensor-core network's wait, exercised alone: every thread waits (max_polls tries, as a
