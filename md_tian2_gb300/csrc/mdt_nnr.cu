@@ -190,23 +190,39 @@ __device__ __forceinline__ bool image_range(float f, float w, int &lo, int &hi) 
 // the atom inside the cutoff: from the skin list when it is valid (cnt >= 0; the skin
 // shell's entries beyond the cutoff are passed too and fn masks them), else by a full image
 // scan of the trajectory.
+// SPREAD: each lane starts its list at its own fraction of the list ((lane * len) / 32) and
+// wraps around.  Neighbouring atoms of a warp have nearly the same sorted lists, so walking
+// them in step sends the lanes to the same neighbour j at once; where fn adds into j's
+// shared-memory force (red.shared) those lanes serialise on one address.  Spread, the lanes
+// meet different j.  (The descriptor walk keeps list order: there equal j make its position
+// loads broadcasts.)
 template <int G> struct GC { static constexpr int value = G; };
 
-template <class Fn>
+template <bool SPREAD = false, class Fn>
 __device__ __forceinline__ void for_neighbours(const RadialNN &R, const SmemR &S, const AtomR &A, const unsigned *sk,
                                                int cnt, Fn &&fn) {
     if (cnt >= 0) {
         const int n0 = cnt & 0xFFFF, n1 = cnt >> 16;
         // entries two iterations ahead are in flight while one is processed
         auto walk = [&](auto gc, int e0, int e1) {
+            const int len = e1 - e0;
             const unsigned *p = sk + (size_t)e0 * A.N + A.i;
-            unsigned w0 = e0 < e1 ? p[0] : 0u;
-            unsigned w1 = e0 + 1 < e1 ? p[A.N] : 0u;
+            // entry q of the walk's order sits at list position q (or at q shifted by the
+            // lane's start, modulo len)
+            int q0 = SPREAD ? (int)(((unsigned)(threadIdx.x & 31) * (unsigned)len) >> 5) : 0;
+            auto next = [&](int q) { return q + 1 == len ? 0 : q + 1; };
+            unsigned w0 = len > 0 ? p[(size_t)q0 * A.N] : 0u;
+            int q1 = next(q0);
+            unsigned w1 = len > 1 ? p[(size_t)q1 * A.N] : 0u;
+            int q2 = next(q1);
 #pragma unroll 2
-            for (int e = e0; e < e1; ++e) {
+            for (int e = 0; e < len; ++e) {
                 const unsigned v = w0;
                 w0 = w1;
-                if (e + 2 < e1) w1 = p[(size_t)(e - e0 + 2) * A.N];
+                if (e + 2 < len) {
+                    w1 = p[(size_t)q2 * A.N];
+                    q2 = next(q2);
+                }
                 const int js = A.st + (int)(v & 1023u);
                 const float m1 = small_to_float((v >> 10) & 127u) - (float)kImgBias;
                 const float m2 = small_to_float((v >> 17) & 127u) - (float)kImgBias;
@@ -548,7 +564,7 @@ __device__ __forceinline__ void nnr_forces(const RadialNN &R, const SmemR &S, co
                                            float &fiz) {
     constexpr int bs = kRS;
     float fx = 0.f, fy = 0.f, fz = 0.f;
-    for_neighbours(R, S, A, sk, cnt, [&](auto gc, int js, float dx, float dy, float dz, float r2) {
+    for_neighbours<true>(R, S, A, sk, cnt, [&](auto gc, int js, float dx, float dy, float dz, float r2) {
         constexpr int g = decltype(gc)::value;
         constexpr int K = g == 0 ? KA : KB, off = g == 0 ? 0 : KA, BL = g == 0 ? BLA : BLB;
         const float ri = rsqrtf(r2);
