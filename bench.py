@@ -60,9 +60,9 @@ def parse():
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"], help="EMT arm precision")
     ap.add_argument("--model", default=str(ROOT / "md_tian2_gb300" / "data" / "surrogate_radial.npz"))
     ap.add_argument("--margin", type=float, default=0.1, help="descriptor range margin before the EMT fallback")
-    ap.add_argument("--skin", type=float, default=0.5,
-                    help="Verlet skin (A) of the surrogate's neighbour lists; results do not depend on it "
-                         "(0.5 A measured fastest on the 4096-trajectory workload: 1.10 vs 1.14 ms at 1 A)")
+    ap.add_argument("--skin", type=float, default=None,
+                    help="Verlet skin (A) of the surrogate's neighbour lists (results do not depend on it); "
+                         "default: the skin and CTA size mdt_autotune picks on the bench's own batch")
     ap.add_argument("--rmse-traj", type=int, default=256)
     ap.add_argument("--scatter-traj", type=int, default=4096,
                     help="trajectories of the whole-run scattering comparison (0: skip)")
@@ -371,7 +371,7 @@ def timed_steps(eng, sp, precision, steps, stream, torch, dist=None, clock_index
     return ev0.elapsed_time(ev1), (clk.summary() if clk else None)
 
 
-def scattering_comparison(args, model, device, prec_surr="fp32"):
+def scattering_comparison(args, model, device, prec_surr="fp32", shape=None):
     """Config-2 trajectories from identical initial states run to their exit (pul) or the
     step limit with the surrogate (FP32 kernels, EMT fallback) and with plain FP64 EMT:
     the analysis script's observables, their two-sample comparison and the wall time of
@@ -390,7 +390,9 @@ def scattering_comparison(args, model, device, prec_surr="fp32"):
         eng.define(us)
         eng.read_nene(model, ["H", "Au"], max_neighbors=80)
         eng.set_pes(kind, args.margin)
-        eng.nn_set_skin(args.skin)
+        shape = shape or {"skin_A": 0.5, "block": 512}
+        eng.nn_set_skin(shape["skin_A"])
+        eng.nn_radial_block(shape["block"])
         eng.upload()
         eng.synchronize()
         t0 = _time.perf_counter()
@@ -636,7 +638,7 @@ def run_ours(args):
     if args.profile_arm:
         prec = "fp64" if args.profile_arm == "emt" else args.profile_arm
         eng.set_pes(PES_EMT if args.profile_arm == "emt" else PES_SURROGATE, args.margin)
-        eng.nn_set_skin(args.skin)
+        eng.nn_set_skin(0.5 if args.skin is None else args.skin)
         eng.upload()
         eng.calc_force(sp, precision=prec)
         for _ in range(args.warmup):
@@ -649,9 +651,22 @@ def run_ours(args):
 
     # ---- surrogate (headline): the same trajectories in every network arithmetic ----------------
     eng.set_pes(PES_SURROGATE, args.margin)
-    eng.nn_set_skin(args.skin)
     fast = eng.nn_fast_path(True)
     radial = eng.nn_radial_kernel(True)
+    # launch shape of the thread-per-atom kernel: the autotuner's pick (CTA size x skin, timed
+    # on this batch from a saved state that it restores), unless --skin fixes the skin
+    tune = None
+    if args.skin is not None:
+        eng.nn_set_skin(args.skin)
+        shape = {"skin_A": args.skin, "block": 512}
+    elif radial:
+        eng.upload()
+        eng.calc_force(sp, precision="fp32")
+        tune = eng.autotune(sp, precision="fp32", nsteps=20)
+        shape = {"skin_A": tune["skin_A"], "block": tune["block"]}
+    else:
+        eng.nn_set_skin(0.5)
+        shape = {"skin_A": 0.5, "block": 512}
     kname = ("nnr_kernel (thread per atom, fused MD step, surrogate)" if radial
              else "nnf_kernel (warp per atom, fused MD step, surrogate)")
     per_launch = steps_per_launch(args.steps, args.steps_per_launch)
@@ -734,7 +749,7 @@ def run_ours(args):
     # ---- scattering observables: whole trajectories to exit, surrogate vs FP64 EMT ----------
     obs = None
     if rank == 0 and args.scatter_traj > 0:
-        obs = scattering_comparison(args, model, local, head)
+        obs = scattering_comparison(args, model, local, head, shape)
 
     peak = ct.c_double()
     lib.mdt_peak_fma(1, 20000, ct.byref(peak))
@@ -786,7 +801,8 @@ def run_ours(args):
                                    "one bench step = one MD step of every trajectory",
                        "steps_per_launch": per_launch, "precision": head,
                        "model": Path(args.model).name, "fast_path": bool(fast), "radial_kernel": bool(radial),
-                       "skin_A": args.skin,
+                       "skin_A": shape["skin_A"], "max_block": shape["block"],
+                       "autotune": tune,
                        "ntraj_per_gpu": args.ntraj,
                        "parallelism": f"replicas x{world}", "range_margin": args.margin,
                        "l2": ("no flush: each MD step reads the state the previous step wrote; the surrogate step "

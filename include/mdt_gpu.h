@@ -181,9 +181,10 @@ int32_t mdt_nn_set_skin(mdt_ctx *ctx, double skin_ang);
 int32_t mdt_nn_repack(mdt_ctx *ctx, int32_t *npacks);
 
 /* Autotuner of the thread-per-atom kernel (no counterpart in the reference): times nsteps
-   fused MD steps (mdt_md_steps with p and precision MDT_PREC_FP32 or MDT_PREC_BF16) of the
-   current batch for every candidate launch shape -- the largest CTA of the pack plan
-   (256, 384 or 512 atoms: waves and warps per SM) times the Verlet skin (0.5, 0.75, 1 A) --
+   fused MD steps (mdt_md_steps with p and precision MDT_PREC_FP32, MDT_PREC_BF16 or
+   MDT_PREC_BF16X3) of the current batch for every candidate launch shape -- the largest CTA
+   of the pack plan (256, 384 or 512 atoms: waves and warps per SM) times the Verlet skin
+   (0.3, 0.5, 0.75, 1 A) --
    each from the same saved state, keeps the fastest (as mdt_nn_radial_block and
    mdt_nn_set_skin would set it) and restores the state, so the batch continues as if the
    call had not happened.  Results do not depend on the choice.  block, skin_ang and

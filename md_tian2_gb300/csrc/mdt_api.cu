@@ -48,7 +48,7 @@ struct mdt_ctx {
     std::vector<int64_t> ba_off;
     Batch B{};
     std::vector<DevBuf> bufs;
-    double *stage = nullptr;   // 3 * total_ba doubles (Fortran-order transfers)
+    double *stage = nullptr;   // 13 * total_ba doubles: one Fortran-order slice per array of a transfer
     int *order = nullptr, *counter = nullptr, *ba_traj = nullptr;
     double *rnd[4] = {nullptr, nullptr, nullptr, nullptr};
     double *summary = nullptr;
@@ -1043,7 +1043,7 @@ int32_t mdt_batch_define(mdt_ctx *c, int32_t ntraj, const int32_t *natoms, const
     for (int k = 0; k < 12; ++k) ALLOC(arr[k], double, ba);
     ALLOC(B.dens, double, ba);
     ALLOC(B.epot, double, bd);
-    ALLOC(c->stage, double, 3 * (size_t)ba);
+    ALLOC(c->stage, double, 13 * (size_t)ba);
     ALLOC(c->order, int, ntraj);
     ALLOC(c->counter, int, 4);
     ALLOC(c->ba_traj, int, ba);
@@ -1161,18 +1161,21 @@ int32_t mdt_state_download(mdt_ctx *c, double *r, double *v, double *f, double *
     Batch &B = c->B;
     double *outs[4] = {r, v, f, a};
     double *src[4][3] = {{B.rx, B.ry, B.rz}, {B.vx, B.vy, B.vz}, {B.fx, B.fy, B.fz}, {B.ax, B.ay, B.az}};
+    // every array packs into its own slice of the stage: the copies queue behind the packs
+    // and one synchronisation ends the call
     for (int k = 0; k < 4 && e == cudaSuccess; ++k) {
         if (!outs[k]) continue;
-        e = launch_pack(c->stream, B, c->stage, src[k][0], src[k][1], src[k][2], c->total_ba, c->ba_traj);
+        double *sk = c->stage + 3 * (size_t)k * c->total_ba;
+        e = launch_pack(c->stream, B, sk, src[k][0], src[k][1], src[k][2], c->total_ba, c->ba_traj);
         c->launches++;
-        if (e == cudaSuccess) e = cudaMemcpyAsync(outs[k], c->stage, bytes, cudaMemcpyDeviceToHost, c->stream);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);  // stage is reused
+        if (e == cudaSuccess) e = cudaMemcpyAsync(outs[k], sk, bytes, cudaMemcpyDeviceToHost, c->stream);
     }
     if (dens && e == cudaSuccess) {
-        e = launch_pack_scalar(c->stream, B, c->stage, B.dens, c->total_ba, c->ba_traj);
+        double *sd = c->stage + 12 * (size_t)c->total_ba;
+        e = launch_pack_scalar(c->stream, B, sd, B.dens, c->total_ba, c->ba_traj);
         c->launches++;
         if (e == cudaSuccess)
-            e = cudaMemcpyAsync(dens, c->stage, sizeof(double) * c->total_ba, cudaMemcpyDeviceToHost, c->stream);
+            e = cudaMemcpyAsync(dens, sd, sizeof(double) * c->total_ba, cudaMemcpyDeviceToHost, c->stream);
     }
     if (epot && e == cudaSuccess)
         e = cudaMemcpyAsync(epot, B.epot, sizeof(double) * c->total_beads, cudaMemcpyDeviceToHost, c->stream);
@@ -1722,13 +1725,13 @@ int32_t mdt_autotune(mdt_ctx *c, int32_t precision, int32_t nsteps, const mdt_pr
     if (e == cudaSuccess) e = cudaEventCreate(&e0);
     if (e == cudaSuccess) e = cudaEventCreate(&e1);
     const int blocks[3] = {256, 384, 512};
-    const double skins[3] = {0.5, 0.75, 1.0};
+    const double skins[4] = {0.3, 0.5, 0.75, 1.0};
     double best = 1e300;
     int bb = keep_block;
     double bs = keep_skin;
     for (int ib = 0; ib < 3 && e == cudaSuccess; ++ib) {
         if (blocks[ib] < ((c->max_atoms + 31) & ~31)) continue;
-        for (int is = 0; is < 3 && e == cudaSuccess; ++is) {
+        for (int is = 0; is < 4 && e == cudaSuccess; ++is) {
             c->rmaxblock = blocks[ib];
             c->skin_ang = skins[is];
             c->skin_dirty = true;
