@@ -512,9 +512,11 @@ def hdnnp_arm(args, device, stream, torch, peak32, peak64):
     """Batched RuNNer-style HDNNP: H on 6x6 graphene (72 C + 1 H, z-ripple 0.05 A), 8 G2 + 16 G3
     per element (6.5 A cosine cutoff), 24-25-25-1 tanh per element with seeded Glorot weights
     and scaling from the batch's own descriptors; Verlet, dt 0.1 fs.  FP64 generic kernels and
-    FP32 warp-per-atom fast kernels; the FP32 error against FP64 (the FP64 kernels equal the
-    FP64 oracle to 1e-10 eV/A in the parity tests).  The tensor-core (BF16) network exists only
-    in the thread-per-atom kernel of radial networks, not for this G3 model."""
+    FP32 warp-per-atom fast kernels (fused MD steps), and the network on the tensor cores
+    (BF16 / split-BF16 operands, FP32 accumulation) as a pass of its own between the FP32
+    generic kernel's descriptor and force passes, stepped as propagate_1 -> calc_force ->
+    propagate_2 (the reference's own loop); every arithmetic's force error against FP64 (the
+    FP64 kernels equal the FP64 oracle to 1e-10 eV/A in the parity tests)."""
     import ctypes as ct
 
     from md_tian2_gb300 import nene
@@ -562,7 +564,32 @@ def hdnnp_arm(args, device, stream, torch, peak32, peak64):
     d = forces["fp32"] - forces["fp64"]
     out["fp32_force_rmse_vs_fp64_eV_per_A"] = float(np.sqrt(np.mean(d ** 2)))
     out["fp32_force_max_err_eV_per_A"] = float(np.max(np.abs(d)))
-    out["bf16"] = "n/a: tensor-core network GEMMs are in the thread-per-atom kernel of radial networks only"
+    for prec in ("bf16", "bf16x3"):
+        eng = engine()
+        eng.calc_force(sp, precision=prec)
+        dq = eng.download()["f"] - forces["fp64"]
+        eng.upload()
+        eng.calc_force(sp, precision=prec)
+        for _ in range(2):  # warm-up
+            eng.propagate_1(sp)
+            eng.calc_force(sp, precision=prec)
+            eng.propagate_2(sp)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.arm_steps):
+            eng.propagate_1(sp)
+            eng.calc_force(sp, precision=prec)
+            eng.propagate_2(sp)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        eng.close()
+        dt = e0.elapsed_time(e1) * 1e-3
+        out[prec] = {"value": atoms * args.arm_steps / dt, "unit": "atom-steps/s", "ms_per_step": 1e3 * dt / args.arm_steps,
+                     "kernel": "nn_force_kernel (FP32 descriptors) + nn_tc_kernel (tcgen05 network) + nn_force_kernel "
+                               "(FP32 descriptor VJP), phase-by-phase propagation",
+                     "force_rmse_vs_fp64_eV_per_A": float(np.sqrt(np.mean(dq ** 2))),
+                     "force_max_err_vs_fp64_eV_per_A": float(np.max(np.abs(dq)))}
     out["flop_per_step"] = flop
     out["flop_convention"] = ("per neighbour pair 720, per valid triplet (r_ij, r_ik, r_jk < rc; counted on a "
                               "32-trajectory sample and scaled) 378, per atom 7,500 (forward + backward)")

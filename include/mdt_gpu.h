@@ -47,8 +47,12 @@ extern "C" {
 #define MDT_PREC_FP64 0
 #define MDT_PREC_FP32 1
 #define MDT_PREC_BF16 2 /* FP32 descriptors and forces, network GEMMs on the tensor cores with
-                           BF16 operands and FP32 accumulation (thread-per-atom kernel of
-                           radial-only networks); no counterpart in the reference */
+                           BF16 operands and FP32 accumulation: fused in the thread-per-atom
+                           kernel of radial-only networks (forces and MD steps); for other
+                           MDT_PES_NENE networks (<= 2 elements, <= 2 hidden layers of <= 32
+                           nodes, <= 48 descriptors) mdt_calc_force runs the network as a pass
+                           of its own between the FP32 descriptor and force passes; no
+                           counterpart in the reference */
 #define MDT_PREC_BF16X3 3 /* as MDT_PREC_BF16 with every operand split in a BF16 high and low
                              part, three MMAs per K step (about 16 significant bits) */
 

@@ -87,6 +87,10 @@ struct mdt_ctx {
     int rnpack = 0, rblock = 0;
     bool rfull = false;         // the plan packs every trajectory of the batch (not a re-pack)
     double *lcoef = nullptr;    // constant-friction Langevin coefficients of the thread-per-atom kernel
+    RadialNN RG{};              // tensor-core network tables of a generic model (own descriptor order)
+    double *tc_G = nullptr;     // its pass buffers: raw descriptors, atomic energies [ba][maxsf], [ba]
+    double *tc_eat = nullptr;
+    float *tc_dg = nullptr;     // dE/dG [ba][maxsf]
     double lc_key[4] = {0, 0, 0, 0};  // (gamma, step, Tsurf, Tproj) they were formed for
     bool lc_valid = false;
     int rmaxblock = kRBlockMax; // largest block the pack plan may use
@@ -104,9 +108,10 @@ struct mdt_ctx {
 namespace {
 
 const char *const kBf16Scope =
-    "MDT_PREC_BF16 / MDT_PREC_BF16X3 run the network GEMMs on the tensor cores in the thread-per-atom kernel only: "
-    "a radial-only "
-    "network (mdt_nn_radial_kernel) on single-bead trajectories of at most 512 atoms";
+    "MDT_PREC_BF16 / MDT_PREC_BF16X3 run the network GEMMs on the tensor cores: fused MD steps and forces of a "
+    "radial-only network in the thread-per-atom kernel (single-bead trajectories of at most 512 atoms), and "
+    "mdt_calc_force of an MDT_PES_NENE model whose network has at most two elements, two hidden layers of <= 32 "
+    "nodes with one activation (p t s l) per layer and <= 48 descriptors";
 
 int fail(mdt_ctx *c, int code, const std::string &msg) {
     if (c) c->err = msg;
@@ -143,6 +148,8 @@ void free_batch(mdt_ctx *c) {
     c->rnpack = c->rblock = 0;
     c->lcoef = nullptr;
     c->lc_valid = false;
+    c->tc_G = c->tc_eat = nullptr;
+    c->tc_dg = nullptr;
     c->have_labels = false;
     c->nn_maxnb_alloc = 0;
     for (auto &b : c->bufs) cudaFree(b.p);
@@ -534,6 +541,54 @@ RadialNN build_radial(const NNDev &M, const mdt_nn_model *m, const FastNN &F, co
     R.inv_rc2 = (float)(1.0 / (rc * rc));
     R.rc_b = (float)rc;
     R.maxnb = M.maxnb;
+    for (int t = 0; t < kMaxTypes; ++t) R.elem_of_type[t] = M.elem_of_type[t];
+    for (int e = 0; e < 2; ++e) R.atom_energy[e] = e < ne ? M.atom_energy[e] : 0.0;
+    R.maxweights = M.maxweights;
+    R.maxsf = M.maxsf;
+    for (int e = 0; e < 2; ++e)
+        for (int l = 0; l <= kMaxLayers; ++l) {
+            R.woff[e][l] = e < ne && l <= M.nlayers ? M.woff[e][l] : 0;
+            R.nodes[e][l] = e < ne && l <= M.nlayers ? M.nodes[e][l] : 0;
+        }
+    R.ok = 1;
+    return R;
+}
+
+// Tensor-core network tables of a model that does not run on the thread-per-atom kernel (any
+// descriptors, e.g. with G3): the network of build_radial's form -- at most two elements, one or
+// two hidden layers of <= 32 nodes, one activation per layer of the kinds p t s l, one output
+// node -- on at most 48 descriptors in the model's own order; the descriptors' scaling comes
+// from the fast path's table (FastNN::scal, dscal).  RadialNN::ok = 0 otherwise.
+RadialNN build_tc_generic(const NNDev &M, const mdt_nn_model *m, const FastNN &F) {
+    RadialNN R{};
+    R.ok = 0;
+    if (!F.ok || M.nelem > 2 || (M.nlayers != 2 && M.nlayers != 3)) return R;
+    const int ne = M.nelem, nh = M.nlayers - 1;
+    int nsf = 0;
+    for (int e = 0; e < ne; ++e) {
+        nsf = std::max(nsf, M.nsf[e]);
+        for (int l = 1; l <= nh; ++l)
+            if (M.nodes[e][l] > 32) return R;
+        if (M.nodes[e][M.nlayers] != 1) return R;
+        if (M.normnodes)
+            for (int l = 0; l <= M.nlayers; ++l)
+                if (M.nodes[e][l] != M.nodes[0][l]) return R;
+    }
+    if (nsf > 48) return R;
+    for (int l = 0; l < M.nlayers; ++l) {
+        const uint8_t a = m->act[((size_t)0 * m->nlayers + l) * m->maxnodes];
+        if (!std::strchr("ptsl", (int)a) || a == 0) return R;
+        for (int e = 0; e < ne; ++e)
+            for (int n = 0; n < M.nodes[e][l + 1]; ++n)
+                if (m->act[((size_t)e * m->nlayers + l) * m->maxnodes + n] != a) return R;
+        R.act[l] = a;
+        R.rn[l] = M.normnodes ? (float)(1.0 / M.nodes[0][l]) : 1.f;
+    }
+    R.nh = nh;
+    R.nelem = ne;
+    R.nin = nsf <= 24 ? 24 : 48;
+    for (int e = 0; e < 2; ++e)
+        for (int q = 0; q < 2 * kRMaxK; ++q) R.qsrc[e][q] = (int8_t)(e < ne && q < M.nsf[e] ? q : -1);
     for (int t = 0; t < kMaxTypes; ++t) R.elem_of_type[t] = M.elem_of_type[t];
     for (int e = 0; e < 2; ++e) R.atom_energy[e] = e < ne ? M.atom_energy[e] : 0.0;
     R.maxweights = M.maxweights;
@@ -1219,6 +1274,50 @@ static int check_params(mdt_ctx *c, const mdt_prop_params *p, bool draws = true)
     return MDT_OK;
 }
 
+// calc_force of a generic model with its network on the tensor cores, in three passes: the
+// generic FP32 kernel exports the raw descriptors (energy-only), the network runs on every
+// bead-atom as 128-row tiles (launch_nn_tc), and the generic FP32 kernel forms the forces from
+// the network's dE/dG by the descriptor VJP.  MDT_PES_NENE only (the surrogate's EMT fallback
+// needs its range test in the same pass).
+int run_tc_generic(mdt_ctx *c, const PropParams &P, int mode, int tcm) {
+    if (c->pes_kind != MDT_PES_NENE || !c->RG.ok)
+        return fail(c, MDT_ERR_UNSUPPORTED, kBf16Scope);
+    cudaError_t e = cudaSuccess;
+    const size_t nsl = (size_t)c->total_ba * c->M.maxsf;
+    if (!c->tc_G) c->tc_G = dalloc<double>(c, nsl, e);
+    if (!c->tc_dg) c->tc_dg = dalloc<float>(c, nsl, e);
+    if (!c->tc_eat) c->tc_eat = dalloc<double>(c, (size_t)c->total_ba, e);
+    if (!c->tc_G || !c->tc_dg || !c->tc_eat) return fail(c, MDT_ERR_NOMEM, "tensor-core network buffers");
+    if (!c->tcerr) {
+        e = cudaMalloc(&c->tcerr, sizeof(int));
+        if (e == cudaSuccess) e = cudaMemsetAsync(c->tcerr, 0, sizeof(int), c->stream);
+        if (e != cudaSuccess) return cuda_fail(c, e, "tensor-core status word");
+    }
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    RadialNN R = c->RG;
+    R.tc = tcm;
+    if (nn_tc_smem(R.nin, R.nh, tcm) > (size_t)optin) return fail(c, MDT_ERR_UNSUPPORTED, kBf16Scope);
+    const LaunchCfg g = nn_cfg(c, MDT_PREC_FP32);
+    NNScratch X = c->X;
+    X.gout = c->tc_G;
+    e = launch_nn(g, c->B, c->M, c->E, X, P, c->ngeta_max, 0, 1, MDT_PREC_FP32, false);  // descriptors
+    c->launches++;
+    const int64_t tiles = ((int64_t)c->total_ba + kRBlockMax - 1) / kRBlockMax;
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(tiles, c->num_sms));
+    if (e == cudaSuccess)
+        e = launch_nn_tc(c->stream, grid, c->B, R, c->tc_G, c->ba_traj, c->total_ba, c->tc_dg, c->tc_eat, c->tcerr,
+                         mode == 0 ? 1 : 0);
+    c->launches++;
+    X.gout = nullptr;
+    X.dgin = c->tc_dg;
+    X.eatin = c->tc_eat;
+    if (e == cudaSuccess) e = launch_nn(g, c->B, c->M, c->E, X, P, c->ngeta_max, 0, mode, MDT_PREC_FP32, false);
+    c->launches++;
+    return e == cudaSuccess ? MDT_OK : cuda_fail(c, e, "mdt_calc_force (tensor-core network)");
+}
+
 int32_t mdt_calc_force(mdt_ctx *c, int32_t flag, int32_t precision, const mdt_prop_params *p) {
     int rc = check_ready(c, c && c->pes_kind == MDT_PES_EMT);
     if (rc) return rc;
@@ -1233,7 +1332,7 @@ int32_t mdt_calc_force(mdt_ctx *c, int32_t flag, int32_t precision, const mdt_pr
         const bool surr = c->pes_kind == MDT_PES_SURROGATE;
         if (use_radial(c, precision, false))
             return run_radial(c, P, 0, flag == MDT_ENERGY_ONLY ? 1 : 0, surr, tc_mode(precision));
-        if (tc_mode(precision)) return fail(c, MDT_ERR_UNSUPPORTED, kBf16Scope);
+        if (tc_mode(precision)) return run_tc_generic(c, P, flag == MDT_ENERGY_ONLY ? 1 : 0, tc_mode(precision));
         const bool fast = use_fast(c, precision);
         const LaunchCfg fcfg = fast ? nnf_cfg(c) : LaunchCfg{};
         if (fast && (rc = ensure_mscr(c, fcfg.grid, 0))) return rc;
@@ -1540,8 +1639,8 @@ int32_t mdt_nn_set_model(mdt_ctx *c, const mdt_nn_model *m, int32_t ntypes, cons
     for (int e = 0; e < ne; ++e) {
         M.g3fast[e] = 0;
         M.nlz[e] = 0;
-        for (int m = 0; m < 4; ++m)
-            for (int q = 0; q < 8; ++q) M.sf_of[e][m][q] = -1;
+        for (int g = 0; g < 4; ++g)
+            for (int q = 0; q < 8; ++q) M.sf_of[e][g][q] = -1;
         bool ok = M.ng3eta[e] <= 4;
         int pe1 = -2, pe2 = -2, nq = 0;
         for (int s = 0; s < M.nsf[e] && ok; ++s) {
@@ -1625,6 +1724,10 @@ int32_t mdt_nn_set_model(mdt_ctx *c, const mdt_nn_model *m, int32_t ntypes, cons
     c->R.wf = M.wf;
     c->R.fscal = F.scal;
     c->R.fdscal = F.dscal;
+    c->RG = build_tc_generic(M, m, F);
+    c->RG.wf = M.wf;
+    c->RG.fscal = F.scal;
+    c->RG.fdscal = F.dscal;
     c->rnpack = c->rblock = 0;
     c->d_scal = (float4 *)F.scal;
     c->d_dscal = (float *)F.dscal;

@@ -57,6 +57,12 @@ size_t nnr_smem(const RadialNN &R);
 size_t nnr_hb_bytes(const RadialNN &R);  // network buffer / tensor-core operand area (EMT fallback area)
 size_t nnr_emt_smem(int max_atoms);  // EMT fallback area (aliases the network buffers)
 int nnr_resident_ctas(const RadialNN &R);
+// network of a generic model (R from build_tc_generic: nin 24 or 48, nh 1 or 2, R.tc 1 or 2)
+// on the tensor cores for every bead-atom: raw descriptors G [ba][maxsf] in, atomic energies
+// (Ha) and dE/dG out; one CTA per SM (the CTA holds all of its SM's TMEM)
+cudaError_t launch_nn_tc(cudaStream_t s, int grid, const Batch &B, const RadialNN &R, const double *G,
+                         const int *ba_traj, int64_t total_ba, float *dg, double *eat, int *err, int do_forces);
+size_t nn_tc_smem(int nin, int nh, int tc);
 // the constant-friction Langevin coefficients of every single-bead slot (8 per slot) for
 // the propagation parameters P: the thread-per-atom kernel reads them instead of forming
 // them (FP64 exp, sqrt and divisions) for every pack of every launch

@@ -130,75 +130,86 @@ __device__ bool nn_bead(const Batch &B, const NNDev &M, const NNScratch &X, cons
         if (ei < 0) continue;
         const int cnt = X.nbcnt[base + i];
         acsf_cache<R>(M, C, i, ei, cnt, X.nbw + (base + i) * (int64_t)M.maxnb, S.px, S.py, S.pz, S.elem, S.lat);
-        acsf_forward<R>(M, C, ei, cnt, G);
         const int nsf = M.nsf[ei];
         const int sfb = ei * M.maxsf;
-        if (X.gout)
-            for (int s = lane; s < nsf; s += 32) X.gout[(base + i) * M.maxsf + s] = (double)G[s];
-        // ---- scaling (getshortatomic.f90:174-236) and range check ------------------
-        for (int s = lane; s < nsf; s += 32) {
-            const double mn = M.smin[sfb + s], mx = M.smax[sfb + s], w = mx - mn;
-            const double g = (double)G[s];
-            if (g < mn - M.margin * w || g > mx + M.margin * w) *S.flag = 1;
-            double gs = g;
-            if (M.centersym && !M.scalesym) gs = g - M.savg[sfb + s];
-            else if (M.scalesym && !M.centersym) gs = (g - mn) / w * (M.scmax - M.scmin) + M.scmin;
-            else if (M.scalesym && M.centersym) gs = (g - M.savg[sfb + s]) / w;
-            hv[s] = (R)gs;  // layer 0 values
-        }
-        __syncwarp();
-        // ---- network forward (calconenn.f90:83-153) --------------------------------
-        const R *we = W + (size_t)ei * M.maxweights;
-        for (int l = 1; l <= M.nlayers; ++l) {
-            const int nprev = M.nodes[ei][l - 1], ncur = M.nodes[ei][l];
-            const R *wl = we + M.woff[ei][l];
-            for (int n = lane; n < ncur; n += 32) {
-                R z = R(0);
-                for (int p = 0; p < nprev; ++p) z += wl[p * ncur + n] * hv[(l - 1) * kMaxNodes + p];
-                z += wl[nprev * ncur + n];
-                if (M.normnodes) z /= (R)nprev;
-                hs[l * kMaxNodes + n] = z;
-                hv[l * kMaxNodes + n] = act_fn<R>(M.act[(ei * kMaxLayers + (l - 1)) * kMaxNodes + n], z);
+        if (X.dgin) {
+            // network on the tensor cores in a prior pass: its atomic energy and dE/dG
+            if (lane == 0) e_warp += X.eatin[base + i] + (M.remove_atom_energies ? M.atom_energy[ei] : 0.0);
+            if (!do_forces) {
+                __syncwarp();
+                continue;
             }
+            for (int s = lane; s < nsf; s += 32) dEdG[s] = (R)X.dgin[(base + i) * M.maxsf + s];
             __syncwarp();
-        }
-        if (lane == 0) e_warp += (double)hv[M.nlayers * kMaxNodes] + (M.remove_atom_energies ? M.atom_energy[ei] : 0.0);
-        if (!do_forces) {
-            __syncwarp();
-            continue;
-        }
-        // ---- backward: dE/dG (getdnodes_values.f90 + the chain of getshortatomic.f90:263-291)
-        R *delta = hs;  // sums are overwritten by deltas, layer by layer from the top
-        for (int l = M.nlayers; l >= 1; --l) {
-            const int ncur = M.nodes[ei][l];
-            const R norm = M.normnodes ? R(1) / (R)M.nodes[ei][l - 1] : R(1);
-            for (int n = lane; n < ncur; n += 32) {
-                const uint8_t a = M.act[(ei * kMaxLayers + (l - 1)) * kMaxNodes + n];
-                const R dn = norm * act_dfn<R>(a, hs[l * kMaxNodes + n], hv[l * kMaxNodes + n]);
-                R up = R(1);
-                if (l < M.nlayers) {
-                    const int nn = M.nodes[ei][l + 1];
-                    const R *wl = we + M.woff[ei][l + 1];
-                    up = R(0);
-                    for (int m = 0; m < nn; ++m) up += wl[n * nn + m] * delta[(l + 1) * kMaxNodes + m];
-                }
-                delta[l * kMaxNodes + n] = dn * up;
-            }
-            __syncwarp();
-        }
-        {
-            const int n1 = M.nodes[ei][1];
-            const R *wl = we + M.woff[ei][1];
+        } else {
+            acsf_forward<R>(M, C, ei, cnt, G);
+            if (X.gout)
+                for (int s = lane; s < nsf; s += 32) X.gout[(base + i) * M.maxsf + s] = (double)G[s];
+            // ---- scaling (getshortatomic.f90:174-236) and range check ------------------
             for (int s = lane; s < nsf; s += 32) {
-                R v = R(0);
-                for (int n = 0; n < n1; ++n) v += wl[s * n1 + n] * delta[1 * kMaxNodes + n];
-                // dG_scaled/dG: (scmax-scmin)/(max-min) whenever scale_symmetry_functions is
-                // set, as getshortatomic.f90:174-190 scales dG/dx
-                if (M.scalesym) v *= (R)((M.scmax - M.scmin) / (M.smax[sfb + s] - M.smin[sfb + s]));
-                dEdG[s] = v;
+                const double mn = M.smin[sfb + s], mx = M.smax[sfb + s], w = mx - mn;
+                const double g = (double)G[s];
+                if (g < mn - M.margin * w || g > mx + M.margin * w) *S.flag = 1;
+                double gs = g;
+                if (M.centersym && !M.scalesym) gs = g - M.savg[sfb + s];
+                else if (M.scalesym && !M.centersym) gs = (g - mn) / w * (M.scmax - M.scmin) + M.scmin;
+                else if (M.scalesym && M.centersym) gs = (g - M.savg[sfb + s]) / w;
+                hv[s] = (R)gs;  // layer 0 values
             }
-        }
-        __syncwarp();
+            __syncwarp();
+            // ---- network forward (calconenn.f90:83-153) --------------------------------
+            const R *we = W + (size_t)ei * M.maxweights;
+            for (int l = 1; l <= M.nlayers; ++l) {
+                const int nprev = M.nodes[ei][l - 1], ncur = M.nodes[ei][l];
+                const R *wl = we + M.woff[ei][l];
+                for (int n = lane; n < ncur; n += 32) {
+                    R z = R(0);
+                    for (int p = 0; p < nprev; ++p) z += wl[p * ncur + n] * hv[(l - 1) * kMaxNodes + p];
+                    z += wl[nprev * ncur + n];
+                    if (M.normnodes) z /= (R)nprev;
+                    hs[l * kMaxNodes + n] = z;
+                    hv[l * kMaxNodes + n] = act_fn<R>(M.act[(ei * kMaxLayers + (l - 1)) * kMaxNodes + n], z);
+                }
+                __syncwarp();
+            }
+            if (lane == 0) e_warp += (double)hv[M.nlayers * kMaxNodes] + (M.remove_atom_energies ? M.atom_energy[ei] : 0.0);
+            if (!do_forces) {
+                __syncwarp();
+                continue;
+            }
+            // ---- backward: dE/dG (getdnodes_values.f90 + the chain of getshortatomic.f90:263-291)
+            R *delta = hs;  // sums are overwritten by deltas, layer by layer from the top
+            for (int l = M.nlayers; l >= 1; --l) {
+                const int ncur = M.nodes[ei][l];
+                const R norm = M.normnodes ? R(1) / (R)M.nodes[ei][l - 1] : R(1);
+                for (int n = lane; n < ncur; n += 32) {
+                    const uint8_t a = M.act[(ei * kMaxLayers + (l - 1)) * kMaxNodes + n];
+                    const R dn = norm * act_dfn<R>(a, hs[l * kMaxNodes + n], hv[l * kMaxNodes + n]);
+                    R up = R(1);
+                    if (l < M.nlayers) {
+                        const int nn = M.nodes[ei][l + 1];
+                        const R *wl = we + M.woff[ei][l + 1];
+                        up = R(0);
+                        for (int m = 0; m < nn; ++m) up += wl[n * nn + m] * delta[(l + 1) * kMaxNodes + m];
+                    }
+                    delta[l * kMaxNodes + n] = dn * up;
+                }
+                __syncwarp();
+            }
+            {
+                const int n1 = M.nodes[ei][1];
+                const R *wl = we + M.woff[ei][1];
+                for (int s = lane; s < nsf; s += 32) {
+                    R v = R(0);
+                    for (int n = 0; n < n1; ++n) v += wl[s * n1 + n] * delta[1 * kMaxNodes + n];
+                    // dG_scaled/dG: (scmax-scmin)/(max-min) whenever scale_symmetry_functions is
+                    // set, as getshortatomic.f90:174-190 scales dG/dx
+                    if (M.scalesym) v *= (R)((M.scmax - M.scmin) / (M.smax[sfb + s] - M.smin[sfb + s]));
+                    dEdG[s] = v;
+                }
+            }
+            __syncwarp();
+        }  // descriptors and network in this pass
         R fix, fiy, fiz;
         acsf_vjp<R>(M, C, ei, cnt, dEdG, fix, fiy, fiz);
         if (lane == 0) {

@@ -189,6 +189,11 @@ struct NNScratch {
     int skcap;
     int *tcerr;        // set when a tensor-core GEMM did not complete within its wait limit
     const double *lcoef;  // thread-per-atom kernel: constant-friction Langevin coefficients, 8 per slot
+    // generic kernels: dE/dG [ba][maxsf] and the atomic energies (Ha, output node) of a prior
+    // tensor-core network pass; when set, the kernels skip descriptors and network and run the
+    // forces (descriptor VJP) from them
+    const float *dgin;
+    const double *eatin;
 };
 
 // ---------------------------------------------------------------------------

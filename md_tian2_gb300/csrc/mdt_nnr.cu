@@ -1467,6 +1467,97 @@ cudaError_t launch_nnr(const LaunchCfg &c, const Batch &B, const RadialNN &R, co
     return cudaErrorInvalidValue;
 }
 
+// The network of a generic model on the tensor cores, as a pass of its own: every bead-atom
+// of the batch is a row of a 128-row tile (four tiles per CTA, persistent over the batch);
+// its scaled descriptors come from the raw symmetry functions G [ba][maxsf] of a descriptor
+// pass, and the atomic energy (Ha) and dE/dG go to eat / dg for a forces pass (the
+// descriptor VJP of the generic kernels).  R holds the network's tables with the model's
+// own descriptor order (qsrc the identity up to nsf).
+template <int NIN, int NH, int TC>
+__global__ void __launch_bounds__(kRBlockMax, 1)
+    nn_tc_kernel(Batch B, RadialNN R, const double *G, const int *ba_traj, int64_t total_ba, float *dg, double *eat,
+                 int *err, int do_forces) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    const SmemR S = carve_r<NIN, NH, TC>(smem_raw);
+    const int tid = threadIdx.x;
+    TcCtx C{0u, S.tcbar, err};
+    uint32_t phase = 0;
+    load_weights_tc<NIN, NH, TC == 2>(R, S);
+    if (tid < 32) {
+        tmem_alloc(S.tslot, kTcCols);
+        tmem_relinquish();
+    }
+    if (tid == 0) {
+        for (int g = 0; g < kTcTiles; ++g) mbar_init(&S.tcbar[g], 1);
+        fence_mbar_init();
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    C.tmem = *S.tslot;
+    // uniform over the CTA: every thread takes part in every tile's GEMMs
+    for (int64_t k0 = (int64_t)blockIdx.x * kRBlockMax; k0 < total_ba; k0 += (int64_t)gridDim.x * kRBlockMax) {
+        const int64_t k = k0 + tid;
+        int ei = -1;
+        float xs[NIN];
+#pragma unroll
+        for (int q = 0; q < NIN; ++q) xs[q] = 0.f;
+        if (k < total_ba) {
+            const TrajView T = traj_view(B, ba_traj[k]);
+            const int i = (int)((k - T.base) % T.N);
+            ei = R.elem_of_type[B.type[T.aoff + i]];
+            if (ei >= 0) {
+                const float4 *sc = S.scal + ei * NIN;
+                const double *g = G + k * R.maxsf;
+#pragma unroll
+                for (int q = 0; q < NIN; ++q) {
+                    const int s = R.qsrc[ei][q];
+                    if (s >= 0) xs[q] = fmaf(sc[q].x, (float)g[s], sc[q].y);
+                }
+            }
+        }
+        float dgv[NIN];
+        const float e = nnr_network_tc<NIN, NH, TC == 2>(R, S, C, ei >= 0 ? ei : 0, xs, do_forces != 0, dgv, phase);
+        if (ei >= 0) {
+            eat[k] = (double)e;
+            if (do_forces)
+#pragma unroll
+                for (int q = 0; q < NIN; ++q) {
+                    const int s = R.qsrc[ei][q];
+                    if (s >= 0) dg[k * R.maxsf + s] = dgv[q];
+                }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (tid < 32) tmem_dealloc(C.tmem, kTcCols);
+}
+
+template <int NIN, int NH, int TC>
+cudaError_t nn_tc_launch_t(cudaStream_t s, int grid, const Batch &B, const RadialNN &R, const double *G,
+                           const int *ba_traj, int64_t total_ba, float *dg, double *eat, int *err, int do_forces) {
+    const size_t sm = smem_r(NIN, NH, TC);
+    cudaError_t e = cudaFuncSetAttribute(nn_tc_kernel<NIN, NH, TC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    nn_tc_kernel<NIN, NH, TC><<<grid, kRBlockMax, sm, s>>>(B, R, G, ba_traj, total_ba, dg, eat, err, do_forces);
+    return cudaGetLastError();
+}
+
+size_t nn_tc_smem(int nin, int nh, int tc) { return smem_r(nin, nh, tc); }
+
+cudaError_t launch_nn_tc(cudaStream_t s, int grid, const Batch &B, const RadialNN &R, const double *G,
+                         const int *ba_traj, int64_t total_ba, float *dg, double *eat, int *err, int do_forces) {
+#define MDT_NNTC(NIN_, NH_)                                                                                  \
+    if (R.nin == NIN_ && R.nh == NH_)                                                                        \
+        return R.tc == 2 ? nn_tc_launch_t<NIN_, NH_, 2>(s, grid, B, R, G, ba_traj, total_ba, dg, eat, err, do_forces) \
+                         : nn_tc_launch_t<NIN_, NH_, 1>(s, grid, B, R, G, ba_traj, total_ba, dg, eat, err, do_forces);
+    MDT_NNTC(24, 2) MDT_NNTC(24, 1) MDT_NNTC(48, 2) MDT_NNTC(48, 1)
+#undef MDT_NNTC
+    return cudaErrorInvalidValue;
+}
+
 __global__ void lcoef_kernel(Batch B, PropParams P, const int *ba_traj, int64_t total_ba, double *lcoef) {
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < total_ba; k += (int64_t)gridDim.x * blockDim.x) {
         const int t = ba_traj[k];

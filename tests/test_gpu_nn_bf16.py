@@ -158,6 +158,48 @@ def test_bf16_outside_its_scope_is_an_error(built_lib):
     m = nene.random_model(["H", "Au"], hidden=(16, 16), act="t", seed=1, neighbours=["Au"])  # G3: not radial
     eng.read_nene(m, ["H", "Au"])
     eng.set_pes(PES_NENE)
-    with pytest.raises(EngineError):
+    if eng.nn_fast_path(True):  # the descriptors' scaling table exists: the generic tensor-core pass runs
         eng.calc_force(SimParams(), precision="bf16")
+    else:
+        with pytest.raises(EngineError):
+            eng.calc_force(SimParams(), precision="bf16")
+    with pytest.raises(EngineError):
+        eng.md_steps(2, SimParams(), precision="bf16")  # fused MD steps: thread-per-atom kernel only
     eng.close()
+
+
+@pytest.mark.parametrize("prec", ["bf16", "bf16x3"])
+def test_bf16_generic_network_at_graphene_benchmark_shape(built_lib, oracle_lib, prec):
+    """The HDNNP benchmark shape (72 C + 1 H on graphene, 8 G2 + 16 G3, 24-25-25-1 tanh) with
+    its network on the tensor cores as a pass of its own (descriptors and forces on the FP32
+    generic kernel): forces and energies against the FP64 oracle within the bars of the
+    radial kernel's tensor-core network, energy-only equal to the energies of the full
+    evaluation."""
+    F_REL, E_REL = BARS[prec]
+    us = W.config4(12, seed=45)
+    for u, z in zip(us, np.random.default_rng(8).uniform(1.0, 4.0, size=len(us))):
+        u.r[0, 0, 2] = z
+    m = nene.random_model(["H", "C"], hidden=(25, 25), act="t", seed=6, neighbours=["C"])
+    eng = _engine(us, m, names=("H", "C"))
+    G = eng.nn_descriptors()
+    eng.close()
+    nene.set_scaling(m, G, np.concatenate([_elems(u) for u in us]))
+    eng = _engine(us, m, names=("H", "C"))
+    eng.calc_force(SimParams(), precision=prec)
+    out = eng.download()
+    eng.calc_force(SimParams(), flag=C.ENERGY_ONLY, precision=prec)
+    e_only = eng.download()["epot"]
+    eng.close()
+    from oracle.oracle import NNOracle
+    o = NNOracle(m)
+    fr, fd = [], []
+    for t, u in enumerate(us):
+        E, F = o.energy_force(_elems(u), u.r[:, 0, :], u.simbox)
+        f = eng.split(out["f"], t)[:, 0, :]
+        fr.append(F)
+        fd.append(f - F)
+        assert abs(out["epot"][t] - E) < E_REL * max(1.0, abs(E)), (t, out["epot"][t], E)
+    rms = np.sqrt(np.mean(np.concatenate(fr) ** 2))
+    err = np.sqrt(np.mean(np.concatenate(fd) ** 2))
+    assert 0.0 < err < F_REL * rms, (err, rms)
+    assert np.allclose(e_only, out["epot"], rtol=0, atol=1e-9)
