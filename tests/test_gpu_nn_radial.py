@@ -116,6 +116,26 @@ def test_radial_md_steps_track_fp64(built_lib, oracle_lib):
     assert np.abs(res["fp32"]["v"] - res["fp64"]["v"]).max() < 1e-6
 
 
+def test_radial_langevin_coefficients_follow_the_parameters(built_lib, oracle_lib):
+    """The thread-per-atom kernel forms its constant-friction Langevin coefficients once
+    per parameter set: ten steps at one friction and time step, then ten at another,
+    track the FP64 kernels (which form them every step) as closely as one parameter set
+    does."""
+    us = W.config2(6, seed=25)
+    m = _radial_model(8)
+    sps = [SimParams(step=0.1, gamma_const=1e-3, seed=5), SimParams(step=0.2, gamma_const=2e-2, seed=6)]
+    res = {}
+    for prec in ("fp32", "fp64"):
+        eng = _engine(us, m)
+        eng.calc_force(sps[0], precision=prec)
+        for sp in sps:
+            eng.md_steps(10, sp, precision=prec)
+        res[prec] = eng.download()
+        eng.close()
+    assert np.abs(res["fp32"]["r"] - res["fp64"]["r"]).max() < 1e-5
+    assert np.abs(res["fp32"]["v"] - res["fp64"]["v"]).max() < 1e-5
+
+
 def test_radial_md_exit_and_skin(built_lib, oracle_lib):
     """Projectiles that leave through pul stop (status and step count as the warp
     kernel gives them); 40 steps with the 1 A skin equal 40 steps built every step.  Each
