@@ -222,7 +222,11 @@ int32_t mdt_nn_neighbors(mdt_ctx *ctx, int32_t *counts, int32_t *words);
 typedef struct mdt_train_opts {
     double w_energy, w_force;
     double lr, beta1, beta2, eps;
-    int32_t precision;          /* MDT_PREC_FP32 for training, MDT_PREC_FP64 for gradient checks */
+    int32_t precision;          /* MDT_PREC_FP32 for training, MDT_PREC_FP64 for gradient checks,
+                                   MDT_PREC_BF16: the network's forward, backward, tangent and
+                                   weight-gradient products as BF16 GEMMs on the tensor cores
+                                   (FP32 accumulation and master weights; two hidden layers of
+                                   <= 32 nodes, <= 48 descriptors) */
 } mdt_train_opts;
 
 /* Labels: energy[T] (eV), forces (3, 1, N) per trajectory (eV/A).  Computes the raw

@@ -18,7 +18,8 @@ CSRC = PKG / "csrc"
 OUT_DIR = PKG / "_build"
 LIB = PKG / "libmdt_gpu.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["mdt_api.cu", "mdt_md.cu", "mdt_peak.cu", "mdt_nn.cu", "mdt_noalloc.cu", "mdt_train.cu", "mdt_nnf.cu", "mdt_nnr.cu"]
+SOURCES = ["mdt_api.cu", "mdt_md.cu", "mdt_peak.cu", "mdt_nn.cu", "mdt_noalloc.cu", "mdt_train.cu", "mdt_train_gemm.cu",
+           "mdt_nnf.cu", "mdt_nnr.cu"]
 
 
 def nvcc() -> str:
@@ -54,7 +55,7 @@ def build(verbose: bool = False, extra: list[str] | None = None, force: bool = F
     objs = [str(OUT_DIR / (s.stem + ".o")) for s in srcs]
     if jobs or not LIB.exists():
         tmp = LIB.with_suffix(".so.tmp")
-        cmd = [nvcc(), *ARCH, "-shared", "-o", str(tmp), *objs, "-lcudart"]
+        cmd = [nvcc(), *ARCH, "-shared", "-o", str(tmp), *objs, "-lcudart", "-lcublas"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

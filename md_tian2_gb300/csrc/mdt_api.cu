@@ -45,6 +45,7 @@ struct mdt_ctx {
     int64_t total_ba = 0, total_pairs = 0;
     int total_atoms = 0, total_beads = 0;
     std::vector<int> natoms, nbeads, atom_off, bead_off;
+    std::vector<int> h_type;  // universe type per atom (host copy)
     std::vector<int64_t> ba_off;
     Batch B{};
     std::vector<DevBuf> bufs;
@@ -91,6 +92,14 @@ struct mdt_ctx {
     double *tc_G = nullptr;     // its pass buffers: raw descriptors, atomic energies [ba][maxsf], [ba]
     double *tc_eat = nullptr;
     float *tc_dg = nullptr;     // dE/dG [ba][maxsf]
+    // BF16 GEMM training (mdt_train_gemm.cu): cuBLAS handle, row list, pools, per-slot buffers
+    cublasHandle_t cublas = nullptr;
+    int *g_slot = nullptr;
+    int g_cap = 0;              // rows the pools hold
+    float *g_f = nullptr, *g_gw = nullptr;
+    __nv_bfloat16 *g_b = nullptr;
+    float *g_dg = nullptr, *g_xdot = nullptr;
+    double *g_eat = nullptr, *g_arow = nullptr;
     double lc_key[4] = {0, 0, 0, 0};  // (gamma, step, Tsurf, Tproj) they were formed for
     bool lc_valid = false;
     int rmaxblock = kRBlockMax; // largest block the pack plan may use
@@ -150,6 +159,12 @@ void free_batch(mdt_ctx *c) {
     c->lc_valid = false;
     c->tc_G = c->tc_eat = nullptr;
     c->tc_dg = nullptr;
+    c->g_slot = nullptr;
+    c->g_cap = 0;
+    c->g_f = c->g_gw = nullptr;
+    c->g_b = nullptr;
+    c->g_dg = c->g_xdot = nullptr;
+    c->g_eat = c->g_arow = nullptr;
     c->have_labels = false;
     c->nn_maxnb_alloc = 0;
     for (auto &b : c->bufs) cudaFree(b.p);
@@ -897,6 +912,7 @@ int32_t mdt_destroy(mdt_ctx *c) {
     for (void *p : c->nnbufs) cudaFree(p);
     if (c->mscr) cudaFree(c->mscr);
     if (c->tcerr) cudaFree(c->tcerr);
+    if (c->cublas) cublasDestroy(c->cublas);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return MDT_OK;
@@ -1024,6 +1040,7 @@ int32_t mdt_batch_define(mdt_ctx *c, int32_t ntraj, const int32_t *natoms, const
     // host-side derived arrays
     std::vector<int8_t> type(at);
     for (int a = 0; a < at; ++a) type[a] = (int8_t)(idx[a] - 1);
+    c->h_type.assign(type.begin(), type.end());
     std::vector<uint8_t> fixed(ba);
     std::vector<int> ba_traj(ba);
     for (int t = 0; t < ntraj; ++t) {
@@ -2001,7 +2018,16 @@ static int train_run(mdt_ctx *c, const mdt_train_opts *o, const int32_t *conf, i
     if (rc) return rc;
     if (!c->have_labels) return fail(c, MDT_ERR_STATE, "no training labels (call mdt_train_set_labels)");
     if (!o || !conf || n < 1 || n > c->T) return fail(c, MDT_ERR_ARG, "bad training arguments");
-    if (o->precision != MDT_PREC_FP32 && o->precision != MDT_PREC_FP64) return fail(c, MDT_ERR_ARG, "bad precision");
+    if (o->precision != MDT_PREC_FP32 && o->precision != MDT_PREC_FP64 && o->precision != MDT_PREC_BF16)
+        return fail(c, MDT_ERR_ARG, "bad precision");
+    const bool gemm = o->precision == MDT_PREC_BF16;
+    if (gemm) {
+        if (c->M.nlayers != 3 || c->M.nelem > 2)
+            return fail(c, MDT_ERR_UNSUPPORTED, "BF16 GEMM training: networks of two hidden layers, at most two elements");
+        for (int e = 0; e < c->M.nelem; ++e)
+            if (c->M.nodes[e][0] > 48 || c->M.nodes[e][1] > 32 || c->M.nodes[e][2] > 32 || c->M.nodes[e][3] != 1)
+                return fail(c, MDT_ERR_UNSUPPORTED, "BF16 GEMM training: <= 48 descriptors, <= 32 nodes per hidden layer");
+    }
     for (int k = 0; k < n; ++k)
         if (conf[k] < 0 || conf[k] >= c->T) return fail(c, MDT_ERR_ARG, "configuration index out of range");
     const size_t nw = (size_t)c->M.nelem * c->M.maxweights;
@@ -2010,10 +2036,70 @@ static int train_run(mdt_ctx *c, const mdt_train_opts *o, const int32_t *conf, i
     if (e == cudaSuccess) e = cudaMemsetAsync(c->t_loss, 0, sizeof(double) * 4, c->stream);
     TrainArgs A{c->t_E, c->t_fx, c->t_fy, c->t_fz, c->t_G, c->t_conf, n, o->w_energy, o->w_force, c->t_theta,
                 c->t_grad, c->t_loss};
+    GemmTrain G{};
+    if (gemm && e == cudaSuccess) {
+        // rows: the atoms of the step's configurations, element 0 first
+        std::vector<int> rows[2];
+        for (int k = 0; k < n; ++k) {
+            const int t = conf[k];
+            for (int i = 0; i < c->natoms[t]; ++i) {
+                const int el = c->M.elem_of_type[c->h_type[c->atom_off[t] + i]];
+                if (el >= 0) rows[el].push_back((int)(c->ba_off[t] + i));
+            }
+        }
+        std::vector<int> slot(rows[0]);
+        slot.insert(slot.end(), rows[1].begin(), rows[1].end());
+        const int R = (int)slot.size();
+        if (R > c->g_cap) {
+            const int cap = std::max(R, 2 * c->g_cap);
+            c->g_slot = dalloc<int>(c, (size_t)cap, e);
+            c->g_f = dalloc<float>(c, gemm_train_floats(cap), e);
+            c->g_b = dalloc<__nv_bfloat16>(c, gemm_train_bf16(cap), e);
+            if (!c->g_gw) c->g_gw = dalloc<float>(c, gemm_train_gw(cap), e);
+            if (!c->g_slot || !c->g_f || !c->g_b || !c->g_gw) return fail(c, MDT_ERR_NOMEM, "GEMM training buffers");
+            c->g_cap = cap;
+        }
+        const size_t nsl = (size_t)c->total_ba * c->M.maxsf;
+        if (!c->g_dg) c->g_dg = dalloc<float>(c, nsl, e);
+        if (!c->g_xdot) c->g_xdot = dalloc<float>(c, nsl, e);
+        if (!c->g_eat) c->g_eat = dalloc<double>(c, (size_t)c->total_ba, e);
+        if (!c->g_arow) c->g_arow = dalloc<double>(c, (size_t)c->total_ba, e);
+        if (!c->g_dg || !c->g_xdot || !c->g_eat || !c->g_arow) return fail(c, MDT_ERR_NOMEM, "GEMM training buffers");
+        if (!c->cublas) {
+            if (cublasCreate(&c->cublas) != CUBLAS_STATUS_SUCCESS) return fail(c, MDT_ERR_CUDA, "cublasCreate failed");
+        }
+        if (R > 0) e = cudaMemcpyAsync(c->g_slot, slot.data(), sizeof(int) * R, cudaMemcpyHostToDevice, c->stream);
+        G.slot = c->g_slot;
+        G.rows[0] = 0;
+        G.rows[1] = (int)rows[0].size();
+        G.rows[2] = R;
+        G.R = R;
+        G.M = c->M;
+        G.theta = c->t_theta;
+        G.G = c->t_G;
+        G.dg = c->g_dg;
+        G.eat = c->g_eat;
+        G.xdot = c->g_xdot;
+        G.arow = c->g_arow;
+        G.grad = c->t_grad;
+        gemm_train_carve(G, c->g_f, c->g_b, c->g_gw, c->g_cap);
+        if (e == cudaSuccess && R > 0 && gemm_train_forward(c->cublas, c->stream, G))
+            return fail(c, MDT_ERR_CUDA, "BF16 GEMM training: forward products failed");
+        A.dgin = c->g_dg;
+        A.eatin = c->g_eat;
+        A.xdot = c->g_xdot;
+        A.arow = c->g_arow;
+        c->launches += 6;
+    }
     if (e == cudaSuccess)
         e = launch_train(c->stream, c->num_sms, c->B, c->M, c->X, A, c->max_atoms, c->ngeta_max, c->counter,
-                         o->precision);
+                         gemm ? MDT_PREC_FP32 : o->precision);
     c->launches++;
+    if (gemm && e == cudaSuccess && G.R > 0) {
+        if (gemm_train_backward(c->cublas, c->stream, G))
+            return fail(c, MDT_ERR_CUDA, "BF16 GEMM training: tangent and gradient products failed");
+        c->launches += 6;
+    }
     if (update && e == cudaSuccess) {
         ++c->t_step;
         e = launch_adam(c->stream, c->t_theta, c->t_m, c->t_v, c->t_grad, (int)nw, 1.0 / n, o->lr, o->beta1, o->beta2,

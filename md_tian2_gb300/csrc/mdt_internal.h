@@ -1,5 +1,7 @@
 // mdt_internal.h -- launchers shared between the engine's translation units.
 #pragma once
+#include <cublas_v2.h>
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include "mdt_common.cuh"
@@ -81,9 +83,48 @@ struct TrainArgs {
     const float *theta;
     double *grad;
     double *loss;
+    // network outside the kernel (BF16 GEMM training): per slot dE/dG [slot][maxsf] and the
+    // output-node value in, the scaled descriptor tangent [slot][maxsf] and dL/dE of the
+    // slot's configuration out; the kernel then runs descriptors, forces, loss and tangent only
+    const float *dgin = nullptr;
+    const double *eatin = nullptr;
+    float *xdot = nullptr;
+    double *arow = nullptr;
 };
 cudaError_t launch_train(cudaStream_t s, int num_sms, const Batch &B, const NNDev &M, const NNScratch &X,
                          const TrainArgs &A, int max_atoms, int ngeta, int *counter, int precision);
+// The network of a training step as BF16 GEMMs (mdt_train_gemm.cu): rows = the atoms of the
+// step's configurations ordered by element (rows[e]..rows[e+1]), slot[r] their bead-atom
+// slots; row arrays carved from one FP32 and one BF16 pool (gemm_train_carve)
+struct GemmTrain {
+    const int *slot = nullptr;
+    int rows[3] = {0, 0, 0};
+    int R = 0;
+    NNDev M{};
+    const float *theta = nullptr;  // live FP32 master weights
+    const double *G = nullptr;     // raw descriptors [slot][maxsf]
+    float *dg = nullptr;           // dE/dG [slot][maxsf] (out)
+    double *eat = nullptr;         // output node per slot (out)
+    float *xdot = nullptr;         // scaled descriptor tangent [slot][maxsf] (in)
+    double *arow = nullptr;        // dL/dE per slot (in)
+    double *grad = nullptr;        // gradient (FP64, += )
+    struct {
+        float *x, *cv, *z1, *h1, *z2, *h2, *dl1, *dl2, *s2, *zd1, *zd2, *sp2;
+    } f{};
+    struct {
+        __nv_bfloat16 *x, *xd, *ax, *h1, *hd1, *ah1, *dl1, *dl2, *dp1, *dp2;
+    } b{};
+    float *z3 = nullptr, *out = nullptr, *dl3 = nullptr, *a = nullptr;
+    __nv_bfloat16 *w = nullptr;  // BF16 weights of both elements
+    float *gw = nullptr;         // weight-gradient products of both elements
+};
+size_t gemm_train_floats(int R);
+size_t gemm_train_bf16(int R);
+size_t gemm_train_gw(int R);
+void gemm_train_carve(GemmTrain &T, float *fpool, __nv_bfloat16 *bpool, float *gw, int R);
+int gemm_train_forward(cublasHandle_t h, cudaStream_t s, const GemmTrain &T);
+int gemm_train_backward(cublasHandle_t h, cudaStream_t s, const GemmTrain &T);
+
 cudaError_t launch_adam(cudaStream_t s, float *theta, float *m, float *v, const double *grad, int n, double scale,
                         double lr, double b1, double b2, double eps, int step, const uint8_t *frozen);
 cudaError_t launch_weights_to_model(cudaStream_t s, const float *theta, float *wf, double *wd, int n);

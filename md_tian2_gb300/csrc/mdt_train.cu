@@ -45,6 +45,10 @@ struct TrainDev {
     const float *theta;                     // live weights [nelem*maxweights]
     double *grad;                           // accumulated gradient
     double *loss;                           // 0: sum (dE/N)^2 eV^2, 1: sum |dF|^2, 2: force components, 3: configs
+    const float *dgin;                      // network outside (see TrainArgs): dE/dG per slot
+    const double *eatin;                    //   output-node value per slot
+    float *xdot;                            //   scaled descriptor tangent per slot (out)
+    double *arow;                           //   dL/dE of the slot's configuration (out)
 };
 
 template <typename R> struct SmemTrain {
@@ -181,39 +185,46 @@ __global__ void __launch_bounds__(32 * TrainCfg<R>::warps) train_kernel(Batch B,
             const int nsf = M.nsf[ei], sfb = ei * M.maxsf;
             const R *we = S.w + (size_t)ei * M.maxweights;
             acsf_cache<R>(M, C, i, ei, cnt, X.nbw + (base + i) * (int64_t)M.maxnb, S.px, S.py, S.pz, S.elem, S.lat);
-            for (int s = lane; s < nsf; s += 32) {
-                const double mn = M.smin[sfb + s], w = M.smax[sfb + s] - mn;
-                h[s] = (R)((D.G[(base + i) * M.maxsf + s] - mn) / w * (M.scmax - M.scmin) + M.scmin);
-            }
-            __syncwarp();
-            net_forward<R>(M, we, ei, z, h, zd, hd, false);
-            if (lane == 0) e_warp += (double)h[M.nlayers * kMaxNodes] + (M.remove_atom_energies ? M.atom_energy[ei] : 0.0);
-            for (int l = M.nlayers; l >= 1; --l) {
-                const int ncur = M.nodes[ei][l];
-                for (int n = lane; n < ncur; n += 32) {
-                    const uint8_t ac = M.act[(ei * kMaxLayers + (l - 1)) * kMaxNodes + n];
-                    const R dn = act_dfn<R>(ac, z[l * kMaxNodes + n], h[l * kMaxNodes + n]);
-                    R up = R(1);
-                    if (l < M.nlayers) {
-                        const int nn = M.nodes[ei][l + 1];
-                        const R *wl = we + M.woff[ei][l + 1];
-                        up = R(0);
-                        for (int m = 0; m < nn; ++m) up += wl[n * nn + m] * dl[(l + 1) * kMaxNodes + m];
-                    }
-                    dl[l * kMaxNodes + n] = dn * up;
+            if (D.dgin) {  // the network ran outside: its output and dE/dG
+                if (lane == 0)
+                    e_warp += D.eatin[base + i] + (M.remove_atom_energies ? M.atom_energy[ei] : 0.0);
+                for (int s = lane; s < nsf; s += 32) cv[s] = (R)D.dgin[(base + i) * M.maxsf + s];
+                __syncwarp();
+            } else {
+                for (int s = lane; s < nsf; s += 32) {
+                    const double mn = M.smin[sfb + s], w = M.smax[sfb + s] - mn;
+                    h[s] = (R)((D.G[(base + i) * M.maxsf + s] - mn) / w * (M.scmax - M.scmin) + M.scmin);
                 }
                 __syncwarp();
-            }
-            {
-                const int n1 = M.nodes[ei][1];
-                const R *wl = we + M.woff[ei][1];
-                for (int s = lane; s < nsf; s += 32) {
-                    R v = R(0);
-                    for (int n = 0; n < n1; ++n) v += wl[s * n1 + n] * dl[1 * kMaxNodes + n];
-                    cv[s] = v * (R)((M.scmax - M.scmin) / (M.smax[sfb + s] - M.smin[sfb + s]));
+                net_forward<R>(M, we, ei, z, h, zd, hd, false);
+                if (lane == 0) e_warp += (double)h[M.nlayers * kMaxNodes] + (M.remove_atom_energies ? M.atom_energy[ei] : 0.0);
+                for (int l = M.nlayers; l >= 1; --l) {
+                    const int ncur = M.nodes[ei][l];
+                    for (int n = lane; n < ncur; n += 32) {
+                        const uint8_t ac = M.act[(ei * kMaxLayers + (l - 1)) * kMaxNodes + n];
+                        const R dn = act_dfn<R>(ac, z[l * kMaxNodes + n], h[l * kMaxNodes + n]);
+                        R up = R(1);
+                        if (l < M.nlayers) {
+                            const int nn = M.nodes[ei][l + 1];
+                            const R *wl = we + M.woff[ei][l + 1];
+                            up = R(0);
+                            for (int m = 0; m < nn; ++m) up += wl[n * nn + m] * dl[(l + 1) * kMaxNodes + m];
+                        }
+                        dl[l * kMaxNodes + n] = dn * up;
+                    }
+                    __syncwarp();
                 }
-            }
-            __syncwarp();
+                {
+                    const int n1 = M.nodes[ei][1];
+                    const R *wl = we + M.woff[ei][1];
+                    for (int s = lane; s < nsf; s += 32) {
+                        R v = R(0);
+                        for (int n = 0; n < n1; ++n) v += wl[s * n1 + n] * dl[1 * kMaxNodes + n];
+                        cv[s] = v * (R)((M.scmax - M.scmin) / (M.smax[sfb + s] - M.smin[sfb + s]));
+                    }
+                }
+                __syncwarp();
+            }  // network in this kernel
             R fix, fiy, fiz;
             acsf_vjp<R>(M, C, ei, cnt, cv, fix, fiy, fiz);
             if (lane == 0) {
@@ -263,6 +274,15 @@ __global__ void __launch_bounds__(32 * TrainCfg<R>::warps) train_kernel(Batch B,
             R *gwe = gw + (size_t)ei * M.maxweights;
             acsf_cache<R>(M, C, i, ei, cnt, X.nbw + (base + i) * (int64_t)M.maxnb, S.px, S.py, S.pz, S.elem, S.lat);
             acsf_jvp<R>(M, C, ei, cnt, i, S.ux, S.uy, S.uz, cv);
+            if (D.xdot) {  // the network's sweep runs outside: its inputs
+                for (int s = lane; s < nsf; s += 32) {
+                    const double w = M.smax[sfb + s] - M.smin[sfb + s];
+                    D.xdot[(base + i) * M.maxsf + s] = (float)(cv[s] * (R)((M.scmax - M.scmin) / w));
+                }
+                if (lane == 0) D.arow[base + i] = (double)a;
+                __syncwarp();
+                continue;
+            }
             for (int s = lane; s < nsf; s += 32) {
                 const double mn = M.smin[sfb + s], w = M.smax[sfb + s] - mn;
                 const R sc = (R)((M.scmax - M.scmin) / w);
@@ -346,7 +366,8 @@ size_t train_total_smem(const NNDev &M, int max_atoms, int ngeta, int precision)
 
 cudaError_t launch_train(cudaStream_t s, int num_sms, const Batch &B, const NNDev &M, const NNScratch &X,
                          const TrainArgs &A, int max_atoms, int ngeta, int *counter, int precision) {
-    TrainDev D{A.E_ref, A.fx_ref, A.fy_ref, A.fz_ref, A.G, A.conf, A.nconf, A.wE, A.wF, A.theta, A.grad, A.loss};
+    TrainDev D{A.E_ref, A.fx_ref, A.fy_ref, A.fz_ref, A.G,    A.conf,  A.nconf, A.wE,  A.wF,
+               A.theta, A.grad,   A.loss,   A.dgin,   A.eatin, A.xdot, A.arow};
     const size_t sm = train_total_smem(M, max_atoms, ngeta, precision);
     cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(int), s);
     if (e != cudaSuccess) return e;

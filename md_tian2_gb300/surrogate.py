@@ -82,7 +82,10 @@ def surrogate_model(seed: int = 11, descriptor: str = "acsf") -> nene.NNModel:
 
 
 def _opts(lr, w_energy, w_force, precision):
-    return TrainOpts(w_energy, w_force, lr, 0.9, 0.999, 1e-8, 0 if precision == "fp64" else 1)
+    """precision: fp64 (gradient checks), fp32 (the training kernel's own network on CUDA
+    cores) or bf16 (the network's products as BF16 GEMMs on the tensor cores, FP32 master
+    weights and accumulation)."""
+    return TrainOpts(w_energy, w_force, lr, 0.9, 0.999, 1e-8, {"fp64": 0, "fp32": 1, "bf16": 2}[precision])
 
 
 class Trainer:
@@ -125,7 +128,7 @@ class Trainer:
 
     def train(self, epochs: float = 10, batch: int = 256, lr: float = 2e-3, lr_final: float = 2e-4,
               w_energy: float = 10.0, w_force: float = 1.0, seed: int = 0, time_budget: float | None = None,
-              log=None):
+              log=None, precision: str = "fp32"):
         rng = np.random.default_rng(seed)
         nsteps = max(1, int(epochs * self.n / batch))
         stats = np.zeros(3)
@@ -140,7 +143,7 @@ class Trainer:
             ids = np.ascontiguousarray(order[pos:pos + batch], np.int32)
             pos += batch
             frac = k / max(1, nsteps - 1)
-            o = _opts(lr * (lr_final / lr) ** frac, w_energy, w_force, "fp32")
+            o = _opts(lr * (lr_final / lr) ** frac, w_energy, w_force, precision)
             self.eng._check(self.eng.lib.mdt_train_step(self.eng.h, ct.byref(o), ids.ctypes.data, len(ids),
                                                         stats.ctypes.data), "mdt_train_step")
             hist.append((k, float(np.sqrt(stats[0])), float(np.sqrt(stats[1]))))

@@ -66,10 +66,30 @@ def test_training_gradient_matches_finite_differences(built_lib, oracle_lib):
     assert np.abs(g32 - g64).max() < 2e-3 * scale
 
 
-def test_training_reduces_loss(built_lib, oracle_lib):
+def test_bf16_gemm_training_gradient(built_lib, oracle_lib):
+    """The training gradient with the network's products as BF16 GEMMs (FP32 accumulation)
+    against the FP64 gradient: within 3e-2 of the largest component (BF16 keeps 8 significant
+    bits of every operand), on every weight."""
+    data = _tiny_dataset()
+    model = nene.random_model(["H", "Au"], hidden=(8, 8), act="p", seed=2, neighbours=["Au"])
+    model.weights = [np.asarray(w, np.float32).astype(np.float64) for w in model.weights]
+    tr = Trainer(data, model)
+    g64 = tr.gradient([0, 1, 2], 3.0, 1.0, "fp64")
+    g16 = tr.gradient([0, 1, 2], 3.0, 1.0, "bf16")
+    g16b = tr.gradient([2, 0], 3.0, 1.0, "bf16")  # another row set, reusing the buffers
+    g64b = tr.gradient([2, 0], 3.0, 1.0, "fp64")
+    tr.close()
+    for a, b in ((g16, g64), (g16b, g64b)):
+        scale = np.abs(b).max()
+        assert np.abs(a - b).max() < 3e-2 * scale, (np.abs(a - b).max(), scale)
+        assert np.corrcoef(a, b)[0, 1] > 0.999
+
+
+@pytest.mark.parametrize("prec", ["fp32", "bf16"])
+def test_training_reduces_loss(built_lib, oracle_lib, prec):
     data = _tiny_dataset(n=6, seed=1)
     model = nene.random_model(["H", "Au"], hidden=(16, 16), act="p", seed=3, neighbours=["Au"])
     tr = Trainer(data, model)
-    hist = tr.train(epochs=200, batch=6, lr=3e-3, lr_final=1e-3, w_energy=1.0, w_force=1.0)
+    hist = tr.train(epochs=200, batch=6, lr=3e-3, lr_final=1e-3, w_energy=1.0, w_force=1.0, precision=prec)
     tr.close()
     assert hist[-1][2] < 0.5 * hist[0][2]
