@@ -226,7 +226,9 @@ typedef struct mdt_train_opts {
                                    MDT_PREC_BF16: the network's forward, backward, tangent and
                                    weight-gradient products as BF16 GEMMs on the tensor cores
                                    (FP32 accumulation and master weights; two hidden layers of
-                                   <= 32 nodes, <= 48 descriptors) */
+                                   <= 32 nodes, <= 48 descriptors); MDT_PREC_BF16X3: the same
+                                   with split operands (hi*hi + hi*lo + lo*hi, about 16 bits),
+                                   for networks whose energy error is below BF16 rounding */
 } mdt_train_opts;
 
 /* Labels: energy[T] (eV), forces (3, 1, N) per trajectory (eV/A).  Computes the raw

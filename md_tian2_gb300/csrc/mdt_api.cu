@@ -2018,9 +2018,8 @@ static int train_run(mdt_ctx *c, const mdt_train_opts *o, const int32_t *conf, i
     if (rc) return rc;
     if (!c->have_labels) return fail(c, MDT_ERR_STATE, "no training labels (call mdt_train_set_labels)");
     if (!o || !conf || n < 1 || n > c->T) return fail(c, MDT_ERR_ARG, "bad training arguments");
-    if (o->precision != MDT_PREC_FP32 && o->precision != MDT_PREC_FP64 && o->precision != MDT_PREC_BF16)
-        return fail(c, MDT_ERR_ARG, "bad precision");
-    const bool gemm = o->precision == MDT_PREC_BF16;
+    if (o->precision < MDT_PREC_FP64 || o->precision > MDT_PREC_BF16X3) return fail(c, MDT_ERR_ARG, "bad precision");
+    const bool gemm = o->precision == MDT_PREC_BF16 || o->precision == MDT_PREC_BF16X3;
     if (gemm) {
         if (c->M.nlayers != 3 || c->M.nelem > 2)
             return fail(c, MDT_ERR_UNSUPPORTED, "BF16 GEMM training: networks of two hidden layers, at most two elements");
@@ -2054,7 +2053,7 @@ static int train_run(mdt_ctx *c, const mdt_train_opts *o, const int32_t *conf, i
             const int cap = std::max(R, 2 * c->g_cap);
             c->g_slot = dalloc<int>(c, (size_t)cap, e);
             c->g_f = dalloc<float>(c, gemm_train_floats(cap), e);
-            c->g_b = dalloc<__nv_bfloat16>(c, gemm_train_bf16(cap), e);
+            c->g_b = dalloc<__nv_bfloat16>(c, 2 * gemm_train_bf16(cap), e);  // high and low parts
             if (!c->g_gw) c->g_gw = dalloc<float>(c, gemm_train_gw(cap), e);
             if (!c->g_slot || !c->g_f || !c->g_b || !c->g_gw) return fail(c, MDT_ERR_NOMEM, "GEMM training buffers");
             c->g_cap = cap;
@@ -2083,6 +2082,7 @@ static int train_run(mdt_ctx *c, const mdt_train_opts *o, const int32_t *conf, i
         G.arow = c->g_arow;
         G.grad = c->t_grad;
         gemm_train_carve(G, c->g_f, c->g_b, c->g_gw, c->g_cap);
+        G.split = o->precision == MDT_PREC_BF16X3 ? 1 : 0;
         if (e == cudaSuccess && R > 0 && gemm_train_forward(c->cublas, c->stream, G))
             return fail(c, MDT_ERR_CUDA, "BF16 GEMM training: forward products failed");
         A.dgin = c->g_dg;

@@ -117,9 +117,11 @@ struct GemmTrain {
     float *z3 = nullptr, *out = nullptr, *dl3 = nullptr, *a = nullptr;
     __nv_bfloat16 *w = nullptr;  // BF16 weights of both elements
     float *gw = nullptr;         // weight-gradient products of both elements
+    int split = 0;               // 1: every BF16 operand has its low part lo elements further on
+    size_t lo = 0;
 };
 size_t gemm_train_floats(int R);
-size_t gemm_train_bf16(int R);
+size_t gemm_train_bf16(int R);  // high parts; the pool holds twice this (low parts after them)
 size_t gemm_train_gw(int R);
 void gemm_train_carve(GemmTrain &T, float *fpool, __nv_bfloat16 *bpool, float *gw, int R);
 int gemm_train_forward(cublasHandle_t h, cudaStream_t s, const GemmTrain &T);

@@ -16,6 +16,11 @@
 // (a: dL/dE of the row's configuration), the forward-over-reverse sweep of the training
 // kernel written as products over rows.  The weight-gradient products sum over atoms
 // (K = rows).  Results land in the same FP64 gradient array as the kernel's own sweep.
+// Split mode (BF16X3) stores every operand as a BF16 high part and the BF16 rounding of the
+// residual (at T.lo elements further on) and forms each product as hi*hi + hi*lo + lo*hi:
+// about 16 significant bits, as the tensor-core inference does.  Plain BF16 rounds the
+// forward sums by ~2^-9, which for a trained network is ~10 meV per atom of energy -- more
+// than its true energy error, so the energy term of the loss gradient is then rounding.
 #include <cublas_v2.h>
 #include <cuda_bf16.h>
 
@@ -37,6 +42,13 @@ __device__ __forceinline__ uint8_t act_of(const NNDev &M, int e, int l, int n) {
 
 __device__ __forceinline__ int elem_of_row(const GemmTrain &T, int r) { return r < T.rows[1] ? 0 : 1; }
 
+// a BF16 operand value; in split mode also its residual in the low part
+__device__ __forceinline__ void st_op(const GemmTrain &T, __nv_bfloat16 *p, size_t k, float v) {
+    const __nv_bfloat16 h = __float2bfloat16_rn(v);
+    p[k] = h;
+    if (T.split) p[k + T.lo] = __float2bfloat16_rn(v - __bfloat162float(h));
+}
+
 // weights of both elements as BF16 row-major blocks: W1 [kIn x kHid], W2 [kHid x kHid]
 __global__ void weights_bf16(GemmTrain T) {
     const NNDev &M = T.M;
@@ -54,7 +66,7 @@ __global__ void weights_bf16(GemmTrain T) {
                 if (p < n1 && n < n2) v = we[M.woff[e][2] + p * n2 + n];
             }
         }
-        T.w[k] = __float2bfloat16_rn(v);
+        st_op(T, T.w, k, v);
     }
 }
 
@@ -70,7 +82,7 @@ __global__ void gather_x(GemmTrain T) {
                 v = (float)((T.G[(size_t)sl * M.maxsf + s] - mn) / w * (M.scmax - M.scmin) + M.scmin);
             }
             T.f.x[(size_t)r * kIn + s] = v;
-            T.b.x[(size_t)r * kIn + s] = __float2bfloat16_rn(v);
+            st_op(T, T.b.x, (size_t)r * kIn + s, v);
         }
     }
 }
@@ -89,7 +101,7 @@ __global__ void after_f1(GemmTrain T) {  // z1 += b1; h1 = f1(z1)
             }
             T.f.z1[k] = z;
             T.f.h1[k] = h;
-            T.b.h1[k] = __float2bfloat16_rn(h);
+            st_op(T, T.b.h1, k, h);
         }
     }
 }
@@ -120,7 +132,7 @@ __global__ void after_f2(GemmTrain T) {  // z2 += b2; h2, z3, output, dl3, dl2
             float d = 0.f;
             if (n < n2) d = act_dfn<float>(act_of(M, e, 2, n), T.f.z2[k], T.f.h2[k]) * w3[n] * dl3;
             T.f.dl2[k] = d;
-            T.b.dl2[k] = __float2bfloat16_rn(d);
+            st_op(T, T.b.dl2, k, d);
         }
     }
 }
@@ -134,7 +146,7 @@ __global__ void after_b1(GemmTrain T) {  // s2 = dl2 W2^T (in f.s2); dl1 = f1'(z
             float d = 0.f;
             if (n < n1) d = act_dfn<float>(act_of(M, e, 1, n), T.f.z1[k], T.f.h1[k]) * T.f.s2[k];
             T.f.dl1[k] = d;
-            T.b.dl1[k] = __float2bfloat16_rn(d);
+            st_op(T, T.b.dl1, k, d);
         }
     }
 }
@@ -159,8 +171,8 @@ __global__ void gather_xd(GemmTrain T) {  // x' and a x + x' of every row
         for (int s = 0; s < kIn; ++s) {
             const float xd = s < M.nsf[e] ? T.xdot[(size_t)sl * M.maxsf + s] : 0.f;
             const size_t k = (size_t)r * kIn + s;
-            T.b.xd[k] = __float2bfloat16_rn(xd);
-            T.b.ax[k] = __float2bfloat16_rn(a * T.f.x[k] + xd);
+            st_op(T, T.b.xd, k, xd);
+            st_op(T, T.b.ax, k, a * T.f.x[k] + xd);
         }
     }
 }
@@ -174,8 +186,8 @@ __global__ void after_t1(GemmTrain T) {  // zd1 = x' W1 (in f.zd1); hd1 = f1'(z1
             const size_t k = (size_t)r * kHid + n;
             float hd = 0.f;
             if (n < n1) hd = act_dfn<float>(act_of(M, e, 1, n), T.f.z1[k], T.f.h1[k]) * T.f.zd1[k];
-            T.b.hd1[k] = __float2bfloat16_rn(hd);
-            T.b.ah1[k] = __float2bfloat16_rn(a * T.f.h1[k] + hd);
+            st_op(T, T.b.hd1, k, hd);
+            st_op(T, T.b.ah1, k, a * T.f.h1[k] + hd);
         }
     }
 }
@@ -210,7 +222,7 @@ __global__ void after_t2(GemmTrain T) {  // zd2 = hd1 W2 (in f.zd2); dp2; dw3, d
                 atomicAdd(&acc[e][n], dl3 * (a * T.f.h2[k] + hd2[n]) + dp3 * T.f.h2[k]);  // w3
                 atomicAdd(&acc[e][kHid + n], a * T.f.dl2[k] + dp);                       // b2
             }
-            T.b.dp2[k] = __float2bfloat16_rn(dp);
+            st_op(T, T.b.dp2, k, dp);
         }
         atomicAdd(&acc[e][2 * kHid], a * dl3 + dp3);  // b3
         (void)n1;
@@ -250,7 +262,7 @@ __global__ void after_s1(GemmTrain T) {  // sp2 = dp2 W2^T (in f.zd2's place: f.
                      act_ddfn<float>(ac, T.f.z1[k], T.f.h1[k]) * T.f.zd1[k] * T.f.s2[k];
                 atomicAdd(&acc[e][n], a * T.f.dl1[k] + dp);
             }
-            T.b.dp1[k] = __float2bfloat16_rn(dp);
+            st_op(T, T.b.dp1, k, dp);
         }
     }
     __syncthreads();
@@ -295,6 +307,22 @@ cublasStatus_t grad_gemm(cublasHandle_t h, int R, int K, int N, const __nv_bfloa
                         C, CUDA_R_32F, ldc, CUBLAS_COMPUTE_32F, CUBLAS_GEMM_DEFAULT);
 }
 
+// split-aware products: C (+)= A B as hi*hi (+ hi*lo + lo*hi)
+bool rows_gemm3(const GemmTrain &T, cublasHandle_t h, int R, int N, int K, const __nv_bfloat16 *A, int lda,
+                const __nv_bfloat16 *B, int ldb, bool transB, float *C, int ldc, float beta) {
+    if (rows_gemm(h, R, N, K, A, lda, B, ldb, transB, C, ldc, beta) != CUBLAS_STATUS_SUCCESS) return false;
+    if (!T.split) return true;
+    return rows_gemm(h, R, N, K, A, lda, B + T.lo, ldb, transB, C, ldc, 1.f) == CUBLAS_STATUS_SUCCESS &&
+           rows_gemm(h, R, N, K, A + T.lo, lda, B, ldb, transB, C, ldc, 1.f) == CUBLAS_STATUS_SUCCESS;
+}
+bool grad_gemm3(const GemmTrain &T, cublasHandle_t h, int R, int K, int N, const __nv_bfloat16 *A, int lda,
+                const __nv_bfloat16 *B, int ldb, float *C, int ldc, float beta) {
+    if (grad_gemm(h, R, K, N, A, lda, B, ldb, C, ldc, beta) != CUBLAS_STATUS_SUCCESS) return false;
+    if (!T.split) return true;
+    return grad_gemm(h, R, K, N, A, lda, B + T.lo, ldb, C, ldc, 1.f) == CUBLAS_STATUS_SUCCESS &&
+           grad_gemm(h, R, K, N, A + T.lo, lda, B, ldb, C, ldc, 1.f) == CUBLAS_STATUS_SUCCESS;
+}
+
 int grid_of(int R) { return std::max(1, std::min(4096, (R + 255) / 256)); }
 
 }  // namespace
@@ -336,6 +364,7 @@ void gemm_train_carve(GemmTrain &T, float *fpool, __nv_bfloat16 *bpool, float *g
     T.b.dp2 = b; b += Rz * kHid;
     T.w = b;
     T.gw = gw;
+    T.lo = gemm_train_bf16(R);
 }
 
 // forward and backward products: atomic outputs to eat, dE/dG to dg (for the training
@@ -349,8 +378,8 @@ int gemm_train_forward(cublasHandle_t h, cudaStream_t s, const GemmTrain &T) {
         if (R <= 0) continue;
         const int n0 = T.M.nodes[e][0], n1 = T.M.nodes[e][1];
         const __nv_bfloat16 *W1 = T.w + (size_t)e * (kIn + kHid) * kHid;
-        if (rows_gemm(h, R, n1, n0, T.b.x + (size_t)r0 * kIn, kIn, W1, kHid, false, T.f.z1 + (size_t)r0 * kHid, kHid,
-                      0.f) != CUBLAS_STATUS_SUCCESS)
+        if (!rows_gemm3(T, h, R, n1, n0, T.b.x + (size_t)r0 * kIn, kIn, W1, kHid, false, T.f.z1 + (size_t)r0 * kHid, kHid,
+                      0.f) )
             return 1;
     }
     after_f1<<<grid_of(T.R), 256, 0, s>>>(T);
@@ -359,8 +388,8 @@ int gemm_train_forward(cublasHandle_t h, cudaStream_t s, const GemmTrain &T) {
         if (R <= 0) continue;
         const int n1 = T.M.nodes[e][1], n2 = T.M.nodes[e][2];
         const __nv_bfloat16 *W2 = T.w + (size_t)e * (kIn + kHid) * kHid + kIn * kHid;
-        if (rows_gemm(h, R, n2, n1, T.b.h1 + (size_t)r0 * kHid, kHid, W2, kHid, false, T.f.z2 + (size_t)r0 * kHid, kHid,
-                      0.f) != CUBLAS_STATUS_SUCCESS)
+        if (!rows_gemm3(T, h, R, n2, n1, T.b.h1 + (size_t)r0 * kHid, kHid, W2, kHid, false, T.f.z2 + (size_t)r0 * kHid, kHid,
+                      0.f) )
             return 1;
     }
     after_f2<<<grid_of(T.R), 256, 0, s>>>(T);
@@ -369,8 +398,8 @@ int gemm_train_forward(cublasHandle_t h, cudaStream_t s, const GemmTrain &T) {
         if (R <= 0) continue;
         const int n1 = T.M.nodes[e][1], n2 = T.M.nodes[e][2];
         const __nv_bfloat16 *W2 = T.w + (size_t)e * (kIn + kHid) * kHid + kIn * kHid;
-        if (rows_gemm(h, R, n1, n2, T.b.dl2 + (size_t)r0 * kHid, kHid, W2, kHid, true, T.f.s2 + (size_t)r0 * kHid, kHid,
-                      0.f) != CUBLAS_STATUS_SUCCESS)
+        if (!rows_gemm3(T, h, R, n1, n2, T.b.dl2 + (size_t)r0 * kHid, kHid, W2, kHid, true, T.f.s2 + (size_t)r0 * kHid, kHid,
+                      0.f) )
             return 1;
     }
     after_b1<<<grid_of(T.R), 256, 0, s>>>(T);
@@ -379,8 +408,8 @@ int gemm_train_forward(cublasHandle_t h, cudaStream_t s, const GemmTrain &T) {
         if (R <= 0) continue;
         const int n0 = T.M.nodes[e][0], n1 = T.M.nodes[e][1];
         const __nv_bfloat16 *W1 = T.w + (size_t)e * (kIn + kHid) * kHid;
-        if (rows_gemm(h, R, n0, n1, T.b.dl1 + (size_t)r0 * kHid, kHid, W1, kHid, true, T.f.cv + (size_t)r0 * kIn, kIn,
-                      0.f) != CUBLAS_STATUS_SUCCESS)
+        if (!rows_gemm3(T, h, R, n0, n1, T.b.dl1 + (size_t)r0 * kHid, kHid, W1, kHid, true, T.f.cv + (size_t)r0 * kIn, kIn,
+                      0.f) )
             return 1;
     }
     after_b0<<<grid_of(T.R), 256, 0, s>>>(T);
@@ -396,8 +425,8 @@ int gemm_train_backward(cublasHandle_t h, cudaStream_t s, const GemmTrain &T) {
         if (R <= 0) continue;
         const int n0 = T.M.nodes[e][0], n1 = T.M.nodes[e][1];
         const __nv_bfloat16 *W1 = T.w + (size_t)e * (kIn + kHid) * kHid;
-        if (rows_gemm(h, R, n1, n0, T.b.xd + (size_t)r0 * kIn, kIn, W1, kHid, false, T.f.zd1 + (size_t)r0 * kHid, kHid,
-                      0.f) != CUBLAS_STATUS_SUCCESS)
+        if (!rows_gemm3(T, h, R, n1, n0, T.b.xd + (size_t)r0 * kIn, kIn, W1, kHid, false, T.f.zd1 + (size_t)r0 * kHid, kHid,
+                      0.f) )
             return 1;
     }
     after_t1<<<grid_of(T.R), 256, 0, s>>>(T);
@@ -406,8 +435,8 @@ int gemm_train_backward(cublasHandle_t h, cudaStream_t s, const GemmTrain &T) {
         if (R <= 0) continue;
         const int n1 = T.M.nodes[e][1], n2 = T.M.nodes[e][2];
         const __nv_bfloat16 *W2 = T.w + (size_t)e * (kIn + kHid) * kHid + kIn * kHid;
-        if (rows_gemm(h, R, n2, n1, T.b.hd1 + (size_t)r0 * kHid, kHid, W2, kHid, false, T.f.zd2 + (size_t)r0 * kHid,
-                      kHid, 0.f) != CUBLAS_STATUS_SUCCESS)
+        if (!rows_gemm3(T, h, R, n2, n1, T.b.hd1 + (size_t)r0 * kHid, kHid, W2, kHid, false, T.f.zd2 + (size_t)r0 * kHid,
+                      kHid, 0.f) )
             return 1;
     }
     after_t2<<<grid_of(T.R), 256, 0, s>>>(T);
@@ -416,8 +445,8 @@ int gemm_train_backward(cublasHandle_t h, cudaStream_t s, const GemmTrain &T) {
         if (R <= 0) continue;
         const int n1 = T.M.nodes[e][1], n2 = T.M.nodes[e][2];
         const __nv_bfloat16 *W2 = T.w + (size_t)e * (kIn + kHid) * kHid + kIn * kHid;
-        if (rows_gemm(h, R, n1, n2, T.b.dp2 + (size_t)r0 * kHid, kHid, W2, kHid, true, T.f.sp2 + (size_t)r0 * kHid,
-                      kHid, 0.f) != CUBLAS_STATUS_SUCCESS)
+        if (!rows_gemm3(T, h, R, n1, n2, T.b.dp2 + (size_t)r0 * kHid, kHid, W2, kHid, true, T.f.sp2 + (size_t)r0 * kHid,
+                      kHid, 0.f) )
             return 1;
     }
     after_s1<<<grid_of(T.R), 256, 0, s>>>(T);
@@ -429,14 +458,12 @@ int gemm_train_backward(cublasHandle_t h, cudaStream_t s, const GemmTrain &T) {
             continue;
         }
         const int n0 = T.M.nodes[e][0], n1 = T.M.nodes[e][1], n2 = T.M.nodes[e][2];
-        if (grad_gemm(h, R, n0, n1, T.b.ax + (size_t)r0 * kIn, kIn, T.b.dl1 + (size_t)r0 * kHid, kHid, g1, kHid, 0.f) !=
-                CUBLAS_STATUS_SUCCESS ||
-            grad_gemm(h, R, n0, n1, T.b.x + (size_t)r0 * kIn, kIn, T.b.dp1 + (size_t)r0 * kHid, kHid, g1, kHid, 1.f) !=
-                CUBLAS_STATUS_SUCCESS ||
-            grad_gemm(h, R, n1, n2, T.b.ah1 + (size_t)r0 * kHid, kHid, T.b.dl2 + (size_t)r0 * kHid, kHid, g2, kHid,
-                      0.f) != CUBLAS_STATUS_SUCCESS ||
-            grad_gemm(h, R, n1, n2, T.b.h1 + (size_t)r0 * kHid, kHid, T.b.dp2 + (size_t)r0 * kHid, kHid, g2, kHid,
-                      1.f) != CUBLAS_STATUS_SUCCESS)
+        if (!grad_gemm3(T, h, R, n0, n1, T.b.ax + (size_t)r0 * kIn, kIn, T.b.dl1 + (size_t)r0 * kHid, kHid, g1, kHid, 0.f) ||
+            !grad_gemm3(T, h, R, n0, n1, T.b.x + (size_t)r0 * kIn, kIn, T.b.dp1 + (size_t)r0 * kHid, kHid, g1, kHid, 1.f) ||
+            !grad_gemm3(T, h, R, n1, n2, T.b.ah1 + (size_t)r0 * kHid, kHid, T.b.dl2 + (size_t)r0 * kHid, kHid, g2, kHid,
+                        0.f) ||
+            !grad_gemm3(T, h, R, n1, n2, T.b.h1 + (size_t)r0 * kHid, kHid, T.b.dp2 + (size_t)r0 * kHid, kHid, g2, kHid,
+                        1.f))
             return 1;
     }
     add_weight_grads<<<64, 256, 0, s>>>(T);

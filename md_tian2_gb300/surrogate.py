@@ -83,9 +83,9 @@ def surrogate_model(seed: int = 11, descriptor: str = "acsf") -> nene.NNModel:
 
 def _opts(lr, w_energy, w_force, precision):
     """precision: fp64 (gradient checks), fp32 (the training kernel's own network on CUDA
-    cores) or bf16 (the network's products as BF16 GEMMs on the tensor cores, FP32 master
-    weights and accumulation)."""
-    return TrainOpts(w_energy, w_force, lr, 0.9, 0.999, 1e-8, {"fp64": 0, "fp32": 1, "bf16": 2}[precision])
+    cores), bf16 (the network's products as BF16 GEMMs on the tensor cores, FP32 master
+    weights and accumulation) or bf16x3 (the same with split BF16 operands)."""
+    return TrainOpts(w_energy, w_force, lr, 0.9, 0.999, 1e-8, {"fp64": 0, "fp32": 1, "bf16": 2, "bf16x3": 3}[precision])
 
 
 class Trainer:

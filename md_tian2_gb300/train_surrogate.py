@@ -41,6 +41,9 @@ def main(argv=None):
                     help="extra samples per trajectory taken every --long-every steps (late-time coverage)")
     ap.add_argument("--long-every", type=int, default=400)
     ap.add_argument("--init", default=None, help="warm start from this .npz model (same descriptor)")
+    ap.add_argument("--precision", choices=("fp32", "bf16", "bf16x3"), default="fp32",
+                    help="arithmetic of the network products: the training kernel's FP32 lanes, BF16 GEMMs, "
+                         "or split-BF16 GEMMs")
     a = ap.parse_args(argv)
     log = lambda m: print(m, file=sys.stderr, flush=True)  # noqa: E731
     t0 = time.perf_counter()
@@ -56,8 +59,8 @@ def main(argv=None):
     tr = Trainer(data, model, scale_margin=a.scale_margin, max_neighbors=a.max_neighbors, keep_function=bool(a.init))
     t_setup = time.perf_counter() - t1
     hist = tr.train(epochs=a.epochs, batch=a.batch, lr=a.lr, lr_final=a.lr_final, w_energy=a.w_energy,
-                    w_force=a.w_force, time_budget=a.time_budget, log=log)
-    report = {"descriptor": a.descriptor, "init": Path(a.init).name if a.init else None,
+                    w_force=a.w_force, time_budget=a.time_budget, log=log, precision=a.precision)
+    report = {"descriptor": a.descriptor, "precision": a.precision, "init": Path(a.init).name if a.init else None,
               "samples": {"every": a.every, "nsamples": a.nsamples, "long_every": a.long_every,
                           "long_samples": a.long_samples}, "max_neighbors": a.max_neighbors, "configs": len(data.universes), "atoms": int(sum(u.natoms for u in data.universes)),
               "dataset_s": t_data, "setup_s": t_setup, "train_s": tr.seconds, "steps": tr.steps,
