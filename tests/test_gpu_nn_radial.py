@@ -163,6 +163,39 @@ def test_radial_md_exit_and_skin(built_lib, oracle_lib):
     assert (qa["status"] == qc["status"]).all() and (qa["steps_done"] == qc["steps_done"]).all()
 
 
+@pytest.mark.parametrize("prec", ["fp32", "bf16x3"])
+def test_radial_md_launch_leaves_every_force_complete(built_lib, oracle_lib, prec):
+    """The state a fused launch leaves carries every force of its last step: after one
+    20-step launch, in which half the trajectories stop early through pul, the forces of
+    all atoms (fixed ones included) equal a fresh force evaluation of the downloaded
+    positions (1e-5 of the largest force: FP32 sums in no fixed order)."""
+    us = W.config2(24, seed=27)
+    for t, u in enumerate(us):  # half the projectiles start just below pul, moving up
+        if t % 2 == 0:
+            u.r[0, :, 2] = 6.0
+            u.v[0, :, 2] = 0.05
+    m = _radial_model(9)
+    sp = SimParams(step=0.5, gamma_const=1e-3, seed=7, pul=6.05, use_exit=True)
+    eng = _engine(us, m)
+    eng.calc_force(sp, precision=prec)
+    eng.md_steps(20, sp, precision=prec)
+    out = eng.download()
+    q = eng.query(sp)
+    eng.close()
+    stopped = q["steps_done"] < 20
+    assert stopped.any() and not stopped.all()
+    fixed = np.concatenate([u.is_fixed.reshape(-1) for u in us]).astype(bool)
+    assert fixed.sum() > len(fixed) // 3
+    ref = _engine(us, m)
+    ref.upload(out["r"], out["v"])
+    ref.calc_force(sp, precision=prec)
+    f = ref.download()["f"]
+    ref.close()
+    bar = 1e-5 * np.abs(f).max()
+    assert np.abs(out["f"] - f)[fixed].max() < bar
+    assert np.abs(out["f"] - f).max() < bar
+
+
 def test_radial_surrogate_fallback_is_fp64_emt(built_lib, oracle_lib):
     from oracle.oracle import OracleUniverse
     rng = np.random.default_rng(4)
