@@ -72,7 +72,7 @@ def parse():
     ap.add_argument("--hdnnp-traj", type=int, default=2048, help="trajectories of the HDNNP arm (0: skip)")
     ap.add_argument("--arm-steps", type=int, default=20, help="timed MD steps of the RPMD and HDNNP arms")
     ap.add_argument("--no-nve", action="store_true", help="skip the surrogate's NVE drift runs")
-    ap.add_argument("--profile-arm", choices=["fp32", "bf16", "bf16x3", "emt"], default=None,
+    ap.add_argument("--profile-arm", choices=["fp32", "bf16", "bf16x3", "emt", "hdnnp"], default=None,
                     help="run only this arm's warm-up and timed MD steps (no report): the workload of the "
                          "ncu captures under profiles/")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
@@ -508,15 +508,9 @@ def _valid_triplets(eng, us, rc_ang, sample):
     return pairs, trip
 
 
-def hdnnp_arm(args, device, stream, torch, peak32, peak64):
-    """Batched RuNNer-style HDNNP: H on 6x6 graphene (72 C + 1 H, z-ripple 0.05 A), 8 G2 + 16 G3
-    per element (6.5 A cosine cutoff), 24-25-25-1 tanh per element with seeded Glorot weights
-    and scaling from the batch's own descriptors; Verlet, dt 0.1 fs.  FP64 generic kernels and
-    FP32 warp-per-atom fast kernels (fused MD steps), and the network on the tensor cores
-    (BF16 / split-BF16 operands, FP32 accumulation) as a pass of its own between the FP32
-    generic kernel's descriptor and force passes, stepped as propagate_1 -> calc_force ->
-    propagate_2 (the reference's own loop); every arithmetic's force error against FP64 (the
-    FP64 kernels equal the FP64 oracle to 1e-10 eV/A in the parity tests)."""
+def _hdnnp_batch(args, device, stream):
+    """The HDNNP arm's batch (--hdnnp-traj H/graphene trajectories), its model with the scaling
+    taken from the batch's own descriptors, and a factory of engines holding them."""
     import ctypes as ct
 
     from md_tian2_gb300 import nene
@@ -539,6 +533,19 @@ def hdnnp_arm(args, device, stream, torch, peak32, peak64):
     G = eng.nn_descriptors()
     eng.close()
     nene.set_scaling(m, G, np.concatenate([[0] + [1] * (u.natoms - 1) for u in us]))
+    return us, engine, sp
+
+
+def hdnnp_arm(args, device, stream, torch, peak32, peak64):
+    """Batched RuNNer-style HDNNP: H on 6x6 graphene (72 C + 1 H, z-ripple 0.05 A), 8 G2 + 16 G3
+    per element (6.5 A cosine cutoff), 24-25-25-1 tanh per element with seeded Glorot weights
+    and scaling from the batch's own descriptors; Verlet, dt 0.1 fs.  FP64 generic kernels and
+    FP32 warp-per-atom fast kernels (fused MD steps), and the network on the tensor cores
+    (BF16 / split-BF16 operands, FP32 accumulation) as a pass of its own between the FP32
+    generic kernel's descriptor and force passes, stepped as propagate_1 -> calc_force ->
+    propagate_2 (the reference's own loop); every arithmetic's force error against FP64 (the
+    FP64 kernels equal the FP64 oracle to 1e-10 eV/A in the parity tests)."""
+    us, engine, sp = _hdnnp_batch(args, device, stream)
     atoms = int(sum(u.natoms for u in us))
     out = {"trajectories": len(us), "atoms": atoms}
     forces = {}
@@ -608,6 +615,20 @@ def run_ours(args):
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     torch.cuda.set_device(local)
+
+    if args.profile_arm == "hdnnp":
+        # the HDNNP arm's FP32 fused MD steps alone (warp-per-atom kernel), for profiling
+        stream = torch.cuda.Stream()
+        us, engine, sp = _hdnnp_batch(args, local, stream)
+        eng = engine()
+        eng.calc_force(sp, precision="fp32")
+        for _ in range(args.warmup):
+            eng.md_steps(1, sp, precision="fp32")
+        eng.md_steps(args.steps, sp, precision="fp32")
+        eng.synchronize()
+        eng.close()
+        print(json.dumps({"profile_arm": "hdnnp", "ntraj": len(us), "steps": args.steps}), flush=True)
+        return
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

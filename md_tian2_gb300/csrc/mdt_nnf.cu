@@ -24,8 +24,10 @@
 //    shuffles for 32 values).
 //  * Triplets (q3 < q4) with r_jk <= rc and the G3 element pair: lane p owns the row
 //    pair (p, n-2-p) of the upper triangle (n candidates together) and marks the valid
-//    second neighbours of both rows in bit masks; the forward and the force walk visit
-//    only set bits.
+//    second neighbours of both rows in bit masks.  The forward and the force walk visit
+//    only set bits, in chunks: the lanes feed their rows' triplets into a warp buffer and
+//    take equal contiguous blocks of it (valid triplets fall unevenly on the row pairs:
+//    walked by their owners, half the lanes idled).
 //  * fc(r_jk) and its derivative come from the Taylor series of cos(pi sqrt(s)/2) in
 //    s = r_jk^2 / rc^2 (no square root, sine or cosine per triplet); with
 //    h = (1 + lambda cos)/2, 2^(1-zeta) (1 + lambda cos)^zeta = 2 h^zeta, and every
@@ -122,17 +124,20 @@ struct WarpF {
     uint8_t *code;         // [q]: bit 0 elem == pair_a, bit 1 elem == pair_b
     unsigned *mask;        // [q][mw]: valid second neighbours q4 > q of row q
     int *rcnt;             // [q]: valid triplets of row q
+    uint16_t *tbuf;        // [kTB]: a chunk of the warp's triplets, q3 | q4 << 8 (G3 models)
     float *sfx, *sfy, *sfz;
     float *gb;             // [kNAmax][sgs]: descriptors G, then dE/dG, of the atoms in flight
 };
 
 constexpr int kNAmax = 4;  // atoms per warp in the network phase
+constexpr int kTB = 1024;  // triplets per chunk of the balanced triplet walk
 
 __host__ __device__ inline size_t r16f(size_t b) { return (b + 15) & ~size_t(15); }
 
 __host__ __device__ inline size_t warp_bytes_f(int maxnb, int mw, int nlayers, int ls, int sgs) {
     const size_t rows = 3 * r16f(16 * (size_t)maxnb) + r16f(maxnb) + r16f(4 * (size_t)maxnb * mw) +
-                        r16f(4 * ((size_t)maxnb + 1)) + 3 * r16f(4 * (size_t)maxnb);
+                        r16f(4 * ((size_t)maxnb + 1)) + (mw > 0 ? r16f(2 * (size_t)kTB) : 0) +
+                        3 * r16f(4 * (size_t)maxnb);
     const size_t net = 2 * r16f(4 * (size_t)kNAmax * (nlayers + 1) * ls);
     return (rows > net ? rows : net) + r16f(4 * (size_t)kNAmax * sgs);
 }
@@ -225,6 +230,7 @@ __device__ WarpF carve_warp(const SmemF &S, const FLaunch &L, int warp) {
     w.code = (uint8_t *)take(nb);
     w.mask = (unsigned *)take(4 * (size_t)nb * L.mw);
     w.rcnt = (int *)take(4 * ((size_t)nb + 1));
+    w.tbuf = (uint16_t *)take(L.mw > 0 ? 2 * (size_t)kTB : 0);
     w.sfx = (float *)take(4 * (size_t)nb);
     w.sfy = (float *)take(4 * (size_t)nb);
     w.sfz = (float *)take(4 * (size_t)nb);
@@ -393,6 +399,58 @@ struct RowBits {
         m &= m - 1;
         q3 = row;
         q4 = (w << 5) + b;
+    }
+};
+
+// The triplets of a warp in chunks of at most kTB, so that every lane takes the same
+// share however unevenly the valid triplets fall on the lanes' row pairs: each lane feeds
+// the triplets of its row pairs (p = lane, lane + 32, ...; row-major) into the warp's
+// buffer behind the lanes before it, and the lanes then take equal contiguous blocks of
+// the chunk (consecutive entries mostly share their first neighbour q3).
+struct TripletFeed {
+    RowBits it;
+    const unsigned *mask;
+    const int *rcnt;
+    int mw, npairs, nrows, p, left, total;  // current row pair, its triplets not yet fed; the lane's
+    __device__ __forceinline__ void init(const unsigned *mk, int mwords, const int *rc, int lane, int np, int nr) {
+        mask = mk;
+        rcnt = rc;
+        mw = mwords;
+        npairs = np;
+        nrows = nr;
+        total = 0;
+        for (int q = lane; q < np; q += 32) {
+            const int r1 = nr - 1 - q;
+            total += rc[q] + (r1 != q ? rc[r1] : 0);
+        }
+        p = lane - 32;
+        left = 0;
+    }
+    __device__ __forceinline__ void next(int &q3, int &q4) {
+        while (left == 0) {  // a later row pair of the lane holds the triplet (total > 0)
+            p += 32;
+            const int r1 = nrows - 1 - p;
+            left = rcnt[p] + (r1 != p ? rcnt[r1] : 0);
+            if (left) it.start(mask, mw, p, nrows);
+        }
+        it.next(q3, q4);
+        --left;
+    }
+    // the next chunk into buf; returns its size (0: every triplet of the warp was fed)
+    __device__ __forceinline__ int fill(uint16_t *buf) {
+        int all;
+        warp_excl_scan(total, all);
+        const int take = all <= kTB ? total : (total < kTB / 32 ? total : kTB / 32);
+        int tot;
+        const int pos = warp_excl_scan(take, tot);
+        for (int e = 0; e < take; ++e) {
+            int q3, q4;
+            next(q3, q4);
+            buf[pos + e] = (uint16_t)(q3 | (q4 << 8));
+        }
+        total -= take;
+        __syncwarp();
+        return tot;
     }
 };
 
@@ -616,17 +674,15 @@ __device__ void nnf_descriptors(const NNDev &M, const FastNN &F, const NNScratch
     float acc[32];
 #pragma unroll
     for (int c = 0; c < 32; ++c) acc[c] = 0.f;
-    for (int p = lane; p < npairs; p += 32) {
-        const int r1 = nrows - 1 - p;
-        const int ntr = W.rcnt[p] + (r1 != p ? W.rcnt[r1] : 0);
-        RowBits it;
-        it.start(W.mask, mw, p, nrows);
+    TripletFeed tf;
+    tf.init(W.mask, mw, W.rcnt, lane, npairs, nrows);
+    for (int tot; (tot = tf.fill(W.tbuf)) > 0;) {
+        const int e0 = (lane * tot) >> 5, e1 = ((lane + 1) * tot) >> 5;
         int cq3 = -1;
         float4 JA = make_float4(0.f, 0.f, 0.f, 0.f), JB = JA;
         float EJ3 = 0.f;
-        for (int e = 0; e < ntr; ++e) {
-            int q3, q4;
-            it.next(q3, q4);
+        for (int e = e0; e < e1; ++e) {
+            const int v = W.tbuf[e], q3 = v & 0xFF, q4 = v >> 8;
             if (q3 != cq3) {
                 cq3 = q3;
                 JA = W.ra[q3];
@@ -656,6 +712,7 @@ __device__ void nnf_descriptors(const NNDev &M, const FastNN &F, const NNScratch
                     acc[m * NQ + 2 * z + 1] = fmaf(Xm[m], Pm[z], acc[m * NQ + 2 * z + 1]);
                 }
         }
+        __syncwarp();  // the chunk is read before the next one overwrites it
     }
     reduce_scatter<32>(acc);
     if (lane < NG * NQ) {
@@ -893,17 +950,15 @@ __device__ void nnf_forces(const NNDev &M, const FastNN &F, const NNScratch &X, 
             }
         }
         __syncwarp();
-        for (int p = lane; p < npairs; p += 32) {
-            const int r1 = nrows - 1 - p;
-            const int ntr = W.rcnt[p] + (r1 != p ? W.rcnt[r1] : 0);
-            RowBits it;
-            it.start(W.mask, mw, p, nrows);
+        TripletFeed tf;
+        tf.init(W.mask, mw, W.rcnt, lane, npairs, nrows);
+        for (int tot; (tot = tf.fill(W.tbuf)) > 0;) {
+            const int e0 = (lane * tot) >> 5, e1 = ((lane + 1) * tot) >> 5;
             int cq3 = -1;
             float4 JA = make_float4(0.f, 0.f, 0.f, 0.f), JB = JA, JC = JA;
             float fjx = 0.f, fjy = 0.f, fjz = 0.f;
-            for (int e = 0; e < ntr; ++e) {
-                int q3, q4;
-                it.next(q3, q4);
+            for (int e = e0; e < e1; ++e) {
+                const int v = W.tbuf[e], q3 = v & 0xFF, q4 = v >> 8;
                 if (q3 != cq3) {
                     if (cq3 >= 0) {
                         red_shared(&W.sfx[cq3], fjx);
@@ -965,6 +1020,7 @@ __device__ void nnf_forces(const NNDev &M, const FastNN &F, const NNScratch &X, 
                 red_shared(&W.sfy[cq3], fjy);
                 red_shared(&W.sfz[cq3], fjz);
             }
+            __syncwarp();  // the chunk is read before the next one overwrites it
         }
     }
     __syncwarp();
@@ -1214,8 +1270,11 @@ __device__ void load_model_smem(const NNDev &M, const FastNN &F, const SmemF &S)
 
 // mode 0: forces, 1: energies only, 2: nsteps fused MD steps (propagate_1, forces,
 // propagate_2, exit test), as the generic network kernels.
+// Angular models run two CTAs per SM with up to 128 registers a thread (at the HDNNP
+// benchmark shape their shared memory, 97 KB a CTA, leaves no room for a third, and under
+// the 80 registers of three CTAs the triplet walks spilled); radial-only models keep three.
 template <int NG, int ZM, bool G3ON>
-__global__ void __launch_bounds__(kFBlock, 3)
+__global__ void __launch_bounds__(kFBlock, G3ON ? 2 : 3)
     nnf_kernel(Batch B, NNDev M, FastNN F, EmtConst E, NNScratch X, PropParams P, FLaunch L, const int *order,
                int *counter, int nsteps, int mode) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
