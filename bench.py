@@ -485,26 +485,28 @@ FLOP_HD_TRIPLET = 3 * (16 * 6 + 30)
 FLOP_HD_ATOM = 3 * 2 * (24 * 25 + 25 * 25 + 25)
 
 
-def _valid_triplets(eng, us, rc_ang, sample):
-    """Triplets (i; j < k) inside the cutoff (r_ij, r_ik, r_jk < rc) from the neighbour lists
-    the kernel built, on the first `sample` trajectories; returns (pairs, triplets) summed."""
-    counts, words = eng.nn_neighbors()
-    off = np.concatenate([[0], np.cumsum([u.natoms for u in us])])
+def _valid_triplets(us, rc_ang, sample):
+    """Pairs (i, j) and triplets (i; j < k) inside the cutoff (r_ij, r_ik, r_jk < rc) of the
+    first `sample` trajectories, counted geometrically over the periodic images of wrapped
+    positions (cell vectors as the columns of simbox); returns (pairs, triplets) summed."""
     pairs = trip = 0
-    for t in range(sample):
-        u = us[t]
-        r = u.r[:, 0, :]
+    for u in us[:sample]:
+        cell = np.asarray(u.simbox, float)
+        frac = np.linalg.solve(cell, u.r[:, 0, :].T).T
+        r = (frac - np.floor(frac)) @ cell.T
+        # image ranges wide enough for the cutoff in every direction
+        inv = np.linalg.inv(cell)
+        reach = [int(np.ceil(rc_ang * np.linalg.norm(inv[d]))) + 1 for d in range(3)]
+        grid = np.stack(np.meshgrid(*[np.arange(-m, m + 1) for m in reach], indexing="ij"), -1).reshape(-1, 3)
+        shifts = grid @ cell.T
         for i in range(u.natoms):
-            a = off[t] + i
-            w = words[a, :counts[a]]
-            j = w & 0xFFFF
-            n = np.stack([((w >> s) & 15) - 8 for s in (16, 20, 24)], axis=1)
-            pos = r[j] + n @ u.simbox.T  # image positions (cell vectors as columns)
-            pairs += len(j)
-            if len(j) > 1:
-                dd = np.sqrt(((pos[:, None, :] - pos[None, :, :]) ** 2).sum(-1))
-                iu = np.triu_indices(len(j), 1)
-                trip += int(np.sum(dd[iu] < rc_ang))
+            d = (r[None, :, :] + shifts[:, None, :] - r[i]).reshape(-1, 3)
+            dd = np.sqrt((d ** 2).sum(-1))
+            pos = d[(dd < rc_ang) & (dd > 1e-8)]
+            pairs += len(pos)
+            if len(pos) > 1:
+                djk = np.sqrt(((pos[:, None, :] - pos[None, :, :]) ** 2).sum(-1))
+                trip += int(np.sum(djk[np.triu_indices(len(pos), 1)] < rc_ang))
     return pairs, trip
 
 
@@ -555,7 +557,7 @@ def hdnnp_arm(args, device, stream, torch, peak32, peak64):
         forces[prec] = eng.download()["f"]
         if prec == "fp64":
             sample = min(32, len(us))
-            pairs, trip = _valid_triplets(eng, us, 6.5, sample)
+            pairs, trip = _valid_triplets(us, 6.5, sample)
             scale = len(us) / sample
             flop = int(scale * (FLOP_HD_PAIR * pairs + FLOP_HD_TRIPLET * trip)) + FLOP_HD_ATOM * atoms
         eng.upload()
