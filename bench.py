@@ -72,7 +72,7 @@ def parse():
     ap.add_argument("--hdnnp-traj", type=int, default=2048, help="trajectories of the HDNNP arm (0: skip)")
     ap.add_argument("--arm-steps", type=int, default=20, help="timed MD steps of the RPMD and HDNNP arms")
     ap.add_argument("--no-nve", action="store_true", help="skip the surrogate's NVE drift runs")
-    ap.add_argument("--profile-arm", choices=["fp32", "bf16", "bf16x3", "emt", "hdnnp"], default=None,
+    ap.add_argument("--profile-arm", choices=["fp32", "bf16", "bf16x3", "emt", "hdnnp", "rpmd"], default=None,
                     help="run only this arm's warm-up and timed MD steps (no report): the workload of the "
                          "ncu captures under profiles/")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
@@ -630,6 +630,24 @@ def run_ours(args):
         eng.synchronize()
         eng.close()
         print(json.dumps({"profile_arm": "hdnnp", "ntraj": len(us), "steps": args.steps}), flush=True)
+        return
+    if args.profile_arm == "rpmd":
+        # the RPMD arm's fused MD steps with FP32 bead forces alone, for profiling
+        from md_tian2_gb300 import workloads as W
+        from md_tian2_gb300.engine import Engine, SimParams
+        us = W.config3(args.rpmd_traj, seed=3)
+        sp = SimParams(step=0.1, Tsurf=300.0, Tproj=300.0, pile_tau=200.0, seed=11)
+        eng = Engine(local)
+        eng.read_emt(W.emt_params("H", "Pt"))
+        eng.define(us)
+        eng.upload()
+        eng.calc_force(sp, precision="fp32")
+        for _ in range(args.warmup):
+            eng.md_steps(1, sp, precision="fp32")
+        eng.md_steps(args.steps, sp, precision="fp32")
+        eng.synchronize()
+        eng.close()
+        print(json.dumps({"profile_arm": "rpmd", "ntraj": len(us), "steps": args.steps}), flush=True)
         return
 
     cpu = None

@@ -54,13 +54,20 @@ struct Cell;
 
 template <typename R> struct SmemEmt {
     double *px, *py, *pz;  // staged bead positions
+    float *xh, *yh, *zh, *xl, *yl, *zl;  // FP32 forces (R = float): their FP32 hi/lo split
     R *sig, *A, *fx, *fy, *fz;
     Cell *cell;
     int8_t *slot;          // EMT species slot per atom (-1: none)
     int8_t *typ;           // universe type per atom
     double *red;           // 64 doubles for block reductions
-    double *cjk;           // max_beads^2 normal-mode table
+    double *cjk;           // the trajectory's normal-mode table, then its per-type, per-mode
+                           // propagator tables (rp_cells doubles in all)
 };
+
+// doubles of the normal-mode area: the nb x nb table and 5 per-type, per-mode tables
+__host__ __device__ constexpr size_t rp_cells(int max_beads) {
+    return (size_t)max_beads * max_beads + 5 * (size_t)kMaxTypes * max_beads;
+}
 
 template <typename R>
 static __device__ SmemEmt<R> carve_smem(unsigned char *base, int max_atoms, int max_beads) {
@@ -74,8 +81,15 @@ static __device__ SmemEmt<R> carve_smem(unsigned char *base, int max_atoms, int 
     s.px = (double *)take(sizeof(double) * max_atoms);
     s.py = (double *)take(sizeof(double) * max_atoms);
     s.pz = (double *)take(sizeof(double) * max_atoms);
+    const size_t nf = sizeof(R) == 4 ? sizeof(float) * max_atoms : 0;
+    s.xh = (float *)take(nf);
+    s.yh = (float *)take(nf);
+    s.zh = (float *)take(nf);
+    s.xl = (float *)take(nf);
+    s.yl = (float *)take(nf);
+    s.zl = (float *)take(nf);
     s.red = (double *)take(sizeof(double) * 64);
-    s.cjk = (double *)take(sizeof(double) * max_beads * max_beads);
+    s.cjk = (double *)take(sizeof(double) * rp_cells(max_beads));
     s.sig = (R *)take(sizeof(R) * max_atoms);
     s.A = (R *)take(sizeof(R) * max_atoms);
     s.fx = (R *)take(sizeof(R) * max_atoms);
@@ -89,7 +103,8 @@ static __device__ SmemEmt<R> carve_smem(unsigned char *base, int max_atoms, int 
 
 inline size_t smem_bytes(int max_atoms, int max_beads, size_t rsize) {
     auto r16 = [](size_t b) { return (b + 15) & ~size_t(15); };
-    return 3 * r16(8 * max_atoms) + r16(8 * 64) + r16(8 * max_beads * max_beads) + 5 * r16(rsize * max_atoms) +
+    return 3 * r16(8 * max_atoms) + (rsize == 4 ? 6 * r16(4 * max_atoms) : 0) + r16(8 * 64) +
+           r16(8 * rp_cells(max_beads)) + 5 * r16(rsize * max_atoms) +
            256 + 2 * r16(max_atoms);
 }
 
@@ -123,9 +138,10 @@ static __device__ __noinline__ double block_min(double v, double *red) {
 // choosing them.  Column major (cell vectors as columns).
 struct Cell {
     double h[9], hi[9];
-    float hif[9];
+    float hif[9], hf[9];  // FP32 inverse and (FP32 bead forces) FP32 matrix
     unsigned nz;  // bit k set when h[k] != 0
 };
+static_assert(sizeof(Cell) <= 256, "the shared-memory carve reserves 256 bytes for the cell");
 
 static __device__ __forceinline__ void load_cell(const Batch &B, int t, Cell &c) {
     unsigned nz = 0;
@@ -133,6 +149,7 @@ static __device__ __forceinline__ void load_cell(const Batch &B, int t, Cell &c)
         c.h[k] = B.box[9 * t + k];
         c.hi[k] = B.ibox[9 * t + k];
         c.hif[k] = (float)c.hi[k];
+        c.hf[k] = (float)c.h[k];
         if (c.h[k] != 0.0) nz |= 1u << k;
     }
     c.nz = nz;
@@ -150,6 +167,28 @@ static __device__ __forceinline__ double image_shift(float wf, const double *hi_
     const double w = __dadd_rn(__dadd_rn(__dmul_rn(hi_row3[row], ex), __dmul_rn(hi_row3[row + 3], ey)),
                                __dmul_rn(hi_row3[row + 6], ez));
     return round(w);
+}
+
+// FP32 bead forces: the minimum image of r_i - r_j from the FP32 hi/lo split of the
+// positions, with the image chosen as min_image chooses it (FP32, exact ties in FP64)
+// and applied in FP32: no FP64 instruction per pair unless a pair sits on a tie.
+template <typename S_>
+static __device__ __forceinline__ void min_image_f(const Cell &c, const S_ &S, int i, int j, float &dx, float &dy,
+                                            float &dz) {
+    const float ex = (S.xh[i] - S.xh[j]) + (S.xl[i] - S.xl[j]);
+    const float ey = (S.yh[i] - S.yh[j]) + (S.yl[i] - S.yl[j]);
+    const float ez = (S.zh[i] - S.zh[j]) + (S.zl[i] - S.zl[j]);
+    float n[3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        const float w = c.hif[r] * ex + c.hif[r + 3] * ey + c.hif[r + 6] * ez;
+        n[r] = roundf(w);
+        if (!(fabsf(fabsf(w - n[r]) - 0.5f) > 1e-4f))
+            n[r] = (float)image_shift(w, c.hi, S.px[i] - S.px[j], S.py[i] - S.py[j], S.pz[i] - S.pz[j], r);
+    }
+    dx = ex - (c.hf[0] * n[0] + c.hf[3] * n[1] + c.hf[6] * n[2]);
+    dy = ey - (c.hf[1] * n[0] + c.hf[4] * n[1] + c.hf[7] * n[2]);
+    dz = ez - (c.hf[2] * n[0] + c.hf[5] * n[1] + c.hf[8] * n[2]);
 }
 
 // minimum image of e = r_i - r_j, src/universe_mod.f90:411-428
@@ -207,6 +246,15 @@ static __device__ void emt_bead(const Batch &B, const EmtConst &E, const SmemEmt
         S.px[i] = B.rx[base + i];
         S.py[i] = B.ry[base + i];
         S.pz[i] = B.rz[base + i];
+        if constexpr (sizeof(R) == 4) {
+            const double x = S.px[i], y = S.py[i], z = S.pz[i];
+            S.xh[i] = (float)x;
+            S.yh[i] = (float)y;
+            S.zh[i] = (float)z;
+            S.xl[i] = (float)(x - (double)S.xh[i]);
+            S.yl[i] = (float)(y - (double)S.yh[i]);
+            S.zl[i] = (float)(z - (double)S.zh[i]);
+        }
         const int ty = B.type[aoff + i];
         S.typ[i] = (int8_t)ty;
         S.slot[i] = (int8_t)E.slot_of_type[ty];
@@ -235,11 +283,15 @@ static __device__ void emt_bead(const Batch &B, const EmtConst &E, const SmemEmt
         const int ti = S.typ[i], tj = S.typ[j];
         R q_ij = R(0), q_ji = R(0), fv = R(0), rx = R(0), ry = R(0), rz = R(0);
         if (!(2 * k == N && i >= K) && ((E.pair_mask >> (ti * kMaxTypes + tj)) & 1u)) {
-            double dx, dy, dz;
-            min_image(cell, S.px[i] - S.px[j], S.py[i] - S.py[j], S.pz[i] - S.pz[j], dx, dy, dz);
-            rx = (R)dx;
-            ry = (R)dy;
-            rz = (R)dz;
+            if constexpr (sizeof(R) == 4) {
+                min_image_f(cell, S, i, j, rx, ry, rz);
+            } else {
+                double dx, dy, dz;
+                min_image(cell, S.px[i] - S.px[j], S.py[i] - S.py[j], S.pz[i] - S.pz[j], dx, dy, dz);
+                rx = (R)dx;
+                ry = (R)dy;
+                rz = (R)dz;
+            }
             const R r2 = rx * rx + ry * ry + rz * rz;
             // skipped only beyond the cutoff, like the reference's `if (r > cutoff*rcut) cycle`
             // (pes_emt_mod.f90:660): a distance that is not a number enters the sums

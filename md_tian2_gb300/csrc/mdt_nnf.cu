@@ -146,7 +146,7 @@ __host__ __device__ inline size_t shared_bytes_f(int max_atoms, int max_beads, i
     return 3 * r16f(8 * (size_t)max_atoms) + 6 * r16f(4 * (size_t)max_atoms) + r16f(max_atoms) +
            r16f(4 * (size_t)max_atoms) + r16f(4 * ((size_t)max_atoms + kMaxElem + 1)) +
            3 * r16f(4 * (size_t)max_atoms) + r16f(8 * 18) + 3 * r16f(4 * 9) + r16f(8 * 64) +
-           r16f(8 * (size_t)max_beads * max_beads) + 16 + r16f(4 * (size_t)wtotal) +
+           r16f(8 * rp_cells(max_beads)) + 16 + r16f(4 * (size_t)wtotal) +
            r16f(16 * (size_t)nelem * kFMaxG2);
 }
 
@@ -205,7 +205,7 @@ __device__ SmemF carve_f(unsigned char *base, const FLaunch &L, int max_beads, i
     s.ginv = (float *)take(4 * 9);
     s.wk = (float *)take(4 * 9);
     s.red = (double *)take(8 * 64);
-    s.cjk = (double *)take(8 * (size_t)max_beads * max_beads);
+    s.cjk = (double *)take(8 * rp_cells(max_beads));
     s.misc = (int *)take(16);
     s.w = (float *)take(4 * (size_t)wtotal);
     s.g2 = (float4 *)take(16 * (size_t)nelem * kFMaxG2);

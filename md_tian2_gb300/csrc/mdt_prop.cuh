@@ -328,13 +328,45 @@ static __device__ void andersen(const Batch &B, const PropParams &P, const TrajV
     }
 }
 
-// pile_thermostat, md_algo.f90:440-502 (one thread per atom, all three dimensions)
-static __device__ void pile(const Batch &B, const PropParams &P, const TrajView &T, const double *cjk, int i, int step) {
+// Per-type, per-mode tables of the ring-polymer propagators, kept in the CTA's shared
+// normal-mode area right after the trajectory's nb x nb cjk table (the area holds
+// kRpTables x kMaxTypes x max_beads more doubles): the free ring-polymer coefficients
+// wk, cos(wk dt), sin(wk dt) of rpmd.f90:360-378 and the PILE damping c1, c2 of
+// md_algo.f90:461-466.  They depend on the type's temperature, nb, dt and pile_tau, not on
+// the atom, so a CTA forms them once per call instead of once per atom and dimension (FP64
+// transcendentals are the slowest instructions of the GPU); the expressions are the
+// per-atom ones.
+enum { kRpWk, kRpCw, kRpSw, kRpC1, kRpC2, kRpTables };
+static_assert(kRpTables * kMaxTypes * 1 + 1 == rp_cells(1), "rp_cells sizes the tables");
+static __device__ __forceinline__ double *rp_table(double *cjk, int nb, int which) {
+    return cjk + nb * nb + which * kMaxTypes * nb;
+}
+
+static __device__ void pile_tables(const Batch &B, const PropParams &P, const TrajView &T, double *cjk) {
+    const int nb = T.nb;
+    double *c1t = rp_table(cjk, nb, kRpC1), *c2t = rp_table(cjk, nb, kRpC2);
+    for (int w = threadIdx.x; w < B.ntypes * nb; w += blockDim.x) {
+        const int ty = w / nb, kk = w - ty * nb;
+        const double betaN = 1.0 / (kBoltz * temp_of(B, P, ty) * nb);
+        double gam;
+        if (kk == 0) gam = 1 / P.pile_tau;
+        else gam = 2 * (2 * (1 / betaN / kHbar) * sin(kk * kPi / nb));
+        const double c1 = exp(-0.5 * P.step * gam);
+        c1t[w] = c1;
+        c2t[w] = sqrt(1 - c1 * c1);
+    }
+    __syncthreads();
+}
+
+// pile_thermostat, md_algo.f90:440-502 (one thread per atom, all three dimensions; the
+// per-type, per-mode damping from pile_tables)
+static __device__ void pile(const Batch &B, const PropParams &P, const TrajView &T, double *cjk, int i, int step) {
     const int nb = T.nb;
     const int ty = B.type[T.aoff + i];
     const double m = B.mass[T.aoff + i];
     const double betaN = 1.0 / (kBoltz * temp_of(B, P, ty) * nb);
     const double sq = sqrt(m / betaN);
+    const double *c1t = rp_table(cjk, nb, kRpC1) + ty * nb, *c2t = rp_table(cjk, nb, kRpC2) + ty * nb;
     for (int d = 0; d < 3; ++d) {
         double newP[32], atomP[32];
         for (int b = 0; b < nb; ++b) atomP[b] = m * comp(B.vx, B.vy, B.vz, d, T.base + (int64_t)b * T.N + i);
@@ -344,12 +376,8 @@ static __device__ void pile(const Batch &B, const PropParams &P, const TrajView 
             newP[b] = s;
         }
         for (int kk = 0; kk < nb; ++kk) {
-            double gam;
-            if (kk == 0) gam = 1 / P.pile_tau;
-            else gam = 2 * (2 * (1 / betaN / kHbar) * sin(kk * kPi / nb));
-            const double c1 = exp(-0.5 * P.step * gam), c2 = sqrt(1 - c1 * c1);
             const double z = rand_normal(P, T, step, kk, i, d, kStreamPile, P.zeta);
-            newP[kk] = c1 * newP[kk] + sq * c2 * z;
+            newP[kk] = c1t[kk] * newP[kk] + sq * c2t[kk] * z;
         }
         for (int b = 0; b < nb; ++b) {
             const int64_t k = T.base + (int64_t)b * T.N + i;
@@ -403,8 +431,9 @@ static __device__ bool traj_has_algo(const Batch &B, int id) {
 }
 
 // propagate_1, md_algo.f90:37-76
-static __device__ void propagate_1(const Batch &B, const PropParams &P, const TrajView &T, const double *cjk, int step,
+static __device__ void propagate_1(const Batch &B, const PropParams &P, const TrajView &T, double *cjk, int step,
                             double *red) {
+    if (traj_has_algo(B, kPropPile)) pile_tables(B, P, T, cjk);
     for (int i = threadIdx.x; i < T.N; i += blockDim.x) {
         const int algo = B.algo[B.type[T.aoff + i]];
         switch (algo) {
@@ -444,11 +473,30 @@ static __device__ void propagate_2(const Batch &B, const PropParams &P, const Tr
     __syncthreads();
 }
 
-// do_ring_polymer_step, rpmd.f90:309-452.  Thread per (atom, dimension).
-static __device__ void ring_polymer_step(const Batch &B, const PropParams &P, const TrajView &T, const double *cjk) {
+// do_ring_polymer_step, rpmd.f90:309-452.  Thread per (atom, dimension); the free
+// ring-polymer coefficients per type and mode in the table after cjk.
+static __device__ void ring_polymer_step(const Batch &B, const PropParams &P, const TrajView &T, double *cjk) {
     const int nb = T.nb;
     const double prefactor = -1 * B.mass[T.aoff] * pow(kBoltz * P.Tproj * nb / kHbar, 2.0);
     const double piN = kPi / nb;
+    double *wkt = rp_table(cjk, nb, kRpWk), *cwt = rp_table(cjk, nb, kRpCw), *swt = rp_table(cjk, nb, kRpSw);
+    for (int w = threadIdx.x; w < B.ntypes * nb; w += blockDim.x) {
+        const int ty = w / nb, b = w - ty * nb;
+        double wk = 0.0, cw = 1.0, sw = 0.0;
+        if (nb > 1 && b > 0) {
+            const double betaN = 1.0 / (kBoltz * temp_of(B, P, ty) * nb);
+            const double twown = 2.0 / betaN / kHbar;
+            const int bb = (b <= nb / 2) ? b : nb - b;
+            wk = twown * sin(bb * piN);
+            const double wt = wk * P.step;
+            cw = cos(wt);
+            sw = sin(wt);
+        }
+        wkt[w] = wk;
+        cwt[w] = cw;
+        swt[w] = sw;
+    }
+    __syncthreads();
     for (int w = threadIdx.x; w < 3 * T.N; w += blockDim.x) {
         const int i = w / 3, d = w - 3 * (w / 3);
         const int ty = B.type[T.aoff + i];
@@ -468,14 +516,11 @@ static __device__ void ring_polymer_step(const Batch &B, const PropParams &P, co
             np[b] = sp;
             nq[b] = sq;
         }
-        const double betaN = 1.0 / (kBoltz * temp_of(B, P, ty) * nb);
-        const double twown = 2.0 / betaN / kHbar;
         for (int b = 0; b < nb; ++b) {
             double c0 = 1.0, c1 = 0.0, c2 = P.step / m, c3 = 1.0;
             if (nb > 1 && b > 0) {
-                const int bb = (b <= nb / 2) ? b : nb - b;
-                const double wk = twown * sin(bb * piN), wt = wk * P.step, wm = wk * m;
-                const double cw = cos(wt), sw = sin(wt);
+                const double wm = wkt[ty * nb + b] * m;
+                const double cw = cwt[ty * nb + b], sw = swt[ty * nb + b];
                 c0 = cw; c1 = -wm * sw; c2 = sw / wm; c3 = cw;
             }
             const double pn = np[b] * c0 + nq[b] * c1;
@@ -488,13 +533,15 @@ static __device__ void ring_polymer_step(const Batch &B, const PropParams &P, co
             const int64_t k = T.base + (int64_t)b * T.N + i;
             if (revert) continue;
             if (B.fixed[k] >> d & 1) continue;
+            // v = sum_k p_k cjk(b,k) / m with the division after the sum (one FP64
+            // division per bead instead of per term; the same value to rounding)
             double sr = 0.0, sv = 0.0;
             for (int kk = 0; kk < nb; ++kk) {
                 sr = sr + nq[kk] * cjk[kk * nb + b];
-                sv = sv + np[kk] * cjk[kk * nb + b] / m;
+                sv = sv + np[kk] * cjk[kk * nb + b];
             }
             comp(B.rx, B.ry, B.rz, d, k) = sr;
-            comp(B.vx, B.vy, B.vz, d, k) = sv;
+            comp(B.vx, B.vy, B.vz, d, k) = sv / m;
         }
         if (revert) {
             // rpmd.f90:418-435: positions/velocities kept, spring force set instead
@@ -546,7 +593,6 @@ static __device__ void end_of_step(const Batch &B, const PropParams &P, const Tr
 
 static __device__ void load_cjk(const Batch &B, int t, double *cjk_s) {
     const int nb = B.nbeads[t];
-    if (nb <= 1) return;
     const double *src = B.cjk + B.cjk_off[t];
     for (int k = threadIdx.x; k < nb * nb; k += blockDim.x) cjk_s[k] = src[k];
     __syncthreads();
