@@ -358,6 +358,68 @@ static __device__ void pile_tables(const Batch &B, const PropParams &P, const Tr
     __syncthreads();
 }
 
+// Normal-mode transforms with the table cjk(j, m) (column major: cjk[m nb + j - 1], beads
+// j = 1..nb, modes m = 0..nb-1).  nm_forward: y_m = sum_j x_j cjk(j, m); nm_back:
+// x_j = sum_m y_m cjk(j, m).  For an even nb >= 4 the table's symmetry halves the products:
+// cjk(nb - j, m) = cjk(j, m) for m <= nb/2 (cosines, the constant and the alternating
+// mode) and -cjk(j, m) for m > nb/2 (sines), j = 1..nb/2-1; beads nb/2 and nb pair with
+// themselves and carry no sine modes (their sine entries are zero up to the rounding of
+// the table).  The sums are the reference's matrix products in another order.
+static __device__ __forceinline__ void nm_forward(const double *cjk, int nb, const double *x, double *y) {
+    if ((nb & 1) || nb < 4) {
+        for (int m = 0; m < nb; ++m) {
+            double s = 0.0;
+            for (int k = 0; k < nb; ++k) s = s + x[k] * cjk[m * nb + k];
+            y[m] = s;
+        }
+        return;
+    }
+    const int h = nb / 2;
+    double sp[16], sm[16];  // x_j + x_(nb-j), x_j - x_(nb-j) at j - 1
+    for (int j = 1; j < h; ++j) {
+        sp[j - 1] = x[j - 1] + x[nb - j - 1];
+        sm[j - 1] = x[j - 1] - x[nb - j - 1];
+    }
+    for (int m = 0; m <= h; ++m) {
+        const double *c = cjk + m * nb;
+        double s = c[h - 1] * x[h - 1] + c[nb - 1] * x[nb - 1];
+        for (int j = 1; j < h; ++j) s = s + c[j - 1] * sp[j - 1];
+        y[m] = s;
+    }
+    for (int m = h + 1; m < nb; ++m) {
+        const double *c = cjk + m * nb;
+        double s = 0.0;
+        for (int j = 1; j < h; ++j) s = s + c[j - 1] * sm[j - 1];
+        y[m] = s;
+    }
+}
+
+static __device__ __forceinline__ void nm_back(const double *cjk, int nb, const double *y, double *x) {
+    if ((nb & 1) || nb < 4) {
+        for (int b = 0; b < nb; ++b) {
+            double s = 0.0;
+            for (int m = 0; m < nb; ++m) s = s + y[m] * cjk[m * nb + b];
+            x[b] = s;
+        }
+        return;
+    }
+    const int h = nb / 2;
+    for (int j = 1; j < h; ++j) {
+        double a = 0.0, c = 0.0;
+        for (int m = 0; m <= h; ++m) a = a + y[m] * cjk[m * nb + j - 1];
+        for (int m = h + 1; m < nb; ++m) c = c + y[m] * cjk[m * nb + j - 1];
+        x[j - 1] = a + c;
+        x[nb - j - 1] = a - c;
+    }
+    double a = 0.0, c = 0.0;
+    for (int m = 0; m <= h; ++m) {
+        a = a + y[m] * cjk[m * nb + h - 1];
+        c = c + y[m] * cjk[m * nb + nb - 1];
+    }
+    x[h - 1] = a;
+    x[nb - 1] = c;
+}
+
 // pile_thermostat, md_algo.f90:440-502 (one thread per atom, all three dimensions; the
 // per-type, per-mode damping from pile_tables)
 static __device__ void pile(const Batch &B, const PropParams &P, const TrajView &T, double *cjk, int i, int step) {
@@ -370,21 +432,15 @@ static __device__ void pile(const Batch &B, const PropParams &P, const TrajView 
     for (int d = 0; d < 3; ++d) {
         double newP[32], atomP[32];
         for (int b = 0; b < nb; ++b) atomP[b] = m * comp(B.vx, B.vy, B.vz, d, T.base + (int64_t)b * T.N + i);
-        for (int b = 0; b < nb; ++b) {
-            double s = 0.0;
-            for (int k = 0; k < nb; ++k) s = s + atomP[k] * cjk[b * nb + k];  // cjk(k,b)
-            newP[b] = s;
-        }
+        nm_forward(cjk, nb, atomP, newP);
         for (int kk = 0; kk < nb; ++kk) {
             const double z = rand_normal(P, T, step, kk, i, d, kStreamPile, P.zeta);
             newP[kk] = c1t[kk] * newP[kk] + sq * c2t[kk] * z;
         }
+        nm_back(cjk, nb, newP, atomP);
         for (int b = 0; b < nb; ++b) {
             const int64_t k = T.base + (int64_t)b * T.N + i;
-            double s = 0.0;
-            if (!(B.fixed[k] >> d & 1))
-                for (int kk = 0; kk < nb; ++kk) s = s + newP[kk] * cjk[kk * nb + b];  // cjk(b,kk)
-            comp(B.vx, B.vy, B.vz, d, k) = s / m;
+            comp(B.vx, B.vy, B.vz, d, k) = (B.fixed[k] >> d & 1) ? 0.0 : atomP[b] / m;
         }
     }
 }
@@ -507,15 +563,8 @@ static __device__ void ring_polymer_step(const Batch &B, const PropParams &P, co
             p[b] = m * comp(B.vx, B.vy, B.vz, d, k);
             q[b] = comp(B.rx, B.ry, B.rz, d, k);
         }
-        for (int b = 0; b < nb; ++b) {
-            double sp = 0.0, sq = 0.0;
-            for (int k = 0; k < nb; ++k) {
-                sp = sp + p[k] * cjk[b * nb + k];
-                sq = sq + q[k] * cjk[b * nb + k];
-            }
-            np[b] = sp;
-            nq[b] = sq;
-        }
+        nm_forward(cjk, nb, p, np);
+        nm_forward(cjk, nb, q, nq);
         for (int b = 0; b < nb; ++b) {
             double c0 = 1.0, c1 = 0.0, c2 = P.step / m, c3 = 1.0;
             if (nb > 1 && b > 0) {
@@ -529,19 +578,17 @@ static __device__ void ring_polymer_step(const Batch &B, const PropParams &P, co
         }
         const int algo = B.algo[ty];
         const bool revert = (algo == kPropLangevin || algo == kPropLangevinConst);
-        for (int b = 0; b < nb; ++b) {
-            const int64_t k = T.base + (int64_t)b * T.N + i;
-            if (revert) continue;
-            if (B.fixed[k] >> d & 1) continue;
-            // v = sum_k p_k cjk(b,k) / m with the division after the sum (one FP64
-            // division per bead instead of per term; the same value to rounding)
-            double sr = 0.0, sv = 0.0;
-            for (int kk = 0; kk < nb; ++kk) {
-                sr = sr + nq[kk] * cjk[kk * nb + b];
-                sv = sv + np[kk] * cjk[kk * nb + b];
+        if (!revert) {
+            // back to beads (p and q reused); v = sum_k p_k cjk(b,k) / m with the division
+            // after the sum (one FP64 division per bead instead of per term)
+            nm_back(cjk, nb, nq, q);
+            nm_back(cjk, nb, np, p);
+            for (int b = 0; b < nb; ++b) {
+                const int64_t k = T.base + (int64_t)b * T.N + i;
+                if (B.fixed[k] >> d & 1) continue;
+                comp(B.rx, B.ry, B.rz, d, k) = q[b];
+                comp(B.vx, B.vy, B.vz, d, k) = p[b] / m;
             }
-            comp(B.rx, B.ry, B.rz, d, k) = sr;
-            comp(B.vx, B.vy, B.vz, d, k) = sv / m;
         }
         if (revert) {
             // rpmd.f90:418-435: positions/velocities kept, spring force set instead
