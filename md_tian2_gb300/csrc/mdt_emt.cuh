@@ -38,14 +38,40 @@ static __device__ __forceinline__ double rsqrt_nr(double x) {
     return fma(y, fma(-h, t, 0.5), y);
 }
 
+// FP64 exp by the table-driven method of Tang (ACM TOMS 15(2), 1989): x = (64 n_hi + j)
+// ln2/64 + r with |r| <= ln2/128, exp(x) = 2^n_hi 2^(j/64) (1 + p(r)), p the Taylor series
+// of exp(r) - 1 to r^5 (truncation below 2^-54).  The 64 entries 2^(j/64) come from exp2
+// (e2t, filled per call); ln2/64 enters in two parts (its double, then the remainder) so
+// that r is exact to ~2^-100, and n = round(64 x / ln2) comes from adding 1.5 * 2^52.
+// About 12 FP64 instructions against ~19 for exp(), within 1 ulp of exp() on [-700, 700]
+// (measured on GB300); outside that range, and for NaN, exp() itself.
+static __device__ __forceinline__ double exp_t64(double x, const double *e2t) {
+    if (!(fabs(x) <= 700.0)) return exp(x);
+    const double shifter = 6755399441055744.0;
+    const double t = fma(x, 92.332482616893657, shifter);
+    const int n = __double2loint(t);
+    const double nd = t - shifter;
+    double r = fma(-nd, 0x1.62e42fefa39efp-7, x);
+    r = fma(-nd, 0x1.abc9e3b39803fp-62, r);
+    double q = fma(r, 1.0 / 120.0, 1.0 / 24.0);
+    q = fma(r, q, 1.0 / 6.0);
+    q = fma(r, q, 0.5);
+    const double pr = fma(r * r, q, r);
+    const double tj = e2t[n & 63];
+    const double y = fma(tj, pr, tj);
+    return __hiloint2double(__double2hiint(y) + (n >> 6) * (1 << 20), __double2loint(y));
+}
+
 template <typename R> struct M;
 template <> struct M<double> {
     static __device__ __forceinline__ double ex(double x) { return exp(x); }
+    static __device__ __forceinline__ double ex(double x, const double *e2t) { return exp_t64(x, e2t); }
     static __device__ __forceinline__ double rcp(double x) { return rcp_nr(x); }
     static __device__ __forceinline__ double rsq(double x) { return rsqrt_nr(x); }
 };
 template <> struct M<float> {
     static __device__ __forceinline__ float ex(float x) { return __expf(x); }
+    static __device__ __forceinline__ float ex(float x, const double *) { return __expf(x); }
     static __device__ __forceinline__ float rcp(float x) { return __frcp_rn(x); }
     static __device__ __forceinline__ float rsq(float x) { return rsqrtf(x); }
 };
@@ -60,6 +86,7 @@ template <typename R> struct SmemEmt {
     int8_t *slot;          // EMT species slot per atom (-1: none)
     int8_t *typ;           // universe type per atom
     double *red;           // 64 doubles for block reductions
+    double *e2t;           // 2^(j/64), j < 64 (exp_t64)
     double *cjk;           // the trajectory's normal-mode table, then its per-type, per-mode
                            // propagator tables (rp_cells doubles in all)
 };
@@ -89,6 +116,7 @@ static __device__ SmemEmt<R> carve_smem(unsigned char *base, int max_atoms, int 
     s.yl = (float *)take(nf);
     s.zl = (float *)take(nf);
     s.red = (double *)take(sizeof(double) * 64);
+    s.e2t = (double *)take(sizeof(double) * 64);
     s.cjk = (double *)take(sizeof(double) * rp_cells(max_beads));
     s.sig = (R *)take(sizeof(R) * max_atoms);
     s.A = (R *)take(sizeof(R) * max_atoms);
@@ -103,7 +131,7 @@ static __device__ SmemEmt<R> carve_smem(unsigned char *base, int max_atoms, int 
 
 inline size_t smem_bytes(int max_atoms, int max_beads, size_t rsize) {
     auto r16 = [](size_t b) { return (b + 15) & ~size_t(15); };
-    return 3 * r16(8 * max_atoms) + (rsize == 4 ? 6 * r16(4 * max_atoms) : 0) + r16(8 * 64) +
+    return 3 * r16(8 * max_atoms) + (rsize == 4 ? 6 * r16(4 * max_atoms) : 0) + 2 * r16(8 * 64) +
            r16(8 * rp_cells(max_beads)) + 5 * r16(rsize * max_atoms) +
            256 + 2 * r16(max_atoms);
 }
@@ -263,6 +291,8 @@ static __device__ void emt_bead(const Batch &B, const EmtConst &E, const SmemEmt
         S.fy[i] = R(0);
         S.fz[i] = R(0);
     }
+    if constexpr (sizeof(R) == 8)
+        for (int k = tid; k < 64; k += nt) S.e2t[k] = exp2((double)k * (1.0 / 64.0));
     if (tid == 0) load_cell(B, t, *S.cell);
     __syncthreads();
     const Cell &cell = *S.cell;
@@ -297,16 +327,16 @@ static __device__ void emt_bead(const Batch &B, const EmtConst &E, const SmemEmt
             // (pes_emt_mod.f90:660): a distance that is not a number enters the sums
             if (!(r2 > cut2)) {
                 const R ir = M<R>::rsq(r2), r = r2 * ir;
-                const R e = M<R>::ex(acut * (r - rcut));
+                const R e = M<R>::ex(acut * (r - rcut), S.e2t);
                 const R theta = M<R>::rcp(R(1) + e);
                 const R rt1 = acut * e * theta;
                 const int si = S.slot[i], sj = S.slot[j];
-                const R phi_j = theta * M<R>::ex(-(R)E.eta2[sj] * (r - (R)E.betas0[sj]));
-                const R psi_j = theta * M<R>::ex(-(R)E.kappadbeta[sj] * (r - (R)E.betas0[sj]));
+                const R phi_j = theta * M<R>::ex(-(R)E.eta2[sj] * (r - (R)E.betas0[sj]), S.e2t);
+                const R psi_j = theta * M<R>::ex(-(R)E.kappadbeta[sj] * (r - (R)E.betas0[sj]), S.e2t);
                 R phi_i = phi_j, psi_i = psi_j;
                 if (si != sj) {
-                    phi_i = theta * M<R>::ex(-(R)E.eta2[si] * (r - (R)E.betas0[si]));
-                    psi_i = theta * M<R>::ex(-(R)E.kappadbeta[si] * (r - (R)E.betas0[si]));
+                    phi_i = theta * M<R>::ex(-(R)E.eta2[si] * (r - (R)E.betas0[si]), S.e2t);
+                    psi_i = theta * M<R>::ex(-(R)E.kappadbeta[si] * (r - (R)E.betas0[si]), S.e2t);
                 }
                 const R gij = (R)(E.igamma1[si] * E.chi[si][sj]);
                 const R gji = (R)(E.igamma1[sj] * E.chi[sj][si]);
