@@ -94,9 +94,12 @@ def test_andersen(built_lib, oracle_lib):
         assert max_abs(out[k], ref[k]) < 1e-9, k
 
 
-@pytest.mark.parametrize("fused,nbeads", [(False, (4, 8)), (True, (4, 8)), (True, (16, 32))])
+@pytest.mark.parametrize("fused,nbeads", [(False, (4, 8)), (True, (4, 8)), (True, (16, 32)), (True, (3, 6)),
+                                          (False, (5, 2)), (True, (1, 4))])
 def test_pile_rpmd(built_lib, oracle_lib, fused, nbeads):
-    """(16, 32): the largest bead counts of the RPMD benchmark mix, on 3x3 and 4x4 Pt(111)."""
+    """(16, 32): the largest bead counts of the RPMD benchmark mix, on 3x3 and 4x4 Pt(111).
+    Odd bead counts and nb <= 2 take the direct normal-mode products, even nb >= 4 the
+    folded ones (6: not a power of two); nb = 1 runs PILE on single beads."""
     us = _batch(C.PROP_ID_PILE, C.PROP_ID_PILE, nbeads=nbeads, metal="Pt", n=2, z0=1.5)
     out, ref = _step_both(us, W.emt_params("H", "Pt"), SimParams(step=0.1, Tsurf=300, Tproj=300), steps=2,
                           fused=fused)
