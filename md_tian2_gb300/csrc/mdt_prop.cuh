@@ -333,9 +333,9 @@ static __device__ void andersen(const Batch &B, const PropParams &P, const TrajV
 // kRpTables x kMaxTypes x max_beads more doubles): the free ring-polymer coefficients
 // wk, cos(wk dt), sin(wk dt) of rpmd.f90:360-378 and the PILE damping c1, c2 of
 // md_algo.f90:461-466.  They depend on the type's temperature, nb, dt and pile_tau, not on
-// the atom, so a CTA forms them once per call instead of once per atom and dimension (FP64
-// transcendentals are the slowest instructions of the GPU); the expressions are the
-// per-atom ones.
+// the atom, so a CTA forms them once per call instead of once per atom and dimension (an
+// FP64 sin, cos or exp is tens of instructions on the FP64 pipe, the GPU's slowest); the
+// expressions are the per-atom ones.
 enum { kRpWk, kRpCw, kRpSw, kRpC1, kRpC2, kRpTables };
 static_assert(kRpTables * kMaxTypes * 1 + 1 == rp_cells(1), "rp_cells sizes the tables");
 static __device__ __forceinline__ double *rp_table(double *cjk, int nb, int which) {
@@ -375,7 +375,7 @@ static __device__ __forceinline__ void nm_forward(const double *cjk, int nb, con
         return;
     }
     const int h = nb / 2;
-    double sp[16], sm[16];  // x_j + x_(nb-j), x_j - x_(nb-j) at j - 1
+    double sp[16], sm[16];  // x_j + x_(nb-j), x_j - x_(nb-j) at j - 1 (nb <= 32)
     for (int j = 1; j < h; ++j) {
         sp[j - 1] = x[j - 1] + x[nb - j - 1];
         sm[j - 1] = x[j - 1] - x[nb - j - 1];
