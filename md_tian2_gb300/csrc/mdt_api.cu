@@ -1199,14 +1199,13 @@ int32_t mdt_state_upload(mdt_ctx *c, const double *r, const double *v) {
     cudaError_t e = cudaSuccess;
     const size_t bytes = sizeof(double) * 3 * (size_t)c->total_ba;
     Batch &B = c->B;
-    if (r) {
-        e = cudaMemcpyAsync(c->stage, r, bytes, cudaMemcpyHostToDevice, c->stream);
-        if (e == cudaSuccess) e = launch_unpack(c->stream, B, c->stage, B.rx, B.ry, B.rz, c->total_ba, c->ba_traj);
-        c->launches++;
-    }
-    if (v && e == cudaSuccess) {
-        e = cudaMemcpyAsync(c->stage, v, bytes, cudaMemcpyHostToDevice, c->stream);
-        if (e == cudaSuccess) e = launch_unpack(c->stream, B, c->stage, B.vx, B.vy, B.vz, c->total_ba, c->ba_traj);
+    // both arrays into their own stage slices, the copies back to back; one kernel unpacks
+    // them and writes the state, uploaded or kept, as the template of mdt_refill
+    double *sr = r ? c->stage : nullptr, *sv = v ? c->stage + 3 * (size_t)c->total_ba : nullptr;
+    if (r) e = cudaMemcpyAsync(sr, r, bytes, cudaMemcpyHostToDevice, c->stream);
+    if (v && e == cudaSuccess) e = cudaMemcpyAsync(sv, v, bytes, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) {
+        e = launch_unpack_state(c->stream, B, sr, sv, c->tmpl, c->total_ba, c->ba_traj);
         c->launches++;
     }
     if (e == cudaSuccess) e = cudaMemsetAsync(B.status, 0, sizeof(int) * c->T, c->stream);
@@ -1216,11 +1215,6 @@ int32_t mdt_state_upload(mdt_ctx *c, const double *r, const double *v) {
     // them (a plan of all trajectories stays: the cells did not change, and the skin lists
     // check every atom's displacement since their build, whatever moved it)
     if (!c->rfull) c->rnpack = 0;
-    // the uploaded state is the template of mdt_refill
-    const double *cur[6] = {B.rx, B.ry, B.rz, B.vx, B.vy, B.vz};
-    for (int a = 0; a < 6 && e == cudaSuccess; ++a)
-        e = cudaMemcpyAsync(c->tmpl + a * (size_t)c->total_ba, cur[a], sizeof(double) * c->total_ba,
-                            cudaMemcpyDeviceToDevice, c->stream);
     if (e == cudaSuccess && r && v) c->have_tmpl = true;
     return e == cudaSuccess ? MDT_OK : cuda_fail(c, e, "mdt_state_upload");
 }
@@ -1232,16 +1226,16 @@ int32_t mdt_state_download(mdt_ctx *c, double *r, double *v, double *f, double *
     const size_t bytes = sizeof(double) * 3 * (size_t)c->total_ba;
     Batch &B = c->B;
     double *outs[4] = {r, v, f, a};
-    double *src[4][3] = {{B.rx, B.ry, B.rz}, {B.vx, B.vy, B.vz}, {B.fx, B.fy, B.fz}, {B.ax, B.ay, B.az}};
-    // every array packs into its own slice of the stage: the copies queue behind the packs
-    // and one synchronisation ends the call
-    for (int k = 0; k < 4 && e == cudaSuccess; ++k) {
-        if (!outs[k]) continue;
-        double *sk = c->stage + 3 * (size_t)k * c->total_ba;
-        e = launch_pack(c->stream, B, sk, src[k][0], src[k][1], src[k][2], c->total_ba, c->ba_traj);
+    // every array packs into its own slice of the stage in one kernel; the copies then run
+    // back to back and one synchronisation ends the call
+    double *sl[4];
+    for (int k = 0; k < 4; ++k) sl[k] = outs[k] ? c->stage + 3 * (size_t)k * c->total_ba : nullptr;
+    if (r || v || f || a) {
+        e = launch_pack_state(c->stream, B, sl[0], sl[1], sl[2], sl[3], c->total_ba, c->ba_traj);
         c->launches++;
-        if (e == cudaSuccess) e = cudaMemcpyAsync(outs[k], sk, bytes, cudaMemcpyDeviceToHost, c->stream);
     }
+    for (int k = 0; k < 4 && e == cudaSuccess; ++k)
+        if (outs[k]) e = cudaMemcpyAsync(outs[k], sl[k], bytes, cudaMemcpyDeviceToHost, c->stream);
     if (dens && e == cudaSuccess) {
         double *sd = c->stage + 12 * (size_t)c->total_ba;
         e = launch_pack_scalar(c->stream, B, sd, B.dens, c->total_ba, c->ba_traj);

@@ -22,8 +22,10 @@ cudaError_t launch_md_steps(const LaunchCfg &c, const Batch &B, const EmtConst &
                             int precision);
 cudaError_t launch_unpack(cudaStream_t s, const Batch &B, const double *src, double *x, double *y, double *z,
                           int64_t total_ba, const int *ba_traj);
-cudaError_t launch_pack(cudaStream_t s, const Batch &B, double *dst, const double *x, const double *y,
-                        const double *z, int64_t total_ba, const int *ba_traj);
+cudaError_t launch_unpack_state(cudaStream_t s, const Batch &B, const double *sr, const double *sv, double *tmpl,
+                                int64_t total_ba, const int *ba_traj);
+cudaError_t launch_pack_state(cudaStream_t s, const Batch &B, double *dr, double *dv, double *df, double *da,
+                              int64_t total_ba, const int *ba_traj);
 cudaError_t launch_pack_scalar(cudaStream_t s, const Batch &B, double *dst, const double *x, int64_t total_ba,
                                const int *ba_traj);
 cudaError_t launch_summary(cudaStream_t s, const Batch &B, const PropParams &P, double *out5);

@@ -250,8 +250,10 @@ __global__ void unpack_kernel(Batch B, const double *src, double *x, double *y, 
     }
 }
 
-__global__ void pack_kernel(Batch B, double *dst, const double *x, const double *y, const double *z,
-                            int64_t total_ba, const int *ba_traj) {
+// A state upload in one pass: positions and velocities (each optional, null: kept) from
+// their stage slices into the SoA arrays, and all six into the refill template.
+__global__ void unpack_state_kernel(Batch B, const double *sr, const double *sv, double *tmpl, int64_t total_ba,
+                                    const int *ba_traj) {
     for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < total_ba;
          s += (int64_t)gridDim.x * blockDim.x) {
         const int t = ba_traj[s];
@@ -259,9 +261,71 @@ __global__ void pack_kernel(Batch B, double *dst, const double *x, const double 
         const int64_t loc = s - B.ba_off[t];
         const int b = (int)(loc / N), i = (int)(loc - (int64_t)b * N);
         const int64_t f = (B.ba_off[t] + (int64_t)i * B.nbeads[t] + b) * 3;
-        dst[f] = x[s];
-        dst[f + 1] = y[s];
-        dst[f + 2] = z[s];
+        double x, y, z;
+        if (sr) {
+            x = sr[f];
+            y = sr[f + 1];
+            z = sr[f + 2];
+            B.rx[s] = x;
+            B.ry[s] = y;
+            B.rz[s] = z;
+        } else {
+            x = B.rx[s];
+            y = B.ry[s];
+            z = B.rz[s];
+        }
+        tmpl[s] = x;
+        tmpl[total_ba + s] = y;
+        tmpl[2 * total_ba + s] = z;
+        if (sv) {
+            x = sv[f];
+            y = sv[f + 1];
+            z = sv[f + 2];
+            B.vx[s] = x;
+            B.vy[s] = y;
+            B.vz[s] = z;
+        } else {
+            x = B.vx[s];
+            y = B.vy[s];
+            z = B.vz[s];
+        }
+        tmpl[3 * total_ba + s] = x;
+        tmpl[4 * total_ba + s] = y;
+        tmpl[5 * total_ba + s] = z;
+    }
+}
+
+// A state download's packs in one pass: positions, velocities, forces, accelerations (each
+// optional, null: skipped) into their stage slices in the Fortran-order host layout.
+__global__ void pack_state_kernel(Batch B, double *dr, double *dv, double *df, double *da, int64_t total_ba,
+                                  const int *ba_traj) {
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < total_ba;
+         s += (int64_t)gridDim.x * blockDim.x) {
+        const int t = ba_traj[s];
+        const int N = B.natoms[t];
+        const int64_t loc = s - B.ba_off[t];
+        const int b = (int)(loc / N), i = (int)(loc - (int64_t)b * N);
+        const int64_t f = (B.ba_off[t] + (int64_t)i * B.nbeads[t] + b) * 3;
+        if (dr) {
+            dr[f] = B.rx[s];
+            dr[f + 1] = B.ry[s];
+            dr[f + 2] = B.rz[s];
+        }
+        if (dv) {
+            dv[f] = B.vx[s];
+            dv[f + 1] = B.vy[s];
+            dv[f + 2] = B.vz[s];
+        }
+        if (df) {
+            df[f] = B.fx[s];
+            df[f + 1] = B.fy[s];
+            df[f + 2] = B.fz[s];
+        }
+        if (da) {
+            da[f] = B.ax[s];
+            da[f + 1] = B.ay[s];
+            da[f + 2] = B.az[s];
+        }
     }
 }
 
@@ -371,10 +435,17 @@ cudaError_t launch_unpack(cudaStream_t s, const Batch &B, const double *src, dou
     return cudaGetLastError();
 }
 
-cudaError_t launch_pack(cudaStream_t s, const Batch &B, double *dst, const double *x, const double *y,
-                        const double *z, int64_t total_ba, const int *ba_traj) {
+cudaError_t launch_unpack_state(cudaStream_t s, const Batch &B, const double *sr, const double *sv, double *tmpl,
+                                int64_t total_ba, const int *ba_traj) {
     const int grid = (int)std::min<int64_t>((total_ba + 255) / 256, 4096);
-    pack_kernel<<<grid > 0 ? grid : 1, 256, 0, s>>>(B, dst, x, y, z, total_ba, ba_traj);
+    unpack_state_kernel<<<grid > 0 ? grid : 1, 256, 0, s>>>(B, sr, sv, tmpl, total_ba, ba_traj);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pack_state(cudaStream_t s, const Batch &B, double *dr, double *dv, double *df, double *da,
+                              int64_t total_ba, const int *ba_traj) {
+    const int grid = (int)std::min<int64_t>((total_ba + 255) / 256, 4096);
+    pack_state_kernel<<<grid > 0 ? grid : 1, 256, 0, s>>>(B, dr, dv, df, da, total_ba, ba_traj);
     return cudaGetLastError();
 }
 
