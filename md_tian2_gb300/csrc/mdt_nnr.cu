@@ -198,7 +198,9 @@ __device__ __forceinline__ bool image_range(float f, float w, int &lo, int &hi) 
 // loads broadcasts.)
 template <int G> struct GC { static constexpr int value = G; };
 
-template <bool SPREAD = false, class Fn>
+// UNR: unroll of the list walk (measured per network arithmetic: 1 with the tensor-core
+// network, 3 with the FP32 network; each about 1-2 % faster than the other choices)
+template <bool SPREAD = false, int UNR = 2, class Fn>
 __device__ __forceinline__ void for_neighbours(const RadialNN &R, const SmemR &S, const AtomR &A, const unsigned *sk,
                                                int cnt, Fn &&fn) {
     if (cnt >= 0) {
@@ -215,7 +217,7 @@ __device__ __forceinline__ void for_neighbours(const RadialNN &R, const SmemR &S
             int q1 = next(q0);
             unsigned w1 = len > 1 ? p[(size_t)q1 * A.N] : 0u;
             int q2 = next(q1);
-#pragma unroll 2
+#pragma unroll UNR
             for (int e = 0; e < len; ++e) {
                 const unsigned v = w0;
                 w0 = w1;
@@ -498,7 +500,7 @@ __device__ __forceinline__ float nnr_network(const RadialNN &R, const SmemR &S, 
 // the trajectory's out-of-range flag, the neighbour-list overflow and the nearest
 // neighbour entry (rmin2) with its atom (near: the first entry of the walk at that
 // distance).
-template <int KA, int KB, int BLA, int BLB>
+template <int KA, int KB, int BLA, int BLB, int UNR>
 __device__ __forceinline__ void nnr_descr(const RadialNN &R, const NNScratch &X, const SmemR &S, const AtomR &A,
                                           const unsigned *sk, int cnt, int *flag, float &rmin2, int &near,
                                           float (&xs)[KA + KB]) {
@@ -507,7 +509,7 @@ __device__ __forceinline__ void nnr_descr(const RadialNN &R, const NNScratch &X,
 #pragma unroll
     for (int k = 0; k < KT; ++k) G[k] = 0.f;
     int nn = 0;
-    for_neighbours(R, S, A, sk, cnt, [&](auto gc, int js, float dx, float dy, float dz, float r2) {
+    for_neighbours<false, UNR>(R, S, A, sk, cnt, [&](auto gc, int js, float dx, float dy, float dz, float r2) {
         constexpr int g = decltype(gc)::value;
         constexpr int K = g == 0 ? KA : KB, off = g == 0 ? 0 : KA, BL = g == 0 ? BLA : BLB;
         const bool inside = r2 < R.rc2;
@@ -558,13 +560,13 @@ __device__ __forceinline__ void nnr_descr(const RadialNN &R, const NNScratch &X,
 
 // Forces of the atom from dE/dG (raw descriptors, padded grouped order) in reverse mode: the
 // centre's share returned in fix/fiy/fiz, the neighbours' by red.shared.
-template <int KA, int KB, int BLA, int BLB>
+template <int KA, int KB, int BLA, int BLB, int UNR>
 __device__ __forceinline__ void nnr_forces(const RadialNN &R, const SmemR &S, const AtomR &A, const unsigned *sk,
                                            int cnt, const float (&dG)[KA + KB], float &fix, float &fiy,
                                            float &fiz) {
     constexpr int bs = kRS;
     float fx = 0.f, fy = 0.f, fz = 0.f;
-    for_neighbours<true>(R, S, A, sk, cnt, [&](auto gc, int js, float dx, float dy, float dz, float r2) {
+    for_neighbours<true, UNR>(R, S, A, sk, cnt, [&](auto gc, int js, float dx, float dy, float dz, float r2) {
         constexpr int g = decltype(gc)::value;
         constexpr int K = g == 0 ? KA : KB, off = g == 0 ? 0 : KA, BL = g == 0 ? BLA : BLB;
         const float ri = rsqrtf(r2);
@@ -1255,7 +1257,7 @@ __global__ void __launch_bounds__(kRBlockMax, 1)
                     r0[2] = B.rz[k];
                 }
                 cnt = R.skin > 0.f ? X.skcnt[k] : -1;
-                nnr_descr<KA, KB, BLA, BLB>(R, X, S, A, sk, cnt, flag, rmin2, near_js, xs);
+                nnr_descr<KA, KB, BLA, BLB, TC ? 1 : 3>(R, X, S, A, sk, cnt, flag, rmin2, near_js, xs);
             }
             float e_at = 0.f;
             if constexpr (TC) {
@@ -1270,7 +1272,7 @@ __global__ void __launch_bounds__(kRBlockMax, 1)
             }
             if (active) {
                 S.ea[tid] = (double)e_at + R.atom_energy[A.ei];
-                if (do_forces) nnr_forces<KA, KB, BLA, BLB>(R, S, A, sk, cnt, dG, fix, fiy, fiz);
+                if (do_forces) nnr_forces<KA, KB, BLA, BLB, TC ? 1 : 3>(R, S, A, sk, cnt, dG, fix, fiy, fiz);
             }
             __syncthreads();  // (B)
             // per-trajectory energy and skin-list state: one warp per trajectory, strided FP64
