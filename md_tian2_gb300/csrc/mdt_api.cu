@@ -1790,7 +1790,7 @@ int32_t mdt_nn_radial_block(mdt_ctx *c, int32_t max_block) {
 
 // Autotuner of the thread-per-atom kernel: times `nsteps` fused MD steps of the current
 // batch for every candidate (largest CTA in {256, 384, 512} atoms -- the pack plan's block
-// cap, which sets the waves and the warps per SM -- times Verlet skin in {0.5, 0.75, 1.0}
+// cap, which sets the waves and the warps per SM -- times Verlet skin in {0.3, 0.5, 0.75, 1.0}
 // A), each from the same saved state, keeps the fastest and puts the state back.
 int32_t mdt_autotune(mdt_ctx *c, int32_t precision, int32_t nsteps, const mdt_prop_params *p, int32_t *block,
                      double *skin_ang, double *ms_per_step) {
