@@ -86,7 +86,7 @@ template <typename R> struct SmemEmt {
     int8_t *slot;          // EMT species slot per atom (-1: none)
     int8_t *typ;           // universe type per atom
     double *red;           // 64 doubles for block reductions
-    double *e2t;           // 2^(j/64), j < 64 (exp_t64)
+    double *e2t;           // 2^(j/64), j < 64 (exp_t64: the pair loop in FP64, the per-atom epilogue)
     double *cjk;           // the trajectory's normal-mode table, then its per-type, per-mode
                            // propagator tables (rp_cells doubles in all)
 };
@@ -291,8 +291,7 @@ static __device__ void emt_bead(const Batch &B, const EmtConst &E, const SmemEmt
         S.fy[i] = R(0);
         S.fz[i] = R(0);
     }
-    if constexpr (sizeof(R) == 8)
-        for (int k = tid; k < 64; k += nt) S.e2t[k] = exp2((double)k * (1.0 / 64.0));
+    for (int k = tid; k < 64; k += nt) S.e2t[k] = exp2((double)k * (1.0 / 64.0));
     if (tid == 0) load_cell(B, t, *S.cell);
     __syncthreads();
     const Cell &cell = *S.cell;
@@ -376,11 +375,11 @@ static __device__ void emt_bead(const Batch &B, const EmtConst &E, const SmemEmt
         }
         const double sc = fmax((double)1e-30f, (double)S.sig[i]);  // single-precision 1e-30, pes_emt_mod.f90:793
         const double sa = -log(fmax(kTolerance, sc) * kTwelfth) / E.betaeta2[s];
-        const double el = exp(-E.lambda[s] * sa), ek = exp(-E.kappa[s] * sa);
+        const double el = exp_t64(-E.lambda[s] * sa, S.e2t), ek = exp_t64(-E.kappa[s] * sa, S.e2t);
         e_atom += E.e0[s] * ((1.0 + E.lambda[s] * sa) * el - 1.0) + 6.0 * E.v0[s] * ek;
         const double W = E.e0[s] * E.lambda[s] * E.lambda[s] * sa * el + 6.0 * E.v0[s] * E.kappa[s] * ek;
         S.A[i] = (R)(W / (E.betaeta2[s] * sc));
-        B.dens[base + i] = E.n0[s] * exp(E.dens_exp[s] * sa);
+        B.dens[base + i] = E.n0[s] * exp_t64(E.dens_exp[s] * sa, S.e2t);
     }
     const double etot = block_sum(e_pair + e_atom, S.red);  // contains __syncthreads
     if (tid == 0) B.epot[B.bead_off[t] + b] += etot;
